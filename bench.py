@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""DMC walker-steps/s of the GB300 walker path.
+
+Workload: the unitary Fermi gas with N = 66 (33 up / 33 down), pair function
+shells 0..6, cosh potential mu = 24 k_F, 4096 walkers, DMC with local
+weights (idmc = 1), dt = 0.001 / E_FG, branching and population control
+(target 4096).  Synthetic seeded inputs (no dataset is involved).
+
+One step = one generation: the drift-diffusion move and full wavefunction /
+local-energy evaluation of every walker, the DMC weight, estimators,
+branching and population control (dmcbcs.f90:436-448).
+
+Prints one JSON line.  Arms:
+  (default)          the CUDA library through its C ABI
+  --impl reference   the reference's CPU algorithm on the host cores: the
+                     reference itself (Fortran + MPI + MKL) cannot be built
+                     on these machines, so the CPU restatement (oracle/) runs
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DMC walker-steps/s @N=66: mixed/batched vs plain FP64 GPU, E_L rel err≤1e-6"
+UNIT = "walker-steps/s"
+WORKLOAD = "n66"
+
+# DRAM bytes per walker-step of the walker kernel from one ncu capture
+# (profiles/walker_kernel_n66.md: dram__bytes_read.sum + dram__bytes_write.sum
+# of one launch divided by the walkers it processed).  None until captured.
+NCU_TRAFFIC_BYTES_PER_WALKER = None
+
+
+def algorithmic_flops(nup, ndn, nd, K, npart):
+    """FP64 flops of one walker-step of the reference algorithm: the five
+    pair-orbital GEMMs, LU + inverse, inverse contractions, the Jastrow /
+    potential pair loop (all pairs, upper bound), beta lookups and the O(N)
+    step work."""
+    P = npart * (npart - 1) // 2
+    return 10 * nup * ndn * K + 2 * nd ** 3 + 8 * nd * (nup + ndn) + 60 * P + 40 * nup * ndn + 30 * npart
+
+
+def executed_flops(nup, ndn, nd, K, npart, nk, npairs_active):
+    """FP64 flops of one walker-step as this library computes it: S = U D^T,
+    Gauss-Jordan inverse (nd^3 multiply-adds), the two contraction products
+    G and H (2 nd^2 K multiply-adds each) and about 90 flops per active pair."""
+    return 2 * nup * ndn * K + 2 * nd ** 3 + 4 * nup * ndn * K + 90 * npairs_active + 30 * npart * nk
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [t.strip() for t in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 peak: cuBLAS DGEMM 4096^3, best of 5 (CUDA events)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def cpu_reference_rate(nwalk, budget_s, threads, gens_max=None):
+    """The oracle (CPU restatement of the reference) on the host cores:
+    walker-steps/s of full DMC generations of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from dmcbcs_project_gb300 import configs
+
+    sysd, rund, _ = configs.workload(WORKLOAD, nwalk=nwalk)
+    o = oracle.Oracle(sysd, rund, threads=threads)
+    o.init_walkers()
+    o.initial_eval()
+    o.generation(False)                       # warm
+    steps, t0 = 0, time.perf_counter()
+    gens = 0
+    while True:
+        steps += o.num_walkers()
+        o.generation(False)
+        gens += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or (gens_max and gens >= gens_max):
+            break
+    return steps / el, steps, gens, el
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from dmcbcs_project_gb300 import configs
+
+    nup, ndn, norb, nwalk, dt, _ = configs.WORKLOADS[WORKLOAD]
+    nsample = args.ref_walkers
+    # warm-up generations, then K timed generations of the sampled population
+    rate_w, _, _, _ = cpu_reference_rate(nsample, 0.0, threads, gens_max=max(1, args.warmup))
+    rate, steps, gens, el = cpu_reference_rate(nsample, 1e9, threads, gens_max=args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / max(gens, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "dmc_n66_33u33d", "walkers": nsample, "target_walkers": nwalk, "idmc": 1,
+                   "dt_efg": dt, "shells": norb},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{gens} DMC generations of {nsample} walkers (N=66) on {threads} host threads; "
+                                   "the reference Fortran/MPI/MKL build is not possible here, so the C "
+                                   "restatement of its algorithm runs"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from dmcbcs_project_gb300 import build as B
+
+    B.build()
+    from dmcbcs_project_gb300 import capi, configs
+
+    nup, ndn, norb, nwalk, dt, _ = configs.WORKLOADS[WORKLOAD]
+    nwalk = args.walkers or nwalk
+    sysd, rund, _ = configs.workload(WORKLOAD, nwalk=nwalk)
+    rund.seed = 17 + 1000003 * rank                     # independent replica per GPU
+    ctx = capi.Context(sysd, rund)
+    info = ctx.info
+    ctx.init_walkers()
+    ctx.initial_eval()
+    # warm-up generations
+    for _ in range(max(args.warmup, 3)):
+        ctx.timed_generations(1, opcomp_last=False, flush_l2=True)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    steps, dev_ms, kern_ms, launches, nsum = 0, 0.0, 0.0, 0, 0
+    for g in range(args.steps):
+        s, ms, nl = ctx.timed_generations(1, opcomp_last=(g == args.steps - 1), flush_l2=True)
+        steps += s
+        dev_ms += ms
+        launches += nl
+        kern_ms += ctx.last_step_ms()
+        nsum += s
+    barrier()
+    clocks = sampler.stop()
+    t_max = dev_ms
+    steps_all = steps
+    if world > 1:
+        t = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+        s_t = torch.tensor([steps], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(s_t)
+        steps_all = int(s_t.item())
+    value = steps_all / (t_max * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers --------------------
+    # the host owns the walker stacks (as the reference's Fortran host does)
+    # and hands the full walker state to the GPU for every generation
+    cap = info.capacity
+    n3 = 3 * info.npart
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    host = {k: pin((cap, info.npart, 3), torch.float64) for k in ("x", "dpsi", "dpsig")}
+    for k in ("psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0", "psigl0", "wt0"):
+        host[k] = pin((cap,), torch.float64)
+    host["is_"] = pin((cap,), torch.int32)
+    host["irn"] = pin((cap,), torch.int64)
+    host["cap"] = cap
+    n_cur = ctx.get_walkers_into(host)
+    per_walker = 3 * n3 * 8 + 10 * 8 + 8 + 4 + 8     # x, dpsi, dpsig, 10 doubles, wt0, is, irn
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    h2d = d2h = 0
+    barrier()
+    t0 = time.perf_counter()
+    for g in range(e2e_steps):
+        ctx.put_walkers(dict(host, n=n_cur))
+        h2d += n_cur * per_walker
+        ctx.generation(g == e2e_steps - 1)
+        n_new = ctx.get_walkers_into(host)
+        d2h += n_new * per_walker + 3 * info.nest * 8
+        ctx.estimators()
+        n_cur = n_new
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    e2e_total_steps = h2d // per_walker          # walkers entering each generation
+    e2e_rate = e2e_total_steps / t_e2e
+    if world > 1:
+        t = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        s_t = torch.tensor([e2e_total_steps], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(s_t)
+        e2e_rate = float(s_t.item()) / float(t.item())
+
+    # ---- roofline of the walker kernel ---------------------------------------
+    avg_n = nsum / max(args.steps, 1)
+    flops_alg = algorithmic_flops(info.nup, info.ndn, info.nd, info.ncol, info.npart)
+    flops_exe = executed_flops(info.nup, info.ndn, info.nd, info.ncol, info.npart, info.nk, info.nup * info.ndn)
+    kern_avg_ms = kern_ms / max(args.steps, 1)
+    achieved = flops_alg * avg_n / (kern_avg_ms * 1e-3) / 1e12
+    peak = fp64_peak_tflops(torch) if rank == 0 else None
+    roofline = {
+        "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "frac": (achieved / peak) if peak else None,
+        "traffic": (NCU_TRAFFIC_BYTES_PER_WALKER * avg_n) if NCU_TRAFFIC_BYTES_PER_WALKER else None,
+        "kernel": "walker_kernel", "kernel_ms_per_launch": kern_avg_ms, "walkers_per_launch": avg_n,
+        "algorithmic_flops_per_walker_step": flops_alg, "executed_flops_per_walker_step": flops_exe,
+        "executed_achieved": flops_exe * avg_n / (kern_avg_ms * 1e-3) / 1e12,
+        "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (the measured-peaks file has no FP64 figure)",
+    }
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            rate, st, gens, el = cpu_reference_rate(args.cpu_walkers, args.cpu_seconds, threads)
+            cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"{gens} DMC generations of {args.cpu_walkers} walkers of the same N=66 system "
+                             f"({st} walker-steps, {el:.1f} s) on {threads} host threads"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": t_max / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "gb300-fp64",
+            "config": {"workload": "dmc_n66_33u33d", "walkers": nwalk, "avg_walkers": avg_n, "idmc": 1,
+                       "dt_efg": dt, "shells": norb, "ncol": info.ncol, "nd": info.nd,
+                       "l2": "2xL2 buffer written between timed generations",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d / e2e_steps),
+                    "d2h_bytes_per_step": int(d2h / e2e_steps), "steps": e2e_steps,
+                    "path": "dmc_put_walkers + dmc_generation + dmc_get_walkers + dmc_get_estimators, pinned host"},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--walkers", type=int, default=None)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-walkers", type=int, default=512)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-walkers", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,300 @@
+"""ctypes binding of the C ABI in ``include/dmcbcs_gpu.h`` and a thin
+Python front end over it.
+
+This is plumbing for tests and the benchmark: every computation runs in the
+CUDA library ``libdmcbcs_gb300.so``.  There is no CPU fallback; loading
+fails loudly when the library has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import DMC_NEST_MAX, DMC_WTISTO, Info, RunDesc, SystemDesc, Walkers
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdmcbcs_gb300.so")
+
+# every entry point declared in include/dmcbcs_gpu.h
+EXPORTS = [
+    "dmc_abi_version", "dmc_status_string", "dmc_last_error", "dmc_create", "dmc_destroy", "dmc_get_info",
+    "dmc_get_table", "dmc_set_vorb", "dmc_hpsi_batch", "dmc_hpsi_device", "dmc_bcs_batch", "dmc_getphi_batch",
+    "dmc_matinv_batch", "dmc_bcsone_batch", "dmc_getphione_batch", "dmc_getderbcs_batch", "dmc_init_walkers",
+    "dmc_load_walkers", "dmc_get_walkers", "dmc_initial_eval", "dmc_num_walkers", "dmc_step", "dmc_branch",
+    "dmc_generation", "dmc_zero_estimators", "dmc_get_estimators", "dmc_block_update", "dmc_get_wtisto",
+    "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers",
+]
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+
+
+class DMCError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def _opt(arr):
+    return None if arr is None else arr.ctypes.data_as(C.c_void_p)
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (built by ``dmcbcs_project_gb300.build``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run __graft_entry__.build() (nvcc, sm_103a) first; "
+                          "there is no CPU fallback")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.dmc_abi_version.restype = C.c_int
+    L.dmc_status_string.restype = C.c_char_p
+    L.dmc_status_string.argtypes = [C.c_int]
+    L.dmc_last_error.restype = C.c_char_p
+    L.dmc_last_error.argtypes = [vp]
+    L.dmc_create.argtypes = [C.POINTER(SystemDesc), C.POINTER(RunDesc), C.POINTER(vp)]
+    L.dmc_destroy.argtypes = [vp]
+    L.dmc_get_info.argtypes = [vp, C.POINTER(Info)]
+    L.dmc_get_table.argtypes = [vp, C.c_int, _dp, C.c_int]
+    L.dmc_set_vorb.argtypes = [vp, _dp, C.c_int]
+    L.dmc_hpsi_batch.argtypes = [vp, C.c_int, _dp] + [vp] * 9
+    L.dmc_hpsi_device.argtypes = [vp, C.c_int, vp] + [vp] * 9 + [vp]
+    L.dmc_bcs_batch.argtypes = [vp, C.c_int, _dp] + [vp] * 5
+    L.dmc_getphi_batch.argtypes = [vp, C.c_int, _dp] + [vp] * 4
+    L.dmc_matinv_batch.argtypes = [vp, C.c_int, C.c_int, _dp, _dp, _ip]
+    L.dmc_bcsone_batch.argtypes = [vp, C.c_int, _dp, _dp, _ip, _dp, _dp]
+    L.dmc_getphione_batch.argtypes = [vp, C.c_int, _dp, _ip, _dp, _dp]
+    L.dmc_getderbcs_batch.argtypes = [vp, C.c_int, _dp, _dp]
+    L.dmc_init_walkers.argtypes = [vp]
+    L.dmc_load_walkers.argtypes = [vp, C.POINTER(Walkers)]
+    L.dmc_get_walkers.argtypes = [vp, C.POINTER(Walkers)]
+    L.dmc_initial_eval.argtypes = [vp, _dp]
+    L.dmc_num_walkers.argtypes = [vp, C.POINTER(C.c_int)]
+    L.dmc_step.argtypes = [vp, C.c_int]
+    L.dmc_branch.argtypes = [vp, C.c_double]
+    L.dmc_generation.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    L.dmc_zero_estimators.argtypes = [vp]
+    L.dmc_get_estimators.argtypes = [vp, _dp, _dp, _dp]
+    L.dmc_block_update.argtypes = [vp, _dp, _dp]
+    L.dmc_get_wtisto.argtypes = [vp, _lp]
+    L.dmc_last_step_ms.argtypes = [vp, C.POINTER(C.c_double)]
+    L.dmc_timed_generations.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    L.dmc_put_walkers.argtypes = [vp, C.POINTER(Walkers)]
+    _lib = L
+    return L
+
+
+class Context:
+    """One system and run on the current CUDA device (``dmc_create``)."""
+
+    def __init__(self, sysdesc, rundesc):
+        L = load()
+        h = C.c_void_p()
+        st = L.dmc_create(C.byref(sysdesc), C.byref(rundesc), C.byref(h))
+        if st != abi.DMC_OK:
+            raise DMCError(st, "dmc_create failed")
+        self._h = h
+        self.info = Info()
+        self._check(L.dmc_get_info(h, C.byref(self.info)))
+        self.npart = self.info.npart
+        self.nd = self.info.nd
+        self.nest = self.info.nest
+        self.norb = int(sysdesc.norb)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().dmc_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st):
+        if st != abi.DMC_OK:
+            msg = load().dmc_last_error(self._h)
+            raise DMCError(st, msg.decode() if msg else "")
+
+    # ---- set-up -----------------------------------------------------------
+    def table(self, which):
+        ntab = self.info.ntab
+        n = {0: 2, 1: 2, 2: 2, 3: 2}.get(which, 1) * (ntab + 1)
+        if which == 7:
+            n = 3 * self.info.nk
+        elif which == 8:
+            n = self.info.nk
+        elif which == 9:
+            n = self.norb
+        out = np.zeros(n)
+        self._check(load().dmc_get_table(self._h, which, out, n))
+        return out
+
+    def set_vorb(self, vorb):
+        v = np.ascontiguousarray(vorb, dtype=np.float64)
+        self._check(load().dmc_set_vorb(self._h, v, len(v)))
+
+    # ---- batched evaluation -------------------------------------------------
+    def _x(self, x):
+        return np.ascontiguousarray(x, dtype=np.float64).reshape(-1, self.npart, 3)
+
+    def hpsi(self, x):
+        x = self._x(x)
+        nw = x.shape[0]
+        o = dict(psil=np.zeros(nw), is_=np.zeros(nw, np.int32), dpsi=np.zeros((nw, self.npart, 3)),
+                 d2psi=np.zeros(nw), v=np.zeros(nw), vext=np.zeros(nw), psigl=np.zeros(nw),
+                 dpsig=np.zeros((nw, self.npart, 3)), d2psig=np.zeros(nw))
+        self._check(load().dmc_hpsi_batch(self._h, nw, x, *[_opt(o[k]) for k in
+                                          ("psil", "is_", "dpsi", "d2psi", "v", "vext", "psigl", "dpsig",
+                                           "d2psig")]))
+        return o
+
+    def bcs(self, x, want_inverse=False):
+        x = self._x(x)
+        nw = x.shape[0]
+        o = dict(phil=np.zeros(nw), is_=np.zeros(nw, np.int32), dphi=np.zeros((nw, self.npart, 3)),
+                 d2phi=np.zeros(nw), smati=np.zeros((nw, self.nd * self.nd)) if want_inverse else None)
+        self._check(load().dmc_bcs_batch(self._h, nw, x, _opt(o["phil"]), _opt(o["is_"]), _opt(o["dphi"]),
+                                         _opt(o["d2phi"]), _opt(o["smati"])))
+        return o
+
+    def getphi(self, x):
+        x = self._x(x)
+        nw = x.shape[0]
+        o = dict(u=np.zeros(nw), du=np.zeros((nw, self.npart, 3)), d2u=np.zeros(nw), v=np.zeros(nw))
+        self._check(load().dmc_getphi_batch(self._h, nw, x, _opt(o["u"]), _opt(o["du"]), _opt(o["d2u"]),
+                                            _opt(o["v"])))
+        return o
+
+    def matinv(self, a):
+        """Batched rmatinv on a[nb, n, n] (row, col); returns inverse, logdet, sign."""
+        a = np.asarray(a, dtype=np.float64)
+        nb, n = a.shape[0], a.shape[1]
+        f = np.array(np.transpose(a, (0, 2, 1)), dtype=np.float64, order="C").reshape(nb, n * n)   # column-major copy
+        d = np.zeros(nb)
+        s = np.zeros(nb, np.int32)
+        self._check(load().dmc_matinv_batch(self._h, n, nb, f, d, s))
+        return np.transpose(f.reshape(nb, n, n), (0, 2, 1)), d, s
+
+    # ---- population ----------------------------------------------------------
+    def init_walkers(self):
+        self._check(load().dmc_init_walkers(self._h))
+
+    def load_walkers(self, x, irn, weight=None, psil0=None, psigl0=None):
+        x = self._x(x)
+        n = x.shape[0]
+        irn = np.ascontiguousarray(irn, dtype=np.int64)
+        keep = [x, irn]
+        w = Walkers()
+        w.n = n
+        w.x = x.ctypes.data_as(C.POINTER(C.c_double))
+        w.irn = irn.ctypes.data_as(C.POINTER(C.c_int64))
+        for name, arr in (("weight", weight), ("psil0", psil0), ("psigl0", psigl0)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, dtype=np.float64)
+                keep.append(a)
+                setattr(w, name, a.ctypes.data_as(C.POINTER(C.c_double)))
+        self._check(load().dmc_load_walkers(self._h, C.byref(w)))
+
+    def num_walkers(self):
+        n = C.c_int()
+        self._check(load().dmc_num_walkers(self._h, C.byref(n)))
+        return n.value
+
+    def walkers(self):
+        n = self.num_walkers()
+        cap = max(n, 1)
+        arrs = {k: np.zeros((cap, self.npart, 3)) for k in ("x", "dpsi", "dpsig")}
+        for k in ("psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0", "psigl0", "wt0"):
+            arrs[k] = np.zeros(cap)
+        arrs["is_"] = np.zeros(cap, np.int32)
+        arrs["irn"] = np.zeros(cap, np.int64)
+        w = Walkers()
+        w.n = cap
+        for k, a in arrs.items():
+            ct = {np.dtype(np.float64): C.c_double, np.dtype(np.int32): C.c_int, np.dtype(np.int64): C.c_int64}[a.dtype]
+            setattr(w, k, a.ctypes.data_as(C.POINTER(ct)))
+        self._check(load().dmc_get_walkers(self._h, C.byref(w)))
+        out = {k: a[:n] for k, a in arrs.items()}
+        out["n"] = n
+        return out
+
+    def initial_eval(self):
+        s = np.zeros(11)
+        self._check(load().dmc_initial_eval(self._h, s))
+        return s[:9], s[9:11]
+
+    def step(self, opcomp):
+        self._check(load().dmc_step(self._h, int(bool(opcomp))))
+
+    def branch(self, factor):
+        self._check(load().dmc_branch(self._h, float(factor)))
+
+    def generation(self, opcomp):
+        nt = C.c_int()
+        self._check(load().dmc_generation(self._h, int(bool(opcomp)), C.byref(nt)))
+        return nt.value
+
+    def zero_estimators(self):
+        self._check(load().dmc_zero_estimators(self._h))
+
+    def estimators(self):
+        a, b, c = np.zeros(self.nest), np.zeros(self.nest), np.zeros(self.nest)
+        self._check(load().dmc_get_estimators(self._h, a, b, c))
+        return a, b, c
+
+    def block_update(self):
+        a, b = np.zeros(self.nest), np.zeros(self.nest)
+        self._check(load().dmc_block_update(self._h, a, b))
+        return a, b
+
+    def wtisto(self):
+        h = np.zeros(DMC_WTISTO, np.int64)
+        self._check(load().dmc_get_wtisto(self._h, h))
+        return h
+
+    def timed_generations(self, ngen, opcomp_last=True, flush_l2=True):
+        """Run ngen generations; returns (walker_steps, device_ms, kernel_launches)."""
+        st, ms, nl = C.c_int64(), C.c_double(), C.c_int64()
+        self._check(load().dmc_timed_generations(self._h, int(ngen), int(bool(opcomp_last)), int(bool(flush_l2)),
+                                                 C.byref(st), C.byref(ms), C.byref(nl)))
+        return st.value, ms.value, nl.value
+
+    def walker_struct(self, arrs):
+        """dmc_walkers view of a dict of arrays (as returned by walkers())."""
+        w = Walkers()
+        w.n = int(arrs["n"])
+        for k in ("x", "dpsi", "dpsig", "psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0",
+                  "psigl0", "wt0"):
+            setattr(w, k, arrs[k].ctypes.data_as(C.POINTER(C.c_double)))
+        w.is_ = arrs["is_"].ctypes.data_as(C.POINTER(C.c_int))
+        w.irn = arrs["irn"].ctypes.data_as(C.POINTER(C.c_int64))
+        return w
+
+    def put_walkers(self, arrs):
+        self._check(load().dmc_put_walkers(self._h, C.byref(self.walker_struct(arrs))))
+
+    def get_walkers_into(self, arrs):
+        """dmc_get_walkers into caller-owned arrays (capacity arrs['cap']); returns n."""
+        w = self.walker_struct(dict(arrs, n=arrs["cap"]))
+        self._check(load().dmc_get_walkers(self._h, C.byref(w)))
+        return w.n
+
+    def last_step_ms(self):
+        ms = C.c_double()
+        self._check(load().dmc_last_step_ms(self._h, C.byref(ms)))
+        return ms.value
+
+
+__all__ = ["Context", "DMCError", "load", "EXPORTS", "LIB_PATH", "DMC_NEST_MAX"]

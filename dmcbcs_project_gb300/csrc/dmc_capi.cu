@@ -1,0 +1,946 @@
+// C ABI of the GB300 DMCBS walker path: contexts, device buffers, walker
+// stacks and the generation driver (dmcbcs.f90:426-449 for one process).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dmcbcs_gpu.h"
+#include "dmc_device.cuh"
+#include "dmc_kernels.h"
+#include "dmc_setup.h"
+
+namespace dmc {
+cudaError_t launch_matinv(const double* a_colmajor, double* inv_colmajor, double* detl, int* is, int n, int nb,
+                          cudaStream_t st);
+cudaError_t launch_reverse(const DevStack& in, const DevStack& out, int n, int n3, cudaStream_t st);
+}  // namespace dmc
+
+using namespace dmc;
+
+namespace {
+
+constexpr unsigned long long kMask48 = (1ull << 48) - 1ull;
+constexpr unsigned long long kMult1 = 44485709377909ull, kAdd1 = 96309754297ull;
+constexpr unsigned long long kMult2 = 34522712143931ull, kAdd2 = 55789347517ull;
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t cnt)
+    {
+        if (cnt <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(cnt, 1) * sizeof(T));
+        if (e == cudaSuccess) n = cnt;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct StackBufs {
+    DevBuf<double> x, dpsi, dpsig, psil, psigl, d2psi, d2psig, v, vext, weight, psil0, psigl0;
+    DevBuf<float> wt0;
+    DevBuf<int> is;
+    DevBuf<unsigned long long> irn;
+    cudaError_t alloc(int cap, int n3)
+    {
+        cudaError_t e = cudaSuccess;
+        auto A = [&](cudaError_t r) {
+            if (e == cudaSuccess) e = r;
+        };
+        A(x.alloc((size_t)cap * n3));
+        A(dpsi.alloc((size_t)cap * n3));
+        A(dpsig.alloc((size_t)cap * n3));
+        A(psil.alloc(cap));
+        A(psigl.alloc(cap));
+        A(d2psi.alloc(cap));
+        A(d2psig.alloc(cap));
+        A(v.alloc(cap));
+        A(vext.alloc(cap));
+        A(weight.alloc(cap));
+        A(psil0.alloc(cap));
+        A(psigl0.alloc(cap));
+        A(wt0.alloc(cap));
+        A(is.alloc(cap));
+        A(irn.alloc(cap));
+        return e;
+    }
+    void release()
+    {
+        x.release(); dpsi.release(); dpsig.release(); psil.release(); psigl.release(); d2psi.release();
+        d2psig.release(); v.release(); vext.release(); weight.release(); psil0.release(); psigl0.release();
+        wt0.release(); is.release(); irn.release();
+    }
+    DevStack view()
+    {
+        DevStack s;
+        s.x = x.p; s.dpsi = dpsi.p; s.dpsig = dpsig.p; s.psil = psil.p; s.psigl = psigl.p; s.d2psi = d2psi.p;
+        s.d2psig = d2psig.p; s.v = v.p; s.vext = vext.p; s.weight = weight.p; s.psil0 = psil0.p;
+        s.psigl0 = psigl0.p; s.wt0 = wt0.p; s.is = is.p; s.irn = irn.p;
+        return s;
+    }
+};
+
+}  // namespace
+
+struct dmc_ctx {
+    Setup S;
+    dmc_system_desc sd;
+    dmc_run_desc rd;
+    DevParams P;
+    SmemLayout L;
+    int device = 0, nsm = 0, grid = 0, cap = 0, n3 = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    // tables
+    DevBuf<KVecDev> kv;
+    DevBuf<TabUD> tud;
+    DevBuf<TabSS> tss;
+    DevBuf<unsigned long long> jumpA, jumpC;
+    DevBuf<double> gscratch;
+    // population
+    StackBufs st[2];
+    int istin = 0;
+    int n = 0;
+    DevBuf<double> est;
+    DevBuf<int> counts, offs, status;
+    DevBuf<unsigned long long> irn1, wtisto;
+    DevBuf<double> vb, vb2, wb;
+    // batch staging
+    DevBuf<double> bx, bpsil, bdpsi, bd2psi, bv, bvext, bpsigl, bdpsig, bd2psig, bsinv;
+    DevBuf<int> bis;
+    DevBuf<unsigned char> flush;
+    int64_t launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(dmc_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(dmc_ctx* c, cudaError_t e, const char* where)
+{
+    return fail(c, DMC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr)                                              \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) return cuda_fail(c, _e, #expr); \
+    } while (0)
+
+int nest_for(int idmc)
+{
+    switch (idmc) {
+    case -1: case 0: return 6;
+    case -2: case 1: return 14;
+    case 2: return 13;
+    }
+    return -1;
+}
+
+void fill_params(dmc_ctx* c)
+{
+    const Setup& S = c->S;
+    DevParams& p = c->P;
+    std::memset(&p, 0, sizeof p);
+    p.npart = S.npart; p.nup = S.nup; p.ndn = S.ndn; p.npair = S.npair; p.nexup = S.nexup; p.nexdn = S.nexdn;
+    p.nd = S.nd; p.nk = S.nk; p.ncol = S.ncol; p.norb = S.norb; p.ntab = S.ntab; p.nmax = S.nmax;
+    p.ieq = S.ieq; p.nobeta = S.nobeta; p.cutdrift = S.cutdrift; p.fn = c->rd.fn; p.idmc = c->rd.idmc;
+    p.onebody = (S.v0ex != 0.0 || S.v0exjas != 0.0);
+    p.nest = nest_for(c->rd.idmc);
+    p.nrand = 2 * ((3 * S.npart + 1) / 2);
+    p.ldS = S.nd | 1;
+    p.ldU = S.ncol | 1;
+    p.el = S.el; p.eli = S.eli; p.range = S.range; p.scale = S.scale; p.rangeb = S.rangeb; p.scaleb = S.scaleb;
+    for (int s = 0; s < 2; ++s) {
+        p.mass[s] = S.mass[s];
+        p.sqm[s] = S.sqm[s];
+        p.imass[s] = 1.0 / S.mass[s];
+        p.isqm[s] = 1.0 / S.sqm[s];
+        p.sigma[s] = S.sigma[s];
+        p.dcut[s] = S.dcut[s];
+    }
+    p.hbar = S.hbar; p.a2 = S.a2; p.dt = c->rd.dt; p.etrial = S.etrial; p.wtcut = c->rd.wtcut; p.nfac = S.nfac;
+    for (int k = 0; k < 3; ++k) p.qex[k] = S.qex[k];
+    p.v0ex = S.v0ex; p.v0exjas = S.v0exjas; p.vorb1 = S.vorb[0];
+    for (int i = 0; i < DMC_MAX_UNPAIRED; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            p.akup[i][k] = S.akup[i][k];
+            p.akdn[i][k] = S.akdn[i][k];
+        }
+        p.ak2up[i] = S.ak2up[i]; p.ak2dn[i] = S.ak2dn[i]; p.sinup[i] = S.sinup[i]; p.sindn[i] = S.sindn[i];
+    }
+}
+
+int upload_kv(dmc_ctx* c)
+{
+    std::vector<KVecDev> kv(c->S.nk);
+    for (int q = 0; q < c->S.nk; ++q) {
+        const KVec& K = c->S.kv[q];
+        KVecDev& d = kv[q];
+        std::memset(&d, 0, sizeof d);
+        for (int k = 0; k < 3; ++k) {
+            d.k[k] = K.k[k];
+            d.n[k] = K.n[k];
+        }
+        d.k2 = K.k2;
+        d.v = q == 0 ? c->S.vorb[0] : 2.0 * c->S.vorb[K.shell - 1];
+    }
+    CK(c->kv.alloc(kv.size()));
+    CK(cudaMemcpy(c->kv.p, kv.data(), kv.size() * sizeof(KVecDev), cudaMemcpyHostToDevice));
+    c->P.vorb1 = c->S.vorb[0];
+    return DMC_OK;
+}
+
+int upload_tables(dmc_ctx* c)
+{
+    const Setup& S = c->S;
+    const int nt = S.ntab + 1;
+    std::vector<TabUD> ud(nt);
+    std::vector<TabSS> ss(nt);
+    for (int i = 0; i < nt; ++i) {
+        ud[i] = TabUD{S.vtab[0][i], S.utab[0][i], S.dutab[0][i], S.d2utab[0][i], S.btab[i], S.dbtab[i], S.d2btab[i], 0.0};
+        ss[i] = TabSS{S.vtab[1][i], S.utab[1][i], S.dutab[1][i], S.d2utab[1][i]};
+    }
+    CK(c->tud.alloc(nt));
+    CK(c->tss.alloc(nt));
+    CK(cudaMemcpy(c->tud.p, ud.data(), nt * sizeof(TabUD), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->tss.p, ss.data(), nt * sizeof(TabSS), cudaMemcpyHostToDevice));
+    // LCG jump tables for t = 0..nrand+1 steps of ran1
+    const int nj = c->P.nrand + 2;
+    std::vector<unsigned long long> A(nj), C(nj);
+    A[0] = 1;
+    C[0] = 0;
+    for (int t = 1; t < nj; ++t) {
+        A[t] = (A[t - 1] * kMult1) & kMask48;
+        C[t] = (C[t - 1] * kMult1 + kAdd1) & kMask48;
+    }
+    CK(c->jumpA.alloc(nj));
+    CK(c->jumpC.alloc(nj));
+    CK(cudaMemcpy(c->jumpA.p, A.data(), nj * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->jumpC.p, C.data(), nj * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    return DMC_OK;
+}
+
+KernelArgs base_args(dmc_ctx* c)
+{
+    KernelArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.kv = c->kv.p;
+    a.tud = c->tud.p;
+    a.tss = c->tss.p;
+    a.jumpA = c->jumpA.p;
+    a.jumpC = c->jumpC.p;
+    a.gscratch = c->gscratch.p;
+    a.status = c->status.p;
+    return a;
+}
+
+int grid_for(dmc_ctx* c, int nw) { return std::max(1, std::min(nw, c->grid)); }
+
+int run_eval(dmc_ctx* c, int mode, int nw, const double* dx, double* psil, int* is, double* dpsi, double* d2psi,
+             double* v, double* vext, double* psigl, double* dpsig, double* d2psig, double* sinv, cudaStream_t st)
+{
+    if (nw <= 0) return DMC_OK;
+    KernelArgs a = base_args(c);
+    a.mode = mode;
+    a.nw = nw;
+    a.xin = dx;
+    a.o_psil = psil; a.o_is = is; a.o_dpsi = dpsi; a.o_d2psi = d2psi; a.o_v = v; a.o_vext = vext;
+    a.o_psigl = psigl; a.o_dpsig = dpsig; a.o_d2psig = d2psig; a.o_sinv = sinv;
+    CK(launch_walker(c->P, a, c->L, grid_for(c, nw), st));
+    return DMC_OK;
+}
+
+// host-staged batch evaluation: copy x in, run, copy requested outputs out
+int batch_eval(dmc_ctx* c, int mode, int nw, const double* x, double* psil, int* is, double* dpsi, double* d2psi,
+               double* v, double* vext, double* psigl, double* dpsig, double* d2psig, double* sinv)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (nw < 0 || (nw > 0 && !x)) return fail(c, DMC_ERR_INVALID, "bad batch arguments");
+    if (nw == 0) return DMC_OK;
+    const size_t n3 = (size_t)c->n3, nd2 = (size_t)c->S.nd * c->S.nd;
+    CK(c->bx.alloc(nw * n3));
+    if (psil) CK(c->bpsil.alloc(nw));
+    if (is) CK(c->bis.alloc(nw));
+    if (dpsi) CK(c->bdpsi.alloc(nw * n3));
+    if (d2psi) CK(c->bd2psi.alloc(nw));
+    if (v) CK(c->bv.alloc(nw));
+    if (vext) CK(c->bvext.alloc(nw));
+    if (psigl) CK(c->bpsigl.alloc(nw));
+    if (dpsig) CK(c->bdpsig.alloc(nw * n3));
+    if (d2psig) CK(c->bd2psig.alloc(nw));
+    if (sinv) CK(c->bsinv.alloc(nw * nd2));
+    CK(cudaMemcpyAsync(c->bx.p, x, nw * n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = run_eval(c, mode, nw, c->bx.p, psil ? c->bpsil.p : nullptr, is ? c->bis.p : nullptr,
+                      dpsi ? c->bdpsi.p : nullptr, d2psi ? c->bd2psi.p : nullptr, v ? c->bv.p : nullptr,
+                      vext ? c->bvext.p : nullptr, psigl ? c->bpsigl.p : nullptr, dpsig ? c->bdpsig.p : nullptr,
+                      d2psig ? c->bd2psig.p : nullptr, sinv ? c->bsinv.p : nullptr, c->stream);
+    if (rc) return rc;
+    auto D2H = [&](void* h, const void* d, size_t bytes) {
+        return cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, c->stream);
+    };
+    if (psil) CK(D2H(psil, c->bpsil.p, nw * sizeof(double)));
+    if (is) CK(D2H(is, c->bis.p, nw * sizeof(int)));
+    if (dpsi) CK(D2H(dpsi, c->bdpsi.p, nw * n3 * sizeof(double)));
+    if (d2psi) CK(D2H(d2psi, c->bd2psi.p, nw * sizeof(double)));
+    if (v) CK(D2H(v, c->bv.p, nw * sizeof(double)));
+    if (vext) CK(D2H(vext, c->bvext.p, nw * sizeof(double)));
+    if (psigl) CK(D2H(psigl, c->bpsigl.p, nw * sizeof(double)));
+    if (dpsig) CK(D2H(dpsig, c->bdpsig.p, nw * n3 * sizeof(double)));
+    if (d2psig) CK(D2H(d2psig, c->bd2psig.p, nw * sizeof(double)));
+    if (sinv) CK(D2H(sinv, c->bsinv.p, nw * nd2 * sizeof(double)));
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmc_abi_version(void) { return DMC_ABI_VERSION; }
+
+const char* dmc_status_string(int s)
+{
+    switch (s) {
+    case DMC_OK: return "ok";
+    case DMC_ERR_INVALID: return "invalid argument";
+    case DMC_ERR_CUDA: return "CUDA error";
+    case DMC_ERR_UNSUPPORTED: return "unsupported";
+    case DMC_ERR_OVERFLOW: return "walker stack overflow";
+    case DMC_ERR_SETUP: return "table set-up failed";
+    case DMC_ERR_EMPTY: return "population died out";
+    case DMC_ERR_NOMEM: return "out of memory";
+    }
+    return "unknown status";
+}
+
+const char* dmc_last_error(const dmc_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
+{
+    if (!sd || !rd || !out) return DMC_ERR_INVALID;
+    *out = nullptr;
+    dmc_ctx* c = new (std::nothrow) dmc_ctx();
+    if (!c) return DMC_ERR_NOMEM;
+    c->sd = *sd;
+    c->rd = *rd;
+    if (nest_for(rd->idmc) < 0) {
+        int r = rd->idmc == 10 ? DMC_ERR_UNSUPPORTED : DMC_ERR_INVALID;
+        delete c;
+        return r;
+    }
+    if (rd->nwalk < 1 || !(rd->dt > 0.0)) {
+        delete c;
+        return DMC_ERR_INVALID;
+    }
+    int rc = c->S.build(*sd, *rd, c->err);
+    if (rc != DMC_OK) {
+        delete c;
+        return rc;
+    }
+    fill_params(c);
+    c->n3 = 3 * c->S.npart;
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
+    int optin = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e != cudaSuccess) {
+        dmc_destroy(c);
+        return DMC_ERR_CUDA;
+    }
+    // on-chip layout; two walker CTAs per SM when they fit
+    const int limit = std::min(optin, 227 * 1024) - 64;
+    walker_smem_bytes(c->P, limit, &c->L);
+    int per_sm = 1;
+    {
+        int regs_ok = 2;   // launch bounds give <= 128 registers at 256 threads
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+        const int need = c->L.total * 8 + 1024;
+        per_sm = std::max(1, std::min(regs_ok, smem_sm / need));
+    }
+    c->grid = c->nsm * per_sm;
+    if (!c->L.pb_in_smem) {
+        e = c->gscratch.alloc((size_t)c->grid * c->L.pb_size);
+        if (e != cudaSuccess) {
+            dmc_destroy(c);
+            return DMC_ERR_NOMEM;
+        }
+    }
+    const double stmax = rd->stmax > 0.0 ? rd->stmax : 10.0;
+    c->cap = std::max(1, (int)(rd->nwalk * stmax));
+    if (upload_kv(c) || upload_tables(c)) {
+        dmc_destroy(c);
+        return DMC_ERR_CUDA;
+    }
+    const int nest = c->P.nest;
+    if (c->st[0].alloc(c->cap, c->n3) || c->st[1].alloc(c->cap, c->n3) || c->est.alloc((size_t)c->cap * nest * 2) ||
+        c->counts.alloc(c->cap) || c->offs.alloc(c->cap + 1) || c->irn1.alloc(c->cap) ||
+        c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(DMC_NEST_MAX) || c->vb2.alloc(DMC_NEST_MAX) ||
+        c->wb.alloc(DMC_NEST_MAX) || c->status.alloc(1)) {
+        dmc_destroy(c);
+        return DMC_ERR_NOMEM;
+    }
+    cudaMemset(c->wtisto.p, 0, DMC_WTISTO * sizeof(unsigned long long));
+    cudaMemset(c->vb.p, 0, DMC_NEST_MAX * sizeof(double));
+    cudaMemset(c->vb2.p, 0, DMC_NEST_MAX * sizeof(double));
+    cudaMemset(c->wb.p, 0, DMC_NEST_MAX * sizeof(double));
+    cudaMemset(c->status.p, 0, sizeof(int));
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        dmc_destroy(c);
+        return DMC_ERR_CUDA;
+    }
+    *out = c;
+    return DMC_OK;
+}
+
+int dmc_destroy(dmc_ctx* c)
+{
+    if (!c) return DMC_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->kv.release(); c->tud.release(); c->tss.release(); c->jumpA.release(); c->jumpC.release();
+    c->gscratch.release(); c->st[0].release(); c->st[1].release(); c->est.release(); c->counts.release();
+    c->offs.release(); c->status.release(); c->irn1.release(); c->wtisto.release(); c->vb.release();
+    c->vb2.release(); c->wb.release(); c->bx.release(); c->bpsil.release(); c->bdpsi.release();
+    c->bd2psi.release(); c->bv.release(); c->bvext.release(); c->bpsigl.release(); c->bdpsig.release();
+    c->bd2psig.release(); c->bsinv.release(); c->bis.release(); c->flush.release();
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return DMC_OK;
+}
+
+int dmc_get_info(const dmc_ctx* c, dmc_info* o)
+{
+    if (!c || !o) return DMC_ERR_INVALID;
+    std::memset(o, 0, sizeof *o);
+    const Setup& S = c->S;
+    o->npart = S.npart; o->nup = S.nup; o->ndn = S.ndn; o->npair = S.npair; o->nexup = S.nexup;
+    o->nexdn = S.nexdn; o->nd = S.nd; o->nk = S.nk; o->ncol = S.ncol; o->ntab = S.ntab; o->capacity = c->cap;
+    o->nest = c->P.nest; o->el = S.el; o->eunit = S.eunit; o->nfac = S.nfac; o->etrial = S.etrial;
+    o->sigma[0] = S.sigma[0]; o->sigma[1] = S.sigma[1];
+    size_t bytes = 0;
+    bytes += 2 * ((size_t)c->cap * (3 * c->n3 + 12) * 8 + (size_t)c->cap * 16);
+    bytes += (size_t)(S.ntab + 1) * (sizeof(TabUD) + sizeof(TabSS));
+    bytes += c->gscratch.n * 8 + c->est.n * 8;
+    o->device_bytes = (int64_t)bytes;
+    return DMC_OK;
+}
+
+int dmc_get_table(const dmc_ctx* c, int which, double* out, int n)
+{
+    if (!c || !out) return DMC_ERR_INVALID;
+    const Setup& S = c->S;
+    const int nt = S.ntab + 1;
+    auto two = [&](const std::vector<double>* t) {
+        if (n < 2 * nt) return DMC_ERR_INVALID;
+        for (int ic = 0; ic < 2; ++ic) std::memcpy(out + ic * nt, t[ic].data(), nt * sizeof(double));
+        return DMC_OK;
+    };
+    auto one = [&](const std::vector<double>& t) {
+        if (n < nt) return DMC_ERR_INVALID;
+        std::memcpy(out, t.data(), nt * sizeof(double));
+        return DMC_OK;
+    };
+    switch (which) {
+    case 0: return two(S.utab);
+    case 1: return two(S.dutab);
+    case 2: return two(S.d2utab);
+    case 3: return two(S.vtab);
+    case 4: return one(S.btab);
+    case 5: return one(S.dbtab);
+    case 6: return one(S.d2btab);
+    case 7:
+        if (n < 3 * S.nk) return DMC_ERR_INVALID;
+        for (int q = 0; q < S.nk; ++q)
+            for (int k = 0; k < 3; ++k) out[3 * q + k] = S.kv[q].k[k];
+        return DMC_OK;
+    case 8:
+        if (n < S.nk) return DMC_ERR_INVALID;
+        for (int q = 0; q < S.nk; ++q) out[q] = S.kv[q].k2;
+        return DMC_OK;
+    case 9:
+        if (n < S.norb) return DMC_ERR_INVALID;
+        for (int q = 0; q < S.norb; ++q) out[q] = S.numsh[q];
+        return DMC_OK;
+    }
+    return DMC_ERR_INVALID;
+}
+
+int dmc_set_vorb(dmc_ctx* c, const double* vorb, int norb)
+{
+    if (!c || !vorb) return DMC_ERR_INVALID;
+    int rc = c->S.set_vorb(vorb, norb, c->err);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return upload_kv(c);
+}
+
+int dmc_hpsi_batch(dmc_ctx* c, int nw, const double* x, double* psil, int* is, double* dpsi, double* d2psi,
+                   double* v, double* vext, double* psigl, double* dpsig, double* d2psig)
+{
+    return batch_eval(c, MODE_HPSI, nw, x, psil, is, dpsi, d2psi, v, vext, psigl, dpsig, d2psig, nullptr);
+}
+
+int dmc_hpsi_device(dmc_ctx* c, int nw, const double* x, double* psil, int* is, double* dpsi, double* d2psi,
+                    double* v, double* vext, double* psigl, double* dpsig, double* d2psig, void* stream)
+{
+    if (!c || nw < 0 || (nw > 0 && !x)) return DMC_ERR_INVALID;
+    return run_eval(c, MODE_HPSI, nw, x, psil, is, dpsi, d2psi, v, vext, psigl, dpsig, d2psig, nullptr,
+                    (cudaStream_t)stream);
+}
+
+int dmc_bcs_batch(dmc_ctx* c, int nw, const double* x, double* phil, int* is, double* dphi, double* d2phi,
+                  double* smati)
+{
+    return batch_eval(c, MODE_BCS, nw, x, phil, is, dphi, d2phi, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      smati);
+}
+
+int dmc_getphi_batch(dmc_ctx* c, int nw, const double* x, double* u, double* du, double* d2u, double* v)
+{
+    return batch_eval(c, MODE_GETPHI, nw, x, u, nullptr, du, d2u, v, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+int dmc_matinv_batch(dmc_ctx* c, int n, int nb, double* a, double* detl, int* is)
+{
+    if (!c || n < 1 || n > 2 * DMC_MAX_PART || nb < 0 || (nb > 0 && (!a || !detl || !is)))
+        return fail(c, DMC_ERR_INVALID, "bad matinv arguments");
+    if (nb == 0) return DMC_OK;
+    const size_t n2 = (size_t)n * n;
+    DevBuf<double> da, dd;
+    DevBuf<int> di;
+    CK(da.alloc(nb * n2));
+    CK(dd.alloc(nb));
+    CK(di.alloc(nb));
+    CK(cudaMemcpyAsync(da.p, a, nb * n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    cudaError_t e = launch_matinv(da.p, da.p, dd.p, di.p, n, nb, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(a, da.p, nb * n2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(detl, dd.p, nb * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(is, di.p, nb * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    da.release();
+    dd.release();
+    di.release();
+    if (e != cudaSuccess) return cuda_fail(c, e, "matinv");
+    return DMC_OK;
+}
+
+// ---- walker population ----------------------------------------------------
+
+int dmc_init_walkers(dmc_ctx* c)
+{
+    if (!c) return DMC_ERR_INVALID;
+    const int np = c->S.npart, n3 = c->n3, nw = c->rd.nwalk;
+    if (nw > c->cap) return fail(c, DMC_ERR_OVERFLOW, "nwalk exceeds the stack capacity");
+    // dmcbcs.f90:238-282: one random configuration, then each walker is the
+    // previous one with npart random transpositions; the walker stream seeds
+    // follow one ran2 chain from the input seed.
+    unsigned long long gs = (unsigned long long)c->rd.seed & kMask48;
+    unsigned long long chain = (unsigned long long)c->rd.seed;
+    auto ran1 = [&](unsigned long long& s) {
+        s = (kMult1 * (s & kMask48) + kAdd1) & kMask48;
+        return (double)(s | 1ull) * (1.0 / 281474976710656.0);
+    };
+    std::vector<double> x(n3), X((size_t)nw * n3), W(nw, 1.0), Z(nw, 0.0);
+    std::vector<unsigned long long> irn(nw);
+    for (int k = 0; k < n3; ++k) x[k] = c->S.el * (ran1(gs) - 0.5);
+    for (int w = 0; w < nw; ++w) {
+        for (int i = 0; i < np; ++i) {
+            const double r = ran1(gs);
+            const int j = (int)(np * r + 1) - 1;
+            for (int k = 0; k < 3; ++k) std::swap(x[3 * i + k], x[3 * j + k]);
+        }
+        std::memcpy(&X[(size_t)w * n3], x.data(), n3 * sizeof(double));
+        chain = (kMult2 * (chain & kMask48) + kAdd2) & kMask48;   // ran2 on the walker seed
+        irn[w] = chain;
+    }
+    StackBufs& s = c->st[c->istin];
+    CK(cudaMemcpy(s.x.p, X.data(), X.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.weight.p, W.data(), nw * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.psil0.p, Z.data(), nw * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.psigl0.p, Z.data(), nw * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.irn.p, irn.data(), nw * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    c->n = nw;
+    return DMC_OK;
+}
+
+int dmc_load_walkers(dmc_ctx* c, const dmc_walkers* w)
+{
+    if (!c || !w || w->n < 0 || (w->n > 0 && (!w->x || !w->irn))) return DMC_ERR_INVALID;
+    const int n = w->n;
+    if (n > c->cap) return fail(c, DMC_ERR_OVERFLOW, "more walkers than the stack capacity");
+    StackBufs& s = c->st[c->istin];
+    std::vector<double> ones(n, 1.0), zeros(n, 0.0);
+    CK(cudaMemcpy(s.x.p, w->x, (size_t)n * c->n3 * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.weight.p, w->weight ? w->weight : ones.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.psil0.p, w->psil0 ? w->psil0 : zeros.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.psigl0.p, w->psigl0 ? w->psigl0 : zeros.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<unsigned long long> irn(n);
+    for (int k = 0; k < n; ++k) irn[k] = (unsigned long long)w->irn[k];
+    CK(cudaMemcpy(s.irn.p, irn.data(), n * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    c->n = n;
+    return DMC_OK;
+}
+
+int dmc_num_walkers(dmc_ctx* c, int* n)
+{
+    if (!c || !n) return DMC_ERR_INVALID;
+    *n = c->n;
+    return DMC_OK;
+}
+
+int dmc_get_walkers(dmc_ctx* c, dmc_walkers* w)
+{
+    if (!c || !w) return DMC_ERR_INVALID;
+    if (w->n < c->n) {
+        w->n = c->n;
+        return fail(c, DMC_ERR_INVALID, "walker arrays too small");
+    }
+    const int n = c->n;
+    const size_t n3 = (size_t)c->n3;
+    StackBufs& s = c->st[c->istin];
+    CK(cudaStreamSynchronize(c->stream));
+    auto D = [&](void* h, const void* d, size_t bytes) {
+        return h ? cudaMemcpy(h, d, bytes, cudaMemcpyDeviceToHost) : cudaSuccess;
+    };
+    CK(D(w->x, s.x.p, n * n3 * 8));
+    CK(D(w->dpsi, s.dpsi.p, n * n3 * 8));
+    CK(D(w->dpsig, s.dpsig.p, n * n3 * 8));
+    CK(D(w->psil, s.psil.p, n * 8));
+    CK(D(w->psigl, s.psigl.p, n * 8));
+    CK(D(w->d2psi, s.d2psi.p, n * 8));
+    CK(D(w->d2psig, s.d2psig.p, n * 8));
+    CK(D(w->v, s.v.p, n * 8));
+    CK(D(w->vext, s.vext.p, n * 8));
+    CK(D(w->weight, s.weight.p, n * 8));
+    CK(D(w->psil0, s.psil0.p, n * 8));
+    CK(D(w->psigl0, s.psigl0.p, n * 8));
+    CK(D(w->is, s.is.p, n * sizeof(int)));
+    if (w->irn) {
+        std::vector<unsigned long long> t(n);
+        CK(cudaMemcpy(t.data(), s.irn.p, n * 8, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < n; ++k) w->irn[k] = (int64_t)t[k];
+    }
+    if (w->wt0) {
+        std::vector<float> t(n);
+        CK(cudaMemcpy(t.data(), s.wt0.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < n; ++k) w->wt0[k] = t[k];
+    }
+    w->n = n;
+    return DMC_OK;
+}
+
+static int reverse_stacks(dmc_ctx* c)
+{
+    CK(launch_reverse(c->st[c->istin].view(), c->st[1 - c->istin].view(), c->n, c->n3, c->stream));
+    c->istin = 1 - c->istin;
+    return DMC_OK;
+}
+
+int dmc_initial_eval(dmc_ctx* c, double* sums)
+{
+    if (!c) return DMC_ERR_INVALID;
+    const int n = c->n;
+    StackBufs& s = c->st[c->istin];
+    int rc = run_eval(c, MODE_HPSI, n, s.x.p, s.psil.p, s.is.p, s.dpsi.p, s.d2psi.p, s.v.p, s.vext.p, s.psigl.p,
+                      s.dpsig.p, s.d2psig.p, nullptr, c->stream);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<double> psil(n), psigl(n), d2psi(n), d2psig(n), v(n), w(n, 1.0);
+    std::vector<int> is(n);
+    std::vector<float> wt0(n);
+    CK(cudaMemcpy(psil.data(), s.psil.p, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(psigl.data(), s.psigl.p, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(d2psi.data(), s.d2psi.p, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(d2psig.data(), s.d2psig.p, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(v.data(), s.v.p, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(is.data(), s.is.p, n * sizeof(int), cudaMemcpyDeviceToHost));
+    // dmcbcs.f90:316-345 in pop order (top of the stack first)
+    const double hb = c->S.hbar, eu = c->S.eunit, np = c->S.npart;
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, (double)n, 0};
+    double e1[3] = {0, 0, 0};
+    const bool dmc = c->rd.idmc != -1 && c->rd.idmc != 0;
+    for (int k = 0; k < n; ++k) {
+        const int j = n - 1 - k;
+        const double el = (-hb * d2psi[j] + v[j]) / eu / np;
+        a[0] += el;
+        a[1] += el * el;
+        a[2] += std::exp(2.0 * psil[j]);
+        a[3] += std::exp(4.0 * psil[j]);
+        a[4] += std::exp(2.0 * psigl[j]);
+        a[5] += std::exp(4.0 * psigl[j]);
+        a[6] += 1.0 * is[j];
+        a[8] += 1.0;
+        wt0[j] = (float)is[j];
+        if (dmc) {
+            const double wt = std::exp(-(-hb * d2psig[j] + v[j] - c->S.etrial) * c->rd.dt);
+            e1[0] += el * wt;
+            e1[1] += el * el * wt;
+            e1[2] += wt;
+        }
+    }
+    CK(cudaMemcpy(s.weight.p, w.data(), n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.wt0.p, wt0.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    if (sums) {
+        std::memcpy(sums, a, sizeof a);
+        if (dmc && e1[2] != 0.0) {
+            const double vn = e1[0] / e1[2], v2 = e1[1] / e1[2];
+            sums[9] = vn;
+            sums[10] = std::sqrt(std::fabs(v2 - vn * vn) / e1[2]);
+        } else {
+            sums[9] = sums[10] = 0.0;
+        }
+    }
+    // the initial pass pops every walker once; at tau = 0 a DMC run pops
+    // them once more for the operators (dmcbcs.f90:385-392)
+    rc = reverse_stacks(c);
+    if (rc) return rc;
+    if (dmc) {
+        rc = reverse_stacks(c);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(c->vb.p, 0, DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->vb2.p, 0, DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->wb.p, 0, DMC_NEST_MAX * 8, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
+int dmc_step(dmc_ctx* c, int opcomp)
+{
+    if (!c) return DMC_ERR_INVALID;
+    const int n = c->n;
+    if (n == 0) return fail(c, DMC_ERR_EMPTY, "no walkers");
+    KernelArgs a = base_args(c);
+    a.mode = MODE_STEP;
+    a.nw = n;
+    a.opcomp = opcomp ? 1 : 0;
+    a.in = c->st[c->istin].view();
+    a.out = c->st[1 - c->istin].view();
+    a.est = c->est.p;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    CK(launch_walker(c->P, a, c->L, grid_for(c, n), c->stream));
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2.p, c->wb.p, c->stream));
+    c->launches += 2;
+    c->istin = 1 - c->istin;
+    return DMC_OK;
+}
+
+int dmc_last_step_ms(dmc_ctx* c, double* ms)
+{
+    if (!c || !ms) return DMC_ERR_INVALID;
+    CK(cudaEventSynchronize(c->ev1));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, c->ev0, c->ev1));
+    *ms = f;
+    return DMC_OK;
+}
+
+int dmc_branch(dmc_ctx* c, double factor)
+{
+    if (!c) return DMC_ERR_INVALID;
+    const int n = c->n;
+    StackBufs& in = c->st[c->istin];
+    StackBufs& out = c->st[1 - c->istin];
+    CK(launch_branch(in.view(), out.view(), n, c->n3, c->cap, factor, c->counts.p, c->offs.p, c->irn1.p,
+                     c->wtisto.p, c->stream));
+    if (n > 0) c->launches += 3;
+    int total = 0;
+    if (n > 0) {
+        CK(cudaMemcpyAsync(&total, c->offs.p + n, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    c->istin = 1 - c->istin;
+    if (total > c->cap) {
+        c->n = c->cap;
+        return fail(c, DMC_ERR_OVERFLOW, "stack overflow in branch");
+    }
+    c->n = total;
+    return DMC_OK;
+}
+
+int dmc_generation(dmc_ctx* c, int opcomp, int* nt)
+{
+    if (!c) return DMC_ERR_INVALID;
+    int rc = dmc_step(c, opcomp);
+    if (rc) return rc;
+    const int idmc = c->rd.idmc;
+    if (idmc > 0 || idmc == -2) {
+        rc = dmc_branch(c, 1.0);
+        if (rc) return rc;
+    }
+    const int n = c->n;
+    const double nw = c->rd.nwalk;
+    if (n > c->rd.popup * nw || n < c->rd.popdn * nw) {
+        if (n == 0) return fail(c, DMC_ERR_EMPTY, "population died out");
+        rc = dmc_branch(c, 1.0 * c->rd.nwalk / n);
+        if (rc) return rc;
+    }
+    if (nt) *nt = c->n;
+    return DMC_OK;
+}
+
+int dmc_zero_estimators(dmc_ctx* c)
+{
+    if (!c) return DMC_ERR_INVALID;
+    CK(cudaMemsetAsync(c->vb.p, 0, DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->vb2.p, 0, DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->wb.p, 0, DMC_NEST_MAX * 8, c->stream));
+    return DMC_OK;
+}
+
+int dmc_get_estimators(dmc_ctx* c, double* valblk, double* valblk2, double* wtblk)
+{
+    if (!c || !valblk || !valblk2 || !wtblk) return DMC_ERR_INVALID;
+    const int ne = c->P.nest;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(valblk, c->vb.p, ne * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(valblk2, c->vb2.p, ne * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(wtblk, c->wb.p, ne * 8, cudaMemcpyDeviceToHost));
+    return DMC_OK;
+}
+
+int dmc_block_update(dmc_ctx* c, double* valnow, double* errnow)
+{
+    if (!c || !valnow || !errnow) return DMC_ERR_INVALID;
+    double a[DMC_NEST_MAX], b[DMC_NEST_MAX], w[DMC_NEST_MAX];
+    int rc = dmc_get_estimators(c, a, b, w);
+    if (rc) return rc;
+    for (int i = 0; i < c->P.nest; ++i) {
+        valnow[i] = a[i] / w[i];
+        const double v2 = b[i] / w[i];
+        errnow[i] = std::sqrt(std::fabs(v2 - valnow[i] * valnow[i]) / w[i]);
+    }
+    return dmc_zero_estimators(c);
+}
+
+int dmc_get_wtisto(dmc_ctx* c, int64_t* hist)
+{
+    if (!c || !hist) return DMC_ERR_INVALID;
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<unsigned long long> h(DMC_WTISTO);
+    CK(cudaMemcpy(h.data(), c->wtisto.p, DMC_WTISTO * 8, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < DMC_WTISTO; ++i) hist[i] = (int64_t)h[i];
+    return DMC_OK;
+}
+
+int dmc_bcsone_batch(dmc_ctx* c, int nw, const double* x, const double* smati, const int* ipart, const double* dr,
+                     double* ratio)
+{
+    (void)nw; (void)x; (void)smati; (void)ipart; (void)dr; (void)ratio;
+    return fail(c, DMC_ERR_UNSUPPORTED, "bcsone is not built yet");
+}
+
+int dmc_getphione_batch(dmc_ctx* c, int nw, const double* x, const int* ipart, const double* drr, double* ratio)
+{
+    (void)nw; (void)x; (void)ipart; (void)drr; (void)ratio;
+    return fail(c, DMC_ERR_UNSUPPORTED, "getphione is not built yet");
+}
+
+int dmc_getderbcs_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)
+{
+    (void)nw; (void)x; (void)dpsi;
+    return fail(c, DMC_ERR_UNSUPPORTED, "getderbcs is not built yet");
+}
+
+int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, int64_t* walker_steps,
+                          double* device_ms, int64_t* launches)
+{
+    if (!c || ngen < 0) return DMC_ERR_INVALID;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    if (flush_l2) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
+        const size_t fb = std::max<size_t>((size_t)2 * l2, 64u << 20);
+        CK(c->flush.alloc(fb));
+    }
+    double total = 0.0;
+    int64_t steps = 0, l0 = 0, lsum = 0;
+    int rc = DMC_OK;
+    for (int g = 0; g < ngen && rc == DMC_OK; ++g) {
+        if (flush_l2) CK(cudaMemsetAsync(c->flush.p, g & 0xff, c->flush.n, c->stream));
+        steps += c->n;
+        l0 = c->launches;
+        CK(cudaEventRecord(e0, c->stream));
+        int nt = 0;
+        rc = dmc_generation(c, (g == ngen - 1) ? opcomp_last : 0, &nt);
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        total += ms;
+        lsum += c->launches - l0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (walker_steps) *walker_steps = steps;
+    if (device_ms) *device_ms = total;
+    if (launches) *launches = lsum;
+    return rc;
+}
+
+int dmc_put_walkers(dmc_ctx* c, const dmc_walkers* w)
+{
+    if (!c || !w || w->n < 0) return DMC_ERR_INVALID;
+    const int n = w->n;
+    if (n > c->cap) return fail(c, DMC_ERR_OVERFLOW, "more walkers than the stack capacity");
+    if (n > 0 && (!w->x || !w->dpsi || !w->dpsig || !w->psil || !w->psigl || !w->d2psi || !w->d2psig || !w->v ||
+                  !w->vext || !w->weight || !w->psil0 || !w->psigl0 || !w->wt0 || !w->is || !w->irn))
+        return fail(c, DMC_ERR_INVALID, "dmc_put_walkers needs every field");
+    StackBufs& s = c->st[c->istin];
+    const size_t n3 = (size_t)c->n3;
+    auto H = [&](void* d, const void* h, size_t bytes) {
+        return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream);
+    };
+    CK(H(s.x.p, w->x, n * n3 * 8));
+    CK(H(s.dpsi.p, w->dpsi, n * n3 * 8));
+    CK(H(s.dpsig.p, w->dpsig, n * n3 * 8));
+    CK(H(s.psil.p, w->psil, n * 8));
+    CK(H(s.psigl.p, w->psigl, n * 8));
+    CK(H(s.d2psi.p, w->d2psi, n * 8));
+    CK(H(s.d2psig.p, w->d2psig, n * 8));
+    CK(H(s.v.p, w->v, n * 8));
+    CK(H(s.vext.p, w->vext, n * 8));
+    CK(H(s.weight.p, w->weight, n * 8));
+    CK(H(s.psil0.p, w->psil0, n * 8));
+    CK(H(s.psigl0.p, w->psigl0, n * 8));
+    CK(H(s.is.p, w->is, n * sizeof(int)));
+    CK(H(s.irn.p, w->irn, n * 8));
+    std::vector<float> t(n);
+    for (int k = 0; k < n; ++k) t[k] = (float)w->wt0[k];
+    CK(H(s.wt0.p, t.data(), n * sizeof(float)));
+    CK(cudaStreamSynchronize(c->stream));
+    c->n = n;
+    return DMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// Device-side data layout of the GB300 DMCBS walker path.
+//
+// HBM layout
+//  - walker stacks: structure of arrays, one walker per row; coordinates and
+//    gradients x/dpsi/dpsig as [cap][npart][3] doubles (the reference's
+//    x(3,npart) per walker), scalars as [cap] arrays, the 48-bit random
+//    state as uint64 [cap].
+//  - tables: one 64-byte record per grid point for up-down pairs
+//    {v, u, u'/., u''-part, beta, beta', lap beta, 0} so that the 4-point
+//    Lagrange stencil of one pair touches 256 contiguous bytes, and a
+//    32-byte record {0, u, u', u''} for same-spin pairs.
+//  - k vectors: 64-byte records (k, |k|^2, 2 vorb(shell), integer n).
+// On-chip layout (one walker per CTA) is described by SmemLayout below.
+#pragma once
+
+#include <cstdint>
+#include "../../include/dmcbcs_gpu.h"
+
+namespace dmc {
+
+constexpr int kThreads = 256;        // threads per walker CTA
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxNest = DMC_NEST_MAX;
+
+// grid record for up-down pairs (coshpot.f90 tables + betafun.f90 tables)
+struct __align__(16) TabUD {
+    double v, u, du, d2u, b, db, d2b, pad;
+};
+// grid record for same-spin pairs (no potential, no beta)
+struct __align__(16) TabSS {
+    double v, u, du, d2u;
+};
+
+struct __align__(16) KVecDev {
+    double k[3];
+    double k2;
+    double v;       // 2 * vorb(shell) (psislaterbcs.f90:259)
+    double pad;
+    int n[3];
+    int pad2;
+};
+
+enum Mode : int {
+    MODE_HPSI = 0,     // x -> hpsi outputs (wavefunction.f90:161-201)
+    MODE_BCS = 1,      // x -> determinant part only (psislaterbcs.f90:155-225)
+    MODE_GETPHI = 2,   // x -> Jastrow + potential only (coshpot.f90:154-205)
+    MODE_STEP = 3,     // one step1 move of every walker (step.f90:43-285)
+};
+
+struct DevParams {
+    int npart, nup, ndn, npair, nexup, nexdn, nd, nk, ncol, norb, ntab, nmax;
+    int ieq, nobeta, cutdrift, fn, idmc, onebody, nest, nrand;
+    int ldS, ldU;
+    double el, eli, range, scale, rangeb, scaleb;
+    double mass[2], sqm[2], imass[2], isqm[2];
+    double hbar, a2, dt, etrial, wtcut, nfac;
+    double sigma[2], dcut[2];
+    double qex[3], v0ex, v0exjas, vorb1;
+    double akup[DMC_MAX_UNPAIRED][3], ak2up[DMC_MAX_UNPAIRED];
+    double akdn[DMC_MAX_UNPAIRED][3], ak2dn[DMC_MAX_UNPAIRED];
+    int sinup[DMC_MAX_UNPAIRED], sindn[DMC_MAX_UNPAIRED];
+};
+
+// SoA walker stack on the device
+struct DevStack {
+    double *x, *dpsi, *dpsig;
+    double *psil, *psigl, *d2psi, *d2psig, *v, *vext, *weight, *psil0, *psigl0;
+    float* wt0;
+    int* is;
+    unsigned long long* irn;
+};
+
+// Arguments of the walker kernel.  For MODE_STEP the input is stack `in`
+// (n walkers, popped from the top) and the output stack `out`; otherwise
+// positions come from `xin` and results go to the `o_*` arrays.
+struct KernelArgs {
+    int mode;
+    int nw;
+    int opcomp;
+    const double* xin;
+    double *o_psil, *o_dpsi, *o_d2psi, *o_v, *o_vext, *o_psigl, *o_dpsig, *o_d2psig, *o_sinv;
+    int* o_is;
+    DevStack in, out;
+    double* est;                 // [nw][nest][2]: (val, wt) per estimator
+    const KVecDev* kv;           // [nk]
+    const TabUD* tud;            // [ntab+1]
+    const TabSS* tss;            // [ntab+1]
+    const unsigned long long* jumpA;   // LCG jump-ahead multipliers, [nrand+1]
+    const unsigned long long* jumpC;   // LCG jump-ahead increments, [nrand+1]
+    double* gscratch;            // per-CTA global scratch when the pair data do not fit on chip
+    int* status;                 // per-walker status flags (bit 0: singular matrix)
+};
+
+// On-chip layout of one walker CTA, offsets in doubles.
+struct SmemLayout {
+    int x, xo, dx, drift, dg, kq, S, pb, R, U, D, E, acc, colk, red, total;
+    int pb_in_smem;
+    int pb_size;          // doubles of pair data per walker
+    int rows_jas, rows_beta;   // rows of the up-down block per reduction chunk
+    int rsize;            // doubles in the union region
+};
+
+__host__ __device__ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+__host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_limit_bytes)
+{
+    SmemLayout L;
+    const int n3 = p.npart * 3;
+    int off = 0;
+    auto take = [&](int nd) { int o = off; off += round_up(nd, 2); return o; };
+    L.x = take(n3);               // positions being evaluated
+    L.xo = take(n3);              // old positions (step)
+    L.dx = take(n3);              // drift + gaussian displacement (step)
+    L.drift = take(n3);           // old drift (step)
+    L.dg = take(n3);              // guide-function gradient when a2 != 0
+    L.kq = take(p.nk * 8);        // k vector records
+    L.S = take(p.nd * p.ldS);     // pair matrix -> inverse
+    L.colk = take(p.nd + 2);      // Gauss-Jordan pivot column
+    L.acc = take(p.npart * 8);    // per particle: drift(3), lap, du(3), spare
+    L.red = take(kThreads * 8);   // reductions and per-thread partial sums
+    // union region: Jastrow pair vectors, then orbitals U|D|E, then beta terms
+    const int nE = p.npart * 3 * (p.nmax + 1) * 2;
+    const int nUDE = p.nup * p.ldU + p.ndn * p.ldU + nE;
+    L.R = off;
+    L.U = L.R;
+    L.D = L.R + p.nup * p.ldU;
+    L.E = L.D + p.ndn * p.ldU;
+    int rsize = nUDE;
+    const int row_pairs = p.ndn > 0 ? p.ndn : 1;
+    const int minrows = 1;
+    // at least one row of pair data must fit
+    if (rsize < row_pairs * 4) rsize = row_pairs * 4;
+    off += round_up(rsize, 2);
+    L.rsize = rsize;
+    L.rows_jas = rsize / (row_pairs * 3);
+    L.rows_beta = rsize / (row_pairs * 4);
+    if (L.rows_jas < minrows) L.rows_jas = minrows;
+    if (L.rows_beta < minrows) L.rows_beta = minrows;
+    // beta pair data (f'/r, lap f) per up-down pair
+    L.pb_size = p.nup * p.ndn * 2;
+    const int with_pb = off + round_up(L.pb_size, 2);
+    if (with_pb * 8 <= smem_limit_bytes) {
+        L.pb = off;
+        off = with_pb;
+        L.pb_in_smem = 1;
+    } else {
+        L.pb = -1;
+        L.pb_in_smem = 0;
+    }
+    L.total = off;
+    return L;
+}
+
+}  // namespace dmc

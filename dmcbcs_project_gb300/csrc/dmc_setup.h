@@ -1,0 +1,63 @@
+// Host-side set-up of one DMCBS system: the module state that the reference
+// builds once in setpsi/setupbcs/setbeta/setphi/setstep before the walker
+// loop.  Everything here runs once per context on the CPU; the tables are
+// then uploaded to the GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/dmcbcs_gpu.h"
+
+namespace dmc {
+
+// One k vector of the s-wave pairing basis: integer lattice vector n and
+// k = 2*pi*n/L (kshell.f90:141-155).
+struct KVec {
+    int n[3];
+    double k[3];
+    double k2;
+    int shell;   // 1-based shell index of the reference's vorb(shell)
+};
+
+struct Setup {
+    // sizes
+    int npart = 0, nup = 0, ndn = 0, npair = 0, nexup = 0, nexdn = 0, nd = 0;
+    int norb = 0, nk = 0, ncol = 0, ntab = 0, nmax = 0;
+    // box and species
+    double el = 0, eli = 0, rho = 0;
+    double mass[2] = {1, 1}, sqm[2] = {1, 1};
+    double hbar = 0.5;
+    double a2 = 0;
+    // s-wave pairing (psislaterbcs.f90:5-21)
+    std::vector<KVec> kv;          // nk entries, kv[0] = 0
+    std::vector<int> numsh;        // half-shell sizes per shell (norb)
+    std::vector<double> vorb;      // norb
+    double akup[DMC_MAX_UNPAIRED][3], ak2up[DMC_MAX_UNPAIRED];
+    double akdn[DMC_MAX_UNPAIRED][3], ak2dn[DMC_MAX_UNPAIRED];
+    int sinup[DMC_MAX_UNPAIRED], sindn[DMC_MAX_UNPAIRED];
+    // one-body and long-range Jastrow
+    double qex[3] = {0, 0, 0}, v0ex = 0, v0exjas = 0;
+    int numq = 0;
+    // beta table (betafun.f90): swbtab, swdbtab, swd2btab on [0, L/2]
+    bool nobeta = true;
+    int ntabb = 0;
+    double rangeb = 0, scaleb = 0;
+    std::vector<double> btab, dbtab, d2btab;
+    // Jastrow + potential tables (coshpot.f90), [ic][0..ntab]
+    double range = 0, scale = 0, hbarp = 1;
+    double cjas[2] = {0, 0};
+    bool iop = false, ieq = false;
+    std::vector<double> utab[2], dutab[2], d2utab[2], vtab[2];
+    // units (dmcbcs.f90:146-170) and step (step.f90:11-41)
+    double eunit = 1, nfac = 1, etrial = 0;
+    double sigma[2] = {0, 0}, dcut[2] = {0, 0};
+    bool cutdrift = false;
+
+    // Returns DMC_OK or an error code with a message in err.
+    int build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string& err);
+    int set_vorb(const double* v, int n, std::string& err);
+};
+
+}  // namespace dmc

@@ -1,0 +1,294 @@
+/*
+ * dmcbcs_gpu.h -- C ABI of the GB300 (sm_103a) DMCBS walker hot path.
+ *
+ * The reference (CalebRHicks/DMCBS_Project, Fortran 90) has no plugin or FFI
+ * layer: its hot path is a set of module procedures whose state is set once
+ * by setup routines and then called once per walker.  Every entry point below
+ * replaces one of those procedures (the replaced routine is cited file:line
+ * beside it) and works on a whole batch of walkers at once.
+ *
+ * Conventions
+ *  - Every function returns an int status (DMC_OK on success).  Nothing calls
+ *    exit() or abort(); the message of the last failure on a context is
+ *    returned by dmc_last_error().
+ *  - Coordinates use the reference layout: one walker is x(3,npart) in
+ *    Fortran column-major order, i.e. C double x[npart][3], up particles
+ *    first (psislaterbcs.f90:44-45).  A batch is x[nw][npart][3].
+ *  - Matrices returned to the caller (the BCS inverse) are column-major
+ *    nd x nd like the Fortran array smati(nd,nd).
+ *  - "_batch" functions take HOST pointers and are synchronous.
+ *    "_device" variants take DEVICE pointers and a cudaStream_t (passed as
+ *    void*), are stream-ordered and return once the work is enqueued.
+ *  - One host thread per context.  Contexts are independent.
+ *  - A singular BCS matrix is not an error: as in the reference
+ *    (matrixlapack.f90:19-25, psislaterbcs.f90:210) log|det| is set to
+ *    DMC_MINUSHUGE and the determinant drift and Laplacian are zero.
+ */
+#ifndef DMCBCS_GPU_H
+#define DMCBCS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DMC_ABI_VERSION 1
+
+#define DMC_MAX_SHELLS 32     /* s-wave pairing shells (norb) */
+#define DMC_MAX_UNPAIRED 16   /* unpaired plane-wave states per spin */
+#define DMC_MAX_PART 256      /* particles per system */
+#define DMC_NEST_MAX 16       /* estimators (14 for DMC, 13 for idmc=2, 6 for VMC) */
+#define DMC_WTISTO 500        /* multiplicity histogram bins (step.f90:9) */
+#define DMC_MINUSHUGE (-1.0e30) /* log|det| of a singular matrix (matrixlapack.f90:19) */
+
+/* status codes */
+#define DMC_OK 0
+#define DMC_ERR_INVALID 1      /* bad argument or deck value */
+#define DMC_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define DMC_ERR_UNSUPPORTED 3  /* valid for the reference, not built here */
+#define DMC_ERR_OVERFLOW 4     /* walker stack full (stack.f90:88-91) */
+#define DMC_ERR_SETUP 5        /* table setup failed (rungekutta.f90:85-88, kshell.f90:137-140) */
+#define DMC_ERR_EMPTY 6        /* population died out */
+#define DMC_ERR_NOMEM 7        /* device or host allocation failed */
+
+/*
+ * System description: the deck values read by setpsi, setupbcs, setbeta and
+ * setphi, as read (before the reference rescales any of them).
+ */
+typedef struct dmc_system_desc {
+    /* main deck, dmcbcs.f90:61-66 */
+    int ntab;             /* table points for Jastrow, potential and beta */
+    double hbar;          /* hbar^2/2 without the mass */
+    int ndim;             /* must be 3 */
+    int nbin[2];          /* number of up and down particles */
+    double mass[2];       /* mass of up and down particles */
+    /* setpsi, wavefunction.f90:36-37 (node type must be 'bcs') */
+    double a2;            /* constant in the importance function */
+    /* setupbcs, psislaterbcs.f90:47-68 */
+    double rho;           /* number density */
+    int nexup;            /* unpaired up plane waves */
+    int ikup[DMC_MAX_UNPAIRED][3];
+    int nexdn;            /* unpaired down plane waves */
+    int ikdn[DMC_MAX_UNPAIRED][3];
+    int norb;             /* s-wave pairing shells */
+    double vorb[DMC_MAX_SHELLS];
+    int nqex[3];          /* q of the external cosine potential */
+    double v0ex;          /* as read; the reference multiplies it by 1/2 */
+    double v0exjas;       /* as read; the reference multiplies it by v0ex */
+    int numq;             /* long-range Jastrow shells (0 = off) */
+    double jbeta, jgamma; /* long-range Jastrow parameters */
+    /* setbeta, betafun.f90:19-21 */
+    double bbeta, dbeta;  /* b and d of the up-down beta function */
+    double bfact;         /* beta strength; 0 = no beta (bfact<0 unsupported) */
+    /* setphi, coshpot.f90:35-41 */
+    double v0, amu;       /* cosh potential strength and width */
+    double cjas[2];       /* opposite- and equal-spin Jastrow strength */
+    double djas;          /* Jastrow healing distance */
+    double v0op, v0eq;    /* effective strengths for the Jastrow (0 = v0) */
+} dmc_system_desc;
+
+/* Run parameters: dmcbcs.f90:44-60 plus the stack size factor (:224-230). */
+typedef struct dmc_run_desc {
+    int64_t seed;         /* random number seed for the initial walkers */
+    int idmc;             /* -2,-1,0 (VMC), 1 (DMC local weight), 2 (DMC Metropolis) */
+    int isite;            /* 1 = random initial walkers, 0 = walkers loaded */
+    int nwalk;            /* target population */
+    int neq, nav, nstep;  /* equilibration blocks, averaging blocks, steps/block */
+    double dt;            /* time step */
+    double etrial;        /* trial energy per particle in energy units */
+    int units;            /* 1 = energies in units of the free Fermi gas */
+    double dcut;          /* drift cut off; <0 = no cut (step.f90:32-37) */
+    int fn;               /* fixed node */
+    double popup, popdn;  /* drastic population control factors */
+    double dobal;         /* rebalance threshold (single process: unused) */
+    double wtcut;         /* weight cut off */
+    double stmax;         /* stack capacity factor: capacity = nwalk*stmax (10) */
+} dmc_run_desc;
+
+/* Derived sizes and units, filled by dmc_get_info. */
+typedef struct dmc_info {
+    int npart, nup, ndn, npair, nexup, nexdn, nd;
+    int nk;               /* k vectors incl. k=0 (kshell.f90:136-143) */
+    int ncol;             /* pair-orbital columns K = 2*nk-1 */
+    int ntab;
+    int capacity;         /* walker slots per stack */
+    int nest;             /* estimators for this idmc */
+    double el;            /* box side L */
+    double eunit;         /* energy unit (dmcbcs.f90:146-159) */
+    double nfac;          /* estimator normalisation (step.f90:24-25) */
+    double etrial;        /* trial energy of the whole system */
+    double sigma[2];      /* diffusion width per species (step.f90:29-30) */
+    int64_t device_bytes; /* device memory held by the context */
+} dmc_info;
+
+typedef struct dmc_ctx dmc_ctx;
+
+/* ---- lifecycle --------------------------------------------------------- */
+
+/* Replaces setpsi (wavefunction.f90:13-96), setupbcs (psislaterbcs.f90:23-153),
+ * setbeta/initbeta (betafun.f90:12-125), setphi (coshpot.f90:14-143),
+ * setstep (step.f90:11-41) and create (stack.f90:51-80).  Builds the k
+ * shells, the beta, Jastrow and potential tables on the host and uploads
+ * them to the current CUDA device. */
+int dmc_create(const dmc_system_desc* sys, const dmc_run_desc* run, dmc_ctx** out);
+int dmc_destroy(dmc_ctx* ctx);
+const char* dmc_last_error(const dmc_ctx* ctx);
+const char* dmc_status_string(int status);
+int dmc_abi_version(void);
+int dmc_get_info(const dmc_ctx* ctx, dmc_info* out);
+
+/* Copy a setup table to host memory.  which: 0 utab, 1 dutab, 2 d2utab,
+ * 3 vtab (each 2*(ntab+1) values, layout [ic][0..ntab] i.e. Fortran
+ * (2,0:ntab) transposed), 4 swbtab, 5 swdbtab, 6 swd2btab (ntab+1 each),
+ * 7 ak (3*nk), 8 ak2 (nk), 9 numsh (norb, as doubles). */
+int dmc_get_table(const dmc_ctx* ctx, int which, double* out, int n);
+
+/* Replaces setbcspar (psislaterbcs.f90:401-419) with optbeta=.false.:
+ * new s-wave amplitudes vorb(1:norb). */
+int dmc_set_vorb(dmc_ctx* ctx, const double* vorb, int norb);
+
+/* ---- wavefunction and local energy, batched ----------------------------- */
+
+/* Replaces hpsi (wavefunction.f90:161-201): Jastrow+potential, one-body,
+ * long-range Jastrow and BCS determinant for nw walkers.
+ * x[nw][npart][3] -> psil[nw], is[nw], dpsi[nw][npart][3], d2psi[nw], v[nw],
+ * vext[nw], psigl[nw], dpsig[nw][npart][3], d2psig[nw].  Any output pointer
+ * may be NULL. */
+int dmc_hpsi_batch(dmc_ctx* ctx, int nw, const double* x, double* psil, int* is,
+                   double* dpsi, double* d2psi, double* v, double* vext,
+                   double* psigl, double* dpsig, double* d2psig);
+int dmc_hpsi_device(dmc_ctx* ctx, int nw, const double* x, double* psil, int* is,
+                    double* dpsi, double* d2psi, double* v, double* vext,
+                    double* psigl, double* dpsig, double* d2psig, void* stream);
+
+/* Replaces bcs (psislaterbcs.f90:155-225): log|det|, sign, drift dphi[nw][npart][3],
+ * Laplacian d2phi and (if smati != NULL) the inverse smati[nw][nd*nd]
+ * column-major, which the reference keeps as smatisave. */
+int dmc_bcs_batch(dmc_ctx* ctx, int nw, const double* x, double* phil, int* is,
+                  double* dphi, double* d2phi, double* smati);
+
+/* Replaces getphi (coshpot.f90:154-205): Jastrow u, du[nw][npart][3], d2u and
+ * the pair potential v. */
+int dmc_getphi_batch(dmc_ctx* ctx, int nw, const double* x, double* u,
+                     double* du, double* d2u, double* v);
+
+/* Replaces rmatinv (matrixlapack.f90:13-41), i.e. MKL dgetrf+dgetri, on nb
+ * column-major n x n matrices a[nb][n*n] in place: inverse, log|det| and
+ * sign.  A singular matrix gives detl = DMC_MINUSHUGE and is left
+ * unspecified, as the reference leaves it. */
+int dmc_matinv_batch(dmc_ctx* ctx, int n, int nb, double* a, double* detl, int* is);
+
+/* Replaces bcsone (psislaterbcs.f90:296-376): determinant ratio for moving
+ * particle ipart[w] (1-based, as in the reference) of walker w by -dr[w][3]
+ * (dr = xold - xnew), from that walker's inverse smati[w] (as returned by
+ * dmc_bcs_batch). */
+int dmc_bcsone_batch(dmc_ctx* ctx, int nw, const double* x, const double* smati,
+                     const int* ipart, const double* dr, double* ratio);
+
+/* Replaces getphione (coshpot.f90:207-264): Jastrow ratio exp(U'-U) for the
+ * same single-particle moves (drr = xold - xnew). */
+int dmc_getphione_batch(dmc_ctx* ctx, int nw, const double* x, const int* ipart,
+                        const double* drr, double* ratio);
+
+/* Replaces getderbcs (psislaterbcs.f90:449-524) with optsw=.true.,
+ * optbeta=.false.: d log|det| / d vorb(k), dpsi[nw][norb]. */
+int dmc_getderbcs_batch(dmc_ctx* ctx, int nw, const double* x, double* dpsi);
+
+/* ---- walker population (device-resident stacks) ------------------------ */
+
+/* Walker records as exchanged with the host; any array pointer may be NULL
+ * on output.  Stack order: index 0 is the bottom of the reference's stack,
+ * index n-1 its top (the next walker pop() returns). */
+typedef struct dmc_walkers {
+    int n;
+    double* x;        /* [n][npart][3] */
+    double* dpsi;     /* [n][npart][3] */
+    double* dpsig;    /* [n][npart][3] */
+    double* psil;     /* [n] */
+    double* psigl;    /* [n] */
+    double* d2psi;    /* [n] */
+    double* d2psig;   /* [n] */
+    double* v;        /* [n] */
+    double* vext;     /* [n] */
+    double* weight;   /* [n] */
+    double* psil0;    /* [n] */
+    double* psigl0;   /* [n] */
+    double* wt0;      /* [n] (single precision in the reference, stack.f90:12) */
+    int* is;          /* [n] */
+    int64_t* irn;     /* [n] per-walker 48-bit random number state */
+} dmc_walkers;
+
+/* Replaces the random-configuration set-up of dmcbcs.f90:238-282 (isite):
+ * nwalk walkers from the seed, pushed on the input stack. */
+int dmc_init_walkers(dmc_ctx* ctx);
+
+/* Replaces the walker read of dmcbcs.f90:254-258,283-294 (fort.9): push
+ * w->n walkers with x, weight, psil0, psigl0 and irn (other fields ignored). */
+int dmc_load_walkers(dmc_ctx* ctx, const dmc_walkers* w);
+
+/* Copy the current walker stack to the host (fort.9 write,
+ * dmcbcs.f90:548-567, and full walker state for checks).  w->n is the
+ * capacity of the caller's arrays on entry and the count on return. */
+int dmc_get_walkers(dmc_ctx* ctx, dmc_walkers* w);
+
+/* Replaces the initial evaluation of dmcbcs.f90:314-395 for a run that
+ * starts at tau = 0: hpsi on every walker, wt0=is, weight=1.  sums[11]:
+ * ene, ene2, psi, psi2, psig, psig2, sgn, n, wtsum (the sums reduced to
+ * rank 0 at dmcbcs.f90:354-362), then for DMC the block value and error of
+ * estimator 1 printed at tau = 0 (dmcbcs.f90:337-340,379-384). */
+int dmc_initial_eval(dmc_ctx* ctx, double* sums);
+
+int dmc_num_walkers(dmc_ctx* ctx, int* n);
+
+/* Replaces step1 (step.f90:43-285): one drift-diffusion move, Metropolis test
+ * or DMC weight for every walker; opcomp selects the estimator step. */
+int dmc_step(dmc_ctx* ctx, int opcomp);
+
+/* Replaces branch (step.f90:287-315): stochastic-rounding copies with
+ * weight*factor. */
+int dmc_branch(dmc_ctx* ctx, double factor);
+
+/* Replaces one generation of dmcbcs.f90:436-448: step1, branch (DMC),
+ * drastic population control; returns the population in *nt. */
+int dmc_generation(dmc_ctx* ctx, int opcomp, int* nt);
+
+/* Replaces zerest (estimator.f90:37-55). */
+int dmc_zero_estimators(dmc_ctx* ctx);
+
+/* Current block sums of the estimators (estimator.f90:72-82):
+ * valblk, valblk2, wtblk, each [nest]. */
+int dmc_get_estimators(dmc_ctx* ctx, double* valblk, double* valblk2, double* wtblk);
+
+/* Replaces update (estimator.f90:84-113): block averages valnow[nest],
+ * errors errnow[nest]; then zero the block sums. */
+int dmc_block_update(dmc_ctx* ctx, double* valnow, double* errnow);
+
+/* Walker multiplicity histogram (step.f90:310,317-334), hist[DMC_WTISTO]. */
+int dmc_get_wtisto(dmc_ctx* ctx, int64_t* hist);
+
+/* Device timing of the last dmc_step: milliseconds of the hpsi-dominated
+ * step kernel, measured with CUDA events on the context's stream. */
+int dmc_last_step_ms(dmc_ctx* ctx, double* ms);
+
+/* Replaces the walker loop of dmcbcs.f90:435-449 for ngen generations (the
+ * last one with opcomp): each generation is bracketed by CUDA events on the
+ * context's stream and, when flush_l2 is set, preceded by a write of a
+ * buffer twice the L2 size outside the timed interval.  Returns the summed
+ * device milliseconds, the walker-steps (walkers entering step1, summed)
+ * and the number of kernels launched inside the timed intervals. */
+int dmc_timed_generations(dmc_ctx* ctx, int ngen, int opcomp_last, int flush_l2, int64_t* walker_steps,
+                          double* device_ms, int64_t* launches);
+
+/* Replace the current stack by w->n walkers with their full state (all
+ * fields of dmc_walkers must be set): the inverse of dmc_get_walkers, for
+ * hosts that keep the walker stacks in their own memory (stack.f90:82-110)
+ * and hand them to the GPU for each generation. */
+int dmc_put_walkers(dmc_ctx* ctx, const dmc_walkers* w);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DMCBCS_GPU_H */

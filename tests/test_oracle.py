@@ -1,0 +1,323 @@
+"""Pins of the CPU oracle (no GPU).
+
+The reference ships no golden outputs and cannot be built here, so the
+oracle is pinned piece by piece: random numbers against the integer
+recurrence, the dense inverse against LAPACK, the wavefunction against
+analytic answers and against the finite-difference self-checks the
+reference itself carries (chkder, chkone: wavefunction.f90:289-391;
+chkderp: optimizer.f90:171-225).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from dmcbcs_project_gb300 import abi, configs
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+# ---- random numbers (ran.f90) ---------------------------------------------
+
+def test_rng_golden():
+    g = json.load(open(os.path.join(GOLD, "rng.json")))
+    fn = {"ran1": oracle.ran1, "ran2": oracle.ran2}
+    for name, per_seed in g.items():
+        for seed, seq in per_seed.items():
+            s = int(seed)
+            for e in seq:
+                u, s = fn[name](s)
+                assert s == e["state"]
+                assert u == e["u"]
+
+
+def test_gaussian_box_muller():
+    g = json.load(open(os.path.join(GOLD, "rng.json")))
+    seq = g["ran1"]["17"]
+    for n in (6, 7):
+        out, st = oracle.gaussian(17, n)
+        u = [e["u"] for e in seq]
+        exp = []
+        for i in range(n // 2):
+            r = np.sqrt(-2.0 * np.log(u[2 * i + 1]))
+            a = 2.0 * np.pi * u[2 * i]
+            exp += [np.sin(a) * r, np.cos(a) * r]
+        if n % 2:
+            exp.append(np.cos(2.0 * np.pi * u[n - 1]) * np.sqrt(-2.0 * np.log(u[n])))
+        assert np.allclose(out, exp, rtol=1e-14, atol=1e-15)
+        assert st == seq[2 * ((n + 1) // 2) - 1]["state"]
+
+
+# ---- dense inverse (matrixlapack.f90 + LAPACK) ------------------------------
+
+def test_matinv_lapack_golden():
+    d = np.load(os.path.join(GOLD, "lapack.npz"))
+    k = 0
+    while f"a{k}" in d:
+        inv, ld, s, info = oracle.matinv(d[f"a{k}"])
+        assert info == 0
+        assert s == int(d[f"sign{k}"])
+        assert abs(ld - float(d[f"logdet{k}"])) < 1e-12 * max(1, abs(float(d[f"logdet{k}"])))
+        ref = d[f"inv{k}"]
+        assert np.max(np.abs(inv - ref)) < 1e-12 * max(1.0, np.max(np.abs(ref)))
+        k += 1
+    assert k >= 6
+
+
+def test_matinv_singular_and_sign():
+    a = np.array([[1.0, 2.0], [2.0, 4.0]])
+    _, ld, _, info = oracle.matinv(a)
+    assert info > 0 and ld == abi.DMC_MINUSHUGE
+    p = np.array([[0.0, 1.0], [1.0, 0.0]])          # a permutation: det = -1
+    inv, ld, s, info = oracle.matinv(p)
+    assert info == 0 and s == -1 and abs(ld) < 1e-15
+    assert np.allclose(inv, p)
+
+
+# ---- set-up tables ----------------------------------------------------------
+
+def test_kshell_counts():
+    g = json.load(open(os.path.join(GOLD, "kshell.json")))
+    sysd, rund, _ = configs.workload("n66", nwalk=4)
+    sysd.norb = 10
+    for i in range(10):
+        sysd.vorb[i] = 0.5 ** i
+    o = oracle.Oracle(sysd, rund, threads=1)
+    numsh = o.table(9)[:10]
+    assert list(numsh.astype(int)) == g["count"][:10]
+    ak = o.table(7).reshape(-1, 3) * o.info.el / (2 * np.pi)
+    n2 = np.rint(np.sum(ak ** 2, axis=1)).astype(int)
+    assert list(n2) == sorted(n2)                     # shells in increasing |n|^2
+    vecs = {tuple(np.rint(v).astype(int)) for v in ak}
+    assert len(vecs) == len(ak)                       # no vector twice
+    assert all(tuple(-np.array(v)) not in vecs for v in vecs if any(v))   # half set only
+
+
+def test_jastrow_and_potential_tables():
+    sysd, rund, _ = configs.workload("n66", nwalk=4)
+    o = oracle.Oracle(sysd, rund, threads=1)
+    nt = o.info.ntab + 1
+    u, du, d2u, vt = (o.table(i).reshape(2, nt) for i in range(4))
+    el = o.info.el
+    dr = 0.5 * el / o.info.ntab
+    n0 = int(o.info.ntab * sysd.djas / (0.5 * el))
+    assert u[0, n0] == 0.0 and np.all(u[0, n0:] == 0.0)   # log f = 0 from the healing distance on
+    assert abs(du[0, n0]) < 1e-7                          # f'/f converged to 0 there
+    assert np.all(du[0, n0 + 1:] == 0.0) and np.all(d2u[0, n0 + 1:] == 0.0)
+    assert np.all(u[1] == 0.0)                            # no same-spin Jastrow (cjas(2)=0)
+    mu = sysd.amu
+    assert abs(vt[0, 0] - (-2.0 * sysd.v0 * mu * mu * 1.0)) < 1e-9
+    r = np.arange(nt) * dr
+    assert np.allclose(vt[0], -2.0 * mu * mu / np.cosh(mu * r) ** 2, rtol=1e-12, atol=1e-300)
+    assert np.all(vt[1] == 0.0)
+    # u'' table is f''/f - (f'/f)^2: check against finite differences of u' inside the Jastrow range
+    i = np.arange(50, n0 - 50, 97)
+    fd = (du[0, i + 1] - du[0, i - 1]) / (2 * dr)
+    assert np.allclose(d2u[0, i], fd, rtol=1e-4, atol=1e-6)
+
+
+def test_beta_table():
+    sysd, rund, _ = configs.workload("n14", nwalk=4)
+    o = oracle.Oracle(sysd, rund, threads=1)
+    b, db, d2b = o.table(4), o.table(5), o.table(6)
+    assert b[-1] == 0.0                          # shifted to zero at L/2
+    assert db[0] == 0.0
+    dr = 0.5 * o.info.el / o.info.ntab
+    i = np.arange(100, o.info.ntab - 100, 211)
+    fd = (b[i + 1] - b[i - 1]) / (2 * dr)
+    assert np.allclose(db[i], fd, rtol=1e-5, atol=1e-8)
+    # beyond L/2 the radial function is zero
+    assert np.all(o.radialfun(0.5 * o.info.el * 1.0001) == 0.0)
+
+
+# ---- known answers ------------------------------------------------------------
+
+def free_gas(nwalk=8):
+    """7 up + 7 down with phi = sum of the 7 lowest plane waves: closed-shell
+    free Fermi gas, E_L = 2 * sum_k k^2/2 exactly."""
+    sp = configs.system_params(7, 7, 2)
+    sp.update(vorb=[1.0, 1.0], bfact=0.0, cjas=[0.0, 0.0], v0=0.0)
+    return abi.make_system(sp), abi.make_run(configs.run_params(nwalk, 0.002))
+
+
+def test_free_fermi_gas_energy():
+    sysd, rund = free_gas()
+    o = oracle.Oracle(sysd, rund, threads=1)
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-0.5, 0.5, size=(16, 14, 3)) * o.info.el
+    h = o.hpsi(x)
+    k2 = (2 * np.pi / o.info.el) ** 2
+    e_free = 2 * 0.5 * 6 * k2                      # two spins, six |k|=2pi/L waves, hbar^2/2m = 0.5
+    el = -0.5 * h["d2psi"] + h["v"]
+    assert np.allclose(el, e_free, rtol=1e-10)
+    assert np.all(h["v"] == 0.0)
+
+
+def test_single_pair_is_pair_function():
+    sp = configs.system_params(1, 1, 3)
+    sp.update(cjas=[0.0, 0.0], v0=0.0)
+    sysd, rund = abi.make_system(sp), abi.make_run(configs.run_params(4, 0.002))
+    o = oracle.Oracle(sysd, rund, threads=1)
+    el = o.info.el
+    rng = np.random.default_rng(2)
+    ak = o.table(7).reshape(-1, 3)
+    numsh = o.table(9).astype(int)
+    for _ in range(5):
+        x = rng.uniform(-0.5, 0.5, size=(2, 3)) * el
+        d = x[0] - x[1]
+        d -= el * np.round(d / el)
+        phi = sysd.vorb[0]
+        k = 1
+        for sh in range(1, sysd.norb):
+            for _ in range(numsh[sh]):
+                phi += 2 * sysd.vorb[sh] * np.cos(ak[k] @ (x[0] - x[1]))
+                k += 1
+        phi += o.radialfun(np.linalg.norm(d))[0]
+        h = o.hpsi(x[None])
+        assert abs(h["psil"][0] - np.log(abs(phi))) < 1e-12
+        assert h["is_"][0] == (1 if phi > 0 else -1)
+
+
+# ---- finite-difference self-checks (the reference's chkder/chkone/chkderp) ----
+
+def _near_half_box(x, nup, el, ntab, cells=6):
+    """True if an up-down pair is within `cells` table spacings of L/2.
+
+    The reference's beta table has a doubled second derivative at its last
+    point r = L/2 (betafun.f90:106-112: the image term beta(el-r) equals
+    beta(L/2) there), so the tabulated Laplacian and the tabulated values
+    disagree within two spacings of L/2; finite differences must stay away."""
+    d = x[:nup, None, :] - x[None, nup:, :]
+    d -= el * np.round(d / el)
+    r = np.linalg.norm(d, axis=-1)
+    return bool(np.any(np.abs(r - 0.5 * el) < cells * 0.5 * el / ntab))
+
+
+def _walkers(name, nw, seed=11):
+    sysd, rund, _ = configs.workload(name, nwalk=nw, seed=seed)
+    o = oracle.Oracle(sysd, rund, threads=1)
+    o.init_walkers()
+    base = o.walkers()["x"]
+    rng = np.random.default_rng(seed)
+    out = []
+    for w in range(nw):
+        while True:
+            x = base[w] + rng.normal(scale=0.2, size=(o.npart, 3))
+            if not _near_half_box(x, o.info.nup, o.info.el, o.info.ntab):
+                break
+        out.append(x)
+    return sysd, o, np.array(out)
+
+
+@pytest.mark.parametrize("name", ["n14", "p38_33"])
+def test_chkder_gradient_and_laplacian(name):
+    """wavefunction.f90:289-321: central differences of log|Psi| give dpsi;
+    differences of dpsi*Psi give the Laplacian d2psi."""
+    sysd, o, x = _walkers(name, 1)
+    x = x[0]
+    h0 = o.hpsi(x[None])
+    h = 1e-5
+    d2num = 0.0
+    for i in range(o.npart):
+        for c in range(3):
+            xp = x.copy(); xp[i, c] += h
+            xm = x.copy(); xm[i, c] -= h
+            hp, hm = o.hpsi(xp[None]), o.hpsi(xm[None])
+            dnum = (hp["psil"][0] - hm["psil"][0]) / (2 * h)
+            assert abs(h0["dpsi"][0, i, c] - dnum) < 1e-5 * max(1.0, abs(dnum)), (i, c)
+            gp = hp["dpsi"][0, i, c] * np.exp(hp["psil"][0] - h0["psil"][0])
+            gm = hm["dpsi"][0, i, c] * np.exp(hm["psil"][0] - h0["psil"][0])
+            d2num += (gp - gm) / (2 * h)
+    assert abs(d2num - h0["d2psi"][0]) < 1e-4 * max(1.0, abs(h0["d2psi"][0]))
+
+
+@pytest.mark.parametrize("name", ["n14", "p38_33"])
+def test_chkone_single_particle_ratios(name):
+    """wavefunction.f90:351-391: bcsone and getphione against full recomputes."""
+    sysd, o, x = _walkers(name, 1, seed=4)
+    x = x[0]
+    b0 = o.bcs(x[None], want_inverse=True)
+    sinv = b0["smati"][0]
+    rng = np.random.default_rng(8)
+    for i1 in (1, o.npart // 2, o.npart):
+        dr = rng.normal(scale=0.3, size=3)
+        xn = x.copy()
+        xn[i1 - 1] -= dr
+        b1 = o.bcs(xn[None])
+        rat_full = np.exp(b1["phil"][0] - b0["phil"][0]) * b1["is_"][0] * b0["is_"][0]
+        rat = o.bcsone(x, dr, i1, sinv)
+        assert abs(rat - rat_full) < 1e-9 * max(1.0, abs(rat_full))
+        j0, j1 = o.getphi(x), o.getphi(xn)
+        assert abs(o.getphione(x, dr, i1) - np.exp(j1["u"] - j0["u"])) < 1e-10 * np.exp(j1["u"] - j0["u"])
+
+
+def test_chkderp_vorb_derivatives():
+    """optimizer.f90:171-225: d log|det| / d vorb(k) against central differences."""
+    sysd, o, x = _walkers("n14", 1, seed=6)
+    x = x[0]
+    d = o.getderbcs(x)
+    vorb = np.array(sysd.vorb[: sysd.norb])
+    hstep = 1e-6
+    for k in range(sysd.norb):
+        vp, vm = vorb.copy(), vorb.copy()
+        vp[k] += hstep
+        vm[k] -= hstep
+        o.set_vorb(vp)
+        lp = o.bcs(x[None])["phil"][0]
+        o.set_vorb(vm)
+        lm = o.bcs(x[None])["phil"][0]
+        o.set_vorb(vorb)
+        fd = (lp - lm) / (2 * hstep)
+        assert abs(d[k] - fd) < 1e-6 * max(1.0, abs(fd)), (k, d[k], fd)
+
+
+# ---- population dynamics -------------------------------------------------------
+
+def test_generation_independent_of_threads():
+    res = []
+    for threads in (1, 4):
+        sysd, rund, _ = configs.workload("n14", nwalk=40)
+        o = oracle.Oracle(sysd, rund, threads=threads)
+        o.init_walkers()
+        o.initial_eval()
+        for g in range(4):
+            o.generation(g == 3)
+        res.append((o.walkers(), o.estimators()))
+    (w1, e1), (w2, e2) = res
+    assert np.array_equal(w1["x"], w2["x"]) and np.array_equal(w1["irn"], w2["irn"])
+    assert all(np.array_equal(a, b) for a, b in zip(e1, e2))
+
+
+def test_branch_copies_are_contiguous_and_advance_ran2():
+    sysd, rund, _ = configs.workload("n14", nwalk=20)
+    o = oracle.Oracle(sysd, rund, threads=1)
+    o.init_walkers()
+    o.initial_eval()
+    o.step(False)
+    before = o.walkers()
+    o.branch(1.0)
+    after = o.walkers()
+    # expected copies, walking the stack from the top (step.f90:295-311)
+    exp_irn = []
+    for j in range(before["n"] - 1, -1, -1):
+        u, s = oracle.ran1(int(before["irn"][j]))
+        iwt = int(before["weight"][j] + u)
+        for _ in range(iwt):
+            _, s = oracle.ran2(s)
+            exp_irn.append(s)
+    assert list(after["irn"]) == exp_irn
+    assert set(np.unique(after["weight"])) <= {1.0, -1.0}
+
+
+def test_vmc_acceptance_reasonable():
+    sysd, rund, _ = configs.workload("n14", nwalk=32, idmc=0)
+    o = oracle.Oracle(sysd, rund, threads=2)
+    o.init_walkers()
+    o.initial_eval()
+    for g in range(5):
+        o.generation(True)
+    vn, en = o.block_update()
+    assert 0.3 < vn[5] <= 1.0            # acceptance (estimator 6)
+    assert o.num_walkers() == 32         # VMC never branches
