@@ -34,10 +34,10 @@ METRIC = "DMC walker-steps/s @N=66: mixed/batched vs plain FP64 GPU, E_L rel err
 UNIT = "walker-steps/s"
 WORKLOAD = "n66"
 
-# DRAM bytes per walker-step of the walker kernel from one ncu capture
-# (profiles/walker_kernel_n66.md: dram__bytes_read.sum + dram__bytes_write.sum
-# of one launch divided by the walkers it processed).  None until captured.
-NCU_TRAFFIC_BYTES_PER_WALKER = None
+# DRAM bytes per walker-step of the FP64 walker kernel from one ncu capture
+# (profiles/walker_kernel_n66_fp64.md: dram__bytes_read.sum +
+# dram__bytes_write.sum = 2.42 MB for one step launch over ~512 walkers).
+NCU_TRAFFIC_BYTES_PER_WALKER = 4730.0
 
 
 def algorithmic_flops(nup, ndn, nd, K, npart):
@@ -327,7 +327,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--walkers", type=int, default=None)
