@@ -23,6 +23,8 @@ DMC_ERR_OVERFLOW = 4
 DMC_ERR_SETUP = 5
 DMC_ERR_EMPTY = 6
 DMC_ERR_NOMEM = 7
+DMC_ERR_NOALLOC_LIMIT = 8
+DMC_NOALLOC_MAX_WALKERS = 65536
 
 STATUS_NAMES = {
     DMC_OK: "ok",
@@ -33,6 +35,7 @@ STATUS_NAMES = {
     DMC_ERR_SETUP: "table set-up failed",
     DMC_ERR_EMPTY: "population died out",
     DMC_ERR_NOMEM: "out of memory",
+    DMC_ERR_NOALLOC_LIMIT: "size above the no-allocation scratch maximum",
 }
 
 
@@ -140,6 +143,12 @@ class Walkers(C.Structure):
         ("is_", C.POINTER(C.c_int)),
         ("irn", C.POINTER(C.c_int64)),
     ]
+
+
+class DevStack(C.Structure):
+    """dmc_dev_stack: a walker stack in caller-owned device memory."""
+    _fields_ = [(k, C.c_void_p) for k in ("x", "dpsi", "dpsig", "psil", "psigl", "d2psi", "d2psig", "v", "vext",
+                                          "weight", "psil0", "psigl0", "wt0", "is_", "irn")]
 
 
 def _set(struct, name, value):

@@ -23,7 +23,7 @@ EXPORTS = [
     "dmc_matinv_batch", "dmc_bcsone_batch", "dmc_getphione_batch", "dmc_getderbcs_batch", "dmc_init_walkers",
     "dmc_load_walkers", "dmc_get_walkers", "dmc_initial_eval", "dmc_num_walkers", "dmc_step", "dmc_branch",
     "dmc_generation", "dmc_zero_estimators", "dmc_get_estimators", "dmc_block_update", "dmc_get_wtisto",
-    "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers",
+    "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers", "dmc_branch_noalloc",
 ]
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -88,6 +88,8 @@ def load(path=LIB_PATH):
     L.dmc_timed_generations.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64),
                                         C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.dmc_put_walkers.argtypes = [vp, C.POINTER(Walkers)]
+    L.dmc_branch_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(abi.DevStack),
+                                     C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
     _lib = L
     return L
 

@@ -330,6 +330,7 @@ const char* dmc_status_string(int s)
     case DMC_ERR_SETUP: return "table set-up failed";
     case DMC_ERR_EMPTY: return "population died out";
     case DMC_ERR_NOMEM: return "out of memory";
+    case DMC_ERR_NOALLOC_LIMIT: return "size above the no-allocation scratch maximum";
     }
     return "unknown status";
 }

@@ -52,6 +52,11 @@ extern "C" {
 #define DMC_ERR_SETUP 5        /* table setup failed (rungekutta.f90:85-88, kshell.f90:137-140) */
 #define DMC_ERR_EMPTY 6        /* population died out */
 #define DMC_ERR_NOMEM 7        /* device or host allocation failed */
+#define DMC_ERR_NOALLOC_LIMIT 8 /* size above the fixed scratch of dmc_branch_noalloc */
+
+/* Largest population dmc_branch_noalloc accepts (input walkers and output
+ * capacity): its scratch is a fixed device array sized for this many. */
+#define DMC_NOALLOC_MAX_WALKERS 65536
 
 /*
  * System description: the deck values read by setpsi, setupbcs, setbeta and
@@ -286,6 +291,41 @@ int dmc_timed_generations(dmc_ctx* ctx, int ngen, int opcomp_last, int flush_l2,
  * hosts that keep the walker stacks in their own memory (stack.f90:82-110)
  * and hand them to the GPU for each generation. */
 int dmc_put_walkers(dmc_ctx* ctx, const dmc_walkers* w);
+
+/* A walker stack in device memory owned by the caller (all pointers are
+ * device pointers; the layout is the library's own device layout). */
+typedef struct dmc_dev_stack {
+    double *x, *dpsi, *dpsig;   /* [cap][npart][3] */
+    double *psil, *psigl, *d2psi, *d2psig, *v, *vext, *weight, *psil0, *psigl0;   /* [cap] */
+    float* wt0;                 /* [cap] */
+    int* is;                    /* [cap] */
+    uint64_t* irn;              /* [cap] 48-bit random states */
+} dmc_dev_stack;
+
+/* No counterpart in the reference: this is the branching step of dmc_branch
+ * for callers that may not allocate GPU memory.  Some hosts keep their walker
+ * stacks in device memory that another allocator owns (a Fortran host with
+ * its own device arrays, a memory pool) and must not call cudaMalloc or
+ * cudaFree inside the walker loop, where an allocation would synchronise the
+ * device and fragment the pool.  This call allocates nothing: the caller
+ * passes the input stack `in` (n walkers, popped from the top as in
+ * step.f90:287-315) and the output stack `out` (room for cap walkers), and the
+ * copy counts, prefix offsets and advanced random states live in one
+ * file-scope device array of about 1 MB that every GPU loading the library
+ * keeps until the process exits.
+ *  - n and cap must not exceed DMC_NOALLOC_MAX_WALKERS (else
+ *    DMC_ERR_NOALLOC_LIMIT, nothing launched); more than cap copies gives
+ *    DMC_ERR_OVERFLOW with *nout = cap.
+ *  - wtisto: optional device array of DMC_WTISTO counters, incremented like
+ *    the reference's multiplicity histogram; NULL to skip it.
+ *  - The first call on a device looks up that device's scratch address; make
+ *    that first call before any stream capture.  The call waits on `stream`
+ *    (a cudaStream_t, NULL for the default stream) to read the new count.
+ *  - All calls share the scratch and every value in it is written before it
+ *    is read within a call, so nothing needs clearing; calls that overlap on
+ *    the GPU (other streams, other host threads) race on it. */
+int dmc_branch_noalloc(int n, int npart, int cap, double factor, const dmc_dev_stack* in,
+                       const dmc_dev_stack* out, uint64_t* wtisto, int* nout, void* stream);
 
 #ifdef __cplusplus
 }
