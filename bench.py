@@ -22,7 +22,6 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -38,6 +37,11 @@ WORKLOAD = "n66"
 # (profiles/walker_kernel_n66_fp64.md: dram__bytes_read.sum +
 # dram__bytes_write.sum = 2.42 MB for one step launch over ~512 walkers).
 NCU_TRAFFIC_BYTES_PER_WALKER = 4730.0
+
+# FP32 flops (FFMA = 2, FADD/FMUL = 1) executed per walker-step by the mixed
+# walker kernel, from the instruction counters of one ncu capture
+# (profiles/walker_kernel_n66_mixed.md).  None until captured.
+MIXED_FP32_FLOPS_PER_WALKER = None
 
 
 def algorithmic_flops(nup, ndn, nd, K, npart):
@@ -183,6 +187,96 @@ def run_reference(args):
     return 0
 
 
+def time_path(ctx, args, world, local, barrier):
+    """W warm-up and K timed generations on one context; device time from
+    CUDA events around every generation (L2 flushed between them)."""
+    import torch
+
+    for _ in range(max(args.warmup, 3)):
+        ctx.timed_generations(1, opcomp_last=False, flush_l2=True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    steps, dev_ms, kern_ms, launches = 0, 0.0, 0.0, 0
+    for g in range(args.steps):
+        s, ms, nl = ctx.timed_generations(1, opcomp_last=(g == args.steps - 1), flush_l2=True)
+        steps += s
+        dev_ms += ms
+        launches += nl
+        kern_ms += ctx.last_step_ms()
+    barrier()
+    clocks = sampler.stop()
+    t_max, steps_all = dev_ms, steps
+    if world > 1:
+        t = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+        s_t = torch.tensor([steps], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(s_t)
+        steps_all = int(s_t.item())
+    return {"value": steps_all / (t_max * 1e-3), "ms_per_step": t_max / max(args.steps, 1), "steps": steps,
+            "kern_ms": kern_ms / max(args.steps, 1), "avg_n": steps / max(args.steps, 1), "launches": launches,
+            "clocks": clocks}
+
+
+def e2e_rate(ctx, info, args, world, barrier):
+    """The same generations through the C ABI with the walker state in pinned
+    host memory: dmc_put_walkers, dmc_generation, dmc_get_walkers and the
+    estimator sums every generation."""
+    import torch
+
+    cap = info.capacity
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    host = {k: pin((cap, info.npart, 3), torch.float64) for k in ("x", "dpsi", "dpsig")}
+    for k in ("psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0", "psigl0", "wt0"):
+        host[k] = pin((cap,), torch.float64)
+    host["is_"] = pin((cap,), torch.int32)
+    host["irn"] = pin((cap,), torch.int64)
+    host["cap"] = cap
+    n_cur = ctx.get_walkers_into(host)
+    per_walker = 3 * 3 * info.npart * 8 + 10 * 8 + 8 + 4 + 8     # x, dpsi, dpsig, 10 doubles, wt0, is, irn
+    nsteps = max(1, min(args.steps, args.e2e_steps))
+    h2d = d2h = 0
+    barrier()
+    t0 = time.perf_counter()
+    for g in range(nsteps):
+        ctx.put_walkers(dict(host, n=n_cur))
+        h2d += n_cur * per_walker
+        ctx.generation(g == nsteps - 1)
+        n_new = ctx.get_walkers_into(host)
+        d2h += n_new * per_walker + 3 * info.nest * 8
+        ctx.estimators()
+        n_cur = n_new
+    barrier()
+    t = time.perf_counter() - t0
+    total = h2d // per_walker                  # walkers entering each generation
+    rate = total / t
+    if world > 1:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        s_t = torch.tensor([total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(s_t)
+        rate = float(s_t.item()) / float(tt.item())
+    return {"value": rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d / nsteps),
+            "d2h_bytes_per_step": int(d2h / nsteps), "steps": nsteps,
+            "path": "dmc_put_walkers + dmc_generation + dmc_get_walkers + dmc_get_estimators, pinned host"}
+
+
+def accuracy_vs_fp64(ctx_mixed, ctx_fp64, hbar, nmax=512):
+    """Per-configuration local-energy error of the mixed path against the
+    FP64 path on the mixed run's current walkers."""
+    w = ctx_mixed.walkers()
+    x = w["x"][:nmax]
+    a = ctx_mixed.hpsi(x)
+    b = ctx_fp64.hpsi(x)
+    ea = -hbar * a["d2psi"] + a["v"]
+    eb = -hbar * b["d2psi"] + b["v"]
+    rel = np.abs(ea - eb) / np.maximum(np.abs(eb), 1.0)
+    dr = np.max(np.abs(a["dpsi"] - b["dpsi"]), axis=(1, 2)) / np.maximum(np.max(np.abs(b["dpsi"]), axis=(1, 2)), 1.0)
+    return {"configs": int(x.shape[0]), "el_rel_err_max": float(rel.max()), "el_rel_err_median": float(np.median(rel)),
+            "drift_rel_err_max": float(dr.max()), "log_psi_abs_err_max": float(np.max(np.abs(a["psil"] - b["psil"])))}
+
+
 def run_gpu(args):
     import torch
 
@@ -197,100 +291,60 @@ def run_gpu(args):
     B.build()
     from dmcbcs_project_gb300 import capi, configs
 
-    nup, ndn, norb, nwalk, dt, _ = configs.WORKLOADS[WORKLOAD]
-    nwalk = args.walkers or nwalk
-    sysd, rund, _ = configs.workload(WORKLOAD, nwalk=nwalk)
-    rund.seed = 17 + 1000003 * rank                     # independent replica per GPU
-    ctx = capi.Context(sysd, rund)
-    info = ctx.info
-    ctx.init_walkers()
-    ctx.initial_eval()
-    # warm-up generations
-    for _ in range(max(args.warmup, 3)):
-        ctx.timed_generations(1, opcomp_last=False, flush_l2=True)
-
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    sampler = ClockSampler(local)
-    sampler.start()
-    barrier()
-    steps, dev_ms, kern_ms, launches, nsum = 0, 0.0, 0.0, 0, 0
-    for g in range(args.steps):
-        s, ms, nl = ctx.timed_generations(1, opcomp_last=(g == args.steps - 1), flush_l2=True)
-        steps += s
-        dev_ms += ms
-        launches += nl
-        kern_ms += ctx.last_step_ms()
-        nsum += s
-    barrier()
-    clocks = sampler.stop()
-    t_max = dev_ms
-    steps_all = steps
-    if world > 1:
-        t = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-        s_t = torch.tensor([steps], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(s_t)
-        steps_all = int(s_t.item())
-    value = steps_all / (t_max * 1e-3)
+    nup, ndn, norb, nwalk, dt, _ = configs.WORKLOADS[WORKLOAD]
+    nwalk = args.walkers or nwalk
+    sysd, rund, _ = configs.workload(WORKLOAD, nwalk=nwalk)
+    rund.seed = 17 + 1000003 * rank                     # independent replica per GPU
+    precisions = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
+    ctxs, res = {}, {}
+    for prec in precisions:
+        ctx = capi.Context(sysd, rund, precision=prec)
+        ctx.init_walkers()
+        ctx.initial_eval()
+        res[prec] = time_path(ctx, args, world, local, barrier)
+        ctxs[prec] = ctx
+    head = precisions[0]
+    ctx = ctxs[head]
+    info = ctx.info
+    e2e = e2e_rate(ctx, info, args, world, barrier)
 
-    # ---- end to end through the C ABI with host buffers --------------------
-    # the host owns the walker stacks (as the reference's Fortran host does)
-    # and hands the full walker state to the GPU for every generation
-    cap = info.capacity
-    n3 = 3 * info.npart
-    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
-    host = {k: pin((cap, info.npart, 3), torch.float64) for k in ("x", "dpsi", "dpsig")}
-    for k in ("psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0", "psigl0", "wt0"):
-        host[k] = pin((cap,), torch.float64)
-    host["is_"] = pin((cap,), torch.int32)
-    host["irn"] = pin((cap,), torch.int64)
-    host["cap"] = cap
-    n_cur = ctx.get_walkers_into(host)
-    per_walker = 3 * n3 * 8 + 10 * 8 + 8 + 4 + 8     # x, dpsi, dpsig, 10 doubles, wt0, is, irn
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
-    h2d = d2h = 0
-    barrier()
-    t0 = time.perf_counter()
-    for g in range(e2e_steps):
-        ctx.put_walkers(dict(host, n=n_cur))
-        h2d += n_cur * per_walker
-        ctx.generation(g == e2e_steps - 1)
-        n_new = ctx.get_walkers_into(host)
-        d2h += n_new * per_walker + 3 * info.nest * 8
-        ctx.estimators()
-        n_cur = n_new
-    barrier()
-    t_e2e = time.perf_counter() - t0
-    e2e_total_steps = h2d // per_walker          # walkers entering each generation
-    e2e_rate = e2e_total_steps / t_e2e
-    if world > 1:
-        t = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        s_t = torch.tensor([e2e_total_steps], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(s_t)
-        e2e_rate = float(s_t.item()) / float(t.item())
-
-    # ---- roofline of the walker kernel ---------------------------------------
-    avg_n = nsum / max(args.steps, 1)
     flops_alg = algorithmic_flops(info.nup, info.ndn, info.nd, info.ncol, info.npart)
     flops_exe = executed_flops(info.nup, info.ndn, info.nd, info.ncol, info.npart, info.nk, info.nup * info.ndn)
-    kern_avg_ms = kern_ms / max(args.steps, 1)
-    achieved = flops_alg * avg_n / (kern_avg_ms * 1e-3) / 1e12
-    peak = fp64_peak_tflops(torch) if rank == 0 else None
-    roofline = {
-        "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-        "frac": (achieved / peak) if peak else None,
-        "traffic": (NCU_TRAFFIC_BYTES_PER_WALKER * avg_n) if NCU_TRAFFIC_BYTES_PER_WALKER else None,
-        "kernel": "walker_kernel", "kernel_ms_per_launch": kern_avg_ms, "walkers_per_launch": avg_n,
-        "algorithmic_flops_per_walker_step": flops_alg, "executed_flops_per_walker_step": flops_exe,
-        "executed_achieved": flops_exe * avg_n / (kern_avg_ms * 1e-3) / 1e12,
-        "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (the measured-peaks file has no FP64 figure)",
-    }
+    peak64 = capi.probe_peak("fp64") if rank == 0 else None
+    peak32 = capi.probe_peak("fp32") if rank == 0 else None
+    dgemm = fp64_peak_tflops(torch) if rank == 0 else None
+
+    def roofline(prec):
+        r = res[prec]
+        kms = r["kern_ms"]
+        alg = flops_alg * r["avg_n"] / (kms * 1e-3) / 1e12
+        if prec == "fp64":
+            return {"bound": "fp64", "achieved": alg, "peak": dgemm, "unit": "TFLOP/s",
+                    "frac": alg / dgemm if dgemm else None,
+                    "traffic": NCU_TRAFFIC_BYTES_PER_WALKER * r["avg_n"] if NCU_TRAFFIC_BYTES_PER_WALKER else None,
+                    "kernel": "walker_kernel<double>", "kernel_ms_per_launch": kms, "walkers_per_launch": r["avg_n"],
+                    "algorithmic_flops_per_walker_step": flops_alg, "executed_flops_per_walker_step": flops_exe,
+                    "executed_achieved": flops_exe * r["avg_n"] / (kms * 1e-3) / 1e12,
+                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the measured-peaks "
+                                   "file); DFMA probe " + (f"{peak64:.3f}" if peak64 else "-") + " TFLOP/s"}
+        ex = MIXED_FP32_FLOPS_PER_WALKER
+        return {"bound": "fp32", "achieved": (ex * r["avg_n"] / (kms * 1e-3) / 1e12) if ex else None,
+                "peak": peak32, "unit": "TFLOP/s",
+                "frac": (ex * r["avg_n"] / (kms * 1e-3) / 1e12 / peak32) if (ex and peak32) else None,
+                "traffic": NCU_TRAFFIC_BYTES_PER_WALKER * r["avg_n"] if NCU_TRAFFIC_BYTES_PER_WALKER else None,
+                "kernel": "walker_kernel<df>", "kernel_ms_per_launch": kms, "walkers_per_launch": r["avg_n"],
+                "executed_fp32_flops_per_walker_step": ex,
+                "fp64_equivalent": {"achieved": alg, "peak": dgemm,
+                                    "frac": alg / dgemm if dgemm else None,
+                                    "algorithmic_flops_per_walker_step": flops_alg},
+                "peak_source": "FFMA throughput probe measured in this run (no FP32 figure in the measured-peaks file)"}
+
+    acc = accuracy_vs_fp64(ctxs["mixed"], ctxs["fp64"], sysd.hbar) if len(ctxs) == 2 and rank == 0 else None
 
     if rank == 0:
         cpu = None
@@ -300,25 +354,32 @@ def run_gpu(args):
             cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{gens} DMC generations of {args.cpu_walkers} walkers of the same N=66 system "
                              f"({st} walker-steps, {el:.1f} s) on {threads} host threads"}
+        r = res[head]
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": t_max / max(args.steps, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "impl": "gb300-fp64",
-            "config": {"workload": "dmc_n66_33u33d", "walkers": nwalk, "avg_walkers": avg_n, "idmc": 1,
-                       "dt_efg": dt, "shells": norb, "ncol": info.ncol, "nd": info.nd,
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "df32+f32 (f64 move/weights)" if head == "mixed" else "f64", "data": "synthetic",
+            "impl": f"gb300-{head}",
+            "config": {"workload": "dmc_n66_33u33d", "walkers": nwalk, "avg_walkers": r["avg_n"], "idmc": 1,
+                       "dt_efg": dt, "shells": norb, "ncol": info.ncol, "nd": info.nd, "precision": head,
                        "l2": "2xL2 buffer written between timed generations",
                        "parallelism": f"replicas{world}"},
-            "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d / e2e_steps),
-                    "d2h_bytes_per_step": int(d2h / e2e_steps), "steps": e2e_steps,
-                    "path": "dmc_put_walkers + dmc_generation + dmc_get_walkers + dmc_get_estimators, pinned host"},
-            "gpu_launches": launches,
-            "clocks": clocks,
-            "roofline": roofline,
+            "e2e": e2e,
+            "gpu_launches": r["launches"],
+            "clocks": r["clocks"],
+            "roofline": roofline(head),
             "cpu_baseline": cpu,
         }
+        if "fp64" in res and head != "fp64":
+            f = res["fp64"]
+            line["fp64_path"] = {"value": f["value"], "ms_per_step": f["ms_per_step"], "gpu_launches": f["launches"],
+                                 "clocks": f["clocks"], "roofline": roofline("fp64")}
+            line["speedup_vs_fp64"] = r["value"] / f["value"]
+            line["accuracy_vs_fp64"] = acc
         print(json.dumps(line), flush=True)
-    ctx.close()
+    for c in ctxs.values():
+        c.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -330,6 +391,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
+                    help="both: the mixed path is the headline, the FP64 path is timed beside it")
     ap.add_argument("--walkers", type=int, default=None)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-walkers", type=int, default=512)

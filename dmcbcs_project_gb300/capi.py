@@ -24,7 +24,11 @@ EXPORTS = [
     "dmc_load_walkers", "dmc_get_walkers", "dmc_initial_eval", "dmc_num_walkers", "dmc_step", "dmc_branch",
     "dmc_generation", "dmc_zero_estimators", "dmc_get_estimators", "dmc_block_update", "dmc_get_wtisto",
     "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers", "dmc_branch_noalloc",
+    "dmc_set_precision", "dmc_get_precision", "dmc_probe_peak",
 ]
+
+PREC_FP64 = 0
+PREC_MIXED = 1
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -88,16 +92,28 @@ def load(path=LIB_PATH):
     L.dmc_timed_generations.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64),
                                         C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.dmc_put_walkers.argtypes = [vp, C.POINTER(Walkers)]
+    L.dmc_set_precision.argtypes = [vp, C.c_int]
+    L.dmc_probe_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.dmc_get_precision.argtypes = [vp, C.POINTER(C.c_int)]
     L.dmc_branch_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(abi.DevStack),
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
     _lib = L
     return L
 
 
+def probe_peak(kind):
+    """Measured FMA throughput (TFLOP/s) of the FP64 ('fp64') or FP32 ('fp32') pipe."""
+    v = C.c_double()
+    st = load().dmc_probe_peak({"fp64": 0, "fp32": 1}[kind], C.byref(v))
+    if st != abi.DMC_OK:
+        raise DMCError(st, "dmc_probe_peak")
+    return v.value
+
+
 class Context:
     """One system and run on the current CUDA device (``dmc_create``)."""
 
-    def __init__(self, sysdesc, rundesc):
+    def __init__(self, sysdesc, rundesc, precision="fp64"):
         L = load()
         h = C.c_void_p()
         st = L.dmc_create(C.byref(sysdesc), C.byref(rundesc), C.byref(h))
@@ -110,6 +126,13 @@ class Context:
         self.nd = self.info.nd
         self.nest = self.info.nest
         self.norb = int(sysdesc.norb)
+        self.set_precision(precision)
+
+    def set_precision(self, precision):
+        """'fp64' (plain FP64) or 'mixed' (double-float determinant, FP32 Jastrow)."""
+        code = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[precision]
+        self._check(load().dmc_set_precision(self._h, code))
+        self.precision = precision
 
     def close(self):
         if getattr(self, "_h", None):

@@ -110,6 +110,10 @@ struct dmc_ctx {
     DevBuf<KVecDev> kv;
     DevBuf<TabUD> tud;
     DevBuf<TabSS> tss;
+    DevBuf<KVecMP> kv_mp;
+    DevBuf<TabUDmp> tud_mp;
+    DevBuf<TabSSmp> tss_mp;
+    int precision = DMC_PREC_FP64;
     DevBuf<unsigned long long> jumpA, jumpC;
     DevBuf<double> gscratch;
     // population
@@ -166,6 +170,7 @@ void fill_params(dmc_ctx* c)
     p.nd = S.nd; p.nk = S.nk; p.ncol = S.ncol; p.norb = S.norb; p.ntab = S.ntab; p.nmax = S.nmax;
     p.ieq = S.ieq; p.nobeta = S.nobeta; p.cutdrift = S.cutdrift; p.fn = c->rd.fn; p.idmc = c->rd.idmc;
     p.onebody = (S.v0ex != 0.0 || S.v0exjas != 0.0);
+    p.ntab0 = S.ntab0;
     p.nest = nest_for(c->rd.idmc);
     p.nrand = 2 * ((3 * S.npart + 1) / 2);
     p.ldS = S.nd | 1;
@@ -182,6 +187,11 @@ void fill_params(dmc_ctx* c)
     p.hbar = S.hbar; p.a2 = S.a2; p.dt = c->rd.dt; p.etrial = S.etrial; p.wtcut = c->rd.wtcut; p.nfac = S.nfac;
     for (int k = 0; k < 3; ++k) p.qex[k] = S.qex[k];
     p.v0ex = S.v0ex; p.v0exjas = S.v0exjas; p.vorb1 = S.vorb[0];
+    p.el_df = from_double(S.el);
+    p.scaleb_df = from_double(S.scaleb);
+    p.rangeb_df = from_double(S.rangeb);
+    p.range_df = from_double(S.range);
+    p.eli_f = (float)S.eli;
     for (int i = 0; i < DMC_MAX_UNPAIRED; ++i) {
         for (int k = 0; k < 3; ++k) {
             p.akup[i][k] = S.akup[i][k];
@@ -207,6 +217,18 @@ int upload_kv(dmc_ctx* c)
     }
     CK(c->kv.alloc(kv.size()));
     CK(cudaMemcpy(c->kv.p, kv.data(), kv.size() * sizeof(KVecDev), cudaMemcpyHostToDevice));
+    std::vector<KVecMP> km(kv.size());
+    for (size_t q = 0; q < kv.size(); ++q) {
+        std::memset(&km[q], 0, sizeof(KVecMP));
+        for (int k = 0; k < 3; ++k) {
+            km[q].k[k] = from_double(kv[q].k[k]);
+            km[q].n[k] = kv[q].n[k];
+        }
+        km[q].k2 = from_double(kv[q].k2);
+        km[q].v = from_double(kv[q].v);
+    }
+    CK(c->kv_mp.alloc(km.size()));
+    CK(cudaMemcpy(c->kv_mp.p, km.data(), km.size() * sizeof(KVecMP), cudaMemcpyHostToDevice));
     c->P.vorb1 = c->S.vorb[0];
     return DMC_OK;
 }
@@ -225,6 +247,24 @@ int upload_tables(dmc_ctx* c)
     CK(c->tss.alloc(nt));
     CK(cudaMemcpy(c->tud.p, ud.data(), nt * sizeof(TabUD), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->tss.p, ss.data(), nt * sizeof(TabSS), cudaMemcpyHostToDevice));
+    // mixed-precision copies in double-float
+    std::vector<TabUDmp> udm(nt);
+    std::vector<TabSSmp> ssm(nt);
+    for (int i = 0; i < nt; ++i) {
+        std::memset(&udm[i], 0, sizeof(TabUDmp));
+        udm[i].v = from_double(S.vtab[0][i]);
+        udm[i].u = from_double(S.utab[0][i]);
+        udm[i].du = from_double(S.dutab[0][i]);
+        udm[i].d2u = from_double(S.d2utab[0][i]);
+        udm[i].b = from_double(S.btab[i]);
+        udm[i].db = from_double(S.dbtab[i]);
+        udm[i].d2b = from_double(S.d2btab[i]);
+        ssm[i] = TabSSmp{(float)S.vtab[1][i], (float)S.utab[1][i], (float)S.dutab[1][i], (float)S.d2utab[1][i]};
+    }
+    CK(c->tud_mp.alloc(nt));
+    CK(c->tss_mp.alloc(nt));
+    CK(cudaMemcpy(c->tud_mp.p, udm.data(), nt * sizeof(TabUDmp), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->tss_mp.p, ssm.data(), nt * sizeof(TabSSmp), cudaMemcpyHostToDevice));
     // LCG jump tables for t = 0..nrand+1 steps of ran1
     const int nj = c->P.nrand + 2;
     std::vector<unsigned long long> A(nj), C(nj);
@@ -248,6 +288,9 @@ KernelArgs base_args(dmc_ctx* c)
     a.kv = c->kv.p;
     a.tud = c->tud.p;
     a.tss = c->tss.p;
+    a.kv_mp = c->kv_mp.p;
+    a.tud_mp = c->tud_mp.p;
+    a.tss_mp = c->tss_mp.p;
     a.jumpA = c->jumpA.p;
     a.jumpC = c->jumpC.p;
     a.gscratch = c->gscratch.p;
@@ -267,7 +310,7 @@ int run_eval(dmc_ctx* c, int mode, int nw, const double* dx, double* psil, int* 
     a.xin = dx;
     a.o_psil = psil; a.o_is = is; a.o_dpsi = dpsi; a.o_d2psi = d2psi; a.o_v = v; a.o_vext = vext;
     a.o_psigl = psigl; a.o_dpsig = dpsig; a.o_d2psig = d2psig; a.o_sinv = sinv;
-    CK(launch_walker(c->P, a, c->L, grid_for(c, nw), st));
+    CK(launch_walker(c->P, a, c->L, grid_for(c, nw), st, c->precision == DMC_PREC_MIXED));
     return DMC_OK;
 }
 
@@ -423,7 +466,8 @@ int dmc_destroy(dmc_ctx* c)
 {
     if (!c) return DMC_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    c->kv.release(); c->tud.release(); c->tss.release(); c->jumpA.release(); c->jumpC.release();
+    c->kv.release(); c->tud.release(); c->tss.release(); c->kv_mp.release(); c->tud_mp.release();
+    c->tss_mp.release(); c->jumpA.release(); c->jumpC.release();
     c->gscratch.release(); c->st[0].release(); c->st[1].release(); c->est.release(); c->counts.release();
     c->offs.release(); c->status.release(); c->irn1.release(); c->wtisto.release(); c->vb.release();
     c->vb2.release(); c->wb.release(); c->bx.release(); c->bpsil.release(); c->bdpsi.release();
@@ -746,7 +790,7 @@ int dmc_step(dmc_ctx* c, int opcomp)
     a.out = c->st[1 - c->istin].view();
     a.est = c->est.p;
     CK(cudaEventRecord(c->ev0, c->stream));
-    CK(launch_walker(c->P, a, c->L, grid_for(c, n), c->stream));
+    CK(launch_walker(c->P, a, c->L, grid_for(c, n), c->stream, c->precision == DMC_PREC_MIXED));
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2.p, c->wb.p, c->stream));
     c->launches += 2;
@@ -942,6 +986,32 @@ int dmc_put_walkers(dmc_ctx* c, const dmc_walkers* w)
     CK(cudaStreamSynchronize(c->stream));
     c->n = n;
     return DMC_OK;
+}
+
+int dmc_set_precision(dmc_ctx* c, int precision)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (precision != DMC_PREC_FP64 && precision != DMC_PREC_MIXED)
+        return fail(c, DMC_ERR_INVALID, "precision must be DMC_PREC_FP64 or DMC_PREC_MIXED");
+    CK(cudaStreamSynchronize(c->stream));
+    c->precision = precision;
+    return DMC_OK;
+}
+
+int dmc_get_precision(const dmc_ctx* c, int* precision)
+{
+    if (!c || !precision) return DMC_ERR_INVALID;
+    *precision = c->precision;
+    return DMC_OK;
+}
+
+int dmc_probe_peak(int kind, double* tflops)
+{
+    if (!tflops || (kind != 0 && kind != 1)) return DMC_ERR_INVALID;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return DMC_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DMC_ERR_CUDA;
+    return probe_fma_peak(kind, nsm, tflops) == cudaSuccess ? DMC_OK : DMC_ERR_CUDA;
 }
 
 }  // extern "C"

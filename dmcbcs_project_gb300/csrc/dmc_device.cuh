@@ -15,6 +15,7 @@
 
 #include <cstdint>
 #include "../../include/dmcbcs_gpu.h"
+#include "dmc_df32.cuh"
 
 namespace dmc {
 
@@ -29,6 +30,23 @@ struct __align__(16) TabUD {
 // grid record for same-spin pairs (no potential, no beta)
 struct __align__(16) TabSS {
     double v, u, du, d2u;
+};
+
+// mixed-precision records, all double-float: the beta values enter the pair
+// matrix, and for close pairs the Jastrow kinetic term and the potential
+// cancel to a few parts in 10^3
+struct __align__(16) TabUDmp {
+    df v, u, du, d2u, b, db, d2b, pad;
+};
+struct __align__(16) TabSSmp {
+    float v, u, du, d2u;
+};
+struct __align__(16) KVecMP {
+    df k[3];
+    df k2;
+    df v;
+    int n[3];
+    int pad;
 };
 
 struct __align__(16) KVecDev {
@@ -50,12 +68,16 @@ enum Mode : int {
 struct DevParams {
     int npart, nup, ndn, npair, nexup, nexdn, nd, nk, ncol, norb, ntab, nmax;
     int ieq, nobeta, cutdrift, fn, idmc, onebody, nest, nrand;
+    int ntab0;            // last non-zero Jastrow grid point (healing distance)
     int ldS, ldU;
     double el, eli, range, scale, rangeb, scaleb;
     double mass[2], sqm[2], imass[2], isqm[2];
     double hbar, a2, dt, etrial, wtcut, nfac;
     double sigma[2], dcut[2];
     double qex[3], v0ex, v0exjas, vorb1;
+    // double-float copies for the mixed-precision kernel
+    df el_df, scaleb_df, rangeb_df, range_df;
+    float eli_f;
     double akup[DMC_MAX_UNPAIRED][3], ak2up[DMC_MAX_UNPAIRED];
     double akdn[DMC_MAX_UNPAIRED][3], ak2dn[DMC_MAX_UNPAIRED];
     int sinup[DMC_MAX_UNPAIRED], sindn[DMC_MAX_UNPAIRED];
@@ -85,6 +107,9 @@ struct KernelArgs {
     const KVecDev* kv;           // [nk]
     const TabUD* tud;            // [ntab+1]
     const TabSS* tss;            // [ntab+1]
+    const KVecMP* kv_mp;         // mixed-precision copies of kv, tud, tss
+    const TabUDmp* tud_mp;
+    const TabSSmp* tss_mp;
     const unsigned long long* jumpA;   // LCG jump-ahead multipliers, [nrand+1]
     const unsigned long long* jumpC;   // LCG jump-ahead increments, [nrand+1]
     double* gscratch;            // per-CTA global scratch when the pair data do not fit on chip
@@ -93,7 +118,7 @@ struct KernelArgs {
 
 // On-chip layout of one walker CTA, offsets in doubles.
 struct SmemLayout {
-    int x, xo, dx, drift, dg, kq, S, pb, R, U, D, E, acc, colk, red, total;
+    int x, xr, xo, dx, drift, dg, kq, S, pb, R, U, D, E, acc, colk, red, total;
     int pb_in_smem;
     int pb_size;          // doubles of pair data per walker
     int rows_jas, rows_beta;   // rows of the up-down block per reduction chunk
@@ -109,6 +134,7 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
     int off = 0;
     auto take = [&](int nd) { int o = off; off += round_up(nd, 2); return o; };
     L.x = take(n3);               // positions being evaluated
+    L.xr = take(n3);              // the same in the kernel's arithmetic type
     L.xo = take(n3);              // old positions (step)
     L.dx = take(n3);              // drift + gaussian displacement (step)
     L.drift = take(n3);           // old drift (step)

@@ -368,7 +368,7 @@ int Setup::build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string&
         d2utab[ic].assign(ntab + 1, 0.0);
     }
     for (int i = 0; i <= ntab; ++i) vtab[0][i] = P.v(sd.v0, i * dr);   // opposite spins only
-    const int ntab0 = (int)(ntab * sd.djas / (0.5 * el));
+    ntab0 = (int)(ntab * sd.djas / (0.5 * el));
     if (ntab0 < 1 || ntab0 > ntab) {
         err = "Jastrow healing distance outside (0, L/2]";
         return DMC_ERR_INVALID;

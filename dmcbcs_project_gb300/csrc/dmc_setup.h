@@ -47,6 +47,7 @@ struct Setup {
     std::vector<double> btab, dbtab, d2btab;
     // Jastrow + potential tables (coshpot.f90), [ic][0..ntab]
     double range = 0, scale = 0, hbarp = 1;
+    int ntab0 = 0;   // grid index of the healing distance
     double cjas[2] = {0, 0};
     bool iop = false, ieq = false;
     std::vector<double> utab[2], dutab[2], d2utab[2], vtab[2];

@@ -1,0 +1,1087 @@
+// Walker kernel stages of the GB300 DMCBS path, templated on the arithmetic
+// of the determinant part:
+//   R = double : the plain FP64 path,
+//   R = df     : the mixed path (pair matrix, inverse and contractions in
+//                double-float on the FP32 pipe; Jastrow and potential in FP32).
+//
+// One CTA of 256 threads owns one walker at a time (persistent grid over
+// the population).  The whole wavefunction evaluation of a walker stays on
+// chip: positions, k-vector records, the nd x nd pair matrix and its
+// inverse, the pair-orbital matrices U (up x K) and D (down x K), the beta
+// pair terms and the reduction scratch.  Global memory is touched only to
+// read the walker, the tables (L2-resident) and to write the results.
+//
+// The reference computes the determinant drift and Laplacian from five
+// GEMMs (psislaterbcs.f90:278-281) and the contractions with the inverse
+// (:211-223).  Here the same quantities come from three products:
+//   S = U D^T (+ beta),  G = D^T-rows . S^-1 (up drift/Laplacian),
+//   H = S^-1 . U (down drift/Laplacian),
+// using that the orbital derivatives are the orbitals of the partner column
+// times k (cos' = -k sin, sin' = k cos) and that the Laplacian is -|k|^2
+// times the orbital: 3 nd^2 K instead of 5 nd^2 K multiply-adds.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "dmc_device.cuh"
+
+namespace dmc {
+namespace walker {
+
+constexpr unsigned long long kMask48 = (1ull << 48) - 1ull;
+constexpr double kTwoM48 = 1.0 / 281474976710656.0;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Deterministic block sum of NV values (fixed tree); the result is returned
+// in v on every thread.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* red)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = warp_sum(v[q]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) red[w * NV + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+        for (int k = 0; k < kWarps; ++k) s += red[k * NV + threadIdx.x];
+        red[kWarps * NV + threadIdx.x] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = red[kWarps * NV + q];
+    __syncthreads();
+}
+
+// 48-bit LCG state after t steps of ran1 (ran.f90:8-27), from jump tables:
+// state_t = A_t * state_0 + C_t (mod 2^48).
+__device__ __forceinline__ unsigned long long lcg_jump(unsigned long long s0, const unsigned long long* A,
+                                                       const unsigned long long* Cc, int t)
+{
+    return (A[t] * s0 + Cc[t]) & kMask48;
+}
+__device__ __forceinline__ double lcg_uniform(unsigned long long s) { return (double)(s | 1ull) * kTwoM48; }
+
+// minimum-image separation component
+__device__ __forceinline__ double min_image(double d, const DevParams& p) { return d - p.el * rint(d * p.eli); }
+__device__ __forceinline__ df min_image(df d, const DevParams& p)
+{
+    const float m = rintf(d.hi * p.eli_f);
+    return d - p.el_df * m;
+}
+
+// ---- precision traits --------------------------------------------------------
+
+template <class R>
+struct Prec;
+template <>
+struct Prec<double> {
+    using J = double;   // Jastrow / potential arithmetic
+    using Tab = TabUD;
+    using TabS = TabSS;
+    using KV = KVecDev;
+    static __device__ const Tab* tud(const KernelArgs& a) { return a.tud; }
+    static __device__ const TabS* tss(const KernelArgs& a) { return a.tss; }
+    static __device__ const KV* kv(const KernelArgs& a) { return a.kv; }
+};
+template <>
+struct Prec<df> {
+    using J = df;
+    using Tab = TabUDmp;
+    using TabS = TabSSmp;
+    using KV = KVecMP;
+    static __device__ const Tab* tud(const KernelArgs& a) { return a.tud_mp; }
+    static __device__ const TabS* tss(const KernelArgs& a) { return a.tss_mp; }
+    static __device__ const KV* kv(const KernelArgs& a) { return a.kv_mp; }
+};
+
+template <class T>
+struct is_df {
+    static constexpr bool value = false;
+};
+template <>
+struct is_df<df> {
+    static constexpr bool value = true;
+};
+
+// convert a double (positions, sincos results) into the arithmetic type
+template <class R>
+__device__ __forceinline__ R from_dbl(double d);
+template <>
+__device__ __forceinline__ double from_dbl<double>(double d) { return d; }
+template <>
+__device__ __forceinline__ df from_dbl<df>(double d) { return from_double(d); }
+
+// x - a*b
+__device__ __forceinline__ double fms(double x, double a, double b) { return fma(-a, b, x); }
+__device__ __forceinline__ df fms(df x, df a, df b)
+{
+    dfacc t{x.hi, x.lo};
+    acc_madd(t, -a, b);
+    return acc_value(t);
+}
+
+// 4-point Lagrange weights on a uniform grid (coshpot.f90:172-179)
+template <class T>
+struct Lagrange {
+    int idx;
+    T c1, c2, c3, c4;
+};
+__device__ __forceinline__ Lagrange<double> lagrange(double r, double scale, int ntab)
+{
+    Lagrange<double> L;
+    double dr = scale * r;
+    int idx = (int)dr;
+    idx = max(1, min(idx, ntab - 2));
+    const double t = dr - (double)idx;
+    const double tm1 = t - 1.0, tm2 = t - 2.0, tp1 = t + 1.0;
+    L.idx = idx;
+    L.c1 = -t * tm1 * tm2 / 6.0;
+    L.c2 = tp1 * tm1 * tm2 / 2.0;
+    L.c3 = -tp1 * t * tm2 / 2.0;
+    L.c4 = tp1 * t * tm1 / 6.0;
+    return L;
+}
+// double-float grid position: index and fraction t = scale*r - idx
+__device__ __forceinline__ int grid_pos(df r, df scale, int ntab, df& frac)
+{
+    const df t = r * scale;
+    int idx = (int)t.hi;
+    df f = fast_two_sum(t.hi - (float)idx, t.lo);
+    if (f.hi < 0.0f) {
+        idx -= 1;
+        f = f + df{1.0f, 0.0f};
+    }
+    const int ic = max(1, min(idx, ntab - 2));
+    if (ic != idx) f = fast_two_sum(t.hi - (float)ic, t.lo);
+    frac = f;
+    return ic;
+}
+__device__ __forceinline__ Lagrange<df> lagrange_df(df t, int idx)
+{
+    Lagrange<df> L;
+    const df tm1 = t - df{1.0f, 0.0f}, tm2 = t - df{2.0f, 0.0f}, tp1 = t + df{1.0f, 0.0f};
+    const df sixth = df{0.16666667163372040f, -4.9670538e-09f};
+    const df p = t * tm1, q = tp1 * tm2;
+    L.idx = idx;
+    L.c1 = -(p * tm2) * sixth;
+    L.c2 = (q * tm1) * 0.5f;
+    L.c3 = -(q * t) * 0.5f;
+    L.c4 = (p * tp1) * sixth;
+    return L;
+}
+// 4-point combination c1 a0 + c2 a1 + c3 a2 + c4 a3 with one lazy accumulator
+__device__ __forceinline__ df lag4(const Lagrange<df>& W, df a0, df a1, df a2, df a3)
+{
+    dfacc s;
+    acc_init(s);
+    acc_madd(s, W.c1, a0);
+    acc_madd(s, W.c2, a1);
+    acc_madd(s, W.c3, a2);
+    acc_madd(s, W.c4, a3);
+    return acc_value(s);
+}
+__device__ __forceinline__ Lagrange<float> lagrange_f(float t, int idx)
+{
+    Lagrange<float> L;
+    const float tm1 = t - 1.0f, tm2 = t - 2.0f, tp1 = t + 1.0f;
+    L.idx = idx;
+    L.c1 = -t * tm1 * tm2 * (1.0f / 6.0f);
+    L.c2 = tp1 * tm1 * tm2 * 0.5f;
+    L.c3 = -tp1 * t * tm2 * 0.5f;
+    L.c4 = tp1 * t * tm1 * (1.0f / 6.0f);
+    return L;
+}
+
+template <class R>
+struct Ctx {
+    const DevParams& p;
+    const KernelArgs& a;
+    const SmemLayout& L;
+    double* sm;
+    double* pb;
+};
+
+// typed views of the shared-memory regions
+template <class T>
+__device__ __forceinline__ T* at(double* sm, int off) { return reinterpret_cast<T*>(sm + off); }
+
+// ---------------------------------------------------------------------------
+// Stage 1: Jastrow + potential over all pairs (coshpot.f90:154-205) fused with
+// the beta pair function (psislaterbcs.f90:283-293, betafun.f90:173-194).
+// Up-down pairs are processed in row chunks; each pair stores its Jastrow
+// gradient vector g = dx * u'/r, whose row sums (up) and column sums (down)
+// are taken in a fixed order.  Writes S[i][j] = beta(r_ij) and the beta pair
+// terms (f'/r, lap f) to pb.  Accumulates per-thread sums of u, v and the
+// pair Laplacian part.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ void pair_stage(const Ctx<R>& c, double& su, double& sv, double& sd2)
+{
+    using J = typename Prec<R>::J;
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const R* x = at<R>(sm, c.L.xr);
+    R* S = at<R>(sm, c.L.S);
+    J* pv = at<J>(sm, c.L.R);
+    R* pb = reinterpret_cast<R*>(c.pb);
+    double* du = sm + c.L.acc + 4 * p.npart;
+    const int nup = p.nup, ndn = p.ndn, ldS = p.ldS;
+    const auto* tud = Prec<R>::tud(c.a);
+    const double imu_ud = 1.0 / (p.mass[0] * p.mass[1] / (p.mass[0] + p.mass[1]));
+    const R imu_df = from_dbl<R>(imu_ud);
+    (void)imu_df;
+    for (int i = threadIdx.x; i < 3 * p.npart; i += kThreads) du[i] = 0.0;
+    // per-thread partial sums in the Jastrow type
+    J tu = rzero<J>(), tv = rzero<J>(), td = rzero<J>();
+    __syncthreads();
+    for (int r0 = 0; r0 < nup; r0 += c.L.rows_jas) {
+        const int r1 = min(nup, r0 + c.L.rows_jas);
+        const int npc = (r1 - r0) * ndn;
+        for (int q = threadIdx.x; q < npc; q += kThreads) {
+            const int i = r0 + q / ndn, j = q % ndn;
+            const R* xi = x + 3 * i;
+            const R* xj = x + 3 * (nup + j);
+            const R d0 = min_image(xi[0] - xj[0], p);
+            const R d1 = min_image(xi[1] - xj[1], p);
+            const R d2 = min_image(xi[2] - xj[2], p);
+            const R rb = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
+            const R rinv = rcp(rb);
+            J g0 = rzero<J>(), g1 = rzero<J>(), g2 = rzero<J>();
+            R f = rzero<R>(), dfr = rzero<R>(), d2f = rzero<R>();
+            if constexpr (!is_df<R>::value) {
+                // FP64: the reference's arithmetic (tiny clamp, separate grids)
+                const double r = fmax(rb, 1.0e-14);
+                if (r < p.range) {
+                    const Lagrange<double> W = lagrange(r, p.scale, p.ntab);
+                    const TabUD* T = c.a.tud + (W.idx - 1);
+                    const TabUD A0 = T[0], A1 = T[1], A2 = T[2], A3 = T[3];
+                    const double vp = W.c1 * A0.v + W.c2 * A1.v + W.c3 * A2.v + W.c4 * A3.v;
+                    const double uj = W.c1 * A0.u + W.c2 * A1.u + W.c3 * A2.u + W.c4 * A3.u;
+                    const double duj = W.c1 * A0.du + W.c2 * A1.du + W.c3 * A2.du + W.c4 * A3.du;
+                    const double d2uj = W.c1 * A0.d2u + W.c2 * A1.d2u + W.c3 * A2.d2u + W.c4 * A3.d2u;
+                    const double ri = (r == rb) ? rinv : 1.0 / r;
+                    tv += vp;
+                    tu += uj;
+                    const double gf = duj * ri;
+                    g0 = d0 * gf;
+                    g1 = d1 * gf;
+                    g2 = d2 * gf;
+                    td += (d2uj + 2.0 * gf) * imu_ud;
+                }
+                if (!p.nobeta && !(rb > p.rangeb)) {
+                    const Lagrange<double> W = lagrange(rb, p.scaleb, p.ntab);
+                    const TabUD* T = c.a.tud + (W.idx - 1);
+                    const TabUD A0 = T[0], A1 = T[1], A2 = T[2], A3 = T[3];
+                    f = W.c1 * A0.b + W.c2 * A1.b + W.c3 * A2.b + W.c4 * A3.b;
+                    const double df_ = W.c1 * A0.db + W.c2 * A1.db + W.c3 * A2.db + W.c4 * A3.db;
+                    d2f = W.c1 * A0.d2b + W.c2 * A1.d2b + W.c3 * A2.d2b + W.c4 * A3.d2b;
+                    dfr = df_ * rinv;
+                }
+            } else {
+                // mixed: one double-float grid position for beta and Jastrow.
+                // Inside the healing distance the Jastrow kinetic term and the
+                // potential nearly cancel, so both stay in double-float there;
+                // beyond it the Jastrow is exactly zero and only the
+                // exponentially small potential tail is left (FP32).
+                const bool in_j = rb.hi < p.range_df.hi;
+                const bool in_b = !p.nobeta && !(rb.hi > p.rangeb_df.hi);
+                if (in_j || in_b) {
+                    df t;
+                    const int idx = grid_pos(rb, p.scaleb_df, p.ntab, t);
+                    const auto* T = tud + (idx - 1);
+                    const auto A0 = T[0], A1 = T[1], A2 = T[2], A3 = T[3];
+                    const Lagrange<df> W = lagrange_df(t, idx);
+                    if (in_j) {
+                        if (idx - 1 <= p.ntab0) {
+                            const df vp = lag4(W, A0.v, A1.v, A2.v, A3.v);
+                            const df uj = lag4(W, A0.u, A1.u, A2.u, A3.u);
+                            const df duj = lag4(W, A0.du, A1.du, A2.du, A3.du);
+                            const df d2uj = lag4(W, A0.d2u, A1.d2u, A2.d2u, A3.d2u);
+                            const df gf = duj * rinv;
+                            tv += vp;
+                            tu += uj;
+                            g0 = d0 * gf;
+                            g1 = d1 * gf;
+                            g2 = d2 * gf;
+                            td += (d2uj + gf * 2.0f) * imu_df;
+                        } else {
+                            const float vp = W.c1.hi * A0.v.hi + W.c2.hi * A1.v.hi + W.c3.hi * A2.v.hi +
+                                             W.c4.hi * A3.v.hi;
+                            tv += df{vp, 0.0f};
+                        }
+                    }
+                    if (in_b) {
+                        f = lag4(W, A0.b, A1.b, A2.b, A3.b);
+                        const df df_ = lag4(W, A0.db, A1.db, A2.db, A3.db);
+                        d2f = lag4(W, A0.d2b, A1.d2b, A2.d2b, A3.d2b);
+                        dfr = df_ * rinv;
+                    }
+                }
+            }
+            S[i * ldS + j] = f;
+            R* pbq = pb + 2 * (i * ndn + j);
+            pbq[0] = dfr;
+            pbq[1] = d2f;
+            pv[3 * q + 0] = g0;
+            pv[3 * q + 1] = g1;
+            pv[3 * q + 2] = g2;
+        }
+        __syncthreads();
+        // row sums -> up particles (+), column sums -> down particles (-);
+        // one thread per (particle, component)
+        const int nr = r1 - r0;
+        for (int tc = threadIdx.x; tc < 3 * (nr + ndn); tc += kThreads) {
+            const int t = tc / 3, cmp = tc % 3;
+            typename AccOf<J>::type sacc;
+            acc_init(sacc);
+            if (t < nr) {
+                const J* row = pv + 3 * (t * ndn) + cmp;
+                for (int j = 0; j < ndn; ++j) acc_add(sacc, row[3 * j]);
+                du[3 * (r0 + t) + cmp] += to_double(acc_value(sacc)) * p.isqm[0];
+            } else {
+                const int j = t - nr;
+                for (int r = 0; r < nr; ++r) acc_add(sacc, pv[3 * (r * ndn + j) + cmp]);
+                du[3 * (nup + j) + cmp] -= to_double(acc_value(sacc)) * p.isqm[1];
+            }
+        }
+        __syncthreads();
+    }
+    su += to_double(tu);
+    sv += to_double(tv);
+    sd2 += to_double(td);
+    if (!p.ieq) return;
+    // same-spin pairs (coshpot.f90:167 with cjas(2) != 0): up-up then down-down,
+    // in FP64 on both paths (off the benchmark configurations)
+    const double* xd = sm + c.L.x;
+    for (int blk = 0; blk < 2; ++blk) {
+        const int n = blk == 0 ? nup : ndn;
+        const int base = blk == 0 ? 0 : nup;
+        const double imu = 1.0 / (p.mass[blk] * 0.5);
+        const double isq = p.isqm[blk];
+        if (n < 2) continue;
+        double* pvd = sm + c.L.R;
+        const int rows = max(1, c.L.rsize / (3 * n));
+        for (int r0 = 0; r0 < n; r0 += rows) {
+            const int r1 = min(n, r0 + rows);
+            const int npc = (r1 - r0) * n;
+            for (int q = threadIdx.x; q < npc; q += kThreads) {
+                const int i = r0 + q / n, j = q % n;
+                double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+                if (j > i) {
+                    const double* xi = xd + 3 * (base + i);
+                    const double* xj = xd + 3 * (base + j);
+                    const double d0 = min_image(xi[0] - xj[0], p);
+                    const double d1 = min_image(xi[1] - xj[1], p);
+                    const double d2 = min_image(xi[2] - xj[2], p);
+                    const double r = fmax(sqrt(d0 * d0 + d1 * d1 + d2 * d2), 1.0e-14);
+                    if (r < p.range) {
+                        const Lagrange<double> W = lagrange(r, p.scale, p.ntab);
+                        const TabSS* T = c.a.tss + (W.idx - 1);
+                        const TabSS A0 = T[0], A1 = T[1], A2 = T[2], A3 = T[3];
+                        const double uj = W.c1 * A0.u + W.c2 * A1.u + W.c3 * A2.u + W.c4 * A3.u;
+                        const double duj = W.c1 * A0.du + W.c2 * A1.du + W.c3 * A2.du + W.c4 * A3.du;
+                        const double d2uj = W.c1 * A0.d2u + W.c2 * A1.d2u + W.c3 * A2.d2u + W.c4 * A3.d2u;
+                        const double vp = W.c1 * A0.v + W.c2 * A1.v + W.c3 * A2.v + W.c4 * A3.v;
+                        const double ri = 1.0 / r;
+                        sv += vp;
+                        su += uj;
+                        const double gf = duj * ri;
+                        g0 = d0 * gf;
+                        g1 = d1 * gf;
+                        g2 = d2 * gf;
+                        sd2 += (d2uj + 2.0 * gf) * imu;
+                    }
+                }
+                pvd[3 * q + 0] = g0;
+                pvd[3 * q + 1] = g1;
+                pvd[3 * q + 2] = g2;
+            }
+            __syncthreads();
+            const int nr = r1 - r0;
+            for (int t = threadIdx.x; t < nr + n; t += kThreads) {
+                double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+                if (t < nr) {
+                    const double* row = pvd + 3 * (t * n);
+                    for (int j = 0; j < n; ++j) {
+                        s0 += row[3 * j];
+                        s1 += row[3 * j + 1];
+                        s2 += row[3 * j + 2];
+                    }
+                    const int i = base + r0 + t;
+                    du[3 * i + 0] += s0 * isq;
+                    du[3 * i + 1] += s1 * isq;
+                    du[3 * i + 2] += s2 * isq;
+                } else {
+                    const int j = t - nr;
+                    for (int r = 0; r < nr; ++r) {
+                        const double* e = pvd + 3 * (r * n + j);
+                        s0 += e[0];
+                        s1 += e[1];
+                        s2 += e[2];
+                    }
+                    du[3 * (base + j) + 0] -= s0 * isq;
+                    du[3 * (base + j) + 1] -= s1 * isq;
+                    du[3 * (base + j) + 2] -= s2 * isq;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// complex product in the arithmetic type
+__device__ __forceinline__ void cmul(double ar, double ai, double br, double bi, double& cr, double& ci)
+{
+    cr = ar * br - ai * bi;
+    ci = ar * bi + ai * br;
+}
+__device__ __forceinline__ void cmul(df ar, df ai, df br, df bi, df& cr, df& ci)
+{
+    dfacc r, i;
+    acc_init(r);
+    acc_init(i);
+    acc_madd(r, ar, br);
+    acc_madd(r, -ai, bi);
+    acc_madd(i, ar, bi);
+    acc_madd(i, ai, br);
+    cr = acc_value(r);
+    ci = acc_value(i);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2: pair orbitals (psislaterbcs.f90:248-277).  exp(i k.x) is built
+// from exp(i 2 pi x_c / L) and its integer powers, so each particle needs
+// three sincos instead of one per k vector.
+// U[i][0] = vorb(1), U[i][2q-1] = v_q cos(k_q.x_i), U[i][2q] = v_q sin(k_q.x_i)
+// D[j][0] = 1,       D[j][2q-1] = cos(k_q.x_j),     D[j][2q] = sin(k_q.x_j)
+// Then the unpaired plane-wave rows and columns of S (:171-206).
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ void orbital_stage(const Ctx<R>& c)
+{
+    using KV = typename Prec<R>::KV;
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const double* x = sm + c.L.x;
+    R* U = at<R>(sm, c.L.U);
+    R* D = at<R>(sm, c.L.D);
+    R* E = at<R>(sm, c.L.E);
+    R* S = at<R>(sm, c.L.S);
+    const KV* kq = reinterpret_cast<const KV*>(sm + c.L.kq);
+    const int np1 = p.nmax + 1;
+    // powers e^{i m theta_c}, m = 0..nmax, E[(p*3+c)*np1 + m] = (re, im)
+    for (int t = threadIdx.x; t < 3 * p.npart; t += kThreads) {
+        double s1d, c1d;
+        sincospi(2.0 * x[t] * p.eli, &s1d, &c1d);
+        const R s1 = from_dbl<R>(s1d), c1 = from_dbl<R>(c1d);
+        R* e = E + 2 * t * np1;
+        e[0] = rone<R>();
+        e[1] = rzero<R>();
+        if (p.nmax >= 1) {
+            e[2] = c1;
+            e[3] = s1;
+        }
+        R cr = c1, ci = s1;
+        for (int m = 2; m <= p.nmax; ++m) {
+            R nr, ni;
+            cmul(cr, ci, c1, s1, nr, ni);
+            cr = nr;
+            ci = ni;
+            e[2 * m] = cr;
+            e[2 * m + 1] = ci;
+        }
+    }
+    __syncthreads();
+    const int nq = p.nk - 1;
+    const int items = p.npart * (nq + 1);
+    for (int t = threadIdx.x; t < items; t += kThreads) {
+        const int part = t / (nq + 1), q = t % (nq + 1);
+        const bool up = part < p.nup;
+        R* row = up ? U + part * p.ldU : D + (part - p.nup) * p.ldU;
+        if (q == 0) {
+            row[0] = up ? kq[0].v : rone<R>();
+            continue;
+        }
+        const KV& K = kq[q];
+        R zr = rone<R>(), zi = rzero<R>();
+        bool first = true;
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) {
+            const int n = K.n[cc];
+            if (n == 0) continue;
+            const R* e = E + 2 * ((part * 3 + cc) * np1 + (n < 0 ? -n : n));
+            const R er = e[0], ei = n < 0 ? -e[1] : e[1];
+            if (first) {
+                zr = er;
+                zi = ei;
+                first = false;
+            } else {
+                R nr, ni;
+                cmul(zr, zi, er, ei, nr, ni);
+                zr = nr;
+                zi = ni;
+            }
+        }
+        if (up) {
+            row[2 * q - 1] = K.v * zr;
+            row[2 * q] = K.v * zi;
+        } else {
+            row[2 * q - 1] = zr;
+            row[2 * q] = zi;
+        }
+    }
+    // unpaired plane waves: up columns ndn.., down rows nup.., zero corner
+    const int ldS = p.ldS;
+    for (int t = threadIdx.x; t < p.nup * p.nexup; t += kThreads) {
+        const int i = t / p.nexup, jj = t % p.nexup;
+        const double* xi = x + 3 * i;
+        const double arg = p.akup[jj][0] * xi[0] + p.akup[jj][1] * xi[1] + p.akup[jj][2] * xi[2];
+        double s, co;
+        sincos(arg, &s, &co);
+        S[i * ldS + p.ndn + jj] = from_dbl<R>(p.sinup[jj] ? s : co);
+    }
+    for (int t = threadIdx.x; t < p.ndn * p.nexdn; t += kThreads) {
+        const int j = t / p.nexdn, jj = t % p.nexdn;
+        const double* xj = x + 3 * (p.nup + j);
+        const double arg = p.akdn[jj][0] * xj[0] + p.akdn[jj][1] * xj[1] + p.akdn[jj][2] * xj[2];
+        double s, co;
+        sincos(arg, &s, &co);
+        S[(p.nup + jj) * ldS + j] = from_dbl<R>(p.sindn[jj] ? s : co);
+    }
+    for (int t = threadIdx.x; t < p.nexdn * p.nexup; t += kThreads) {
+        const int r = t / p.nexup, cc = t % p.nexup;
+        S[(p.nup + r) * ldS + p.ndn + cc] = rzero<R>();
+    }
+    __syncthreads();
+}
+
+// Stage 3: S[i][j] = sum_q U[i][q] D[j][q] + beta (psislaterbcs.f90:278,289)
+template <class R>
+__device__ void gemm_stage(const Ctx<R>& c)
+{
+    using Acc = typename AccOf<R>::type;
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const R* U = at<R>(sm, c.L.U);
+    const R* D = at<R>(sm, c.L.D);
+    R* S = at<R>(sm, c.L.S);
+    const int ncol = p.ncol, ldU = p.ldU;
+    // two outputs of one row per thread (shared U row)
+    const int half = (p.ndn + 1) / 2;
+    for (int t = threadIdx.x; t < p.nup * half; t += kThreads) {
+        const int i = t / half, j0 = t % half, j1 = j0 + half;
+        const R* u = U + i * ldU;
+        const R* d0 = D + j0 * ldU;
+        const bool two = j1 < p.ndn;
+        const R* d1 = D + (two ? j1 : j0) * ldU;
+        Acc a0, a1;
+        acc_init(a0);
+        acc_init(a1);
+#pragma unroll 4
+        for (int q = 0; q < ncol; ++q) {
+            const R uq = u[q];
+            acc_madd(a0, uq, d0[q]);
+            acc_madd(a1, uq, d1[q]);
+        }
+        S[i * p.ldS + j0] = acc_value(a0) + S[i * p.ldS + j0];
+        if (two) S[i * p.ldS + j1] = acc_value(a1) + S[i * p.ldS + j1];
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Stage 4: in-place Gauss-Jordan inverse with partial pivoting (first
+// maximum wins, as LAPACK idamax).  The pivot sequence is the one dgetrf
+// takes (matrixlapack.f90:20), so log|det| = sum log|pivot| and the sign
+// follow matrixlapack.f90:27-33.  Row interchanges are undone on the columns
+// of the inverse at the end.  Returns false for an exactly singular matrix.
+// ---------------------------------------------------------------------------
+// pivot search over rows k..n-1 of column k by one warp (first maximum
+// wins); lane 0 returns the row (n when the column is empty)
+template <class R>
+__device__ __forceinline__ int warp_pivot(const R* A, int ld, int n, int k, R& pv)
+{
+    const int lane = threadIdx.x & 31;
+    R best = rzero<R>();
+    int bi = n;
+    for (int i = k + lane; i < n; i += 32) {
+        const R v = A[i * ld + k];
+        if (bi == n || abs_gt(v, best)) {
+            best = v;
+            bi = i;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        R ob;
+        if constexpr (is_df<R>::value) {
+            ob.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
+            ob.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
+        } else {
+            ob = __shfl_xor_sync(0xffffffffu, best, o);
+        }
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        const bool take = (oi != n) && (bi == n || abs_gt(ob, best) || (!abs_gt(best, ob) && oi < bi));
+        if (take) {
+            best = ob;
+            bi = oi;
+        }
+    }
+    pv = best;
+    return bi;
+}
+
+template <class R>
+__device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
+{
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    R* A = at<R>(sm, c.L.S);
+    R* colk = at<R>(sm, c.L.colk);
+    int* piv = reinterpret_cast<int*>(sm + c.L.red + 512);   // nd ints
+    __shared__ R s_pinv;
+    __shared__ int s_piv;
+    __shared__ int s_sing;
+    __shared__ double s_logdet;
+    __shared__ int s_sgn;
+    const int n = p.nd, ld = p.ldS;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double mant = 1.0;
+    int expo = 0;
+    int sg = 1;
+    // pivot of column 0
+    if (warp == 0) {
+        R pv;
+        const int bi = warp_pivot<R>(A, ld, n, 0, pv);
+        if (lane == 0) {
+            s_sing = is_zero(pv) ? 1 : 0;
+            s_piv = bi;
+            piv[0] = bi;
+            if (!is_zero(pv)) s_pinv = rcp(pv);
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        if (s_sing) break;
+        const int pr = s_piv;
+        const R pinv = s_pinv;
+        // save column k (rows in swapped order), swap rows k/pr, scale row k
+        for (int t = threadIdx.x; t < n; t += kThreads) {
+            const int src = (t == k) ? pr : ((t == pr) ? k : t);
+            colk[t] = A[src * ld + k];
+            if (t != k) {
+                const R a = A[k * ld + t];
+                const R b = A[pr * ld + t];
+                R nk = a;
+                if (pr != k) {
+                    A[pr * ld + t] = a;
+                    nk = b;
+                }
+                A[k * ld + t] = nk * pinv;
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // look-ahead: warp 0 eliminates column k+1 and finds its pivot
+            // while the other warps eliminate the rest of the matrix
+            if (lane == 0) {
+                // |det| kept as mantissa * 2^exponent; one log at the end
+                int ex;
+                const R pvv = colk[k];
+                mant = frexp(mant * fabs(to_double(pvv)), &ex);
+                expo += ex;
+                sg = is_neg(pvv) ? -sg : sg;
+                if (pr != k) sg = -sg;
+            }
+            if (k + 1 < n) {
+                const R akn = A[k * ld + k + 1];
+                for (int i = lane; i < n; i += 32)
+                    if (i != k) A[i * ld + k + 1] = fms(A[i * ld + k + 1], colk[i], akn);
+                __syncwarp();
+                R pv;
+                const int bi = warp_pivot<R>(A, ld, n, k + 1, pv);
+                if (lane == 0) {
+                    if (is_zero(pv)) {
+                        s_sing = 1;
+                    } else {
+                        s_piv = bi;
+                        piv[k + 1] = bi;
+                        s_pinv = rcp(pv);
+                    }
+                }
+            }
+        } else {
+            const int tot = n * n;
+            for (int t = threadIdx.x - 32; t < tot; t += kThreads - 32) {
+                const int i = t / n, cc = t % n;
+                if (i == k || cc == k + 1) continue;
+                if (cc == k)
+                    A[i * ld + k] = -(colk[i] * pinv);
+                else
+                    A[i * ld + cc] = fms(A[i * ld + cc], colk[i], A[k * ld + cc]);
+            }
+            if (threadIdx.x == 32) A[k * ld + k] = pinv;
+        }
+        __syncthreads();
+    }
+    const bool sing = s_sing != 0;
+    if (!sing) {
+        // undo the row interchanges on the columns: inv(S) = inv(P S) P
+        for (int k = n - 1; k >= 0; --k) {
+            const int pr = piv[k];
+            if (pr != k)
+                for (int t = threadIdx.x; t < n; t += kThreads) {
+                    const R a = A[t * ld + k];
+                    A[t * ld + k] = A[t * ld + pr];
+                    A[t * ld + pr] = a;
+                }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        s_logdet = log(mant) + expo * 0.69314718055994530942;
+        s_sgn = sg;
+    }
+    __syncthreads();
+    logdet = s_logdet;
+    sgn = s_sgn;
+    return !sing;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 5: drift and Laplacian of log det from the inverse.
+//  up i:   sum_q k_q (U_c G_s - U_s G_c), lap -|k|^2 (U_c G_c + U_s G_s),
+//          G_{c,s} = sum_j D[j][c,s] Sinv[j][i]
+//  down j: sum_q k_q (H_s D_c - H_c D_s), lap -|k|^2 (H_c D_c + H_s D_s),
+//          H_{c,s} = sum_i Sinv[j][i] U[i][c,s]
+// Work items (particle, k vector) are split into contiguous per-thread
+// chunks; each thread sums its chunk per particle and the partial sums of a
+// particle are added in thread order.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ void drift_stage(const Ctx<R>& c)
+{
+    using KV = typename Prec<R>::KV;
+    using Acc = typename AccOf<R>::type;
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const R* U = at<R>(sm, c.L.U);
+    const R* D = at<R>(sm, c.L.D);
+    const R* Si = at<R>(sm, c.L.S);
+    const KV* kq = reinterpret_cast<const KV*>(sm + c.L.kq);
+    double* acc = sm + c.L.acc;             // drift [3N], lap [N]
+    R* part = at<R>(sm, c.L.red);           // per thread: 2 segments x 4 sums
+    const int nq = p.nk - 1, P = p.npart, ld = p.ldS, ldU = p.ldU;
+    const int items = P * nq;
+    const int chunk = (items + kThreads - 1) / kThreads;
+    const int b = threadIdx.x * chunk, e = min(items, b + chunk);
+    R s0[4], s1[4];
+    for (int k = 0; k < 4; ++k) s0[k] = s1[k] = rzero<R>();
+    const int first = b < e ? b / nq : -1;
+    for (int it = b; it < e; ++it) {
+        const int pt = it / nq, q = it % nq + 1;
+        const KV& K = kq[q];
+        const int qc = 2 * q - 1, qs = 2 * q;
+        R t, l;
+        if (pt < p.nup) {
+            const int i = pt;
+            Acc gc, gs;
+            acc_init(gc);
+            acc_init(gs);
+            for (int j = 0; j < p.ndn; ++j) {
+                const R sji = Si[j * ld + i];
+                acc_madd(gc, D[j * ldU + qc], sji);
+                acc_madd(gs, D[j * ldU + qs], sji);
+            }
+            const R uc = U[i * ldU + qc], us = U[i * ldU + qs];
+            const R vgc = acc_value(gc), vgs = acc_value(gs);
+            t = uc * vgs - us * vgc;
+            l = uc * vgc + us * vgs;
+        } else {
+            const int j = pt - p.nup;
+            Acc hc, hs;
+            acc_init(hc);
+            acc_init(hs);
+            for (int i = 0; i < p.nup; ++i) {
+                const R sji = Si[j * ld + i];
+                acc_madd(hc, sji, U[i * ldU + qc]);
+                acc_madd(hs, sji, U[i * ldU + qs]);
+            }
+            const R dc = D[j * ldU + qc], ds = D[j * ldU + qs];
+            const R vhc = acc_value(hc), vhs = acc_value(hs);
+            t = vhs * dc - vhc * ds;
+            l = vhc * dc + vhs * ds;
+        }
+        const R lk = -(K.k2 * l);
+        if (pt == first) {
+            s0[0] = fma(K.k[0], t, s0[0]);
+            s0[1] = fma(K.k[1], t, s0[1]);
+            s0[2] = fma(K.k[2], t, s0[2]);
+            s0[3] = s0[3] + lk;
+        } else {
+            s1[0] = fma(K.k[0], t, s1[0]);
+            s1[1] = fma(K.k[1], t, s1[1]);
+            s1[2] = fma(K.k[2], t, s1[2]);
+            s1[3] = s1[3] + lk;
+        }
+    }
+    // publish the (at most two) particle segments of this thread's chunk;
+    // a chunk never spans more than two particles because chunk <= nq
+    R* my = part + threadIdx.x * 8;
+    for (int k = 0; k < 4; ++k) {
+        my[k] = s0[k];
+        my[4 + k] = s1[k];
+    }
+    __syncthreads();
+    // particle pt is covered by threads floor(pt*nq/chunk) .. floor((pt*nq+nq-1)/chunk)
+    for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+        R r[4];
+        for (int k = 0; k < 4; ++k) r[k] = rzero<R>();
+        const int t0 = (pt * nq) / chunk, t1 = (pt * nq + nq - 1) / chunk;
+        for (int t = t0; t <= t1 && t < kThreads; ++t) {
+            const int tb = t * chunk, te = min(items, tb + chunk);
+            if (tb >= te) continue;
+            const R* o = part + t * 8;
+            const int sl = (tb / nq == pt) ? 0 : (((te - 1) / nq == pt) ? 4 : -1);
+            if (sl < 0) continue;
+            for (int k = 0; k < 4; ++k) r[k] = r[k] + o[sl + k];
+        }
+        acc[3 * pt + 0] = to_double(r[0]);
+        acc[3 * pt + 1] = to_double(r[1]);
+        acc[3 * pt + 2] = to_double(r[2]);
+        acc[3 * P + pt] = to_double(r[3]);
+    }
+    __syncthreads();
+}
+
+// Stage 6: beta terms of the drift and Laplacian (psislaterbcs.f90:290-291
+// through :213-222): per up-down pair h = Sinv[j][i] f'/r dx, l = Sinv[j][i]
+// lap f; row sums go to the up particle, column sums (negated drift) to the
+// down particle.  Then the unpaired plane waves.
+template <class R>
+__device__ void beta_drift_stage(const Ctx<R>& c)
+{
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const R* xr = at<R>(sm, c.L.xr);
+    const double* x = sm + c.L.x;
+    const R* Si = at<R>(sm, c.L.S);
+    R* pv = at<R>(sm, c.L.R);
+    const R* pb = reinterpret_cast<const R*>(c.pb);
+    double* acc = sm + c.L.acc;
+    const int nup = p.nup, ndn = p.ndn, ld = p.ldS, P = p.npart;
+    if (!p.nobeta) {
+        for (int r0 = 0; r0 < nup; r0 += c.L.rows_beta) {
+            const int r1 = min(nup, r0 + c.L.rows_beta);
+            const int npc = (r1 - r0) * ndn;
+            for (int q = threadIdx.x; q < npc; q += kThreads) {
+                const int i = r0 + q / ndn, j = q % ndn;
+                const R* xi = xr + 3 * i;
+                const R* xj = xr + 3 * (nup + j);
+                const R* pbq = pb + 2 * (i * ndn + j);
+                const R sij = Si[j * ld + i];
+                const R w = sij * pbq[0];
+                pv[4 * q + 0] = w * min_image(xi[0] - xj[0], p);
+                pv[4 * q + 1] = w * min_image(xi[1] - xj[1], p);
+                pv[4 * q + 2] = w * min_image(xi[2] - xj[2], p);
+                pv[4 * q + 3] = sij * pbq[1];
+            }
+            __syncthreads();
+            const int nr = r1 - r0;
+            for (int tc = threadIdx.x; tc < 4 * (nr + ndn); tc += kThreads) {
+                const int t = tc / 4, cmp = tc % 4;
+                typename AccOf<R>::type sacc;
+                acc_init(sacc);
+                if (t < nr) {
+                    const R* row = pv + 4 * (t * ndn) + cmp;
+                    for (int j = 0; j < ndn; ++j) acc_add(sacc, row[4 * j]);
+                    const int i = r0 + t;
+                    acc[cmp < 3 ? 3 * i + cmp : 3 * P + i] += to_double(acc_value(sacc));
+                } else {
+                    const int j = t - nr;
+                    for (int r = 0; r < nr; ++r) acc_add(sacc, pv[4 * (r * ndn + j) + cmp]);
+                    if (cmp < 3)
+                        acc[3 * (nup + j) + cmp] -= to_double(acc_value(sacc));
+                    else
+                        acc[3 * P + nup + j] += to_double(acc_value(sacc));
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // unpaired plane waves (psislaterbcs.f90:171-206 with :211-223)
+    if (p.nexup > 0 || p.nexdn > 0) {
+        for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+            const double* xp = x + 3 * pt;
+            double g0 = 0, g1 = 0, g2 = 0, lp = 0;
+            if (pt < nup) {
+                for (int jj = 0; jj < p.nexup; ++jj) {
+                    const double* k = p.akup[jj];
+                    double s, co;
+                    sincos(k[0] * xp[0] + k[1] * xp[1] + k[2] * xp[2], &s, &co);
+                    const double w = to_double(Si[(ndn + jj) * ld + pt]);
+                    // sin: grad k cos, lap -k2 sin; cos: grad -k sin, lap -k2 cos
+                    const double gcoef = p.sinup[jj] ? co : -s;
+                    const double val = p.sinup[jj] ? s : co;
+                    g0 += w * k[0] * gcoef;
+                    g1 += w * k[1] * gcoef;
+                    g2 += w * k[2] * gcoef;
+                    lp += w * (-p.ak2up[jj] * val);
+                }
+            } else {
+                const int j = pt - nup;
+                for (int jj = 0; jj < p.nexdn; ++jj) {
+                    const double* k = p.akdn[jj];
+                    double s, co;
+                    sincos(k[0] * xp[0] + k[1] * xp[1] + k[2] * xp[2], &s, &co);
+                    const double w = to_double(Si[j * ld + (nup + jj)]);
+                    const double gcoef = p.sindn[jj] ? co : -s;
+                    const double val = p.sindn[jj] ? s : co;
+                    g0 += w * k[0] * gcoef;
+                    g1 += w * k[1] * gcoef;
+                    g2 += w * k[2] * gcoef;
+                    lp += w * (-p.ak2dn[jj] * val);
+                }
+            }
+            acc[3 * pt + 0] += g0;
+            acc[3 * pt + 1] += g1;
+            acc[3 * pt + 2] += g2;
+            acc[3 * P + pt] += lp;
+        }
+        __syncthreads();
+    }
+}
+
+// Scalars of one evaluation.
+struct HRes {
+    double psil, d2psi, v, vext, psigl, d2psig, u, d2u, logdet, d2phi;
+    int is;
+    bool singular;
+};
+
+// ---------------------------------------------------------------------------
+// hpsi (wavefunction.f90:161-201) for the positions in sm[L.x].  Leaves
+// dpsi in acc[0..3N) and dpsig in sm[L.dg] when a2 != 0.
+// mode MODE_GETPHI stops after the Jastrow; MODE_BCS skips the Jastrow.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
+{
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const int P = p.npart, n3 = 3 * P;
+    double* acc = sm + c.L.acc;
+    double* du = acc + 4 * P;
+    const double* x = sm + c.L.x;
+    {
+        R* xr = at<R>(sm, c.L.xr);
+        for (int i = threadIdx.x; i < n3; i += kThreads) xr[i] = from_dbl<R>(x[i]);
+        __syncthreads();
+    }
+    HRes h;
+    double su = 0.0, sv = 0.0, sd2 = 0.0;
+    pair_stage<R>(c, su, sv, sd2);   // also fills the beta part of S (needed by MODE_BCS too)
+    if (mode == MODE_BCS) {
+        su = sv = sd2 = 0.0;
+        for (int i = threadIdx.x; i < n3; i += kThreads) du[i] = 0.0;
+        __syncthreads();
+    }
+    double logdet = 0.0;
+    int sgn = 1;
+    bool ok = true;
+    if (mode != MODE_GETPHI) {
+        orbital_stage<R>(c);
+        gemm_stage<R>(c);
+        ok = inverse_stage<R>(c, logdet, sgn);
+        if (ok) {
+            drift_stage<R>(c);
+            beta_drift_stage<R>(c);
+        } else {
+            for (int i = threadIdx.x; i < 4 * P; i += kThreads) acc[i] = 0.0;
+            __syncthreads();
+        }
+    } else {
+        for (int i = threadIdx.x; i < 4 * P; i += kThreads) acc[i] = 0.0;
+        __syncthreads();
+    }
+    // one-body term (psislaterbcs.f90:378-395) and per-particle combination
+    double sums[8] = {su, sv, sd2, 0.0, 0.0, 0.0, 0.0, 0.0};
+    // sums[3]: sum lap/m (d2phi), [4]: |du|^2, [5]: du.dphi, [6]: one-body g, [7]: vext
+    double g1 = 0.0, d2g = 0.0, dudg = 0.0;
+    for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+        const int sp = pt < p.nup ? 0 : 1;
+        const double isq = p.isqm[sp], im = p.imass[sp];
+        double dph[3], dj[3];
+        for (int k = 0; k < 3; ++k) {
+            dph[k] = ok ? acc[3 * pt + k] * isq : 0.0;
+            dj[k] = du[3 * pt + k];
+        }
+        sums[3] += (ok ? acc[3 * P + pt] : 0.0) * im;
+        sums[4] += dj[0] * dj[0] + dj[1] * dj[1] + dj[2] * dj[2];
+        double dg[3] = {0.0, 0.0, 0.0};
+        if (p.onebody && (mode == MODE_HPSI || mode == MODE_STEP)) {
+            double s, co;
+            sincos(p.qex[0] * x[3 * pt] + p.qex[1] * x[3 * pt + 1] + p.qex[2] * x[3 * pt + 2], &s, &co);
+            sums[7] -= p.v0ex * co;
+            g1 -= p.v0exjas * co;
+            const double q2 = p.qex[0] * p.qex[0] + p.qex[1] * p.qex[1] + p.qex[2] * p.qex[2];
+            d2g += p.v0exjas * q2 * (p.v0exjas * s * s + co);
+            for (int k = 0; k < 3; ++k) dg[k] = p.v0exjas * p.qex[k] * s;
+            dudg += dj[0] * dg[0] + dj[1] * dg[1] + dj[2] * dg[2];
+        }
+        double dtot[3];
+        for (int k = 0; k < 3; ++k) dtot[k] = dj[k] + dg[k];
+        sums[5] += dtot[0] * dph[0] + dtot[1] * dph[1] + dtot[2] * dph[2];
+        // dpsi = dphi + du (+ dg)
+        for (int k = 0; k < 3; ++k) acc[3 * pt + k] = dph[k] + dtot[k];
+    }
+    sums[6] = g1;
+    double more[2] = {d2g, dudg};
+    block_sum<8>(sums, sm + c.L.red);
+    block_sum<2>(more, sm + c.L.red);
+    const double u = sums[0] + sums[6];
+    const double d2u_j = sums[2] + sums[4];                        // getphi d2u
+    const double d2u = d2u_j + more[0] + 2.0 * more[1];            // + one-body terms
+    h.u = u;
+    h.d2u = mode == MODE_GETPHI ? d2u_j : d2u;
+    h.v = sums[1] + sums[7];
+    h.vext = sums[7];
+    h.logdet = ok ? logdet : DMC_MINUSHUGE;
+    h.d2phi = ok ? sums[3] : 0.0;
+    h.is = ok ? sgn : 1;
+    h.singular = !ok;
+    h.psil = h.logdet + u;
+    h.d2psi = h.d2phi + d2u + 2.0 * sums[5];
+    if (mode == MODE_GETPHI) h.psil = u;
+    if (p.a2 == 0.0 || (mode != MODE_HPSI && mode != MODE_STEP)) {
+        h.psigl = h.psil;
+        h.d2psig = h.d2psi;
+    } else {
+        double sd[1] = {0.0};
+        for (int i = threadIdx.x; i < n3; i += kThreads) sd[0] += acc[i] * acc[i];
+        block_sum<1>(sd, sm + c.L.red);
+        const double psi = exp(h.psil);
+        const double psig2 = psi * psi + p.a2;
+        const double f = psi * psi / psig2;
+        double* dg = sm + c.L.dg;
+        for (int i = threadIdx.x; i < n3; i += kThreads) dg[i] = f * acc[i];
+        h.d2psig = (sd[0] + h.d2psi) * f - psi * psi * psi * psi * sd[0] / (psig2 * psig2);
+        h.psigl = 0.5 * log(psig2);
+        __syncthreads();
+    }
+    return h;
+}
+
+}  // namespace walker
+}  // namespace dmc

@@ -150,6 +150,22 @@ int dmc_get_info(const dmc_ctx* ctx, dmc_info* out);
  * 7 ak (3*nk), 8 ak2 (nk), 9 numsh (norb, as doubles). */
 int dmc_get_table(const dmc_ctx* ctx, int which, double* out, int n);
 
+/* Arithmetic of the walker kernel.  DMC_PREC_FP64 (the default) computes
+ * everything in FP64.  DMC_PREC_MIXED computes the pair matrix, its inverse,
+ * log-determinant and the drift/Laplacian contractions in double-float
+ * arithmetic on the FP32 pipe (~48-bit significands) and the Jastrow and
+ * potential in FP32, keeping the move, weights, branching and estimator
+ * sums in FP64.  No counterpart in the reference (which is FP64 only). */
+#define DMC_PREC_FP64 0
+#define DMC_PREC_MIXED 1
+int dmc_set_precision(dmc_ctx* ctx, int precision);
+int dmc_get_precision(const dmc_ctx* ctx, int* precision);
+
+/* Measured FMA throughput of the current device, TFLOP/s: kind 0 the FP64
+ * pipe (DFMA), kind 1 the FP32 pipe (FFMA).  A measurement aid for roofline
+ * fractions; no counterpart in the reference. */
+int dmc_probe_peak(int kind, double* tflops);
+
 /* Replaces setbcspar (psislaterbcs.f90:401-419) with optbeta=.false.:
  * new s-wave amplitudes vorb(1:norb). */
 int dmc_set_vorb(dmc_ctx* ctx, const double* vorb, int norb);

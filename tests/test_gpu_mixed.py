@@ -1,0 +1,71 @@
+"""Mixed-precision walker path against the FP64 oracle.
+
+The mixed path computes the pair matrix, inverse and drift/Laplacian
+contractions in double-float arithmetic and the Jastrow and potential in
+FP32.  Bars (per configuration, against the FP64 oracle): local energy and
+Laplacian within 1e-6 relative (the benchmark's requirement), log|Psi|
+within 1e-6 absolute, drift within 1e-6 relative to the largest component.
+The measured errors are printed.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from dmcbcs_project_gb300 import capi, configs
+
+pytestmark = pytest.mark.gpu
+
+EL_TOL = 1e-6
+
+
+def walkers(name, nw, seed):
+    sysd, rund, _ = configs.workload(name, nwalk=nw, seed=seed)
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    x = orc.walkers()["x"] + np.random.default_rng(seed).normal(scale=0.3, size=(nw, orc.npart, 3))
+    return sysd, rund, orc, x
+
+
+@pytest.mark.parametrize("name,nw", [("n14", 64), ("n66", 128), ("p33_30", 32), ("p38_33", 32)])
+def test_mixed_hpsi_against_fp64_oracle(name, nw):
+    sysd, rund, orc, x = walkers(name, nw, 21)
+    ref = orc.hpsi(x)
+    with capi.Context(sysd, rund, precision="mixed") as ctx:
+        got = ctx.hpsi(x)
+    hb = sysd.hbar
+    el_g = -hb * got["d2psi"] + got["v"]
+    el_r = -hb * ref["d2psi"] + ref["v"]
+    el_err = np.abs(el_g - el_r) / np.maximum(np.abs(el_r), 1.0)
+    lap_err = np.abs(got["d2psi"] - ref["d2psi"]) / np.maximum(np.abs(ref["d2psi"]), 1.0)
+    psil_err = np.abs(got["psil"] - ref["psil"])
+    dr_err = np.array([np.max(np.abs(got["dpsi"][w] - ref["dpsi"][w])) / max(1.0, np.max(np.abs(ref["dpsi"][w])))
+                       for w in range(nw)])
+    print(f"{name}: max rel err E_L {el_err.max():.2e}, d2psi {lap_err.max():.2e}, "
+          f"drift {dr_err.max():.2e}; max abs err log|Psi| {psil_err.max():.2e}")
+    assert np.array_equal(got["is_"], ref["is_"])
+    assert el_err.max() < EL_TOL
+    assert lap_err.max() < EL_TOL
+    assert dr_err.max() < EL_TOL
+    assert psil_err.max() < 1e-6
+
+
+def test_mixed_generations_track_fp64():
+    """Short DMC runs from the same walkers: the mixed path follows the FP64
+    trajectories (same random streams; weights differ only in the last bits)."""
+    sysd, rund, _ = configs.workload("n66", nwalk=64)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with capi.Context(sysd, rund, precision=prec) as ctx:
+            ctx.init_walkers()
+            ctx.initial_eval()
+            for g in range(4):
+                ctx.generation(g == 3)
+            res[prec] = (ctx.walkers(), ctx.estimators())
+    (w64, e64), (wmx, emx) = res["fp64"], res["mixed"]
+    assert w64["n"] == wmx["n"]
+    assert np.array_equal(w64["irn"], wmx["irn"])
+    assert np.max(np.abs(w64["x"] - wmx["x"])) < 1e-9
+    el64 = -sysd.hbar * w64["d2psi"] + w64["v"]
+    elmx = -sysd.hbar * wmx["d2psi"] + wmx["v"]
+    assert np.max(np.abs(el64 - elmx) / np.maximum(np.abs(el64), 1.0)) < EL_TOL
+    assert np.allclose(e64[0], emx[0], rtol=1e-6)
