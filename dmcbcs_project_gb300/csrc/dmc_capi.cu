@@ -174,7 +174,14 @@ void fill_params(dmc_ctx* c)
     p.nest = nest_for(c->rd.idmc);
     p.nrand = 2 * ((3 * S.npart + 1) / 2);
     p.ldS = S.nd | 1;
-    p.ldU = S.ncol | 1;
+    // U/D row pitch: even (16-byte pairs) with an odd number of 16-byte
+    // units, so rows read by neighbouring lanes fall in different banks
+    {
+        const int nq = S.nk - 1;
+        int half = nq + 1;
+        if (half % 2 == 0) ++half;
+        p.ldU = 2 * half;
+    }
     p.el = S.el; p.eli = S.eli; p.range = S.range; p.scale = S.scale; p.rangeb = S.rangeb; p.scaleb = S.scaleb;
     for (int s = 0; s < 2; ++s) {
         p.mass[s] = S.mass[s];

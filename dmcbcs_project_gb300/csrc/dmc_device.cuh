@@ -119,6 +119,7 @@ struct KernelArgs {
 // On-chip layout of one walker CTA, offsets in doubles.
 struct SmemLayout {
     int x, xr, xo, dx, drift, dg, kq, S, pb, R, U, D, E, acc, colk, red, total;
+    int S2;               // second nd x ldS buffer of the blocked inverse (-1: none)
     int pb_in_smem;
     int pb_size;          // doubles of pair data per walker
     int rows_jas, rows_beta;   // rows of the up-down block per reduction chunk
@@ -141,7 +142,7 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
     L.dg = take(n3);              // guide-function gradient when a2 != 0
     L.kq = take(p.nk * 8);        // k vector records
     L.S = take(p.nd * p.ldS);     // pair matrix -> inverse
-    L.colk = take(p.nd + 2);      // Gauss-Jordan pivot column
+    L.colk = take(2 * p.nd + 2);  // pivot column of the unblocked Gauss-Jordan
     L.acc = take(p.npart * 8);    // per particle: drift(3), lap, du(3), spare
     L.red = take(kThreads * 8);   // reductions and per-thread partial sums
     // union region: Jastrow pair vectors, then orbitals U|D|E, then beta terms
@@ -151,7 +152,11 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
     L.U = L.R;
     L.D = L.R + p.nup * p.ldU;
     L.E = L.D + p.ndn * p.ldU;
-    int rsize = nUDE;
+    // the blocked inverse ping-pongs the pair matrix with a second buffer at
+    // E (the orbital powers are dead once S is formed)
+    const int nUDS = p.nup * p.ldU + p.ndn * p.ldU + p.nd * p.ldS;
+    int rsize = nUDE > nUDS ? nUDE : nUDS;
+    L.S2 = L.E;
     const int row_pairs = p.ndn > 0 ? p.ndn : 1;
     const int minrows = 1;
     // at least one row of pair data must fit

@@ -71,7 +71,7 @@ using ::fma;   // keep the double overloads visible next to the double-float one
 // reciprocal: one Newton step from the FP32 reciprocal of the leading part
 __device__ __forceinline__ df rcp(df x)
 {
-    const float y = 1.0f / x.hi;
+    const float y = __frcp_rn(x.hi);
     const df e = df{1.0f, 0.0f} - x * y;          // 1 - x*y, exact to double-float accuracy
     return fast_two_sum(y, y * e.hi);
 }
@@ -94,6 +94,9 @@ __device__ __forceinline__ bool abs_gt(df a, df b)
     const df x = dabs(a), y = dabs(b);
     return x.hi > y.hi || (x.hi == y.hi && x.lo > y.lo);
 }
+// a < b for normalised values (|lo| <= ulp(hi)/2): the leading parts
+// decide unless they are equal
+__device__ __forceinline__ bool lt(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool is_zero(df a) { return a.hi == 0.0f; }
 __device__ __forceinline__ bool is_neg(df a) { return a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f); }
 __host__ __device__ __forceinline__ double to_double(df a) { return (double)a.hi + (double)a.lo; }
@@ -136,9 +139,14 @@ __device__ __forceinline__ df acc_value(const dfacc& a) { return fast_two_sum(a.
 __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
 __device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ double dabs(double x) { return fabs(x); }
-__device__ __forceinline__ bool abs_gt(double a, double b) { return fabs(a) > fabs(b); }
-__device__ __forceinline__ bool is_zero(double a) { return a == 0.0; }
-__device__ __forceinline__ bool is_neg(double a) { return a < 0.0; }
+// magnitude comparisons on the bit patterns (integer pipe, finite values)
+__device__ __forceinline__ bool abs_gt(double a, double b)
+{
+    const unsigned long long m = 0x7fffffffffffffffull;
+    return ((unsigned long long)__double_as_longlong(a) & m) > ((unsigned long long)__double_as_longlong(b) & m);
+}
+__device__ __forceinline__ bool is_zero(double a) { return ((unsigned long long)__double_as_longlong(a) << 1) == 0ull; }
+__device__ __forceinline__ bool is_neg(double a) { return __double_as_longlong(a) < 0 && !is_zero(a); }
 __host__ __device__ __forceinline__ double to_double(double a) { return a; }
 
 struct dacc64 {

@@ -517,8 +517,17 @@ cudaError_t launch_matinv(const double* a, double* inv, double* detl, int* is, i
     memset(&L, 0, sizeof L);
     L.S = 0;
     L.colk = round_up(n * p.ldS, 2);
-    L.red = L.colk + round_up(n + 2, 2);
+    L.red = L.colk + round_up(2 * n + 2, 2);
     L.total = L.red + kThreads * 8;
+    // second buffer of the blocked inverse, when both copies fit on chip
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    L.S2 = -1;
+    if ((size_t)(L.total + round_up(n * p.ldS, 2)) * 8 + 1024 <= (size_t)optin) {
+        L.S2 = L.total;
+        L.total += round_up(n * p.ldS, 2);
+    }
     const size_t smem = (size_t)L.total * 8;
     cudaError_t e = cudaFuncSetAttribute(matinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -212,6 +212,20 @@ struct Ctx {
     double* pb;
 };
 
+// two consecutive values (16-byte aligned) with one shared-memory load
+__device__ __forceinline__ void ld2(const double* p, double& a, double& b)
+{
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    a = v.x;
+    b = v.y;
+}
+__device__ __forceinline__ void ld2(const df* p, df& a, df& b)
+{
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a = df{v.x, v.y};
+    b = df{v.z, v.w};
+}
+
 // typed views of the shared-memory regions
 template <class T>
 __device__ __forceinline__ T* at(double* sm, int off) { return reinterpret_cast<T*>(sm + off); }
@@ -294,8 +308,10 @@ __device__ void pair_stage(const Ctx<R>& c, double& su, double& sv, double& sd2)
                 // potential nearly cancel, so both stay in double-float there;
                 // beyond it the Jastrow is exactly zero and only the
                 // exponentially small potential tail is left (FP32).
-                const bool in_j = rb.hi < p.range_df.hi;
-                const bool in_b = !p.nobeta && !(rb.hi > p.rangeb_df.hi);
+                // full double-float comparisons: a pair within an FP32 ulp of
+                // a range end must fall on the same side as in FP64
+                const bool in_j = lt(rb, p.range_df);
+                const bool in_b = !p.nobeta && !lt(p.rangeb_df, rb);
                 if (in_j || in_b) {
                     df t;
                     const int idx = grid_pos(rb, p.scaleb_df, p.ntab, t);
@@ -503,6 +519,8 @@ __device__ void orbital_stage(const Ctx<R>& c)
         }
     }
     __syncthreads();
+    // columns: (cos, sin) of k vector q at 2(q-1), 2(q-1)+1; the constant
+    // term at 2 nq; zero padding up to ldU
     const int nq = p.nk - 1;
     const int items = p.npart * (nq + 1);
     for (int t = threadIdx.x; t < items; t += kThreads) {
@@ -510,7 +528,8 @@ __device__ void orbital_stage(const Ctx<R>& c)
         const bool up = part < p.nup;
         R* row = up ? U + part * p.ldU : D + (part - p.nup) * p.ldU;
         if (q == 0) {
-            row[0] = up ? kq[0].v : rone<R>();
+            row[2 * nq] = up ? kq[0].v : rone<R>();
+            for (int z = 2 * nq + 1; z < p.ldU; ++z) row[z] = rzero<R>();
             continue;
         }
         const KV& K = kq[q];
@@ -534,11 +553,11 @@ __device__ void orbital_stage(const Ctx<R>& c)
             }
         }
         if (up) {
-            row[2 * q - 1] = K.v * zr;
-            row[2 * q] = K.v * zi;
+            row[2 * q - 2] = K.v * zr;
+            row[2 * q - 1] = K.v * zi;
         } else {
-            row[2 * q - 1] = zr;
-            row[2 * q] = zi;
+            row[2 * q - 2] = zr;
+            row[2 * q - 1] = zi;
         }
     }
     // unpaired plane waves: up columns ndn.., down rows nup.., zero corner
@@ -576,8 +595,9 @@ __device__ void gemm_stage(const Ctx<R>& c)
     const R* U = at<R>(sm, c.L.U);
     const R* D = at<R>(sm, c.L.D);
     R* S = at<R>(sm, c.L.S);
-    const int ncol = p.ncol, ldU = p.ldU;
-    // two outputs of one row per thread (shared U row)
+    const int ldU = p.ldU;
+    // two outputs of one row per thread (shared U row); 16-byte pair loads
+    // over the padded rows (the padding is zero)
     const int half = (p.ndn + 1) / 2;
     for (int t = threadIdx.x; t < p.nup * half; t += kThreads) {
         const int i = t / half, j0 = t % half, j1 = j0 + half;
@@ -588,11 +608,16 @@ __device__ void gemm_stage(const Ctx<R>& c)
         Acc a0, a1;
         acc_init(a0);
         acc_init(a1);
-#pragma unroll 4
-        for (int q = 0; q < ncol; ++q) {
-            const R uq = u[q];
-            acc_madd(a0, uq, d0[q]);
-            acc_madd(a1, uq, d1[q]);
+#pragma unroll 2
+        for (int q = 0; q < ldU; q += 2) {
+            R ua, ub, xa, xb, ya, yb;
+            ld2(u + q, ua, ub);
+            ld2(d0 + q, xa, xb);
+            ld2(d1 + q, ya, yb);
+            acc_madd(a0, ua, xa);
+            acc_madd(a1, ua, ya);
+            acc_madd(a0, ub, xb);
+            acc_madd(a1, ub, yb);
         }
         S[i * p.ldS + j0] = acc_value(a0) + S[i * p.ldS + j0];
         if (two) S[i * p.ldS + j1] = acc_value(a1) + S[i * p.ldS + j1];
@@ -601,55 +626,279 @@ __device__ void gemm_stage(const Ctx<R>& c)
 }
 
 // ---------------------------------------------------------------------------
-// Stage 4: in-place Gauss-Jordan inverse with partial pivoting (first
-// maximum wins, as LAPACK idamax).  The pivot sequence is the one dgetrf
-// takes (matrixlapack.f90:20), so log|det| = sum log|pivot| and the sign
-// follow matrixlapack.f90:27-33.  Row interchanges are undone on the columns
-// of the inverse at the end.  Returns false for an exactly singular matrix.
+// Stage 4: inverse and log|det| of the pair matrix (matrixlapack.f90:13-41:
+// dgetrf + dgetri, log|det| = sum log|pivot|, sign from the pivots and the
+// row interchanges).  Partial pivoting, first maximum of |a| wins (idamax).
+// On return sm[L.S] holds inv(S) in natural order; returns false for an
+// exactly singular matrix.
+//
+// Main path (nd <= 128): blocked Gauss-Jordan with implicit row pivoting.
+// Column blocks of B are factored as n x B panels by warp 0 in registers
+// (a REDUX max/min pivot search, the pivot row broadcast by shuffles, no
+// block barrier inside a panel), and each factored panel is applied to the
+// other columns as one rank-B update
+//     A'[i][j] = [i not a pivot row of the block] A[i][j]
+//                + sum_c P[i][c] A[piv(k0+c)][j]
+// from one buffer into the other (sm[L.S] <-> sm[L.S2]).  Warp 0 factors
+// the next panel while warps 1..7 apply the current one: one block barrier
+// per B columns.  With pivot row p_k for column k, the final buffer M holds
+// M[p_a][b'] = inv(S)[a][p_b'], so inv(S)[a][b] = M[p_a][pos(b)] with
+// pos(p_k) = k; the last pass writes it in natural order.
 // ---------------------------------------------------------------------------
-// pivot search over rows k..n-1 of column k by one warp (first maximum
-// wins); lane 0 returns the row (n when the column is empty)
+__device__ __forceinline__ unsigned mag_hi(double v) { return (unsigned)(__double_as_longlong(v) >> 32) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned mag_lo(double v) { return (unsigned)(__double_as_longlong(v) & 0xffffffffll); }
+__device__ __forceinline__ unsigned mag_hi(df v) { return __float_as_uint(v.hi) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned mag_lo(df) { return 0u; }
+__device__ __forceinline__ double shfl_r(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ df shfl_r(df v, int src)
+{
+    return df{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// Named barrier 1 over the whole CTA: warp 0 waits, the others only arrive.
+__device__ __forceinline__ void bar1_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
+__device__ __forceinline__ void bar1_arrive() { asm volatile("bar.arrive 1, %0;" ::"n"(kThreads) : "memory"); }
+
+// Factor columns k0..k0+bw-1 of A (all n rows, rows pivoted in earlier
+// blocks excluded from the pivot search) by Gauss-Jordan steps restricted
+// to the panel.  Called by warp 0; lane l holds rows l + 32 s.  Records
+// piv[k], pvals[k] and rowpos[piv[k]] = k.  Returns false on a zero pivot.
+template <class R, int RPL, int B>
+__device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, int* piv, R* pvals, int* rowpos)
+{
+    const int lane = threadIdx.x & 31;
+    R v[RPL][B];
+    bool done[RPL];
+#pragma unroll
+    for (int s = 0; s < RPL; ++s) {
+        const int r = lane + 32 * s;
+        const bool ok = r < n;
+        done[s] = !ok || rowpos[r] < k0;
+#pragma unroll
+        for (int c = 0; c < B; ++c) v[s][c] = (ok && c < bw) ? A[r * ld + k0 + c] : rzero<R>();
+    }
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+        if (c >= bw) break;
+        // largest |a| among the rows not yet pivoted; smallest row on ties
+        unsigned kh[RPL], mh = 0u;
+#pragma unroll
+        for (int s = 0; s < RPL; ++s) {
+            kh[s] = done[s] ? 0u : mag_hi(v[s][c]);
+            mh = kh[s] > mh ? kh[s] : mh;
+        }
+        const unsigned gh = __reduce_max_sync(0xffffffffu, mh);
+        unsigned gl = 0u;
+        if constexpr (!is_df<R>::value) {
+            unsigned ml = 0u;
+#pragma unroll
+            for (int s = 0; s < RPL; ++s)
+                if (!done[s] && kh[s] == gh) {
+                    const unsigned l = mag_lo(v[s][c]);
+                    ml = l > ml ? l : ml;
+                }
+            gl = __reduce_max_sync(0xffffffffu, ml);
+        }
+        if (gh == 0u && gl == 0u) return false;   // no non-zero candidate: singular
+        unsigned mine = 0xffffffffu;
+#pragma unroll
+        for (int s = RPL - 1; s >= 0; --s)
+            if (!done[s] && kh[s] == gh && mag_lo(v[s][c]) == gl) mine = (unsigned)(lane + 32 * s);
+        const int pr = (int)__reduce_min_sync(0xffffffffu, mine);
+        const int op = pr & 31, sp = pr >> 5;
+        // pivot row, scaled; its column-c entry becomes 1/pivot
+        R rr[B];
+#pragma unroll
+        for (int c2 = 0; c2 < B; ++c2) {
+            R val = v[0][c2];
+#pragma unroll
+            for (int s = 1; s < RPL; ++s)
+                if (sp == s) val = v[s][c2];
+            rr[c2] = shfl_r(val, op);
+        }
+        const R pv = rr[c];
+        const R pinv = rcp(pv);
+#pragma unroll
+        for (int c2 = 0; c2 < B; ++c2) rr[c2] = (c2 == c) ? pinv : rr[c2] * pinv;
+#pragma unroll
+        for (int s = 0; s < RPL; ++s) {
+            const bool isp = (lane + 32 * s) == pr;
+            const R m = v[s][c];
+#pragma unroll
+            for (int c2 = 0; c2 < B; ++c2) v[s][c2] = isp ? rr[c2] : fms(c2 == c ? rzero<R>() : v[s][c2], m, rr[c2]);
+            done[s] = done[s] || isp;
+        }
+        if (lane == 0) {
+            piv[k0 + c] = pr;
+            pvals[k0 + c] = pv;
+            rowpos[pr] = k0 + c;
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < RPL; ++s) {
+        const int r = lane + 32 * s;
+        if (r < n)
+#pragma unroll
+            for (int c = 0; c < B; ++c)
+                if (c < bw) A[r * ld + k0 + c] = v[s][c];
+    }
+    __syncwarp();
+    return true;
+}
+
+// One element of the rank-B update of a factored block (see above).
+template <class R, int B>
+__device__ __forceinline__ R gj_apply(const R* cur, int ld, int i, int j, int k0, int bw, const int (&prow)[B],
+                                      const int* rowpos)
+{
+    typename AccOf<R>::type a;
+    acc_init(a);
+    const int rp = rowpos[i];
+    if (rp < k0 || rp >= k0 + bw) acc_add(a, cur[i * ld + j]);
+    const R* ri = cur + i * ld + k0;
+#pragma unroll
+    for (int c = 0; c < B; ++c)
+        if (c < bw) acc_madd(a, ri[c], cur[prow[c] * ld + j]);
+    return acc_value(a);
+}
+
+template <class R, int RPL, int B>
+__device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
+{
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    R* const A0 = at<R>(sm, c.L.S);
+    R* const A1 = at<R>(sm, c.L.S2);
+    int* piv = reinterpret_cast<int*>(sm + c.L.red + 512);                           // nd ints
+    R* pvals = reinterpret_cast<R*>(sm + c.L.red + 512 + 2 * DMC_MAX_PART);          // nd pivots
+    int* rowpos = reinterpret_cast<int*>(sm + c.L.red + 512 + 4 * DMC_MAX_PART);     // nd ints
+    __shared__ int s_sing;
+    __shared__ double s_logdet;
+    const int n = p.nd, ld = p.ldS;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < n; i += kThreads) rowpos[i] = n;
+    if (threadIdx.x == 0) s_sing = 0;
+    __syncthreads();
+    if (warp == 0 && !gj_panel<R, RPL, B>(A0, ld, n, 0, min(B, n), piv, pvals, rowpos) && lane == 0) s_sing = 1;
+    __syncthreads();
+    R* cur = A0;
+    R* nxt = A1;
+    for (int k0 = 0; k0 < n; k0 += B) {
+        if (s_sing) break;
+        const int bw = min(B, n - k0), k1 = k0 + bw, bw1 = min(B, n - k1);
+        int prow[B];
+#pragma unroll
+        for (int q = 0; q < B; ++q) prow[q] = q < bw ? piv[k0 + q] : 0;
+        // the last block writes the natural order directly when it lands in S
+        const bool scatter = (bw1 == 0) && (nxt == A0);
+        if (bw1 > 0) {
+            // columns of the next panel first, by everyone
+            for (int e = threadIdx.x; e < n * bw1; e += kThreads) {
+                const int i = e / bw1, j = k1 + e % bw1;
+                nxt[i * ld + j] = gj_apply<R, B>(cur, ld, i, j, k0, bw, prow, rowpos);
+            }
+            if (warp == 0) {
+                bar1_sync();
+                if (!gj_panel<R, RPL, B>(nxt, ld, n, k1, bw1, piv, pvals, rowpos) && lane == 0) s_sing = 1;
+            } else {
+                bar1_arrive();
+            }
+        }
+        if (bw1 == 0 || warp > 0) {
+            // every other column: warps 1..7 (all warps in the last block)
+            const int nt = bw1 > 0 ? kThreads - 32 : kThreads;
+            const int t0 = bw1 > 0 ? (int)threadIdx.x - 32 : (int)threadIdx.x;
+            const int nc = n - bw1;
+            for (int e = t0; e < n * nc; e += nt) {
+                const int i = e / nc, jj = e % nc;
+                const int j = jj < k1 ? jj : jj + bw1;
+                // the block's own (factored) columns pass through unchanged
+                const R val = (j >= k0 && j < k1) ? cur[i * ld + j] : gj_apply<R, B>(cur, ld, i, j, k0, bw, prow, rowpos);
+                if (scatter)
+                    nxt[rowpos[i] * ld + piv[j]] = val;
+                else
+                    nxt[i * ld + j] = val;
+            }
+        }
+        __syncthreads();
+        R* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    const bool sing = s_sing != 0;
+    // natural order, sign of the row permutation and of the pivots, log|det|
+    int odd = 0;
+    if (!sing) {
+        const bool copy = (cur == A1);
+        for (int e = threadIdx.x; e < n * n; e += kThreads) {
+            const int a = e / n, b = e % n;
+            if (copy) A0[a * ld + b] = A1[piv[a] * ld + rowpos[b]];
+            if (a < b && piv[a] > piv[b]) odd ^= 1;
+        }
+        for (int q = threadIdx.x; q < n; q += kThreads)
+            if (is_neg(pvals[q])) odd ^= 1;
+        if (warp == 0) {
+            double ls = 0.0;
+            for (int q = lane; q < n; q += 32) ls += log(fabs(to_double(pvals[q])));
+            ls = warp_sum(ls);
+            if (lane == 0) s_logdet = ls;
+        }
+    }
+    const int nodd = __syncthreads_count(odd);
+    logdet = sing ? 0.0 : s_logdet;
+    sgn = (nodd & 1) ? -1 : 1;
+    return !sing;
+}
+
+// Unblocked in-place Gauss-Jordan with explicit row interchanges, for
+// matrices the blocked path does not take (nd > 128 or no second buffer).
+// Pivot search by warp 0 one column ahead of the elimination.
+__device__ __forceinline__ unsigned long long pivot_key(double v, int row)
+{
+    const unsigned long long m = ((unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull) >> 12;
+    return (m << 12) | (unsigned long long)(4095 - row);
+}
+__device__ __forceinline__ unsigned long long pivot_key(df v, int row)
+{
+    const unsigned long long m = (unsigned long long)((unsigned)__float_as_uint(v.hi) & 0x7fffffffu);
+    return (m << 32) | (unsigned long long)(0xffffffffu - (unsigned)row);
+}
+
+// pivot search over rows k..n-1 of column k by one warp; every lane
+// returns the pivot row and its value
 template <class R>
 __device__ __forceinline__ int warp_pivot(const R* A, int ld, int n, int k, R& pv)
 {
     const int lane = threadIdx.x & 31;
-    R best = rzero<R>();
-    int bi = n;
+    unsigned long long best = 0ull;
     for (int i = k + lane; i < n; i += 32) {
-        const R v = A[i * ld + k];
-        if (bi == n || abs_gt(v, best)) {
-            best = v;
-            bi = i;
-        }
+        const unsigned long long key = pivot_key(A[i * ld + k], i);
+        best = key > best ? key : best;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        R ob;
-        if constexpr (is_df<R>::value) {
-            ob.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
-            ob.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
-        } else {
-            ob = __shfl_xor_sync(0xffffffffu, best, o);
-        }
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        const bool take = (oi != n) && (bi == n || abs_gt(ob, best) || (!abs_gt(best, ob) && oi < bi));
-        if (take) {
-            best = ob;
-            bi = oi;
-        }
+        const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+        best = ob > best ? ob : best;
     }
-    pv = best;
+    int bi;
+    if constexpr (is_df<R>::value)
+        bi = (int)(0xffffffffu - (unsigned)(best & 0xffffffffull));
+    else
+        bi = 4095 - (int)(best & 4095ull);
+    if (best == 0ull || bi < k || bi >= n) bi = k;   // empty column: report row k (its value is zero)
+    pv = A[bi * ld + k];
     return bi;
 }
 
 template <class R>
-__device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
+__device__ bool inverse_unblocked(const Ctx<R>& c, double& logdet, int& sgn)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
     R* A = at<R>(sm, c.L.S);
     R* colk = at<R>(sm, c.L.colk);
-    int* piv = reinterpret_cast<int*>(sm + c.L.red + 512);   // nd ints
+    int* piv = reinterpret_cast<int*>(sm + c.L.red + 512);                    // nd ints
+    R* pvals = reinterpret_cast<R*>(sm + c.L.red + 512 + 2 * DMC_MAX_PART);   // nd pivots
     __shared__ R s_pinv;
     __shared__ int s_piv;
     __shared__ int s_sing;
@@ -657,10 +906,6 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
     __shared__ int s_sgn;
     const int n = p.nd, ld = p.ldS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double mant = 1.0;
-    int expo = 0;
-    int sg = 1;
-    // pivot of column 0
     if (warp == 0) {
         R pv;
         const int bi = warp_pivot<R>(A, ld, n, 0, pv);
@@ -668,10 +913,14 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
             s_sing = is_zero(pv) ? 1 : 0;
             s_piv = bi;
             piv[0] = bi;
+            pvals[0] = pv;
             if (!is_zero(pv)) s_pinv = rcp(pv);
         }
     }
     __syncthreads();
+    const int ew = kThreads - 32;
+    const int e0 = (int)threadIdx.x - 32;
+    const int di = ew / n, dc = ew % n;
     for (int k = 0; k < n; ++k) {
         if (s_sing) break;
         const int pr = s_piv;
@@ -679,10 +928,11 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
         // save column k (rows in swapped order), swap rows k/pr, scale row k
         for (int t = threadIdx.x; t < n; t += kThreads) {
             const int src = (t == k) ? pr : ((t == pr) ? k : t);
-            colk[t] = A[src * ld + k];
+            const R ck = A[src * ld + k];
+            const R a = A[k * ld + t];
+            const R b = A[pr * ld + t];
+            colk[t] = ck;
             if (t != k) {
-                const R a = A[k * ld + t];
-                const R b = A[pr * ld + t];
                 R nk = a;
                 if (pr != k) {
                     A[pr * ld + t] = a;
@@ -693,17 +943,7 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
         }
         __syncthreads();
         if (warp == 0) {
-            // look-ahead: warp 0 eliminates column k+1 and finds its pivot
-            // while the other warps eliminate the rest of the matrix
-            if (lane == 0) {
-                // |det| kept as mantissa * 2^exponent; one log at the end
-                int ex;
-                const R pvv = colk[k];
-                mant = frexp(mant * fabs(to_double(pvv)), &ex);
-                expo += ex;
-                sg = is_neg(pvv) ? -sg : sg;
-                if (pr != k) sg = -sg;
-            }
+            // look-ahead: column k+1 and its pivot
             if (k + 1 < n) {
                 const R akn = A[k * ld + k + 1];
                 for (int i = lane; i < n; i += 32)
@@ -712,6 +952,7 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
                 R pv;
                 const int bi = warp_pivot<R>(A, ld, n, k + 1, pv);
                 if (lane == 0) {
+                    pvals[k + 1] = pv;
                     if (is_zero(pv)) {
                         s_sing = 1;
                     } else {
@@ -722,14 +963,16 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
                 }
             }
         } else {
-            const int tot = n * n;
-            for (int t = threadIdx.x - 32; t < tot; t += kThreads - 32) {
-                const int i = t / n, cc = t % n;
-                if (i == k || cc == k + 1) continue;
-                if (cc == k)
-                    A[i * ld + k] = -(colk[i] * pinv);
-                else
-                    A[i * ld + cc] = fms(A[i * ld + cc], colk[i], A[k * ld + cc]);
+            int i = e0 / n, cc = e0 % n;
+            for (int t = e0; t < n * n; t += ew) {
+                if (i != k && cc != k + 1)
+                    A[i * ld + cc] = (cc == k) ? -(colk[i] * pinv) : fms(A[i * ld + cc], colk[i], A[k * ld + cc]);
+                i += di;
+                cc += dc;
+                if (cc >= n) {
+                    cc -= n;
+                    ++i;
+                }
             }
             if (threadIdx.x == 32) A[k * ld + k] = pinv;
         }
@@ -737,26 +980,55 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
     }
     const bool sing = s_sing != 0;
     if (!sing) {
-        // undo the row interchanges on the columns: inv(S) = inv(P S) P
-        for (int k = n - 1; k >= 0; --k) {
-            const int pr = piv[k];
-            if (pr != k)
-                for (int t = threadIdx.x; t < n; t += kThreads) {
-                    const R a = A[t * ld + k];
-                    A[t * ld + k] = A[t * ld + pr];
-                    A[t * ld + pr] = a;
+        // undo the row interchanges on the columns, last first (dgetri);
+        // each thread owns whole rows, so no barrier between swaps
+        for (int r = threadIdx.x; r < n; r += kThreads)
+            for (int q = n - 1; q >= 0; --q) {
+                const int pq = piv[q];
+                if (pq != q) {
+                    const R t = A[r * ld + q];
+                    A[r * ld + q] = A[r * ld + pq];
+                    A[r * ld + pq] = t;
                 }
-            __syncthreads();
-        }
+            }
     }
-    if (threadIdx.x == 0) {
-        s_logdet = log(mant) + expo * 0.69314718055994530942;
-        s_sgn = sg;
+    if (warp == 0) {
+        double ls = 0.0;
+        int neg = 0, swp = 0;
+        if (!sing)
+            for (int q = lane; q < n; q += 32) {
+                const R v = pvals[q];
+                ls += log(fabs(to_double(v)));
+                neg += is_neg(v) ? 1 : 0;
+                swp += (piv[q] != q) ? 1 : 0;
+            }
+        ls = warp_sum(ls);
+        for (int o = 16; o > 0; o >>= 1) {
+            neg += __shfl_xor_sync(0xffffffffu, neg, o);
+            swp += __shfl_xor_sync(0xffffffffu, swp, o);
+        }
+        if (lane == 0) {
+            s_logdet = ls;
+            s_sgn = ((neg + swp) & 1) ? -1 : 1;
+        }
     }
     __syncthreads();
     logdet = s_logdet;
     sgn = s_sgn;
     return !sing;
+}
+
+template <class R>
+__device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
+{
+    const int n = c.p.nd;
+    if (c.L.S2 >= 0) {
+        if (n <= 32) return inverse_blocked<R, 1, 8>(c, logdet, sgn);
+        if (n <= 64) return inverse_blocked<R, 2, 8>(c, logdet, sgn);
+        if (n <= 96) return inverse_blocked<R, 3, 8>(c, logdet, sgn);
+        if (n <= 128) return inverse_blocked<R, 4, 4>(c, logdet, sgn);
+    }
+    return inverse_unblocked<R>(c, logdet, sgn);
 }
 
 // ---------------------------------------------------------------------------
@@ -792,19 +1064,24 @@ __device__ void drift_stage(const Ctx<R>& c)
     for (int it = b; it < e; ++it) {
         const int pt = it / nq, q = it % nq + 1;
         const KV& K = kq[q];
-        const int qc = 2 * q - 1, qs = 2 * q;
+        const int qc = 2 * q - 2;   // (cos, sin) pair of k vector q
         R t, l;
         if (pt < p.nup) {
             const int i = pt;
             Acc gc, gs;
             acc_init(gc);
             acc_init(gs);
+            const R* dq = D + qc;
+            const R* sc = Si + i;
             for (int j = 0; j < p.ndn; ++j) {
-                const R sji = Si[j * ld + i];
-                acc_madd(gc, D[j * ldU + qc], sji);
-                acc_madd(gs, D[j * ldU + qs], sji);
+                const R sji = sc[j * ld];
+                R dc_, ds_;
+                ld2(dq + j * ldU, dc_, ds_);
+                acc_madd(gc, dc_, sji);
+                acc_madd(gs, ds_, sji);
             }
-            const R uc = U[i * ldU + qc], us = U[i * ldU + qs];
+            R uc, us;
+            ld2(U + i * ldU + qc, uc, us);
             const R vgc = acc_value(gc), vgs = acc_value(gs);
             t = uc * vgs - us * vgc;
             l = uc * vgc + us * vgs;
@@ -813,12 +1090,17 @@ __device__ void drift_stage(const Ctx<R>& c)
             Acc hc, hs;
             acc_init(hc);
             acc_init(hs);
+            const R* srow = Si + j * ld;
+            const R* uq = U + qc;
             for (int i = 0; i < p.nup; ++i) {
-                const R sji = Si[j * ld + i];
-                acc_madd(hc, sji, U[i * ldU + qc]);
-                acc_madd(hs, sji, U[i * ldU + qs]);
+                const R sji = srow[i];
+                R uc_, us_;
+                ld2(uq + i * ldU, uc_, us_);
+                acc_madd(hc, sji, uc_);
+                acc_madd(hs, sji, us_);
             }
-            const R dc = D[j * ldU + qc], ds = D[j * ldU + qs];
+            R dc, ds;
+            ld2(D + j * ldU + qc, dc, ds);
             const R vhc = acc_value(hc), vhs = acc_value(hs);
             t = vhs * dc - vhc * ds;
             l = vhc * dc + vhs * ds;
@@ -945,7 +1227,7 @@ __device__ void beta_drift_stage(const Ctx<R>& c)
                     const double* k = p.akdn[jj];
                     double s, co;
                     sincos(k[0] * xp[0] + k[1] * xp[1] + k[2] * xp[2], &s, &co);
-                    const double w = to_double(Si[j * ld + (nup + jj)]);
+                    const double w = to_double(Si[j * ld + nup + jj]);
                     const double gcoef = p.sindn[jj] ? co : -s;
                     const double val = p.sindn[jj] ? s : co;
                     g0 += w * k[0] * gcoef;

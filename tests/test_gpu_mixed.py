@@ -69,3 +69,25 @@ def test_mixed_generations_track_fp64():
     elmx = -sysd.hbar * wmx["d2psi"] + wmx["v"]
     assert np.max(np.abs(el64 - elmx) / np.maximum(np.abs(el64), 1.0)) < EL_TOL
     assert np.allclose(e64[0], emx[0], rtol=1e-6)
+
+
+@pytest.mark.parametrize("rel", [1.3e-8, -1.3e-8])
+def test_mixed_pair_within_fp32_ulp_of_half_box(rel):
+    """An up-down pair whose distance is within one FP32 ulp of L/2 (the end
+    of the beta table) must land on the same side of the range as in FP64."""
+    sysd, rund, orc, x = walkers("n66", 8, 5)
+    el = orc.info.el
+    u = np.array([0.3, 0.5, -0.81])
+    u /= np.linalg.norm(u)
+    nup = sysd.nbin[0]
+    for w in range(x.shape[0]):
+        x[w, nup + w] = x[w, w] + 0.5 * el * (1.0 + rel) * u
+    ref = orc.hpsi(x)
+    with capi.Context(sysd, rund, precision="mixed") as ctx:
+        got = ctx.hpsi(x)
+    hb = sysd.hbar
+    el_g = -hb * got["d2psi"] + got["v"]
+    el_r = -hb * ref["d2psi"] + ref["v"]
+    err = np.abs(el_g - el_r) / np.maximum(np.abs(el_r), 1.0)
+    print(f"rel {rel:+.1e}: max rel err E_L {err.max():.2e}")
+    assert err.max() < EL_TOL
