@@ -1,6 +1,6 @@
 """Build the in-tree CUDA library ``libdmcbcs_gb300.so`` for sm_103a.
 
-Three translation units are compiled in parallel with nvcc (one -gencode,
+The translation units are compiled in parallel with nvcc (one -gencode,
 no cmake) and linked into a shared library next to this file.  The build is
 skipped when the library is newer than every source.
 """
@@ -16,7 +16,7 @@ LIB = os.path.join(HERE, "libdmcbcs_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["dmc_kernels.cu", "dmc_capi.cu", "dmc_setup.cpp", "dmc_noalloc.cu"]
+SOURCES = ["dmc_kernels.cu", "dmc_capi.cu", "dmc_setup.cpp", "dmc_noalloc.cu", "dmc_single.cu"]
 
 
 def _nvcc():

@@ -24,7 +24,8 @@ EXPORTS = [
     "dmc_load_walkers", "dmc_get_walkers", "dmc_initial_eval", "dmc_num_walkers", "dmc_step", "dmc_branch",
     "dmc_generation", "dmc_zero_estimators", "dmc_get_estimators", "dmc_block_update", "dmc_get_wtisto",
     "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers", "dmc_branch_noalloc",
-    "dmc_set_precision", "dmc_get_precision", "dmc_probe_peak",
+    "dmc_set_precision", "dmc_get_precision", "dmc_probe_peak", "dmc_sr_accumulate", "dmc_sr_get_sums",
+    "dmc_sr_zero", "dmc_sr_update",
 ]
 
 PREC_FP64 = 0
@@ -95,6 +96,10 @@ def load(path=LIB_PATH):
     L.dmc_set_precision.argtypes = [vp, C.c_int]
     L.dmc_probe_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.dmc_get_precision.argtypes = [vp, C.POINTER(C.c_int)]
+    L.dmc_sr_accumulate.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.dmc_sr_get_sums.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_int64)]
+    L.dmc_sr_zero.argtypes = [vp]
+    L.dmc_sr_update.argtypes = [vp, C.c_double, C.c_double, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.dmc_branch_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(abi.DevStack),
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
     _lib = L
@@ -160,7 +165,7 @@ class Context:
             n = 3 * self.info.nk
         elif which == 8:
             n = self.info.nk
-        elif which == 9:
+        elif which in (9, 10):
             n = self.norb
         out = np.zeros(n)
         self._check(load().dmc_get_table(self._h, which, out, n))
@@ -211,6 +216,71 @@ class Context:
         s = np.zeros(nb, np.int32)
         self._check(load().dmc_matinv_batch(self._h, n, nb, f, d, s))
         return np.transpose(f.reshape(nb, n, n), (0, 2, 1)), d, s
+
+    # ---- single-particle moves and parameter derivatives --------------------
+    def _moves(self, x, ipart, d):
+        x = self._x(x)
+        nw = x.shape[0]
+        ip = np.ascontiguousarray(np.broadcast_to(np.asarray(ipart, dtype=np.int32), (nw,)))
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(d, dtype=np.float64), (nw, 3)))
+        return x, nw, ip, d
+
+    def bcsone(self, x, smati, ipart, dr):
+        """Determinant ratio for moving particle ipart (1-based) of each walker
+        by -dr (dr = xold - xnew), from the inverse smati returned by bcs()."""
+        x, nw, ip, d = self._moves(x, ipart, dr)
+        sm = np.ascontiguousarray(smati, dtype=np.float64).reshape(nw, self.nd * self.nd)
+        out = np.zeros(nw)
+        self._check(load().dmc_bcsone_batch(self._h, nw, x, sm, ip, d, out))
+        return out
+
+    def getphione(self, x, ipart, drr):
+        """Jastrow ratio exp(U' - U) for the same single-particle moves."""
+        x, nw, ip, d = self._moves(x, ipart, drr)
+        out = np.zeros(nw)
+        self._check(load().dmc_getphione_batch(self._h, nw, x, ip, d, out))
+        return out
+
+    def move1(self, x, smati, ipart, xnew):
+        """Psi ratio of move1 (wavefunction.f90:393-404): xnew[nw, 3]."""
+        x = self._x(x)
+        ip = np.broadcast_to(np.asarray(ipart, dtype=np.int64), (x.shape[0],))
+        drr = x[np.arange(x.shape[0]), ip - 1] - np.asarray(xnew, dtype=np.float64)
+        return self.getphione(x, ipart, drr) * self.bcsone(x, smati, ipart, drr)
+
+    def getderbcs(self, x):
+        """d log|det| / d vorb(shell), shape [nw, norb]."""
+        x = self._x(x)
+        nw = x.shape[0]
+        out = np.zeros((nw, self.norb))
+        self._check(load().dmc_getderbcs_batch(self._h, nw, x, out))
+        return out
+
+    def sr_accumulate(self):
+        n = C.c_int64()
+        self._check(load().dmc_sr_accumulate(self._h, C.byref(n)))
+        return n.value
+
+    def sr_sums(self):
+        npr = self.norb
+        o = dict(ovec=np.zeros(npr), ovecw=np.zeros(npr), pmat=np.zeros(npr * npr), e=np.zeros(2))
+        n = C.c_int64()
+        self._check(load().dmc_sr_get_sums(self._h, *[_opt(o[k]) for k in ("ovec", "ovecw", "pmat", "e")],
+                                           C.byref(n)))
+        o["pmat"] = o["pmat"].reshape(npr, npr, order="F")
+        o["n"] = n.value
+        return o
+
+    def sr_zero(self):
+        self._check(load().dmc_sr_zero(self._h))
+
+    def sr_update(self, delta0, eps):
+        """One SR step; returns (newpars, eave, eerr) and applies newpars to vorb."""
+        newp = np.zeros(self.norb)
+        ea, ee = C.c_double(), C.c_double()
+        self._check(load().dmc_sr_update(self._h, float(delta0), float(eps), _opt(newp), C.byref(ea),
+                                         C.byref(ee)))
+        return newp, ea.value, ee.value
 
     # ---- population ----------------------------------------------------------
     def init_walkers(self):

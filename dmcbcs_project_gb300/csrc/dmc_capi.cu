@@ -128,6 +128,10 @@ struct dmc_ctx {
     DevBuf<double> bx, bpsil, bdpsi, bd2psi, bv, bvext, bpsigl, bdpsig, bd2psig, bsinv;
     DevBuf<int> bis;
     DevBuf<unsigned char> flush;
+    // single-particle moves and parameter derivatives
+    DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
+    DevBuf<int> sip;
+    int64_t sr_count = 0;
     int64_t launches = 0;
     std::string err;
 };
@@ -221,6 +225,7 @@ int upload_kv(dmc_ctx* c)
         }
         d.k2 = K.k2;
         d.v = q == 0 ? c->S.vorb[0] : 2.0 * c->S.vorb[K.shell - 1];
+        d.shell = q == 0 ? 1 : K.shell;
     }
     CK(c->kv.alloc(kv.size()));
     CK(cudaMemcpy(c->kv.p, kv.data(), kv.size() * sizeof(KVecDev), cudaMemcpyHostToDevice));
@@ -539,6 +544,10 @@ int dmc_get_table(const dmc_ctx* c, int which, double* out, int n)
     case 9:
         if (n < S.norb) return DMC_ERR_INVALID;
         for (int q = 0; q < S.norb; ++q) out[q] = S.numsh[q];
+        return DMC_OK;
+    case 10:
+        if (n < S.norb) return DMC_ERR_INVALID;
+        for (int q = 0; q < S.norb; ++q) out[q] = S.vorb[q];
         return DMC_OK;
     }
     return DMC_ERR_INVALID;
@@ -903,23 +912,228 @@ int dmc_get_wtisto(dmc_ctx* c, int64_t* hist)
     return DMC_OK;
 }
 
+// ---- single-particle moves and parameter derivatives ---------------------
+
+static int check_moves(dmc_ctx* c, int nw, const double* x, const int* ipart, const double* d, const double* ratio)
+{
+    if (nw < 0 || (nw > 0 && (!x || !ipart || !d || !ratio))) return fail(c, DMC_ERR_INVALID, "bad move arguments");
+    for (int w = 0; w < nw; ++w)
+        if (ipart[w] < 1 || ipart[w] > c->S.npart) return fail(c, DMC_ERR_INVALID, "particle index out of range");
+    return DMC_OK;
+}
+
+static int stage_moves(dmc_ctx* c, int nw, const double* x, const int* ipart, const double* d)
+{
+    const size_t n3 = (size_t)c->n3;
+    CK(c->sx.alloc(nw * n3));
+    CK(c->sip.alloc(nw));
+    CK(c->sdr.alloc(3 * (size_t)nw));
+    CK(c->sratio.alloc(nw));
+    CK(cudaMemcpyAsync(c->sx.p, x, nw * n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->sip.p, ipart, nw * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->sdr.p, d, 3 * nw * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return DMC_OK;
+}
+
 int dmc_bcsone_batch(dmc_ctx* c, int nw, const double* x, const double* smati, const int* ipart, const double* dr,
                      double* ratio)
 {
-    (void)nw; (void)x; (void)smati; (void)ipart; (void)dr; (void)ratio;
-    return fail(c, DMC_ERR_UNSUPPORTED, "bcsone is not built yet");
+    if (!c) return DMC_ERR_INVALID;
+    int rc = check_moves(c, nw, x, ipart, dr, ratio);
+    if (rc || nw == 0) return rc;
+    if (!smati) return fail(c, DMC_ERR_INVALID, "bcsone needs the stored inverse");
+    const size_t nd2 = (size_t)c->S.nd * c->S.nd;
+    if ((rc = stage_moves(c, nw, x, ipart, dr))) return rc;
+    CK(c->ssinv.alloc(nw * nd2));
+    CK(cudaMemcpyAsync(c->ssinv.p, smati, nw * nd2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_bcsone(c->P, c->kv.p, c->tud.p, c->sx.p, c->ssinv.p, c->sip.p, c->sdr.p, c->sratio.p, nw, c->stream));
+    ++c->launches;
+    CK(cudaMemcpyAsync(ratio, c->sratio.p, nw * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
 }
 
 int dmc_getphione_batch(dmc_ctx* c, int nw, const double* x, const int* ipart, const double* drr, double* ratio)
 {
-    (void)nw; (void)x; (void)ipart; (void)drr; (void)ratio;
-    return fail(c, DMC_ERR_UNSUPPORTED, "getphione is not built yet");
+    if (!c) return DMC_ERR_INVALID;
+    int rc = check_moves(c, nw, x, ipart, drr, ratio);
+    if (rc || nw == 0) return rc;
+    if ((rc = stage_moves(c, nw, x, ipart, drr))) return rc;
+    CK(launch_getphione(c->P, c->tud.p, c->tss.p, c->sx.p, c->sip.p, c->sdr.p, c->sratio.p, nw, c->stream));
+    ++c->launches;
+    CK(cudaMemcpyAsync(ratio, c->sratio.p, nw * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
+// d log|det| / d vorb for nw device-resident configurations (FP64 inverse)
+static int derbcs_device(dmc_ctx* c, int nw, const double* dx, double* dder)
+{
+    const size_t nd2 = (size_t)c->S.nd * c->S.nd;
+    CK(c->ssinv.alloc(nw * nd2));
+    const int prec = c->precision;
+    c->precision = DMC_PREC_FP64;
+    int rc = run_eval(c, MODE_BCS, nw, dx, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, c->ssinv.p, c->stream);
+    c->precision = prec;
+    if (rc) return rc;
+    ++c->launches;
+    CK(launch_derbcs(c->P, c->kv.p, dx, c->ssinv.p, dder, nw, c->grid, c->stream));
+    ++c->launches;
+    return DMC_OK;
 }
 
 int dmc_getderbcs_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)
 {
-    (void)nw; (void)x; (void)dpsi;
-    return fail(c, DMC_ERR_UNSUPPORTED, "getderbcs is not built yet");
+    if (!c) return DMC_ERR_INVALID;
+    if (nw < 0 || (nw > 0 && (!x || !dpsi))) return fail(c, DMC_ERR_INVALID, "bad getderbcs arguments");
+    if (nw == 0) return DMC_OK;
+    const size_t n3 = (size_t)c->n3, np = (size_t)c->S.norb;
+    CK(c->sx.alloc(nw * n3));
+    CK(c->sder.alloc(nw * np));
+    CK(cudaMemcpyAsync(c->sx.p, x, nw * n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = derbcs_device(c, nw, c->sx.p, c->sder.p);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dpsi, c->sder.p, nw * np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
+// ---- stochastic reconfiguration ---------------------------------------------
+
+static int sr_buffers(dmc_ctx* c)
+{
+    const size_t np = (size_t)c->S.norb, nout = np * np + 2 * np + 2;
+    if (c->srsum.n < nout) {
+        CK(c->srsum.alloc(nout));
+        CK(cudaMemset(c->srsum.p, 0, nout * sizeof(double)));
+        c->sr_count = 0;
+    }
+    return DMC_OK;
+}
+
+int dmc_sr_accumulate(dmc_ctx* c, int64_t* nsamples)
+{
+    if (!c) return DMC_ERR_INVALID;
+    int rc = sr_buffers(c);
+    if (rc) return rc;
+    const int n = c->n, np = c->S.norb;
+    if (n > 0) {
+        StackBufs& s = c->st[c->istin];
+        CK(c->sder.alloc((size_t)n * np));
+        if ((rc = derbcs_device(c, n, s.x.p, c->sder.p))) return rc;
+        CK(launch_sr_sums(c->sder.p, s.d2psi.p, s.v.p, n, np, c->S.hbar, c->S.eunit, c->S.npart, c->srsum.p,
+                          c->stream));
+        ++c->launches;
+        if ((rc = reverse_stacks(c))) return rc;
+        ++c->launches;
+        c->sr_count += n;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    if (nsamples) *nsamples = c->sr_count;
+    return DMC_OK;
+}
+
+int dmc_sr_get_sums(dmc_ctx* c, double* ovec, double* ovecw, double* pmat, double* e, int64_t* nsamples)
+{
+    if (!c) return DMC_ERR_INVALID;
+    int rc = sr_buffers(c);
+    if (rc) return rc;
+    const size_t np = (size_t)c->S.norb, nout = np * np + 2 * np + 2;
+    std::vector<double> h(nout);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(h.data(), c->srsum.p, nout * sizeof(double), cudaMemcpyDeviceToHost));
+    if (ovec) std::copy(h.begin(), h.begin() + np, ovec);
+    if (ovecw) std::copy(h.begin() + np, h.begin() + 2 * np, ovecw);
+    if (pmat) std::copy(h.begin() + 2 * np, h.begin() + 2 * np + np * np, pmat);
+    if (e) {
+        e[0] = h[nout - 2];
+        e[1] = h[nout - 1];
+    }
+    if (nsamples) *nsamples = c->sr_count;
+    return DMC_OK;
+}
+
+int dmc_sr_zero(dmc_ctx* c)
+{
+    if (!c) return DMC_ERR_INVALID;
+    int rc = sr_buffers(c);
+    if (rc) return rc;
+    const size_t np = (size_t)c->S.norb, nout = np * np + 2 * np + 2;
+    CK(cudaMemsetAsync(c->srsum.p, 0, nout * sizeof(double), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->sr_count = 0;
+    return DMC_OK;
+}
+
+// In-place inverse of a column-major n x n matrix by Gauss-Jordan elimination
+// with partial pivoting (the SR matrix: n = norb, at most a few dozen).
+// Returns false for an exactly singular matrix.
+static bool host_inverse(int n, double* a)
+{
+    std::vector<int> piv(n);
+    auto A = [&](int i, int j) -> double& { return a[i + (size_t)j * n]; };
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int i = k + 1; i < n; ++i)
+            if (std::fabs(A(i, k)) > std::fabs(A(p, k))) p = i;
+        if (A(p, k) == 0.0) return false;
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < n; ++j) std::swap(A(k, j), A(p, j));
+        const double pinv = 1.0 / A(k, k);
+        A(k, k) = 1.0;
+        for (int j = 0; j < n; ++j) A(k, j) *= pinv;
+        for (int i = 0; i < n; ++i) {
+            if (i == k) continue;
+            const double m = A(i, k);
+            A(i, k) = 0.0;
+            for (int j = 0; j < n; ++j) A(i, j) -= m * A(k, j);
+        }
+    }
+    for (int k = n - 1; k >= 0; --k)
+        if (piv[k] != k)
+            for (int i = 0; i < n; ++i) std::swap(A(i, k), A(i, piv[k]));
+    return true;
+}
+
+int dmc_sr_update(dmc_ctx* c, double delta0, double eps, double* newpars, double* eave, double* eerr)
+{
+    if (!c) return DMC_ERR_INVALID;
+    const int np = c->S.norb;
+    if (c->sr_count <= 0) return fail(c, DMC_ERR_INVALID, "no samples accumulated for the SR step");
+    std::vector<double> ovec(np), ovecw(np), pmat((size_t)np * np), e(2);
+    int64_t ns = 0;
+    int rc = dmc_sr_get_sums(c, ovec.data(), ovecw.data(), pmat.data(), e.data(), &ns);
+    if (rc) return rc;
+    const double cnt = (double)ns;
+    for (int i = 0; i < np; ++i) {
+        ovec[i] /= cnt;
+        ovecw[i] /= cnt;
+    }
+    for (auto& q : pmat) q /= cnt;
+    const double esum = e[0] / cnt, esum2 = e[1] / cnt;
+    const double err = std::sqrt(std::fabs(esum * esum - esum2) / cnt);
+    std::vector<double> f(np), dpar(np);
+    for (int i = 0; i < np; ++i) f[i] = -2.0 * ovecw[i] + 2.0 * ovec[i] * esum;
+    for (int i = 0; i < np; ++i) {
+        for (int j = 0; j < np; ++j) pmat[i + (size_t)j * np] -= ovec[i] * ovec[j];
+        pmat[i + (size_t)i * np] += eps;
+    }
+    if (!host_inverse(np, pmat.data())) return fail(c, DMC_ERR_INVALID, "singular SR matrix");
+    std::vector<double> vorb(c->S.vorb);
+    for (int i = 0; i < np; ++i) {
+        double sm = 0.0;
+        for (int j = 0; j < np; ++j) sm += pmat[i + (size_t)j * np] * f[j];
+        dpar[i] = delta0 * sm;
+        vorb[i] += dpar[i];
+    }
+    if ((rc = dmc_set_vorb(c, vorb.data(), np))) return rc;
+    if ((rc = dmc_sr_zero(c))) return rc;
+    if (newpars) std::copy(dpar.begin(), dpar.end(), newpars);
+    if (eave) *eave = esum;
+    if (eerr) *eerr = err;
+    return DMC_OK;
 }
 
 int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, int64_t* walker_steps,

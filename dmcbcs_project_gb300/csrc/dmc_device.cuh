@@ -55,7 +55,7 @@ struct __align__(16) KVecDev {
     double v;       // 2 * vorb(shell) (psislaterbcs.f90:259)
     double pad;
     int n[3];
-    int pad2;
+    int shell;      // 1-based shell index (1 for k = 0)
 };
 
 enum Mode : int {

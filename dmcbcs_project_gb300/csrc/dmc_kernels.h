@@ -21,6 +21,20 @@ cudaError_t launch_branch(const DevStack& in, const DevStack& out, int n, int n3
                           int* counts, int* offs, unsigned long long* irn1, unsigned long long* wtisto,
                           cudaStream_t st);
 
+// Single-particle ratios and parameter derivatives (dmc_single.cu)
+cudaError_t launch_bcsone(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x,
+                          const double* smati, const int* ipart, const double* dr, double* ratio, int nw,
+                          cudaStream_t st);
+cudaError_t launch_getphione(const DevParams& p, const TabUD* tud, const TabSS* tss, const double* x,
+                             const int* ipart, const double* drr, double* ratio, int nw, cudaStream_t st);
+size_t derbcs_smem_bytes(const DevParams& p);
+cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x, const double* smati, double* dpsi,
+                          int nw, int grid, cudaStream_t st);
+// adds the calder sums of n walkers (pop order) to sums[np*np + 2*np + 2]:
+// ovec, ovecw, pmat (column-major), esum, esum2
+cudaError_t launch_sr_sums(const double* der, const double* d2psi, const double* v, int n, int np, double hbar,
+                           double eunit, int npart, double* sums, cudaStream_t st);
+
 // FMA throughput of the FP64 (kind 0) or FP32 (kind 1) pipe, TFLOP/s
 cudaError_t probe_fma_peak(int kind, int nsm, double* tflops);
 
