@@ -633,15 +633,16 @@ __device__ void gemm_stage(const Ctx<R>& c)
 // exactly singular matrix.
 //
 // Main path (nd <= 128): blocked Gauss-Jordan with implicit row pivoting.
-// Column blocks of B are factored as n x B panels by warp 0 in registers
-// (a REDUX max/min pivot search, the pivot row broadcast by shuffles, no
-// block barrier inside a panel), and each factored panel is applied to the
-// other columns as one rank-B update
+// Column blocks of B are factored as n x B panels by warps 0 and 1 in
+// registers (REDUX max/min pivot search per warp, the two candidates
+// compared through shared memory under a 64-thread barrier, no block barrier
+// inside a panel), and each factored panel is applied to the other columns
+// as one rank-B update
 //     A'[i][j] = [i not a pivot row of the block] A[i][j]
 //                + sum_c P[i][c] A[piv(k0+c)][j]
-// from one buffer into the other (sm[L.S] <-> sm[L.S2]).  Warp 0 factors
-// the next panel while warps 1..7 apply the current one: one block barrier
-// per B columns.  With pivot row p_k for column k, the final buffer M holds
+// from one buffer into the other (sm[L.S] <-> sm[L.S2]).  The panel warps
+// factor the next panel while warps 2..7 apply the current one: one block
+// barrier per B columns.  With pivot row p_k for column k, the final buffer M holds
 // M[p_a][b'] = inv(S)[a][p_b'], so inv(S)[a][b] = M[p_a][pos(b)] with
 // pos(p_k) = k; the last pass writes it in natural order.
 // ---------------------------------------------------------------------------
@@ -655,23 +656,33 @@ __device__ __forceinline__ df shfl_r(df v, int src)
     return df{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
 }
 
-// Named barrier 1 over the whole CTA: warp 0 waits, the others only arrive.
+// Named barrier 1 over the whole CTA: the panel warps wait, the others only
+// arrive.  Named barrier 2 pairs the two panel warps.
 __device__ __forceinline__ void bar1_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
 __device__ __forceinline__ void bar1_arrive() { asm volatile("bar.arrive 1, %0;" ::"n"(kThreads) : "memory"); }
+__device__ __forceinline__ void bar2_panel() { asm volatile("bar.sync 2, 64;" ::: "memory"); }
+
+constexpr int kPanelWarps = 2;
 
 // Factor columns k0..k0+bw-1 of A (all n rows, rows pivoted in earlier
 // blocks excluded from the pivot search) by Gauss-Jordan steps restricted
-// to the panel.  Called by warp 0; lane l holds rows l + 32 s.  Records
-// piv[k], pvals[k] and rowpos[piv[k]] = k.  Returns false on a zero pivot.
+// to the panel.  Called by warps 0 and 1 (threads 0..63); thread t holds rows
+// t + 64 s in registers.  Each warp finds its best candidate with REDUX
+// max/min and publishes key, row and the candidate's panel row in shared
+// memory (double-buffered by step parity); after the pair barrier both
+// warps pick the same winner.  Records piv[k], pvals[k] and
+// rowpos[piv[k]] = k.  Returns false on a zero pivot.
 template <class R, int RPL, int B>
 __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, int* piv, R* pvals, int* rowpos)
 {
-    const int lane = threadIdx.x & 31;
+    __shared__ unsigned s_kh[2][kPanelWarps], s_kl[2][kPanelWarps], s_row[2][kPanelWarps];
+    __shared__ R s_cand[2][kPanelWarps][B];
+    const int t = threadIdx.x, pw = t >> 5;
     R v[RPL][B];
     bool done[RPL];
 #pragma unroll
     for (int s = 0; s < RPL; ++s) {
-        const int r = lane + 32 * s;
+        const int r = t + 64 * s;
         const bool ok = r < n;
         done[s] = !ok || rowpos[r] < k0;
 #pragma unroll
@@ -680,7 +691,8 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
 #pragma unroll
     for (int c = 0; c < B; ++c) {
         if (c >= bw) break;
-        // largest |a| among the rows not yet pivoted; smallest row on ties
+        const int buf = c & 1;
+        // this warp's largest |a| among rows not yet pivoted; smallest row on ties
         unsigned kh[RPL], mh = 0u;
 #pragma unroll
         for (int s = 0; s < RPL; ++s) {
@@ -699,36 +711,49 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
                 }
             gl = __reduce_max_sync(0xffffffffu, ml);
         }
-        if (gh == 0u && gl == 0u) return false;   // no non-zero candidate: singular
         unsigned mine = 0xffffffffu;
 #pragma unroll
         for (int s = RPL - 1; s >= 0; --s)
-            if (!done[s] && kh[s] == gh && mag_lo(v[s][c]) == gl) mine = (unsigned)(lane + 32 * s);
-        const int pr = (int)__reduce_min_sync(0xffffffffu, mine);
-        const int op = pr & 31, sp = pr >> 5;
+            if (!done[s] && kh[s] == gh && mag_lo(v[s][c]) == gl) mine = (unsigned)(t + 64 * s);
+        const unsigned wrow = __reduce_min_sync(0xffffffffu, mine);
+#pragma unroll
+        for (int s = 0; s < RPL; ++s)
+            if ((unsigned)(t + 64 * s) == wrow)
+#pragma unroll
+                for (int c2 = 0; c2 < B; ++c2) s_cand[buf][pw][c2] = v[s][c2];
+        if ((t & 31) == 0) {
+            s_kh[buf][pw] = gh;
+            s_kl[buf][pw] = gl;
+            s_row[buf][pw] = wrow;
+        }
+        bar2_panel();
+        const unsigned h0 = s_kh[buf][0], h1 = s_kh[buf][1], l0 = s_kl[buf][0], l1 = s_kl[buf][1];
+        const unsigned r0 = s_row[buf][0], r1 = s_row[buf][1];
+        const int win = (h1 > h0 || (h1 == h0 && (l1 > l0 || (l1 == l0 && r1 < r0)))) ? 1 : 0;
+        if ((win ? h1 : h0) == 0u && (win ? l1 : l0) == 0u) return false;   // no non-zero candidate
+        const int pr = (int)(win ? r1 : r0);
         // pivot row, scaled; its column-c entry becomes 1/pivot
         R rr[B];
 #pragma unroll
-        for (int c2 = 0; c2 < B; ++c2) {
-            R val = v[0][c2];
-#pragma unroll
-            for (int s = 1; s < RPL; ++s)
-                if (sp == s) val = v[s][c2];
-            rr[c2] = shfl_r(val, op);
-        }
+        for (int c2 = 0; c2 < B; ++c2) rr[c2] = s_cand[buf][win][c2];
         const R pv = rr[c];
         const R pinv = rcp(pv);
 #pragma unroll
         for (int c2 = 0; c2 < B; ++c2) rr[c2] = (c2 == c) ? pinv : rr[c2] * pinv;
 #pragma unroll
         for (int s = 0; s < RPL; ++s) {
-            const bool isp = (lane + 32 * s) == pr;
             const R m = v[s][c];
 #pragma unroll
-            for (int c2 = 0; c2 < B; ++c2) v[s][c2] = isp ? rr[c2] : fms(c2 == c ? rzero<R>() : v[s][c2], m, rr[c2]);
-            done[s] = done[s] || isp;
+            for (int c2 = 0; c2 < B; ++c2) v[s][c2] = fms(c2 == c ? rzero<R>() : v[s][c2], m, rr[c2]);
         }
-        if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < RPL; ++s)
+            if (t + 64 * s == pr) {
+#pragma unroll
+                for (int c2 = 0; c2 < B; ++c2) v[s][c2] = rr[c2];
+                done[s] = true;
+            }
+        if (t == 0) {
             piv[k0 + c] = pr;
             pvals[k0 + c] = pv;
             rowpos[pr] = k0 + c;
@@ -736,13 +761,12 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
     }
 #pragma unroll
     for (int s = 0; s < RPL; ++s) {
-        const int r = lane + 32 * s;
+        const int r = t + 64 * s;
         if (r < n)
 #pragma unroll
             for (int c = 0; c < B; ++c)
                 if (c < bw) A[r * ld + k0 + c] = v[s][c];
     }
-    __syncwarp();
     return true;
 }
 
@@ -779,7 +803,9 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
     for (int i = threadIdx.x; i < n; i += kThreads) rowpos[i] = n;
     if (threadIdx.x == 0) s_sing = 0;
     __syncthreads();
-    if (warp == 0 && !gj_panel<R, RPL, B>(A0, ld, n, 0, min(B, n), piv, pvals, rowpos) && lane == 0) s_sing = 1;
+    if (warp < kPanelWarps && !gj_panel<R, RPL, B>(A0, ld, n, 0, min(B, n), piv, pvals, rowpos) &&
+        threadIdx.x == 0)
+        s_sing = 1;
     __syncthreads();
     R* cur = A0;
     R* nxt = A1;
@@ -797,17 +823,17 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
                 const int i = e / bw1, j = k1 + e % bw1;
                 nxt[i * ld + j] = gj_apply<R, B>(cur, ld, i, j, k0, bw, prow, rowpos);
             }
-            if (warp == 0) {
+            if (warp < kPanelWarps) {
                 bar1_sync();
-                if (!gj_panel<R, RPL, B>(nxt, ld, n, k1, bw1, piv, pvals, rowpos) && lane == 0) s_sing = 1;
+                if (!gj_panel<R, RPL, B>(nxt, ld, n, k1, bw1, piv, pvals, rowpos) && threadIdx.x == 0) s_sing = 1;
             } else {
                 bar1_arrive();
             }
         }
-        if (bw1 == 0 || warp > 0) {
-            // every other column: warps 1..7 (all warps in the last block)
-            const int nt = bw1 > 0 ? kThreads - 32 : kThreads;
-            const int t0 = bw1 > 0 ? (int)threadIdx.x - 32 : (int)threadIdx.x;
+        if (bw1 == 0 || warp >= kPanelWarps) {
+            // every other column: the non-panel warps (all warps in the last block)
+            const int nt = bw1 > 0 ? kThreads - 32 * kPanelWarps : kThreads;
+            const int t0 = bw1 > 0 ? (int)threadIdx.x - 32 * kPanelWarps : (int)threadIdx.x;
             const int nc = n - bw1;
             for (int e = t0; e < n * nc; e += nt) {
                 const int i = e / nc, jj = e % nc;
@@ -1023,10 +1049,8 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
 {
     const int n = c.p.nd;
     if (c.L.S2 >= 0) {
-        if (n <= 32) return inverse_blocked<R, 1, 8>(c, logdet, sgn);
-        if (n <= 64) return inverse_blocked<R, 2, 8>(c, logdet, sgn);
-        if (n <= 96) return inverse_blocked<R, 3, 8>(c, logdet, sgn);
-        if (n <= 128) return inverse_blocked<R, 4, 4>(c, logdet, sgn);
+        if (n <= 64) return inverse_blocked<R, 1, 8>(c, logdet, sgn);
+        if (n <= 128) return inverse_blocked<R, 2, 8>(c, logdet, sgn);
     }
     return inverse_unblocked<R>(c, logdet, sgn);
 }
