@@ -58,6 +58,9 @@ struct __align__(16) KVecDev {
     int shell;      // 1-based shell index (1 for k = 0)
 };
 
+// the kernels stage k-vector records as 8 doubles each
+static_assert(sizeof(KVecMP) == 64 && sizeof(KVecDev) == 64, "k-vector records must be 64 bytes");
+
 enum Mode : int {
     MODE_HPSI = 0,     // x -> hpsi outputs (wavefunction.f90:161-201)
     MODE_BCS = 1,      // x -> determinant part only (psislaterbcs.f90:155-225)

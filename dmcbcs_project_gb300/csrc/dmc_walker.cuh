@@ -1063,8 +1063,49 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
 //          H_{c,s} = sum_i Sinv[j][i] U[i][c,s]
 // Work items (particle, k vector) are split into contiguous per-thread
 // chunks; each thread sums its chunk per particle and the partial sums of a
-// particle are added in thread order.
+// particle are added in thread order.  Up and down items go to disjoint
+// warps (in proportion to the particle counts), so that no warp runs both
+// loop bodies one after the other.
 // ---------------------------------------------------------------------------
+struct DriftSplit {
+    int pbeg[2], np[2], tbeg[2], nth[2], chunk[2];
+};
+
+// Half 0 = up particles on the first warps, half 1 = down particles on the
+// rest.  A chunk must not span more than two particles (chunk <= nq); when a
+// split cannot guarantee that, half 0 takes every particle on all threads.
+__device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int nq)
+{
+    DriftSplit s;
+    const int P = nup + ndn;
+    int wu = P > 0 ? (kWarps * nup + P / 2) / P : 0;
+    if (nup > 0 && wu < 1) wu = 1;
+    if (ndn > 0 && wu > kWarps - 1) wu = kWarps - 1;
+    s.pbeg[0] = 0;
+    s.np[0] = nup;
+    s.tbeg[0] = 0;
+    s.nth[0] = 32 * wu;
+    s.pbeg[1] = nup;
+    s.np[1] = ndn;
+    s.tbeg[1] = 32 * wu;
+    s.nth[1] = kThreads - 32 * wu;
+    bool ok = nup > 0 && ndn > 0;
+    for (int h = 0; h < 2; ++h) {
+        s.chunk[h] = s.nth[h] > 0 ? (s.np[h] * nq + s.nth[h] - 1) / s.nth[h] : 0;
+        if (s.chunk[h] > nq) ok = false;
+    }
+    if (!ok) {
+        s.np[0] = P;
+        s.nth[0] = kThreads;
+        s.chunk[0] = (P * nq + kThreads - 1) / kThreads;
+        s.np[1] = 0;
+        s.tbeg[1] = kThreads;
+        s.nth[1] = 0;
+        s.chunk[1] = 1;
+    }
+    return s;
+}
+
 template <class R>
 __device__ void drift_stage(const Ctx<R>& c)
 {
@@ -1079,14 +1120,16 @@ __device__ void drift_stage(const Ctx<R>& c)
     double* acc = sm + c.L.acc;             // drift [3N], lap [N]
     R* part = at<R>(sm, c.L.red);           // per thread: 2 segments x 4 sums
     const int nq = p.nk - 1, P = p.npart, ld = p.ldS, ldU = p.ldU;
-    const int items = P * nq;
-    const int chunk = (items + kThreads - 1) / kThreads;
-    const int b = threadIdx.x * chunk, e = min(items, b + chunk);
+    const DriftSplit sp = drift_split(p.nup, p.ndn, nq);
+    const int h = (int)threadIdx.x >= sp.tbeg[1] ? 1 : 0;
+    const int lt = (int)threadIdx.x - sp.tbeg[h];
+    const int items = sp.np[h] * nq, chunk = sp.chunk[h], pbeg = sp.pbeg[h];
+    const int b = lt * chunk, e = min(items, b + chunk);
     R s0[4], s1[4];
     for (int k = 0; k < 4; ++k) s0[k] = s1[k] = rzero<R>();
-    const int first = b < e ? b / nq : -1;
+    const int first = b < e ? pbeg + b / nq : -1;
     for (int it = b; it < e; ++it) {
-        const int pt = it / nq, q = it % nq + 1;
+        const int pt = pbeg + it / nq, q = it % nq + 1;
         const KV& K = kq[q];
         const int qc = 2 * q - 2;   // (cos, sin) pair of k vector q
         R t, l;
@@ -1150,16 +1193,19 @@ __device__ void drift_stage(const Ctx<R>& c)
         my[4 + k] = s1[k];
     }
     __syncthreads();
-    // particle pt is covered by threads floor(pt*nq/chunk) .. floor((pt*nq+nq-1)/chunk)
+    // particle pl of a half is covered by that half's local threads
+    // floor(pl*nq/chunk) .. floor((pl*nq+nq-1)/chunk)
     for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+        const int hh = (sp.nth[1] > 0 && pt >= sp.pbeg[1]) ? 1 : 0;
+        const int pl = pt - sp.pbeg[hh], ch = sp.chunk[hh], ni = sp.np[hh] * nq;
         R r[4];
         for (int k = 0; k < 4; ++k) r[k] = rzero<R>();
-        const int t0 = (pt * nq) / chunk, t1 = (pt * nq + nq - 1) / chunk;
-        for (int t = t0; t <= t1 && t < kThreads; ++t) {
-            const int tb = t * chunk, te = min(items, tb + chunk);
+        const int l0 = (pl * nq) / ch, l1 = (pl * nq + nq - 1) / ch;
+        for (int u = l0; u <= l1 && u < sp.nth[hh]; ++u) {
+            const int tb = u * ch, te = min(ni, tb + ch);
             if (tb >= te) continue;
-            const R* o = part + t * 8;
-            const int sl = (tb / nq == pt) ? 0 : (((te - 1) / nq == pt) ? 4 : -1);
+            const R* o = part + (sp.tbeg[hh] + u) * 8;
+            const int sl = (tb / nq == pl) ? 0 : (((te - 1) / nq == pl) ? 4 : -1);
             if (sl < 0) continue;
             for (int k = 0; k < 4; ++k) r[k] = r[k] + o[sl + k];
         }
@@ -1171,6 +1217,7 @@ __device__ void drift_stage(const Ctx<R>& c)
     __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
 // Stage 6: beta terms of the drift and Laplacian (psislaterbcs.f90:290-291
 // through :213-222): per up-down pair h = Sinv[j][i] f'/r dx, l = Sinv[j][i]
 // lap f; row sums go to the up particle, column sums (negated drift) to the
