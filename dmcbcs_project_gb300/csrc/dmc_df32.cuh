@@ -23,21 +23,25 @@ struct __align__(8) df {
     float hi, lo;
 };
 
+// The error-free transformations below spell their roundings with the _rn
+// intrinsics, which the compiler never fuses into an FMA: a contracted
+// s = fma(a, b, c) in place of s = fl(fl(a*b) + c) would break the identities
+// the error terms rely on.
 __device__ __forceinline__ df mkdf(float h, float l) { return df{h, l}; }
 __device__ __forceinline__ df two_sum(float a, float b)
 {
-    const float s = a + b;
-    const float bb = s - a;
-    return df{s, (a - (s - bb)) + (b - bb)};
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return df{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
 }
 __device__ __forceinline__ df fast_two_sum(float a, float b)
 {
-    const float s = a + b;
-    return df{s, b - (s - a)};
+    const float s = __fadd_rn(a, b);
+    return df{s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 __device__ __forceinline__ df two_prod(float a, float b)
 {
-    const float p = a * b;
+    const float p = __fmul_rn(a, b);
     return df{p, fmaf(a, b, -p)};
 }
 
@@ -114,25 +118,56 @@ struct dfacc {
 __device__ __forceinline__ void acc_init(dfacc& a) { a.hi = a.lo = 0.0f; }
 __device__ __forceinline__ void acc_madd(dfacc& a, df x, df y)
 {
-    const float p = x.hi * y.hi;
+    const float p = __fmul_rn(x.hi, y.hi);
     float pe = fmaf(x.hi, y.hi, -p);
     pe = fmaf(x.hi, y.lo, pe);
     pe = fmaf(x.lo, y.hi, pe);
-    const float s = a.hi + p;
-    const float bb = s - a.hi;
-    const float e = (a.hi - (s - bb)) + (p - bb);
+    const float s = __fadd_rn(a.hi, p);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
     a.hi = s;
     a.lo += e + pe;
 }
 __device__ __forceinline__ void acc_add(dfacc& a, df x)
 {
-    const float s = a.hi + x.hi;
-    const float bb = s - a.hi;
-    const float e = (a.hi - (s - bb)) + (x.hi - bb);
+    const float s = __fadd_rn(a.hi, x.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(x.hi, bb));
     a.hi = s;
     a.lo += e + x.lo;
 }
 __device__ __forceinline__ df acc_value(const dfacc& a) { return fast_two_sum(a.hi, a.lo); }
+
+// Dot products with a known bound on sum |x_j y_j|, after Rump, Ogita and
+// Oishi's ExtractScalar (Accurate floating-point summation part I, SIAM J.
+// Sci. Comput. 31(1), 2008).  With sigma = 2^k >= 4 sum |x_j y_j|,
+// t = fl(sigma + x*y) lies in [sigma/2, 2 sigma], so q = t - sigma is exact
+// and a multiple of 2^(k-24); the partial sums of the q stay below sigma/2
+// and are therefore exact in FP32.  The remainder x*y - q (one FMA, one
+// rounding) and the products with the low parts go into an FP32 tail.
+// 7 FP32 instructions per multiply-add (12 for dfacc); error of order
+// n 2^-48 sigma for n terms.
+struct bacc {
+    float hi, lo;
+};
+__device__ __forceinline__ void bacc_init(bacc& a) { a.hi = a.lo = 0.0f; }
+__device__ __forceinline__ void bacc_madd(bacc& a, df x, df y, float sigma)
+{
+    const float t = fmaf(x.hi, y.hi, sigma);
+    const float q = __fsub_rn(t, sigma);
+    a.hi = __fadd_rn(a.hi, q);
+    a.lo += fmaf(x.hi, y.hi, -q);
+    a.lo = fmaf(x.hi, y.lo, a.lo);
+    a.lo = fmaf(x.lo, y.hi, a.lo);
+}
+__device__ __forceinline__ df bacc_value(const bacc& a) { return two_sum(a.hi, a.lo); }
+// smallest power of two >= v for finite v > 0 (2^-100 for v = 0)
+__device__ __forceinline__ float pow2_ceil(float v)
+{
+    if (!(v > 0.0f)) return 7.8886091e-31f;
+    const int b = __float_as_int(v);
+    return __int_as_float((b + 0x007fffff) & 0x7f800000);
+}
 
 // ---- the same interface for double, so kernels can be written once --------
 

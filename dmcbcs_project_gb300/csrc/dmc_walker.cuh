@@ -619,8 +619,9 @@ __device__ void gemm_stage(const Ctx<R>& c)
             acc_madd(a0, ub, xb);
             acc_madd(a1, ub, yb);
         }
-        S[i * p.ldS + j0] = acc_value(a0) + S[i * p.ldS + j0];
-        if (two) S[i * p.ldS + j1] = acc_value(a1) + S[i * p.ldS + j1];
+        const R s0 = acc_value(a0), s1 = acc_value(a1);
+        S[i * p.ldS + j0] = s0 + S[i * p.ldS + j0];
+        if (two) S[i * p.ldS + j1] = s1 + S[i * p.ldS + j1];
     }
     __syncthreads();
 }
@@ -1121,6 +1122,20 @@ __device__ void drift_stage(const Ctx<R>& c)
     R* part = at<R>(sm, c.L.red);           // per thread: 2 segments x 4 sums
     const int nq = p.nk - 1, P = p.npart, ld = p.ldS, ldU = p.ldU;
     const DriftSplit sp = drift_split(p.nup, p.ndn, nq);
+    // double-float path: abs column sums (bound[i], for G) and row sums
+    // (bound[nd + j], for H) of the inverse bound the dot products
+    float* bound = reinterpret_cast<float*>(sm + c.L.colk);
+    if constexpr (is_df<R>::value) {
+        for (int t = threadIdx.x; t < 2 * p.nd; t += kThreads) {
+            float sacc = 0.0f;
+            if (t < p.nd)
+                for (int j = 0; j < p.nd; ++j) sacc += fabsf(Si[j * ld + t].hi);
+            else
+                for (int i = 0; i < p.nd; ++i) sacc += fabsf(Si[(t - p.nd) * ld + i].hi);
+            bound[t] = sacc * 1.001f;
+        }
+        __syncthreads();
+    }
     const int h = (int)threadIdx.x >= sp.tbeg[1] ? 1 : 0;
     const int lt = (int)threadIdx.x - sp.tbeg[h];
     const int items = sp.np[h] * nq, chunk = sp.chunk[h], pbeg = sp.pbeg[h];
@@ -1135,40 +1150,77 @@ __device__ void drift_stage(const Ctx<R>& c)
         R t, l;
         if (pt < p.nup) {
             const int i = pt;
-            Acc gc, gs;
-            acc_init(gc);
-            acc_init(gs);
             const R* dq = D + qc;
             const R* sc = Si + i;
-            for (int j = 0; j < p.ndn; ++j) {
-                const R sji = sc[j * ld];
-                R dc_, ds_;
-                ld2(dq + j * ldU, dc_, ds_);
-                acc_madd(gc, dc_, sji);
-                acc_madd(gs, ds_, sji);
+            R vgc, vgs;
+            if constexpr (is_df<R>::value) {
+                const float sig = pow2_ceil(4.0f * bound[i]);   // |D| <= 1
+                bacc gc, gs;
+                bacc_init(gc);
+                bacc_init(gs);
+                for (int j = 0; j < p.ndn; ++j) {
+                    const R sji = sc[j * ld];
+                    R dc_, ds_;
+                    ld2(dq + j * ldU, dc_, ds_);
+                    bacc_madd(gc, dc_, sji, sig);
+                    bacc_madd(gs, ds_, sji, sig);
+                }
+                vgc = bacc_value(gc);
+                vgs = bacc_value(gs);
+            } else {
+                Acc gc, gs;
+                acc_init(gc);
+                acc_init(gs);
+                for (int j = 0; j < p.ndn; ++j) {
+                    const R sji = sc[j * ld];
+                    R dc_, ds_;
+                    ld2(dq + j * ldU, dc_, ds_);
+                    acc_madd(gc, dc_, sji);
+                    acc_madd(gs, ds_, sji);
+                }
+                vgc = acc_value(gc);
+                vgs = acc_value(gs);
             }
             R uc, us;
             ld2(U + i * ldU + qc, uc, us);
-            const R vgc = acc_value(gc), vgs = acc_value(gs);
             t = uc * vgs - us * vgc;
             l = uc * vgc + us * vgs;
         } else {
             const int j = pt - p.nup;
-            Acc hc, hs;
-            acc_init(hc);
-            acc_init(hs);
             const R* srow = Si + j * ld;
             const R* uq = U + qc;
-            for (int i = 0; i < p.nup; ++i) {
-                const R sji = srow[i];
-                R uc_, us_;
-                ld2(uq + i * ldU, uc_, us_);
-                acc_madd(hc, sji, uc_);
-                acc_madd(hs, sji, us_);
+            R vhc, vhs;
+            if constexpr (is_df<R>::value) {
+                // |U[i][q]| <= |v_q|
+                const float sig = pow2_ceil(4.0f * fabsf(K.v.hi) * 1.001f * bound[p.nd + j]);
+                bacc hc, hs;
+                bacc_init(hc);
+                bacc_init(hs);
+                for (int i = 0; i < p.nup; ++i) {
+                    const R sji = srow[i];
+                    R uc_, us_;
+                    ld2(uq + i * ldU, uc_, us_);
+                    bacc_madd(hc, sji, uc_, sig);
+                    bacc_madd(hs, sji, us_, sig);
+                }
+                vhc = bacc_value(hc);
+                vhs = bacc_value(hs);
+            } else {
+                Acc hc, hs;
+                acc_init(hc);
+                acc_init(hs);
+                for (int i = 0; i < p.nup; ++i) {
+                    const R sji = srow[i];
+                    R uc_, us_;
+                    ld2(uq + i * ldU, uc_, us_);
+                    acc_madd(hc, sji, uc_);
+                    acc_madd(hs, sji, us_);
+                }
+                vhc = acc_value(hc);
+                vhs = acc_value(hs);
             }
             R dc, ds;
             ld2(D + j * ldU + qc, dc, ds);
-            const R vhc = acc_value(hc), vhs = acc_value(hs);
             t = vhs * dc - vhc * ds;
             l = vhc * dc + vhs * ds;
         }
