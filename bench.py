@@ -33,15 +33,16 @@ METRIC = "DMC walker-steps/s @N=66: mixed/batched vs plain FP64 GPU, E_L rel err
 UNIT = "walker-steps/s"
 WORKLOAD = "n66"
 
-# DRAM bytes per walker-step of the FP64 walker kernel from one ncu capture
-# (profiles/walker_kernel_n66_fp64.md: dram__bytes_read.sum +
-# dram__bytes_write.sum = 2.42 MB for one step launch over ~512 walkers).
-NCU_TRAFFIC_BYTES_PER_WALKER = 4730.0
+# DRAM bytes per walker-step (dram__bytes_read.sum + dram__bytes_write.sum of
+# one step launch over 1024 walkers, ncu): FP64 walker kernel 4.16 MB,
+# mixed walker kernel 4.22 MB (profiles/walker_kernel_n66_fp64.md,
+# profiles/walker_kernel_n66_mixed.md).
+NCU_TRAFFIC_BYTES_PER_WALKER = {"fp64": 4064.0, "mixed": 4121.0}
 
 # FP32 flops (FFMA = 2, FADD/FMUL = 1) executed per walker-step by the mixed
-# walker kernel, from the instruction counters of one ncu capture
-# (profiles/walker_kernel_n66_mixed.md).  None until captured.
-MIXED_FP32_FLOPS_PER_WALKER = None
+# walker kernel, from the instruction counters of the same capture:
+# 6.269e9 over 1024 walkers.
+MIXED_FP32_FLOPS_PER_WALKER = 6.122e6
 
 
 def algorithmic_flops(nup, ndn, nd, K, npart):
@@ -326,7 +327,7 @@ def run_gpu(args):
         if prec == "fp64":
             return {"bound": "fp64", "achieved": alg, "peak": dgemm, "unit": "TFLOP/s",
                     "frac": alg / dgemm if dgemm else None,
-                    "traffic": NCU_TRAFFIC_BYTES_PER_WALKER * r["avg_n"] if NCU_TRAFFIC_BYTES_PER_WALKER else None,
+                    "traffic": NCU_TRAFFIC_BYTES_PER_WALKER["fp64"] * r["avg_n"],
                     "kernel": "walker_kernel<double>", "kernel_ms_per_launch": kms, "walkers_per_launch": r["avg_n"],
                     "algorithmic_flops_per_walker_step": flops_alg, "executed_flops_per_walker_step": flops_exe,
                     "executed_achieved": flops_exe * r["avg_n"] / (kms * 1e-3) / 1e12,
@@ -336,7 +337,7 @@ def run_gpu(args):
         return {"bound": "fp32", "achieved": (ex * r["avg_n"] / (kms * 1e-3) / 1e12) if ex else None,
                 "peak": peak32, "unit": "TFLOP/s",
                 "frac": (ex * r["avg_n"] / (kms * 1e-3) / 1e12 / peak32) if (ex and peak32) else None,
-                "traffic": NCU_TRAFFIC_BYTES_PER_WALKER * r["avg_n"] if NCU_TRAFFIC_BYTES_PER_WALKER else None,
+                "traffic": NCU_TRAFFIC_BYTES_PER_WALKER["mixed"] * r["avg_n"],
                 "kernel": "walker_kernel<df>", "kernel_ms_per_launch": kms, "walkers_per_launch": r["avg_n"],
                 "executed_fp32_flops_per_walker_step": ex,
                 "fp64_equivalent": {"achieved": alg, "peak": dgemm,
