@@ -25,7 +25,7 @@ EXPORTS = [
     "dmc_generation", "dmc_zero_estimators", "dmc_get_estimators", "dmc_block_update", "dmc_get_wtisto",
     "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers", "dmc_branch_noalloc",
     "dmc_set_precision", "dmc_get_precision", "dmc_probe_peak", "dmc_sr_accumulate", "dmc_sr_get_sums",
-    "dmc_sr_zero", "dmc_sr_update",
+    "dmc_sr_zero", "dmc_sr_update", "dmc_fort9_write", "dmc_fort9_read", "dmc_save_walkers", "dmc_restore_walkers",
 ]
 
 PREC_FP64 = 0
@@ -96,6 +96,11 @@ def load(path=LIB_PATH):
     L.dmc_set_precision.argtypes = [vp, C.c_int]
     L.dmc_probe_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.dmc_get_precision.argtypes = [vp, C.POINTER(C.c_int)]
+    L.dmc_fort9_write.argtypes = [C.c_char_p, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.c_double]
+    L.dmc_fort9_read.argtypes = [C.c_char_p, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double)]
+    L.dmc_save_walkers.argtypes = [vp, C.c_char_p, C.c_double]
+    L.dmc_restore_walkers.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double)]
     L.dmc_sr_accumulate.argtypes = [vp, C.POINTER(C.c_int64)]
     L.dmc_sr_get_sums.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_int64)]
     L.dmc_sr_zero.argtypes = [vp]
@@ -104,6 +109,37 @@ def load(path=LIB_PATH):
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
     _lib = L
     return L
+
+
+def fort9_write(path, x, weight, psil, psigl, irn, tau=0.0):
+    """Write walkers (file order) in the reference's fort.9 layout; no GPU used."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n, npart = x.shape[0], x.shape[1]
+    arr = [np.ascontiguousarray(a, dtype=t) for a, t in ((weight, np.float64), (psil, np.float64),
+                                                           (psigl, np.float64), (irn, np.int64))]
+    st = load().dmc_fort9_write(os.fsencode(path), npart, n, _opt(x), *[_opt(a) for a in arr], float(tau))
+    if st != abi.DMC_OK:
+        raise DMCError(st, f"fort9_write {path}")
+
+
+def fort9_read(path, npart, cap=None):
+    """Read a fort.9 file; returns dict(x, weight, psil0, psigl0, irn, tau) in file order."""
+    n = C.c_int()
+    tau = C.c_double()
+    st = load().dmc_fort9_read(os.fsencode(path), npart, 0, None, None, None, None, None, C.byref(n), C.byref(tau))
+    if st not in (abi.DMC_OK, abi.DMC_ERR_OVERFLOW):
+        raise DMCError(st, f"fort9_read {path}")
+    m = n.value if cap is None else cap
+    o = dict(x=np.zeros((max(m, 1), npart, 3)), weight=np.zeros(max(m, 1)), psil0=np.zeros(max(m, 1)),
+             psigl0=np.zeros(max(m, 1)), irn=np.zeros(max(m, 1), np.int64))
+    st = load().dmc_fort9_read(os.fsencode(path), npart, m, *[_opt(o[k]) for k in ("x", "weight", "psil0", "psigl0",
+                                                                                    "irn")],
+                               C.byref(n), C.byref(tau))
+    if st != abi.DMC_OK:
+        raise DMCError(st, f"fort9_read {path}")
+    out = {k: v[: n.value] for k, v in o.items()}
+    out["tau"] = tau.value
+    return out
 
 
 def probe_peak(kind):
@@ -256,6 +292,16 @@ class Context:
         self._check(load().dmc_getderbcs_batch(self._h, nw, x, out))
         return out
 
+    def save_walkers(self, path, tau=0.0):
+        """Write the population to a fort.9 file (top of the stack first)."""
+        self._check(load().dmc_save_walkers(self._h, os.fsencode(path), float(tau)))
+
+    def restore_walkers(self, path):
+        """Push the walkers of a fort.9 file; returns its tau."""
+        t = C.c_double()
+        self._check(load().dmc_restore_walkers(self._h, os.fsencode(path), C.byref(t)))
+        return t.value
+
     def sr_accumulate(self):
         n = C.c_int64()
         self._check(load().dmc_sr_accumulate(self._h, C.byref(n)))
@@ -392,4 +438,4 @@ class Context:
         return ms.value
 
 
-__all__ = ["Context", "DMCError", "load", "EXPORTS", "LIB_PATH", "DMC_NEST_MAX"]
+__all__ = ["Context", "DMCError", "load", "EXPORTS", "LIB_PATH", "DMC_NEST_MAX", "fort9_write", "fort9_read"]

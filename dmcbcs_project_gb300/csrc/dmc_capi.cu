@@ -669,6 +669,66 @@ int dmc_load_walkers(dmc_ctx* c, const dmc_walkers* w)
     return DMC_OK;
 }
 
+int dmc_save_walkers(dmc_ctx* c, const char* path, double tau)
+{
+    if (!c || !path) return DMC_ERR_INVALID;
+    const int n = c->n;
+    const size_t n3 = (size_t)c->n3;
+    std::vector<double> x(std::max<size_t>(1, n * n3)), w(n + 1), pl(n + 1), pg(n + 1);
+    std::vector<int64_t> irn(n + 1);
+    dmc_walkers h;
+    std::memset(&h, 0, sizeof h);
+    h.n = n;
+    h.x = x.data();
+    h.weight = w.data();
+    h.psil = pl.data();
+    h.psigl = pg.data();
+    h.irn = irn.data();
+    int rc = dmc_get_walkers(c, &h);
+    if (rc) return rc;
+    // pop order: the top of the stack (last index) first
+    std::vector<double> xr(x.size()), wr(n + 1), plr(n + 1), pgr(n + 1);
+    std::vector<int64_t> ir(n + 1);
+    for (int k = 0; k < n; ++k) {
+        const int j = n - 1 - k;
+        std::copy(x.begin() + (size_t)j * n3, x.begin() + (size_t)(j + 1) * n3, xr.begin() + (size_t)k * n3);
+        wr[k] = w[j];
+        plr[k] = pl[j];
+        pgr[k] = pg[j];
+        ir[k] = irn[j];
+    }
+    rc = dmc_fort9_write(path, c->S.npart, n, xr.data(), wr.data(), plr.data(), pgr.data(), ir.data(), tau);
+    if (rc) return fail(c, rc, std::string("cannot write ") + path);
+    return DMC_OK;
+}
+
+int dmc_restore_walkers(dmc_ctx* c, const char* path, double* tau)
+{
+    if (!c || !path) return DMC_ERR_INVALID;
+    const size_t n3 = (size_t)c->n3;
+    int n = 0;
+    double t = 0.0;
+    int rc = dmc_fort9_read(path, c->S.npart, 0, nullptr, nullptr, nullptr, nullptr, nullptr, &n, &t);
+    if (rc != DMC_OK && rc != DMC_ERR_OVERFLOW) return fail(c, DMC_ERR_INVALID, std::string("cannot read ") + path);
+    if (n > c->cap) return fail(c, DMC_ERR_OVERFLOW, "more walkers in the file than the stack capacity");
+    std::vector<double> x(std::max<size_t>(1, n * n3)), w(n + 1), p0(n + 1), pg0(n + 1);
+    std::vector<int64_t> irn(n + 1);
+    rc = dmc_fort9_read(path, c->S.npart, n, x.data(), w.data(), p0.data(), pg0.data(), irn.data(), &n, &t);
+    if (rc) return fail(c, DMC_ERR_INVALID, std::string("malformed walker file ") + path);
+    dmc_walkers h;
+    std::memset(&h, 0, sizeof h);
+    h.n = n;
+    h.x = x.data();
+    h.weight = w.data();
+    h.psil0 = p0.data();
+    h.psigl0 = pg0.data();
+    h.irn = irn.data();
+    rc = dmc_load_walkers(c, &h);
+    if (rc) return rc;
+    if (tau) *tau = t;
+    return DMC_OK;
+}
+
 int dmc_num_walkers(dmc_ctx* c, int* n)
 {
     if (!c || !n) return DMC_ERR_INVALID;

@@ -274,6 +274,31 @@ int dmc_init_walkers(dmc_ctx* ctx);
  * w->n walkers with x, weight, psil0, psigl0 and irn (other fields ignored). */
 int dmc_load_walkers(dmc_ctx* ctx, const dmc_walkers* w);
 
+/* ---- fort.9 walker files (dmcbcs.f90:254-294 read, :548-567 write) ----- */
+
+/* Write n walkers in the reference's fort.9 layout: an (i10,f15.8) header
+ * n, tau; per walker x (6e15.7, 3*npart values), weight, psil, psigl
+ * (e15.7,2e25.15) and irn (i20).  Arrays are in file order (the reference
+ * writes its stack top first).  No device or context is used. */
+int dmc_fort9_write(const char* path, int npart, int n, const double* x, const double* weight, const double* psil,
+                    const double* psigl, const int64_t* irn, double tau);
+
+/* Read a fort.9 file (also the (i10)-header files of pairsconfig.f90):
+ * *n walkers (DMC_ERR_OVERFLOW if more than cap; *n is still set), tau,
+ * x[cap][3*npart], weight, psil0, psigl0 (may be NULL) and irn, in file
+ * order.  Blank fields read as zero, as Fortran formatted input does. */
+int dmc_fort9_read(const char* path, int npart, int cap, double* x, double* weight, double* psil0, double* psigl0,
+                   int64_t* irn, int* n, double* tau);
+
+/* Write the context's population to a fort.9 file, top of the stack first
+ * (dmcbcs.f90:548-567). */
+int dmc_save_walkers(dmc_ctx* ctx, const char* path, double tau);
+
+/* Push the walkers of a fort.9 file in file order (dmcbcs.f90:283-294),
+ * with x, weight, psil0, psigl0 and irn; *tau (may be NULL) gets the file's
+ * tau.  Follow with dmc_initial_eval, as the reference does. */
+int dmc_restore_walkers(dmc_ctx* ctx, const char* path, double* tau);
+
 /* Copy the current walker stack to the host (fort.9 write,
  * dmcbcs.f90:548-567, and full walker state for checks).  w->n is the
  * capacity of the caller's arrays on entry and the count on return. */
