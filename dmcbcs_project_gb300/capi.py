@@ -26,6 +26,8 @@ EXPORTS = [
     "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers", "dmc_branch_noalloc",
     "dmc_set_precision", "dmc_get_precision", "dmc_probe_peak", "dmc_sr_accumulate", "dmc_sr_get_sums",
     "dmc_sr_zero", "dmc_sr_update", "dmc_fort9_write", "dmc_fort9_read", "dmc_save_walkers", "dmc_restore_walkers",
+    "dmc_set_operators", "dmc_zero_operators", "dmc_add_operators", "dmc_update_operators", "dmc_get_operators",
+    "dmc_write_operators",
 ]
 
 PREC_FP64 = 0
@@ -101,6 +103,12 @@ def load(path=LIB_PATH):
                                  C.POINTER(C.c_double)]
     L.dmc_save_walkers.argtypes = [vp, C.c_char_p, C.c_double]
     L.dmc_restore_walkers.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double)]
+    L.dmc_set_operators.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.dmc_zero_operators.argtypes = [vp]
+    L.dmc_add_operators.argtypes = [vp]
+    L.dmc_update_operators.argtypes = [vp]
+    L.dmc_get_operators.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    L.dmc_write_operators.argtypes = [vp, C.c_char_p, C.c_double]
     L.dmc_sr_accumulate.argtypes = [vp, C.POINTER(C.c_int64)]
     L.dmc_sr_get_sums.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_int64)]
     L.dmc_sr_zero.argtypes = [vp]
@@ -301,6 +309,34 @@ class Context:
         t = C.c_double()
         self._check(load().dmc_restore_walkers(self._h, os.fsencode(path), C.byref(t)))
         return t.value
+
+    # ---- operators: g(r) + density profile, S(q), n(k) ----------------------
+    def set_operators(self, ntabg, ntabq, ntabk):
+        self._check(load().dmc_set_operators(self._h, int(ntabg), int(ntabq), int(ntabk)))
+
+    def zero_operators(self):
+        self._check(load().dmc_zero_operators(self._h))
+
+    def add_operators(self):
+        self._check(load().dmc_add_operators(self._h))
+
+    def update_operators(self):
+        self._check(load().dmc_update_operators(self._h))
+
+    def operators(self, which, raw=False):
+        """which: 0 g(r) [3][ntabg+1], 1 density [6][2 ntabg+1], 2 S(q)
+        [3][nqtot], 3 n(k); returns (values, errors, weight sum); raw=True:
+        the running sums before the block update."""
+        code = int(which) + (4 if raw else 0)
+        n = C.c_int()
+        ws = C.c_double()
+        self._check(load().dmc_get_operators(self._h, code, None, None, 0, C.byref(n), None))
+        v, e = np.zeros(max(n.value, 1)), np.zeros(max(n.value, 1))
+        self._check(load().dmc_get_operators(self._h, code, _opt(v), _opt(e), n.value, C.byref(n), C.byref(ws)))
+        return v[: n.value], e[: n.value], ws.value
+
+    def write_operators(self, directory, tau=0.0):
+        self._check(load().dmc_write_operators(self._h, os.fsencode(str(directory)), float(tau)))
 
     def sr_accumulate(self):
         n = C.c_int64()

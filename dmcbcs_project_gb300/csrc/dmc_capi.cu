@@ -13,6 +13,7 @@
 #include "dmc_device.cuh"
 #include "dmc_kernels.h"
 #include "dmc_setup.h"
+#include "dmc_text.h"
 
 namespace dmc {
 cudaError_t launch_matinv(const double* a_colmajor, double* inv_colmajor, double* detl, int* is, int n, int nb,
@@ -132,6 +133,18 @@ struct dmc_ctx {
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
     DevBuf<int> sip;
     int64_t sr_count = 0;
+    // operators (g(r), density profile, S(q), n(k))
+    struct Ops {
+        bool on = false;
+        OpsDev dev{};
+        std::vector<double> akq;
+        std::vector<int> ik, indk, nkk, numshq;
+        DevBuf<double> akq_d, sv, tk, sums;
+        DevBuf<int> ik_d, indk_d, nkk_d, hg, hd;
+        DevBuf<unsigned long long> jA, jC;
+        std::vector<double> val[4], err[4];   // after the last update: g, density, S(q), n(k)
+        double totw[3] = {0, 0, 0};
+    } ops;
     int64_t launches = 0;
     std::string err;
 };
@@ -1056,6 +1069,327 @@ int dmc_getderbcs_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)
     if (rc) return rc;
     CK(cudaMemcpyAsync(dpsi, c->sder.p, nw * np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
+// ---- operators: operators.f90 with gofr.f90, sofq.f90, momentum3d.f90 ------
+
+namespace {
+int ops_counts(const dmc_ctx* c, int which)
+{
+    const OpsDev& o = c->ops.dev;
+    switch (which) {
+    case 0: return o.ntabg > 0 ? 3 * (o.ntabg + 1) : 0;
+    case 1: return o.ntabg > 0 ? 6 * (2 * o.ntabg + 1) : 0;
+    case 2: return 3 * o.nqtot;
+    case 3: return o.nkv > 0 ? o.ntabk + 1 : 0;
+    }
+    return 0;
+}
+int ops_nsums(const dmc_ctx* c) { return 2 * (ops_counts(c, 0) + ops_counts(c, 1) + ops_counts(c, 2) + ops_counts(c, 3)) + 3; }
+}  // namespace
+
+int dmc_set_operators(dmc_ctx* c, int ntabg, int ntabq, int ntabk)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (ntabg < 0 || ntabq < 0 || ntabk < 0 || ntabg > 100000) return fail(c, DMC_ERR_INVALID, "bad operator table sizes");
+    if (ntabk > 80) return fail(c, DMC_ERR_UNSUPPORTED, "n(k) is built for |ik|^2 <= 80");
+    auto& O = c->ops;
+    O = dmc_ctx::Ops();
+    OpsDev& o = O.dev;
+    std::memset(&o, 0, sizeof o);
+    const Setup& S = c->S;
+    o.el = S.el;
+    o.ntabg = ntabg;
+    if (ntabg > 0) o.scaleg = 1.0 / (0.5 * S.el / ntabg);   // dr = el/(2 ntab), gofr.f90:33-34
+    if (ntabq > 0) {
+        // setupsofq (sofq.f90:17-33): kstates3d half shells, k = 0 first
+        std::vector<KVec> kq;
+        std::string err;
+        if (ntabq > DMC_MAX_SHELLS) return fail(c, DMC_ERR_UNSUPPORTED, "too many S(q) shells");
+        int rc = k_shells(S.el, ntabq, kq, O.numshq, err);
+        if (rc) return fail(c, rc, err);
+        o.ntabq = ntabq;
+        o.nqtot = 0;
+        for (int i = 0; i < ntabq; ++i) o.nqtot += O.numshq[i];
+        if (o.nqtot > (int)kq.size()) return fail(c, DMC_ERR_SETUP, "S(q) k vectors");
+        O.akq.resize(3 * (size_t)o.nqtot);
+        for (int q = 0; q < o.nqtot; ++q)
+            for (int k = 0; k < 3; ++k) O.akq[3 * q + k] = kq[q].k[k];
+    }
+    if (ntabk > 0) {
+        // setupenk (momentum3d.f90:14-71): ik in [0, nnk]^3 with |ik|^2 <= ntab,
+        // exchange-sorted by |ik|^2, grouped into shells
+        o.nsamp = 10;
+        o.dk = 2.0 * (4.0 * std::atan(1.0)) / S.el;
+        o.nnk = (int)(std::sqrt((double)ntabk) + 1.0);
+        std::vector<int> ik2;
+        for (int ix = 0; ix <= o.nnk; ++ix)
+            for (int iy = 0; iy <= o.nnk; ++iy)
+                for (int iz = 0; iz <= o.nnk; ++iz)
+                    if (ix * ix + iy * iy + iz * iz <= ntabk) {
+                        ik2.push_back(ix * ix + iy * iy + iz * iz);
+                        O.ik.push_back(ix);
+                        O.ik.push_back(iy);
+                        O.ik.push_back(iz);
+                    }
+        const int ntot = (int)ik2.size();
+        for (int i = 1; i < ntot; ++i)
+            for (int j = 0; j < i; ++j)
+                if (ik2[i] < ik2[j]) {
+                    std::swap(ik2[i], ik2[j]);
+                    for (int k = 0; k < 3; ++k) std::swap(O.ik[3 * i + k], O.ik[3 * j + k]);
+                }
+        O.indk.assign(1, 0);
+        O.nkk.assign(1, 1);
+        for (int i = 1; i < ntot; ++i) {
+            if (ik2[i] != ik2[i - 1]) {
+                O.indk.push_back(i);
+                O.nkk.push_back(0);
+            }
+            O.nkk.back()++;
+        }
+        o.nkv = ntot;
+        o.ntabk = (int)O.nkk.size() - 1;
+        if (3 * (o.nnk + 1) > 32) return fail(c, DMC_ERR_UNSUPPORTED, "n(k) table too large");
+        // ran1 jump-ahead for the 3 N nsamp draws of a walker
+        const int nj = 3 * S.npart * o.nsamp + 1;
+        std::vector<unsigned long long> A(nj), C(nj);
+        A[0] = 1;
+        C[0] = 0;
+        for (int t = 1; t < nj; ++t) {
+            A[t] = (A[t - 1] * 44485709377909ull) & ((1ull << 48) - 1);
+            C[t] = (C[t - 1] * 44485709377909ull + 96309754297ull) & ((1ull << 48) - 1);
+        }
+        CK(O.jA.alloc(nj));
+        CK(O.jC.alloc(nj));
+        CK(cudaMemcpy(O.jA.p, A.data(), nj * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(O.jC.p, C.data(), nj * 8, cudaMemcpyHostToDevice));
+        CK(O.ik_d.alloc(O.ik.size()));
+        CK(O.indk_d.alloc(O.indk.size()));
+        CK(O.nkk_d.alloc(O.nkk.size()));
+        CK(cudaMemcpy(O.ik_d.p, O.ik.data(), O.ik.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(O.indk_d.p, O.indk.data(), O.indk.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(O.nkk_d.p, O.nkk.data(), O.nkk.size() * sizeof(int), cudaMemcpyHostToDevice));
+        o.ik = O.ik_d.p;
+        o.indk = O.indk_d.p;
+        o.nkk = O.nkk_d.p;
+        o.jA = O.jA.p;
+        o.jC = O.jC.p;
+    }
+    if (o.nqtot > 0) {
+        CK(O.akq_d.alloc(O.akq.size()));
+        CK(cudaMemcpy(O.akq_d.p, O.akq.data(), O.akq.size() * 8, cudaMemcpyHostToDevice));
+        o.akq = O.akq_d.p;
+    }
+    const int ns = ops_nsums(c);
+    CK(O.sums.alloc(ns));
+    CK(cudaMemset(O.sums.p, 0, ns * sizeof(double)));
+    O.on = ntabg > 0 || ntabq > 0 || ntabk > 0;
+    for (int w = 0; w < 4; ++w) {
+        O.val[w].assign(ops_counts(c, w), 0.0);
+        O.err[w].assign(ops_counts(c, w), 0.0);
+    }
+    return DMC_OK;
+}
+
+int dmc_zero_operators(dmc_ctx* c)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (!c->ops.on) return DMC_OK;
+    CK(cudaMemsetAsync(c->ops.sums.p, 0, ops_nsums(c) * sizeof(double), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int w = 0; w < 4; ++w) {
+        std::fill(c->ops.val[w].begin(), c->ops.val[w].end(), 0.0);
+        std::fill(c->ops.err[w].begin(), c->ops.err[w].end(), 0.0);
+    }
+    return DMC_OK;
+}
+
+int dmc_add_operators(dmc_ctx* c)
+{
+    if (!c) return DMC_ERR_INVALID;
+    auto& O = c->ops;
+    if (!O.on) return fail(c, DMC_ERR_INVALID, "operators are not set up");
+    const int n = c->n;
+    if (n > 0) {
+        StackBufs& s = c->st[c->istin];
+        const OpsDev& o = O.dev;
+        const int ng = ops_counts(c, 0), ndh = ops_counts(c, 1), nk = ops_counts(c, 3);
+        CK(O.hg.alloc((size_t)n * ng));
+        CK(O.hd.alloc((size_t)n * ndh));
+        CK(O.sv.alloc((size_t)n * o.nqtot * 4));
+        CK(O.tk.alloc((size_t)n * nk));
+        if (o.ntabg > 0 || o.nqtot > 0) {
+            CK(launch_ops_walker(c->P, o, s.x.p, n, O.hg.p, O.hd.p, O.sv.p, c->grid, c->stream));
+            ++c->launches;
+        }
+        if (o.nkv > 0) {
+            // hpsi(w) of addenk leaves the walker's inverse in smatisave
+            const size_t nd2 = (size_t)c->S.nd * c->S.nd;
+            CK(c->ssinv.alloc(n * nd2));
+            const int prec = c->precision;
+            c->precision = DMC_PREC_FP64;
+            int rc = run_eval(c, MODE_BCS, n, s.x.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              nullptr, nullptr, c->ssinv.p, c->stream);
+            c->precision = prec;
+            if (rc) return rc;
+            ++c->launches;
+            CK(launch_ops_enk(c->P, o, c->kv.p, c->tud.p, c->tss.p, s.x.p, s.irn.p, c->ssinv.p, n, O.tk.p, c->grid,
+                              c->stream));
+            ++c->launches;
+        }
+        CK(launch_ops_reduce(o, n, s.view(), O.hg.p, O.hd.p, O.sv.p, O.tk.p, O.sums.p, c->stream));
+        ++c->launches;
+        int rc = reverse_stacks(c);   // the pop/push pass of dmcbcs.f90:465-473
+        if (rc) return rc;
+        ++c->launches;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
+int dmc_update_operators(dmc_ctx* c)
+{
+    if (!c) return DMC_ERR_INVALID;
+    auto& O = c->ops;
+    if (!O.on) return fail(c, DMC_ERR_INVALID, "operators are not set up");
+    const int ns = ops_nsums(c);
+    std::vector<double> h(ns);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(h.data(), O.sums.p, ns * sizeof(double), cudaMemcpyDeviceToHost));
+    const double ws[4] = {h[ns - 3], h[ns - 3], h[ns - 2], h[ns - 1]};
+    size_t off = 0;
+    for (int w = 0; w < 4; ++w) {
+        const int m = ops_counts(c, w);
+        const double* now = h.data() + off;
+        const double* er = now + m;
+        off += 2 * (size_t)m;
+        if (m == 0 || ws[w] == 0.0) continue;
+        // updategofr / updatesofq / updateenk: block average and error
+        const double norm = 1.0 / ws[w];
+        for (int k = 0; k < m; ++k) {
+            const double v = now[k] * norm;
+            O.val[w][k] = v;
+            O.err[w][k] = std::sqrt(std::fabs(er[k] * norm - v * v) / ws[w]);
+        }
+    }
+    if (ws[0] != 0.0) O.totw[0] = ws[0];
+    if (ws[2] != 0.0) O.totw[1] = ws[2];
+    if (ws[3] != 0.0) O.totw[2] = ws[3];
+    CK(cudaMemset(O.sums.p, 0, ns * sizeof(double)));
+    return DMC_OK;
+}
+
+int dmc_get_operators(dmc_ctx* c, int which, double* values, double* errors, int cap, int* n, double* wsum)
+{
+    if (!c || which < 0 || which > 7) return DMC_ERR_INVALID;
+    auto& O = c->ops;
+    const int w = which & 3;
+    const int m = O.on ? ops_counts(c, w) : 0;
+    if (n) *n = m;
+    if (m == 0 || (!values && !errors && !wsum)) return DMC_OK;
+    if ((values || errors) && cap < m) return fail(c, DMC_ERR_INVALID, "operator arrays too small");
+    if (which < 4) {
+        if (values) std::copy(O.val[w].begin(), O.val[w].end(), values);
+        if (errors) std::copy(O.err[w].begin(), O.err[w].end(), errors);
+        if (wsum) *wsum = O.totw[w == 0 || w == 1 ? 0 : (w == 2 ? 1 : 2)];
+        return DMC_OK;
+    }
+    // running sums before the block update
+    const int ns = ops_nsums(c);
+    std::vector<double> h(ns);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(h.data(), O.sums.p, ns * sizeof(double), cudaMemcpyDeviceToHost));
+    size_t off = 0;
+    for (int k = 0; k < w; ++k) off += 2 * (size_t)ops_counts(c, k);
+    if (values) std::copy(h.begin() + off, h.begin() + off + m, values);
+    if (errors) std::copy(h.begin() + off + m, h.begin() + off + 2 * m, errors);
+    if (wsum) *wsum = h[ns - 3 + (w == 0 || w == 1 ? 0 : (w == 2 ? 1 : 2))];
+    return DMC_OK;
+}
+
+int dmc_write_operators(dmc_ctx* c, const char* dir, double tau)
+{
+    if (!c || !dir) return DMC_ERR_INVALID;
+    auto& O = c->ops;
+    if (!O.on) return fail(c, DMC_ERR_INVALID, "operators are not set up");
+    const Setup& S = c->S;
+    const std::string d(dir);
+    auto E = [](double v) { return fortran_e(v, 15, 7); };
+    const double pi = 4.0 * std::atan(1.0);
+    const int npart = S.npart;
+    if (O.dev.ntabg > 0) {
+        // writegofr, gofr.f90:132-176 (gofr.out, rho.out)
+        const int ntab = O.dev.ntabg;
+        const double dr = 0.5 * S.el / ntab, rho = npart / (S.el * S.el * S.el);
+        FILE* f = std::fopen((d + "/gofr.out").c_str(), "a");
+        if (!f) return fail(c, DMC_ERR_INVALID, "cannot open gofr.out");
+        std::fprintf(f, "# r*kF, g(r), err\n# total weight = %s\n# tau = %s\n", E(O.totw[0]).c_str(), E(tau).c_str());
+        for (int i = 0; i < ntab; ++i) {
+            const double r0 = i * dr, r1 = (i + 1) * dr, r = (i + 0.5) * dr;
+            const double vol = 4.0 * pi * (r1 * r1 * r1 - r0 * r0 * r0) / 3.0;
+            const double facl = 1.0 / (rho * npart * vol);
+            std::string line = E(r);
+            for (int t = 0; t < 3; ++t)
+                line += E(O.val[0][t * (ntab + 1) + i] * facl) + E(O.err[0][t * (ntab + 1) + i] * facl);
+            std::fprintf(f, "%s\n", line.c_str());
+        }
+        std::fprintf(f, " \n \n");
+        std::fclose(f);
+        f = std::fopen((d + "/rho.out").c_str(), "a");
+        if (!f) return fail(c, DMC_ERR_INVALID, "cannot open rho.out");
+        std::fprintf(f, "# r, xrhoup, err, xrhodn, err, yrhoup, err, yrhodn, err, zrhoup, err, zrhodn, err\n");
+        std::fprintf(f, "# total weight = %s\n# tau = %s\n", E(O.totw[0]).c_str(), E(tau).c_str());
+        const int order[6] = {0, 3, 1, 4, 2, 5};
+        for (int i = -ntab; i <= ntab; ++i) {
+            std::string line = E(i * dr);
+            for (int t : order) {
+                const size_t at = (size_t)t * (2 * ntab + 1) + (i + ntab);
+                line += E(O.val[1][at] / npart) + E(O.err[1][at] / npart);
+            }
+            std::fprintf(f, "%s\n", line.c_str());
+        }
+        std::fprintf(f, " \n \n");
+        std::fclose(f);
+    }
+    if (O.dev.ntabq > 0) {
+        // writesofq, sofq.f90:90-117
+        FILE* f = std::fopen((d + "/sofq.out").c_str(), "a");
+        if (!f) return fail(c, DMC_ERR_INVALID, "cannot open sofq.out");
+        std::fprintf(f, "# q/kF, s(q), err\n# total weight = %s\n# tau = %s\n", E(O.totw[1]).c_str(), E(tau).c_str());
+        const int nq = O.dev.nqtot;
+        int k = 0;
+        for (int iq = 0; iq < O.dev.ntabq; ++iq) {
+            double ave[3] = {0, 0, 0}, err[3] = {0, 0, 0};
+            for (int j = 0; j < O.numshq[iq]; ++j, ++k)
+                for (int t = 0; t < 3; ++t) {
+                    ave[t] += O.val[2][t * nq + k];
+                    err[t] += O.err[2][t * nq + k];
+                }
+            const double* a = &O.akq[3 * (k - 1)];
+            const double q = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+            std::string line = E(q / S.kunit);
+            for (int t = 0; t < 3; ++t)
+                line += E(ave[t] / O.numshq[iq] / npart) + E(err[t] / O.numshq[iq] / npart);
+            std::fprintf(f, "%s\n", line.c_str());
+        }
+        std::fprintf(f, "  \n  \n");
+        std::fclose(f);
+    }
+    if (O.dev.nkv > 0) {
+        // writeenk, momentum3d.f90:172-190
+        FILE* f = std::fopen((d + "/nofk.out").c_str(), "a");
+        if (!f) return fail(c, DMC_ERR_INVALID, "cannot open nofk.out");
+        std::fprintf(f, "# k/kF, n(k), err\n# total weight = %s\n# tau = %s\n", E(O.totw[2]).c_str(), E(tau).c_str());
+        for (int ir = 0; ir <= O.dev.ntabk; ++ir) {
+            const int* v = &O.ik[3 * O.indk[ir]];
+            const double kk = std::sqrt(O.dev.dk * O.dev.dk * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+            std::fprintf(f, "%s%s%s\n", E(kk).c_str(), E(O.val[3][ir]).c_str(), E(O.err[3][ir]).c_str());
+        }
+        std::fprintf(f, " \n \n");
+        std::fclose(f);
+    }
     return DMC_OK;
 }
 

@@ -86,6 +86,17 @@ struct DevParams {
     int sinup[DMC_MAX_UNPAIRED], sindn[DMC_MAX_UNPAIRED];
 };
 
+// Operators (g(r), density profile, S(q), n(k)) on the device
+struct OpsDev {
+    int ntabg, ntabq, ntabk, nsamp, nqtot, nkv, nnk;
+    double scaleg, el, dk;
+    const double* akq;                 // [nqtot][3], k = 0 first
+    const int* ik;                     // [nkv][3], sorted by |ik|^2
+    const int* indk;                   // [ntabk+1] first vector of each shell
+    const int* nkk;                    // [ntabk+1] vectors per shell
+    const unsigned long long *jA, *jC; // LCG jump-ahead, [3 npart nsamp + 1]
+};
+
 // SoA walker stack on the device
 struct DevStack {
     double *x, *dpsi, *dpsig;

@@ -32,10 +32,12 @@
 
 #include "../../include/dmcbcs_gpu.h"
 
-namespace {
+#include "dmc_text.h"
 
-// Fortran Ew.d for finite values
-std::string edit_e(double v, int w, int d)
+namespace dmc {
+
+// Fortran Ew.d output
+std::string fortran_e(double v, int w, int d)
 {
     std::string body;
     if (!std::isfinite(v)) {
@@ -64,6 +66,12 @@ std::string edit_e(double v, int w, int d)
     if ((int)body.size() > w) return std::string(w, '*');
     return std::string(w - body.size(), ' ') + body;
 }
+
+}  // namespace dmc
+
+namespace {
+
+using dmc::fortran_e;
 
 // Fortran Ew.d / Fw.d input of one fixed-width field (blank = 0)
 bool read_real(const std::string& field, int d, double& out)
@@ -158,12 +166,12 @@ int dmc_fort9_write(const char* path, int npart, int n, const double* x, const d
     for (int k = 0; k < n; ++k) {
         const double* xk = x + (size_t)k * n3;
         for (int e = 0; e < n3; ++e) {
-            std::fputs(edit_e(xk[e], 15, 7).c_str(), f);
+            std::fputs(fortran_e(xk[e], 15, 7).c_str(), f);
             if (e % 6 == 5 || e == n3 - 1) std::fputc('\n', f);
         }
-        std::fputs(edit_e(weight[k], 15, 7).c_str(), f);
-        std::fputs(edit_e(psil[k], 25, 15).c_str(), f);
-        std::fputs(edit_e(psigl[k], 25, 15).c_str(), f);
+        std::fputs(fortran_e(weight[k], 15, 7).c_str(), f);
+        std::fputs(fortran_e(psil[k], 25, 15).c_str(), f);
+        std::fputs(fortran_e(psigl[k], 25, 15).c_str(), f);
         std::fputc('\n', f);
         std::fprintf(f, "%20lld\n", (long long)irn[k]);
     }

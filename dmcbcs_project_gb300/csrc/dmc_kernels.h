@@ -35,6 +35,19 @@ cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x
 cudaError_t launch_sr_sums(const double* der, const double* d2psi, const double* v, int n, int np, double hbar,
                            double eunit, int npart, double* sums, cudaStream_t st);
 
+// Operators (dmc_ops.cu): per-walker histograms and S(q) values, n(k) per
+// walker, and the weighted sums over the population in pop order.  sums:
+// gnow, gerr [3(ntabg+1)], dnow, derr [6(2 ntabg+1)], snow, serr [3 nqtot],
+// enknow, enkerr [ntabk+1], then wsg, wsq, wsk.
+size_t ops_walker_smem(const DevParams& p, const OpsDev& o);
+cudaError_t launch_ops_walker(const DevParams& p, const OpsDev& o, const double* x, int n, int* hg, int* hd,
+                              double* sv, int grid, cudaStream_t st);
+cudaError_t launch_ops_enk(const DevParams& p, const OpsDev& o, const KVecDev* kv, const TabUD* tud,
+                           const TabSS* tss, const double* x, const unsigned long long* irn, const double* sinv,
+                           int n, double* tk, int grid, cudaStream_t st);
+cudaError_t launch_ops_reduce(const OpsDev& o, int n, const DevStack& s, const int* hg, const int* hd,
+                              const double* sv, const double* tk, double* sums, cudaStream_t st);
+
 // FMA throughput of the FP64 (kind 0) or FP32 (kind 1) pipe, TFLOP/s
 cudaError_t probe_fma_peak(int kind, int nsm, double* tflops);
 

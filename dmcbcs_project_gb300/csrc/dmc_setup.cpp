@@ -15,6 +15,8 @@ namespace {
 
 const double kPi = 3.14159265358979323846;
 
+}  // namespace
+
 // kstates3d (kshell.f90:20-156): integer vectors of the half set of each
 // |n|^2 shell, in the order the reference's exchange sort leaves them.
 int k_shells(double el, int nsh0, std::vector<KVec>& out, std::vector<int>& numsh0, std::string& err)
@@ -76,6 +78,8 @@ int k_shells(double el, int nsh0, std::vector<KVec>& out, std::vector<int>& nums
     }
     return DMC_OK;
 }
+
+namespace {
 
 // ---- beta function (betafun.f90) ----------------------------------------
 
@@ -410,9 +414,10 @@ int Setup::build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string&
     ieq = cjas[1] != 0.0;
     // units, dmcbcs.f90:146-170
     if (rd.units) {
-        const double kunit = std::pow(3.0 * (kPi * kPi) * (npart / (el * el * el)), 1.0 / 3.0);
+        kunit = std::pow(3.0 * (kPi * kPi) * (npart / (el * el * el)), 1.0 / 3.0);
         eunit = 3.0 / 5.0 * hbar / (2.0 * mu) * (kunit * kunit);
     } else {
+        kunit = 1.0;
         eunit = 1.0;
     }
     etrial = rd.etrial * eunit * npart;

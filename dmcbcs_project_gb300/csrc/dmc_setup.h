@@ -21,6 +21,10 @@ struct KVec {
     int shell;   // 1-based shell index of the reference's vorb(shell)
 };
 
+// kstates3d (kshell.f90:20-156): the half set of k vectors of shells
+// 1..nsh0 (k = 0 first) and the half-shell sizes numsh0[nsh0].
+int k_shells(double el, int nsh0, std::vector<KVec>& out, std::vector<int>& numsh0, std::string& err);
+
 struct Setup {
     // sizes
     int npart = 0, nup = 0, ndn = 0, npair = 0, nexup = 0, nexdn = 0, nd = 0;
@@ -53,6 +57,7 @@ struct Setup {
     std::vector<double> utab[2], dutab[2], d2utab[2], vtab[2];
     // units (dmcbcs.f90:146-170) and step (step.f90:11-41)
     double eunit = 1, nfac = 1, etrial = 0;
+    double kunit = 1;              // k_F of the unit system (dmcbcs.f90:150,158)
     double sigma[2] = {0, 0}, dcut[2] = {0, 0};
     bool cutdrift = false;
 

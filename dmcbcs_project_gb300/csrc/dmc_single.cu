@@ -16,39 +16,12 @@
 #include "dmc_device.cuh"
 #include "dmc_kernels.h"
 #include "dmc_walker.cuh"
+#include "dmc_single.cuh"
 
 namespace dmc {
 
-using walker::Lagrange;
-using walker::lagrange;
-using walker::warp_sum;
 
 namespace {
-
-// Fortran nint: nearest integer, halves away from zero
-__device__ __forceinline__ double fnint(double a) { return round(a); }
-
-// beta(r) (radialfun, betafun.f90:173-194), value only; zero beyond L/2
-__device__ double beta_value(const DevParams& p, const TabUD* tud, double r)
-{
-    if (p.nobeta || r > p.rangeb) return 0.0;
-    const Lagrange<double> W = lagrange(r, p.scaleb, p.ntab);
-    const TabUD* T = tud + (W.idx - 1);
-    return W.c1 * T[0].b + W.c2 * T[1].b + W.c3 * T[2].b + W.c4 * T[3].b;
-}
-
-// Jastrow u(r) of one pair type (coshpot.f90:236-250): 0 beyond the range
-__device__ double jastrow_u(const DevParams& p, const TabUD* tud, const TabSS* tss, bool opposite, double r)
-{
-    if (!(r < p.range)) return 0.0;
-    const Lagrange<double> W = lagrange(r, p.scale, p.ntab);
-    if (opposite) {
-        const TabUD* T = tud + (W.idx - 1);
-        return W.c1 * T[0].u + W.c2 * T[1].u + W.c3 * T[2].u + W.c4 * T[3].u;
-    }
-    const TabSS* T = tss + (W.idx - 1);
-    return W.c1 * T[0].u + W.c2 * T[1].u + W.c3 * T[2].u + W.c4 * T[3].u;
-}
 
 __global__ void bcsone_kernel(const __grid_constant__ DevParams p, const KVecDev* __restrict__ kv,
                               const TabUD* __restrict__ tud, const double* __restrict__ x,
@@ -62,37 +35,8 @@ __global__ void bcsone_kernel(const __grid_constant__ DevParams p, const KVecDev
     const double* xw = x + (size_t)w * 3 * P;
     const int i = ipart[w] - 1;   // checked on the host
     const double xi[3] = {xw[3 * i] - dr[3 * w], xw[3 * i + 1] - dr[3 * w + 1], xw[3 * i + 2] - dr[3 * w + 2]};
-    const bool isup = i < p.nup;
-    const int nloop = isup ? p.npair + p.nexdn : p.npair + p.nexup;
-    const double* S = smati + (size_t)w * nd * nd;
-    double acc = 0.0;
-    for (int q = lane; q < nd; q += 32) {
-        double ph;
-        if (q < nloop) {
-            // new pair-function entry phi(r_i' - r_jj) (psislaterbcs.f90:318-350)
-            const int jj = isup ? q + p.npair + p.nexup : q;
-            double d[3];
-            for (int c = 0; c < 3; ++c) {
-                d[c] = xi[c] - xw[3 * jj + c];
-                d[c] = d[c] - p.el * fnint(d[c] / p.el);
-            }
-            ph = kv[0].v;
-            for (int k = 1; k < p.nk; ++k) ph += kv[k].v * cos(kv[k].k[0] * d[0] + kv[k].k[1] * d[1] + kv[k].k[2] * d[2]);
-            ph += beta_value(p, tud, sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
-        } else {
-            // unpaired plane wave of the moved particle (psislaterbcs.f90:352-365)
-            const int j = q - nloop;
-            const double* a = isup ? p.akup[j] : p.akdn[j];
-            const int sn = isup ? p.sinup[j] : p.sindn[j];
-            const double arg = a[0] * xi[0] + a[1] * xi[1] + a[2] * xi[2];
-            ph = sn ? sin(arg) : cos(arg);
-        }
-        // up: row i of S replaced, ratio = sum_q Sinv(q,i) phi_q; down: column
-        const double s = isup ? S[q + (size_t)i * nd] : S[(i - p.nup) + (size_t)q * nd];
-        acc = fma(s, ph, acc);
-    }
-    acc = warp_sum(acc);
-    if (lane == 0) ratio[w] = acc;
+    const double r = single::warp_bcsone(p, kv, tud, xw, smati + (size_t)w * nd * nd, i, xi);
+    if (lane == 0) ratio[w] = r;
 }
 
 __global__ void getphione_kernel(const __grid_constant__ DevParams p, const TabUD* __restrict__ tud,
@@ -103,29 +47,10 @@ __global__ void getphione_kernel(const __grid_constant__ DevParams p, const TabU
     const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= nw) return;
-    const int P = p.npart;
-    const double* xw = x + (size_t)w * 3 * P;
-    const int i = ipart[w] - 1;
-    const bool upi = i < p.nup;
-    double u = 0.0;
-    for (int j = lane; j < P; j += 32) {
-        if (j == i) continue;
-        const bool opposite = upi != (j < p.nup);
-        if (!opposite && !p.ieq) continue;   // opposite-spin pairs are always on
-        for (int pass = 0; pass < 2; ++pass) {
-            double d[3];
-            for (int c = 0; c < 3; ++c) {
-                d[c] = xw[3 * i + c] - xw[3 * j + c];
-                if (pass) d[c] -= drr[3 * w + c];
-                d[c] = d[c] - p.el * fnint(d[c] * p.eli);
-            }
-            const double r = fmax(sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), 1.0e-14);
-            const double uj = jastrow_u(p, tud, tss, opposite, r);
-            u = pass ? u + uj : u - uj;
-        }
-    }
-    u = warp_sum(u);
-    if (lane == 0) ratio[w] = exp(u);
+    const double* xw = x + (size_t)w * 3 * p.npart;
+    const double d[3] = {drr[3 * w], drr[3 * w + 1], drr[3 * w + 2]};
+    const double r = single::warp_getphione(p, tud, tss, xw, ipart[w] - 1, d);
+    if (lane == 0) ratio[w] = r;
 }
 
 // d log|det| / d vorb(shell) for one walker per CTA.  smati is the inverse in

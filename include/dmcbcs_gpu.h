@@ -274,6 +274,37 @@ int dmc_init_walkers(dmc_ctx* ctx);
  * w->n walkers with x, weight, psil0, psigl0 and irn (other fields ignored). */
 int dmc_load_walkers(dmc_ctx* ctx, const dmc_walkers* w);
 
+/* ---- operators (operators.f90, gofr.f90, sofq.f90, momentum3d.f90) ------ */
+
+/* Replaces setoperators for a periodic box (operators.f90:7-74): ntabg g(r)
+ * bins on [0, L/2] with the density profile (gofr.f90:14-37), ntabq S(q)
+ * shells (sofq.f90:17-33), n(k) for |ik|^2 <= ntabk (momentum3d.f90:14-71;
+ * at most 80 here); 0 switches one off.  Clears the sums. */
+int dmc_set_operators(dmc_ctx* ctx, int ntabg, int ntabq, int ntabk);
+
+/* zerooperators (operators.f90:75-88). */
+int dmc_zero_operators(dmc_ctx* ctx);
+
+/* The operator pass of dmcbcs.f90:465-473: every walker's addgofr, addsofq
+ * and addenk with weight w exp(psil - psigl) is wt0 (operators.f90:90-107),
+ * in pop order; the walkers are left in reverse order, as the pass leaves
+ * them.  n(k) draws from each walker's stream without advancing it. */
+int dmc_add_operators(dmc_ctx* ctx);
+
+/* updateoperators (operators.f90:109-124): block averages and errors. */
+int dmc_update_operators(dmc_ctx* ctx);
+
+/* Results of the last update: which 0 g(r) [3][ntabg+1] (up-down, up-up,
+ * down-down), 1 density profile [6][2 ntabg + 1] (x, y, z of up, then of
+ * down; bin i at i + ntabg), 2 S(q) [3][nqtot] (up, down, up-down), 3 n(k)
+ * [nshells]; which + 4: the running sums and their second-moment sums
+ * instead.  *n gets the count (0 if off), *wsum the weight sum. */
+int dmc_get_operators(dmc_ctx* ctx, int which, double* values, double* errors, int cap, int* n, double* wsum);
+
+/* writeoperators (operators.f90:126-141): appends gofr.out, rho.out,
+ * sofq.out and nofk.out in directory dir, in the reference's layouts. */
+int dmc_write_operators(dmc_ctx* ctx, const char* dir, double tau);
+
 /* ---- fort.9 walker files (dmcbcs.f90:254-294 read, :548-567 write) ----- */
 
 /* Write n walkers in the reference's fort.9 layout: an (i10,f15.8) header

@@ -155,7 +155,10 @@ typedef struct orc_state {
     int nest;
     double valblk[DMC_NEST_MAX], valblk2[DMC_NEST_MAX], wtblk[DMC_NEST_MAX];
     int nthreads;
+    /* operators.f90 (g(r), S(q), n(k)); NULL until orc_set_operators */
+    struct orc_ops* ops;
 } orc_state;
+static void free_ops(struct orc_ops* o);
 
 /* ------------------------------------------------------------------------ */
 /* k shells: kshell.f90:20-156                                              */
@@ -553,6 +556,7 @@ void orc_destroy(orc_state* s)
     free(s->utab); free(s->dutab); free(s->d2utab); free(s->vtab);
     free_stack(&s->st[0]);
     free_stack(&s->st[1]);
+    free_ops(s->ops);
     free(s);
 }
 
@@ -1933,4 +1937,348 @@ int orc_sr_update(int nparm, const double* ovec_s, const double* ovecw_s, const 
     *eave = esum;
     free(ovec); free(ovecw); free(pmat); free(fvec);
     return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* operators: operators.f90:7-141 with gofr.f90 (g(r) and the density       */
+/* profile), sofq.f90 (S(q)) and momentum3d.f90 (n(k))                      */
+/* ------------------------------------------------------------------------ */
+
+struct orc_ops {
+    int ntabg, ntabq, ntabk, nsamp;
+    /* gofr.f90:14-37: gnow(3,0:ntab), dnow(6,-ntab:ntab) */
+    double drg, scaleg, wsg, totwg;
+    double *gnow, *gerr, *g, *ge;       /* [itab][0..ntabg] */
+    double *dnow, *derr, *d, *de;       /* [itab][-ntabg..ntabg] at i + ntabg */
+    /* sofq.f90:17-33: snow(3,nqtot) */
+    int nqtot, numshq[DMC_MAX_SHELLS];
+    double *akq, *ak2q, wsq, totwq;
+    double *snow, *serr, *sq, *se;      /* [itab][iq] */
+    /* momentum3d.f90:14-71 */
+    int nkv;
+    int *ik, *indk, *nkk;               /* ik[3*nkv], indk/nkk[0..ntabk] */
+    double dk, wsk, totwk;
+    double *enknow, *enkerr, *enk, *enke;
+};
+
+static void free_ops(struct orc_ops* o)
+{
+    if (!o) return;
+    free(o->gnow); free(o->gerr); free(o->g); free(o->ge);
+    free(o->dnow); free(o->derr); free(o->d); free(o->de);
+    free(o->akq); free(o->ak2q); free(o->snow); free(o->serr); free(o->sq); free(o->se);
+    free(o->ik); free(o->indk); free(o->nkk);
+    free(o->enknow); free(o->enkerr); free(o->enk); free(o->enke);
+    free(o);
+}
+
+static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
+
+/* zerooperators, operators.f90:75-88 */
+void orc_zero_operators(orc_state* s)
+{
+    struct orc_ops* o = s->ops;
+    if (!o) return;
+    size_t ng = 3 * (size_t)(o->ntabg + 1), nd = 6 * (size_t)(2 * o->ntabg + 1), nq = 3 * (size_t)o->nqtot;
+    size_t nk = (size_t)o->ntabk + 1;
+    if (o->ntabg > 0) {
+        memset(o->gnow, 0, ng * 8); memset(o->gerr, 0, ng * 8); memset(o->g, 0, ng * 8); memset(o->ge, 0, ng * 8);
+        memset(o->dnow, 0, nd * 8); memset(o->derr, 0, nd * 8); memset(o->d, 0, nd * 8); memset(o->de, 0, nd * 8);
+    }
+    if (o->ntabq > 0) {
+        memset(o->snow, 0, nq * 8); memset(o->serr, 0, nq * 8); memset(o->sq, 0, nq * 8); memset(o->se, 0, nq * 8);
+    }
+    if (o->nkv > 0) {
+        memset(o->enknow, 0, nk * 8); memset(o->enkerr, 0, nk * 8); memset(o->enk, 0, nk * 8);
+        memset(o->enke, 0, nk * 8);
+    }
+    o->wsg = o->wsq = o->wsk = 0.0;
+}
+
+/* setoperators for a periodic box (operators.f90:33-41,65-74): ntabg g(r)
+ * bins (setupgofr, gofr.f90:14-37), ntabq S(q) shells (setupsofq,
+ * sofq.f90:17-33), n(k) up to |ik|^2 <= ntabk (setupenk, momentum3d.f90:
+ * 14-71).  Zero switches an operator off.  Returns the number of n(k)
+ * shells + 1 (0 when off), or -1. */
+int orc_set_operators(orc_state* s, int ntabg, int ntabq, int ntabk)
+{
+    free_ops(s->ops);
+    struct orc_ops* o = (struct orc_ops*)calloc(1, sizeof(struct orc_ops));
+    if (!o) return -1;
+    s->ops = o;
+    o->ntabg = ntabg > 0 ? ntabg : 0;
+    o->ntabq = ntabq > 0 ? ntabq : 0;
+    if (o->ntabg > 0) {
+        size_t ng = 3 * (size_t)(o->ntabg + 1), nd = 6 * (size_t)(2 * o->ntabg + 1);
+        o->gnow = zalloc(ng); o->gerr = zalloc(ng); o->g = zalloc(ng); o->ge = zalloc(ng);
+        o->dnow = zalloc(nd); o->derr = zalloc(nd); o->d = zalloc(nd); o->de = zalloc(nd);
+        o->drg = 0.5 * s->el / o->ntabg;
+        o->scaleg = 1.0 / o->drg;
+    }
+    if (o->ntabq > 0) {
+        int nq = 0;
+        if (o->ntabq > DMC_MAX_SHELLS || kstates3d(s->el, o->ntabq, o->numshq, &o->akq, &o->ak2q, &nq) != 0) return -1;
+        /* kstates3d lists k = 0 first (numsh(1) = 1); S(q) runs over all nqtot vectors */
+        o->nqtot = 0;
+        for (int i = 0; i < o->ntabq; i++) o->nqtot += o->numshq[i];
+        if (o->nqtot > nq) return -1;
+        size_t n3 = 3 * (size_t)o->nqtot;
+        o->snow = zalloc(n3); o->serr = zalloc(n3); o->sq = zalloc(n3); o->se = zalloc(n3);
+    }
+    if (ntabk > 0) {
+        o->nsamp = 10;
+        o->dk = 2.0 * (4.0 * atan(1.0)) / s->el;   /* pi = 4 atan(1), momentum3d.f90:27-28 */
+        int nnk = (int)(sqrt((double)ntabk) + 1.0);
+        int ntot = 0;
+        for (int ix = 0; ix <= nnk; ix++)
+            for (int iy = 0; iy <= nnk; iy++)
+                for (int iz = 0; iz <= nnk; iz++)
+                    if (ix * ix + iy * iy + iz * iz <= ntabk) ntot++;
+        o->nkv = ntot;
+        o->ik = (int*)calloc(3 * (size_t)ntot, sizeof(int));
+        int* ik2 = (int*)calloc(ntot, sizeof(int));
+        ntot = 0;
+        for (int ix = 0; ix <= nnk; ix++)
+            for (int iy = 0; iy <= nnk; iy++)
+                for (int iz = 0; iz <= nnk; iz++)
+                    if (ix * ix + iy * iy + iz * iz <= ntabk) {
+                        ik2[ntot] = ix * ix + iy * iy + iz * iz;
+                        o->ik[3 * ntot] = ix; o->ik[3 * ntot + 1] = iy; o->ik[3 * ntot + 2] = iz;
+                        ntot++;
+                    }
+        /* exchange sort of momentum3d.f90:46-57 */
+        for (int i = 1; i < ntot; i++)
+            for (int j = 0; j < i; j++)
+                if (ik2[i] < ik2[j]) {
+                    int t = ik2[i]; ik2[i] = ik2[j]; ik2[j] = t;
+                    for (int c = 0; c < 3; c++) { t = o->ik[3 * i + c]; o->ik[3 * i + c] = o->ik[3 * j + c]; o->ik[3 * j + c] = t; }
+                }
+        o->indk = (int*)calloc((size_t)ntabk + 1, sizeof(int));
+        o->nkk = (int*)calloc((size_t)ntabk + 1, sizeof(int));
+        int itab = 0;
+        o->indk[0] = 0;
+        o->nkk[0] = 1;
+        for (int i = 1; i < ntot; i++) {
+            if (ik2[i] != ik2[i - 1]) {
+                itab++;
+                o->indk[itab] = i;
+            }
+            o->nkk[itab]++;
+        }
+        o->ntabk = itab;
+        free(ik2);
+        size_t nk = (size_t)o->ntabk + 1;
+        o->enknow = zalloc(nk); o->enkerr = zalloc(nk); o->enk = zalloc(nk); o->enke = zalloc(nk);
+    }
+    orc_zero_operators(s);
+    return o->nkv > 0 ? o->ntabk + 1 : 0;
+}
+
+/* addgofr, gofr.f90:53-92 */
+static void addgofr(struct orc_ops* o, const orc_state* s, const double* x, double weight)
+{
+    int npart = s->npart, nup = s->nbin[0], ntab = o->ntabg;
+    for (int i = 0; i < npart - 1; i++)
+        for (int j = i + 1; j < npart; j++) {
+            int itab = 0;
+            if (i < nup && j < nup) itab = 1;
+            if (i >= nup && j >= nup) itab = 2;
+            double dx[3], r2 = 0.0;
+            for (int c = 0; c < 3; c++) {
+                dx[c] = x[3 * i + c] - x[3 * j + c];
+                dx[c] = dx[c] - s->el * fnint(dx[c] / s->el);
+                r2 += dx[c] * dx[c];
+            }
+            double r = sqrt(r2);
+            int index = r < 0.5 * s->el ? (int)(o->scaleg * r) : ntab;
+            o->gnow[itab * (ntab + 1) + index] += 2.0 * weight;
+            o->gerr[itab * (ntab + 1) + index] += 4.0 * weight;
+        }
+    o->wsg += weight;
+    for (int i = 0; i < npart; i++) {
+        double dx[3];
+        for (int c = 0; c < 3; c++) {
+            dx[c] = x[3 * i + c];
+            dx[c] = dx[c] - s->el * fnint(dx[c] / s->el);
+        }
+        for (int is = 0; is < 3; is++) {
+            int itab = i < nup ? is : is + 3;
+            int index = (int)(o->scaleg * dx[is]);
+            size_t at = (size_t)itab * (2 * ntab + 1) + (index + ntab);
+            if (index == 0) {
+                o->dnow[at] += 0.5 * weight;
+                o->derr[at] += 0.25 * weight;
+            } else {
+                o->dnow[at] += weight;
+                o->derr[at] += weight;
+            }
+        }
+    }
+}
+
+/* addsofq, sofq.f90:43-64 */
+static void addsofq(struct orc_ops* o, const orc_state* s, const double* x, double weight)
+{
+    int nup = s->nbin[0], npart = s->npart, nq = o->nqtot;
+    for (int iq = 0; iq < nq; iq++) {
+        const double* a = &o->akq[3 * iq];   /* ak(:,1..nqtot): k = 0 first, as kstates3d lists it */
+        double ur = 0, ui = 0, dr = 0, di = 0;
+        for (int i = 0; i < nup; i++) {
+            double arg = a[0] * x[3 * i] + a[1] * x[3 * i + 1] + a[2] * x[3 * i + 2];
+            ur += cos(arg);
+            ui -= sin(arg);
+        }
+        for (int i = nup; i < npart; i++) {
+            double arg = a[0] * x[3 * i] + a[1] * x[3 * i + 1] + a[2] * x[3 * i + 2];
+            dr += cos(arg);
+            di -= sin(arg);
+        }
+        double uu = ur * ur + ui * ui, dd = dr * dr + di * di;
+        double zr = ur * dr + ui * di, zi = ui * dr - ur * di;   /* rhokup * conjg(rhokdn) */
+        o->snow[iq] += uu * weight;
+        o->serr[iq] += uu * uu * weight;
+        o->snow[nq + iq] += dd * weight;
+        o->serr[nq + iq] += dd * dd * weight;
+        o->snow[2 * nq + iq] += zr * weight;
+        o->serr[2 * nq + iq] += (zr * zr - zi * zi) * weight;
+    }
+    o->wsq += weight;
+}
+
+/* addenk, momentum3d.f90:89-124: nsamp uniform displacements of every
+ * particle from the walker's own random stream (not saved back), psi ratios
+ * from move1 (getphione * bcsone with the walker's inverse), and the
+ * symmetrised plane-wave products per |ik|^2 shell */
+static void addenk(struct orc_ops* o, const orc_state* s, const walker* w, double wt)
+{
+    int npart = s->npart, nd = s->nd, ntab = o->ntabk;
+    double* sinv = (double*)malloc(sizeof(double) * ((size_t)nd * nd + 1));
+    double* dphi = (double*)malloc(sizeof(double) * 3 * npart);
+    double* tmp = zalloc((size_t)ntab + 1);
+    double phil, d2phi;
+    int is;
+    orc_bcs(s, w->x, &phil, &is, dphi, &d2phi, sinv);   /* hpsi(w) leaves the inverse in smatisave */
+    int64_t irn = w->irn;                              /* setrn(w%irn) */
+    for (int i = 0; i < npart; i++)
+        for (int ii = 0; ii < o->nsamp; ii++) {
+            double dx[3], drr[3];
+            for (int c = 0; c < 3; c++) dx[c] = (orc_ran1(&irn) - 0.5) * s->el;
+            for (int c = 0; c < 3; c++) drr[c] = -dx[c];   /* move1: drr = x - xnew */
+            double rat1 = orc_getphione(s, w->x, drr, i + 1);
+            double rat2 = orc_bcsone(s, w->x, drr, i + 1, sinv);
+            double psirat = rat1 * rat2;
+            for (int k = 0; k <= ntab; k++) {
+                int in = o->indk[k];
+                for (int j = 0; j < o->nkk[k]; j++) {
+                    const int* v = &o->ik[3 * (in + j)];
+                    tmp[k] += psirat * cos(o->dk * v[0] * dx[0]) * cos(o->dk * v[1] * dx[1]) * cos(o->dk * v[2] * dx[2]);
+                }
+            }
+        }
+    for (int k = 0; k <= ntab; k++) {
+        double e = tmp[k] / o->nkk[k];
+        o->enknow[k] += e * wt;
+        o->enkerr[k] += e * e * wt;
+    }
+    o->wsk += wt * o->nsamp;
+    free(sinv); free(dphi); free(tmp);
+}
+
+/* The operator pass of dmcbcs.f90:465-475 (addoperators, operators.f90:90-
+ * 107): every walker popped, its estimators added with weight
+ * w = weight exp(psil - psigl) is wt0, and pushed on the other stack. */
+int orc_add_operators(orc_state* s)
+{
+    struct orc_ops* o = s->ops;
+    if (!o) return -1;
+    wstack* in = &s->st[s->istin];
+    wstack* out = &s->st[1 - s->istin];
+    walker w;
+    out->n = 0;
+    while (in->n > 0) {
+        wget(s, in, in->n - 1, &w);
+        in->n--;
+        double wt = w.weight * exp(w.psil - w.psigl) * w.is * (double)w.wt0;
+        if (o->ntabg > 0) addgofr(o, s, w.x, wt);
+        if (o->ntabq > 0) addsofq(o, s, w.x, wt);
+        if (o->nkv > 0) addenk(o, s, &w, wt);
+        wput(s, out, out->n, &w);
+        out->n++;
+    }
+    s->istin = 1 - s->istin;
+    return 0;
+}
+
+static void block_norm(double* now, double* err, double* val, double* e, size_t n, double ws)
+{
+    double norm = 1.0 / ws;
+    for (size_t k = 0; k < n; k++) {
+        now[k] *= norm;
+        val[k] = now[k];
+        err[k] *= norm;
+        e[k] = sqrt(fabs(err[k] - now[k] * now[k]) / ws);
+        now[k] = 0.0;
+        err[k] = 0.0;
+    }
+}
+
+/* updateoperators (operators.f90:109-124): updategofr (gofr.f90:94-130),
+ * updatesofq (sofq.f90:66-88), updateenk (momentum3d.f90:148-170) for one
+ * process */
+void orc_update_operators(orc_state* s)
+{
+    struct orc_ops* o = s->ops;
+    if (!o) return;
+    if (o->ntabg > 0 && o->wsg != 0.0) {
+        block_norm(o->gnow, o->gerr, o->g, o->ge, 3 * (size_t)(o->ntabg + 1), o->wsg);
+        block_norm(o->dnow, o->derr, o->d, o->de, 6 * (size_t)(2 * o->ntabg + 1), o->wsg);
+        o->totwg = o->wsg;
+        o->wsg = 0.0;
+    }
+    if (o->ntabq > 0 && o->wsq != 0.0) {
+        block_norm(o->snow, o->serr, o->sq, o->se, 3 * (size_t)o->nqtot, o->wsq);
+        o->totwq = o->wsq;
+        o->wsq = 0.0;
+    }
+    if (o->nkv > 0 && o->wsk != 0.0) {
+        block_norm(o->enknow, o->enkerr, o->enk, o->enke, (size_t)o->ntabk + 1, o->wsk);
+        o->totwk = o->wsk;
+        o->wsk = 0.0;
+    }
+}
+
+/* Copy operator arrays: which 0 g(r) [3][ntabg+1] and its error, 1 the
+ * density profile [6][2 ntabg+1] and error, 2 S(q) [3][nqtot] and error,
+ * 3 n(k) [ntabk+1] and error; out gets values then errors; returns the
+ * count of values (0 if off).  which +4: the running sums before the update
+ * (now, err) instead. */
+int orc_get_operators(const orc_state* s, int which, double* out, double* wsum)
+{
+    const struct orc_ops* o = s->ops;
+    if (!o) return 0;
+    int raw = which >= 4;
+    which &= 3;
+    size_t n = 0;
+    const double *a = NULL, *b = NULL;
+    double ws = 0.0;
+    if (which == 0 && o->ntabg > 0) {
+        n = 3 * (size_t)(o->ntabg + 1);
+        a = raw ? o->gnow : o->g; b = raw ? o->gerr : o->ge; ws = raw ? o->wsg : o->totwg;
+    } else if (which == 1 && o->ntabg > 0) {
+        n = 6 * (size_t)(2 * o->ntabg + 1);
+        a = raw ? o->dnow : o->d; b = raw ? o->derr : o->de; ws = raw ? o->wsg : o->totwg;
+    } else if (which == 2 && o->ntabq > 0) {
+        n = 3 * (size_t)o->nqtot;
+        a = raw ? o->snow : o->sq; b = raw ? o->serr : o->se; ws = raw ? o->wsq : o->totwq;
+    } else if (which == 3 && o->nkv > 0) {
+        n = (size_t)o->ntabk + 1;
+        a = raw ? o->enknow : o->enk; b = raw ? o->enkerr : o->enke; ws = raw ? o->wsk : o->totwk;
+    }
+    if (!n) return 0;
+    if (out) {
+        memcpy(out, a, n * 8);
+        memcpy(out + n, b, n * 8);
+    }
+    if (wsum) *wsum = ws;
+    return (int)n;
 }

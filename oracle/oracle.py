@@ -75,6 +75,11 @@ def lib():
         L.orc_get_wtisto.argtypes = [C.c_void_p, _lp]
         L.orc_sr_update.argtypes = [C.c_int, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, C.c_double,
                                     C.c_double, _dp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_set_operators.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.orc_zero_operators.argtypes = [C.c_void_p]
+        L.orc_add_operators.argtypes = [C.c_void_p]
+        L.orc_update_operators.argtypes = [C.c_void_p]
+        L.orc_get_operators.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -268,6 +273,34 @@ class Oracle:
         out.update(n=n, x=x[:n], dpsi=dpsi[:n], dpsig=dpsig[:n], is_=is_[:n], irn=irn[:n],
                    wt0=wt0[:n].astype(np.float64))
         return out
+
+    # ---- operators: g(r) + density profile, S(q), n(k) ----------------------
+    def set_operators(self, ntabg, ntabq, ntabk):
+        """Returns the number of n(k) shells (0 when n(k) is off)."""
+        r = lib().orc_set_operators(self._h, int(ntabg), int(ntabq), int(ntabk))
+        if r < 0:
+            raise RuntimeError("set_operators failed")
+        return r
+
+    def zero_operators(self):
+        lib().orc_zero_operators(self._h)
+
+    def add_operators(self):
+        lib().orc_add_operators(self._h)
+
+    def update_operators(self):
+        lib().orc_update_operators(self._h)
+
+    def operators(self, which, raw=False):
+        """which: 0 g(r) [3][ntabg+1], 1 density [6][2 ntabg+1], 2 S(q)
+        [3][nqtot], 3 n(k) [ntabk+1]; returns (values, errors, weight sum);
+        raw=True gives the running sums before the block update."""
+        code = int(which) + (4 if raw else 0)
+        n = lib().orc_get_operators(self._h, code, None, None)
+        out = np.zeros(2 * max(n, 1))
+        ws = C.c_double()
+        lib().orc_get_operators(self._h, code, out.ctypes.data_as(C.c_void_p), C.byref(ws))
+        return out[:n].copy(), out[n:2 * n].copy(), ws.value
 
     def wtisto(self):
         h = np.zeros(DMC_WTISTO, np.int64)

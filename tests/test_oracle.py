@@ -321,3 +321,101 @@ def test_vmc_acceptance_reasonable():
     vn, en = o.block_update()
     assert 0.3 < vn[5] <= 1.0            # acceptance (estimator 6)
     assert o.num_walkers() == 32         # VMC never branches
+
+
+def _operator_setup(nwalk=6):
+    sysd, rund, _ = configs.workload("n14", nwalk=nwalk)
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    orc.initial_eval()
+    orc.generation(False)
+    return sysd, orc
+
+
+def test_oracle_gofr_and_sofq_against_numpy():
+    """addgofr / addsofq (gofr.f90:53-92, sofq.f90:43-64) recomputed with numpy
+    on the same population, walkers in pop order (top of the stack first)."""
+    sysd, orc = _operator_setup()
+    ntabg, ntabq = 16, 3
+    orc.set_operators(ntabg, ntabq, 0)
+    w = orc.walkers()
+    el = orc.info.el
+    nup = sysd.nbin[0]
+    orc.add_operators()
+    g, g2, ws = orc.operators(0, raw=True)
+    d, d2, _ = orc.operators(1, raw=True)
+    s, s2, _ = orc.operators(2, raw=True)
+    scale = ntabg / (0.5 * el)
+    G = np.zeros((3, ntabg + 1))
+    Dn = np.zeros((6, 2 * ntabg + 1))
+    wt = w["weight"] * np.exp(w["psil"] - w["psigl"]) * w["is_"] * w["wt0"]
+    npart = w["x"].shape[1]
+    for k in range(w["n"])[::-1]:
+        x = w["x"][k]
+        for i in range(npart - 1):
+            for j in range(i + 1, npart):
+                itab = 1 if (i < nup and j < nup) else (2 if (i >= nup and j >= nup) else 0)
+                dx = x[i] - x[j]
+                dx = dx - el * np.sign(dx / el) * np.floor(np.abs(dx / el) + 0.5)
+                r = np.sqrt(np.sum(dx * dx))
+                G[itab, int(scale * r) if r < 0.5 * el else ntabg] += 2 * wt[k]
+        for i in range(npart):
+            dx = x[i] - el * np.sign(x[i] / el) * np.floor(np.abs(x[i] / el) + 0.5)
+            for c in range(3):
+                idx = int(scale * dx[c])
+                Dn[c + (0 if i < nup else 3), idx + ntabg] += (0.5 if idx == 0 else 1.0) * wt[k]
+    assert np.allclose(g, G.ravel(), rtol=1e-12, atol=0)
+    assert np.allclose(d, Dn.ravel(), rtol=1e-12, atol=1e-300)
+    assert abs(ws - wt.sum()) < 1e-12 * abs(ws)
+    # S(q): half-shell k vectors k = 0 first; rho_k = sum exp(-i k.x)
+    ak = orc.table(7).reshape(-1, 3)
+    nq = s.size // 3
+    S = np.zeros((3, nq))
+    for k in range(w["n"])[::-1]:
+        x = w["x"][k]
+        ru = np.exp(-1j * (x[:nup] @ ak[:nq].T)).sum(axis=0)
+        rd = np.exp(-1j * (x[nup:] @ ak[:nq].T)).sum(axis=0)
+        S[0] += np.real(ru * np.conj(ru)) * wt[k]
+        S[1] += np.real(rd * np.conj(rd)) * wt[k]
+        S[2] += np.real(ru * np.conj(rd)) * wt[k]
+    assert np.allclose(s, S.ravel(), rtol=1e-11, atol=1e-9)
+    assert np.allclose(s[:1], wt.sum() * nup ** 2)            # k = 0: |rho_0|^2 = N_up^2
+
+
+def test_oracle_nofk_against_python_loop():
+    """addenk (momentum3d.f90:89-124) for one walker from the oracle's own
+    primitives: ran1 draws from the walker's stream, move1 = getphione *
+    bcsone with the walker's inverse, the plane-wave products per shell."""
+    sysd, orc = _operator_setup(nwalk=1)
+    ntabk = 6
+    nsh = orc.set_operators(0, 0, ntabk)
+    w = orc.walkers()
+    el = orc.info.el
+    x = w["x"][0]
+    wt = (w["weight"] * np.exp(w["psil"] - w["psigl"]) * w["is_"] * w["wt0"])[0]
+    sm = orc.bcs(x[None], want_inverse=True)["smati"][0]
+    nnk = int(np.sqrt(ntabk) + 1)
+    ik = [(a, b, c) for a in range(nnk + 1) for b in range(nnk + 1) for c in range(nnk + 1)
+          if a * a + b * b + c * c <= ntabk]
+    shells = sorted(set(a * a + b * b + c * c for a, b, c in ik))
+    dk = 2 * np.pi / el
+    tmp = np.zeros(len(shells))
+    irn = int(w["irn"][0])
+    for i in range(x.shape[0]):
+        for _ in range(10):
+            dx = np.zeros(3)
+            for c in range(3):
+                u, irn = oracle.ran1(irn)
+                dx[c] = (u - 0.5) * el
+            rat = orc.getphione(x, -dx, i + 1) * orc.bcsone(x, -dx, i + 1, sm)
+            for si, s2 in enumerate(shells):
+                for v in ik:
+                    if v[0] ** 2 + v[1] ** 2 + v[2] ** 2 == s2:
+                        tmp[si] += rat * np.cos(dk * v[0] * dx[0]) * np.cos(dk * v[1] * dx[1]) * np.cos(dk * v[2] * dx[2])
+    nk = np.array([sum(1 for v in ik if v[0] ** 2 + v[1] ** 2 + v[2] ** 2 == s2) for s2 in shells])
+    orc.add_operators()
+    e, e2, ws = orc.operators(3, raw=True)
+    assert nsh == len(shells)
+    assert np.allclose(e, tmp / nk * wt, rtol=1e-10, atol=1e-12)
+    assert np.allclose(e2, (tmp / nk) ** 2 * wt, rtol=1e-10, atol=1e-12)
+    assert abs(ws - 10 * wt) < 1e-12
