@@ -27,7 +27,7 @@ EXPORTS = [
     "dmc_set_precision", "dmc_get_precision", "dmc_probe_peak", "dmc_sr_accumulate", "dmc_sr_get_sums",
     "dmc_sr_zero", "dmc_sr_update", "dmc_fort9_write", "dmc_fort9_read", "dmc_save_walkers", "dmc_restore_walkers",
     "dmc_set_operators", "dmc_zero_operators", "dmc_add_operators", "dmc_update_operators", "dmc_get_operators",
-    "dmc_write_operators",
+    "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure",
 ]
 
 PREC_FP64 = 0
@@ -109,6 +109,8 @@ def load(path=LIB_PATH):
     L.dmc_update_operators.argtypes = [vp]
     L.dmc_get_operators.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     L.dmc_write_operators.argtypes = [vp, C.c_char_p, C.c_double]
+    L.dmc_getjasder_batch.argtypes = [vp, C.c_int, _dp, _dp]
+    L.dmc_sr_configure.argtypes = [vp, C.c_int, C.c_int]
     L.dmc_sr_accumulate.argtypes = [vp, C.POINTER(C.c_int64)]
     L.dmc_sr_get_sums.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_int64)]
     L.dmc_sr_zero.argtypes = [vp]
@@ -211,6 +213,8 @@ class Context:
             n = self.info.nk
         elif which in (9, 10):
             n = self.norb
+        elif which == 11:
+            n = 2
         out = np.zeros(n)
         self._check(load().dmc_get_table(self._h, which, out, n))
         return out
@@ -338,13 +342,28 @@ class Context:
     def write_operators(self, directory, tau=0.0):
         self._check(load().dmc_write_operators(self._h, os.fsencode(str(directory)), float(tau)))
 
+    def getjasder(self, x):
+        """d U_long / d beta, d U_long / d gamma per walker, shape [nw, 2]."""
+        x = self._x(x)
+        out = np.zeros((x.shape[0], 2))
+        self._check(load().dmc_getjasder_batch(self._h, x.shape[0], x, out))
+        return out
+
+    def sr_configure(self, opt_jastrow, opt_det):
+        self._check(load().dmc_sr_configure(self._h, int(bool(opt_jastrow)), int(bool(opt_det))))
+        self._nparm = 2 * bool(opt_jastrow) + self.norb * bool(opt_det)
+
+    @property
+    def nparm(self):
+        return getattr(self, "_nparm", self.norb)
+
     def sr_accumulate(self):
         n = C.c_int64()
         self._check(load().dmc_sr_accumulate(self._h, C.byref(n)))
         return n.value
 
     def sr_sums(self):
-        npr = self.norb
+        npr = self.nparm
         o = dict(ovec=np.zeros(npr), ovecw=np.zeros(npr), pmat=np.zeros(npr * npr), e=np.zeros(2))
         n = C.c_int64()
         self._check(load().dmc_sr_get_sums(self._h, *[_opt(o[k]) for k in ("ovec", "ovecw", "pmat", "e")],
@@ -358,7 +377,7 @@ class Context:
 
     def sr_update(self, delta0, eps):
         """One SR step; returns (newpars, eave, eerr) and applies newpars to vorb."""
-        newp = np.zeros(self.norb)
+        newp = np.zeros(self.nparm)
         ea, ee = C.c_double(), C.c_double()
         self._check(load().dmc_sr_update(self._h, float(delta0), float(eps), _opt(newp), C.byref(ea),
                                          C.byref(ee)))

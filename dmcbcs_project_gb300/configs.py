@@ -22,19 +22,21 @@ _UNPAIRED = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0),
              (0, 0, 1), (0, 0, -1), (1, 1, 0)]
 
 
-def system_params(nup, ndn, norb, seed=1234, ntab=10000):
-    """Deck values of one synthetic system with nup >= ndn."""
+def system_params(nup, ndn, norb, seed=1234, ntab=10000, longrange=None):
+    """Deck values of one synthetic system with nup >= ndn; longrange =
+    (numq, beta, gamma) switches the long-range Jastrow on."""
     if ndn > nup:
         raise ValueError("put the larger spin species first")
     rng = np.random.default_rng(seed)
     vorb = (rng.uniform(0.2, 1.0, size=norb) * 0.5 ** np.arange(norb)).tolist()
     b = float(rng.uniform(0.5, 1.5))
     nexup = nup - ndn
+    numq, jbeta, jgamma = longrange if longrange else (0, 0.0, 0.0)
     return dict(
         ntab=ntab, hbar=0.5, ndim=3, nbin=[nup, ndn], mass=[1.0, 1.0], a2=0.0,
         rho=RHO_KF1, nexup=nexup, ikup=[list(k) for k in _UNPAIRED[:nexup]],
         nexdn=0, ikdn=[], norb=norb, vorb=vorb, nqex=[0, 0, 0], v0ex=0.0, v0exjas=0.0,
-        numq=0, jbeta=0.0, jgamma=0.0, bbeta=b, dbeta=5.0, bfact=1.0,
+        numq=numq, jbeta=jbeta, jgamma=jgamma, bbeta=b, dbeta=5.0, bfact=1.0,
         v0=1.0, amu=24.0, cjas=[1.0, 0.0], djas=1.15, v0op=0.0, v0eq=-10.0,
     )
 
@@ -61,12 +63,12 @@ WORKLOADS = {
 }
 
 
-def workload(name, nwalk=None, idmc=1, seed=1234, ntab=10000):
+def workload(name, nwalk=None, idmc=1, seed=1234, ntab=10000, longrange=None):
     """Return ``(SystemDesc, RunDesc, meta)`` for a named workload."""
     nup, ndn, norb, nw, dt, steps = WORKLOADS[name]
     if nwalk is not None:
         nw = nwalk
-    sp = system_params(nup, ndn, norb, seed=seed, ntab=ntab)
+    sp = system_params(nup, ndn, norb, seed=seed, ntab=ntab, longrange=longrange)
     rp = run_params(nw, dt, idmc=idmc)
     meta = dict(name=name, nup=nup, ndn=ndn, norb=norb, nwalk=nw, dt_efg=dt, steps=steps)
     return make_system(sp), make_run(rp), meta

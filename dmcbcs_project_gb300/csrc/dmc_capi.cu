@@ -117,6 +117,7 @@ struct dmc_ctx {
     int precision = DMC_PREC_FP64;
     DevBuf<unsigned long long> jumpA, jumpC;
     DevBuf<double> gscratch;
+    DevBuf<double> jq;
     // population
     StackBufs st[2];
     int istin = 0;
@@ -133,6 +134,7 @@ struct dmc_ctx {
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
     DevBuf<int> sip;
     int64_t sr_count = 0;
+    bool sr_jas = false, sr_det = true;   // iopt(1), iopt(2) of the optimizer deck
     // operators (g(r), density profile, S(q), n(k))
     struct Ops {
         bool on = false;
@@ -188,6 +190,9 @@ void fill_params(dmc_ctx* c)
     p.ieq = S.ieq; p.nobeta = S.nobeta; p.cutdrift = S.cutdrift; p.fn = c->rd.fn; p.idmc = c->rd.idmc;
     p.onebody = (S.v0ex != 0.0 || S.v0exjas != 0.0);
     p.ntab0 = S.ntab0;
+    p.nql = S.nql;
+    p.jbeta = S.jbeta;
+    p.jgamma = S.jgamma;
     p.nest = nest_for(c->rd.idmc);
     p.nrand = 2 * ((3 * S.npart + 1) / 2);
     p.ldS = S.nd | 1;
@@ -290,6 +295,10 @@ int upload_tables(dmc_ctx* c)
     CK(c->tss_mp.alloc(nt));
     CK(cudaMemcpy(c->tud_mp.p, udm.data(), nt * sizeof(TabUDmp), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->tss_mp.p, ssm.data(), nt * sizeof(TabSSmp), cudaMemcpyHostToDevice));
+    if (S.nql > 0) {
+        CK(c->jq.alloc(S.jq.size()));
+        CK(cudaMemcpy(c->jq.p, S.jq.data(), S.jq.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
     // LCG jump tables for t = 0..nrand+1 steps of ran1
     const int nj = c->P.nrand + 2;
     std::vector<unsigned long long> A(nj), C(nj);
@@ -319,6 +328,7 @@ KernelArgs base_args(dmc_ctx* c)
     a.jumpA = c->jumpA.p;
     a.jumpC = c->jumpC.p;
     a.gscratch = c->gscratch.p;
+    a.jq = c->jq.p;
     a.status = c->status.p;
     return a;
 }
@@ -492,7 +502,7 @@ int dmc_destroy(dmc_ctx* c)
     if (!c) return DMC_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
     c->kv.release(); c->tud.release(); c->tss.release(); c->kv_mp.release(); c->tud_mp.release();
-    c->tss_mp.release(); c->jumpA.release(); c->jumpC.release();
+    c->tss_mp.release(); c->jumpA.release(); c->jumpC.release(); c->jq.release();
     c->gscratch.release(); c->st[0].release(); c->st[1].release(); c->est.release(); c->counts.release();
     c->offs.release(); c->status.release(); c->irn1.release(); c->wtisto.release(); c->vb.release();
     c->vb2.release(); c->wb.release(); c->bx.release(); c->bpsil.release(); c->bdpsi.release();
@@ -561,6 +571,11 @@ int dmc_get_table(const dmc_ctx* c, int which, double* out, int n)
     case 10:
         if (n < S.norb) return DMC_ERR_INVALID;
         for (int q = 0; q < S.norb; ++q) out[q] = S.vorb[q];
+        return DMC_OK;
+    case 11:
+        if (n < 2) return DMC_ERR_INVALID;
+        out[0] = S.jbeta;
+        out[1] = S.jgamma;
         return DMC_OK;
     }
     return DMC_ERR_INVALID;
@@ -1040,7 +1055,7 @@ int dmc_getphione_batch(dmc_ctx* c, int nw, const double* x, const int* ipart, c
 }
 
 // d log|det| / d vorb for nw device-resident configurations (FP64 inverse)
-static int derbcs_device(dmc_ctx* c, int nw, const double* dx, double* dder)
+static int derbcs_device(dmc_ctx* c, int nw, const double* dx, double* dder, int stride = -1, int off = 0)
 {
     const size_t nd2 = (size_t)c->S.nd * c->S.nd;
     CK(c->ssinv.alloc(nw * nd2));
@@ -1051,8 +1066,25 @@ static int derbcs_device(dmc_ctx* c, int nw, const double* dx, double* dder)
     c->precision = prec;
     if (rc) return rc;
     ++c->launches;
-    CK(launch_derbcs(c->P, c->kv.p, dx, c->ssinv.p, dder, nw, c->grid, c->stream));
+    CK(launch_derbcs(c->P, c->kv.p, dx, c->ssinv.p, dder, nw, c->grid, c->stream, stride, off));
     ++c->launches;
+    return DMC_OK;
+}
+
+int dmc_getjasder_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (nw < 0 || (nw > 0 && (!x || !dpsi))) return fail(c, DMC_ERR_INVALID, "bad getjasder arguments");
+    if (c->S.nql == 0) return fail(c, DMC_ERR_INVALID, "the long-range Jastrow is off (numq = 0)");
+    if (nw == 0) return DMC_OK;
+    const size_t n3 = (size_t)c->n3;
+    CK(c->sx.alloc(nw * n3));
+    CK(c->sder.alloc(2 * (size_t)nw));
+    CK(cudaMemcpyAsync(c->sx.p, x, nw * n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_jasder(c->P, c->jq.p, c->sx.p, c->sder.p, nw, c->grid, c->stream, 2));
+    ++c->launches;
+    CK(cudaMemcpyAsync(dpsi, c->sder.p, 2 * nw * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return DMC_OK;
 }
 
@@ -1395,9 +1427,13 @@ int dmc_write_operators(dmc_ctx* c, const char* dir, double tau)
 
 // ---- stochastic reconfiguration ---------------------------------------------
 
+// SR parameters: (beta, gamma) of the long-range Jastrow when iopt(1), then
+// vorb when iopt(2) (calder, optimizer.f90:100-104)
+static int sr_nparm(const dmc_ctx* c) { return (c->sr_jas ? 2 : 0) + (c->sr_det ? c->S.norb : 0); }
+
 static int sr_buffers(dmc_ctx* c)
 {
-    const size_t np = (size_t)c->S.norb, nout = np * np + 2 * np + 2;
+    const size_t np = (size_t)sr_nparm(c), nout = np * np + 2 * np + 2;
     if (c->srsum.n < nout) {
         CK(c->srsum.alloc(nout));
         CK(cudaMemset(c->srsum.p, 0, nout * sizeof(double)));
@@ -1406,16 +1442,32 @@ static int sr_buffers(dmc_ctx* c)
     return DMC_OK;
 }
 
+int dmc_sr_configure(dmc_ctx* c, int opt_jastrow, int opt_det)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (!opt_jastrow && !opt_det) return fail(c, DMC_ERR_INVALID, "no parameters to optimise");
+    if (opt_jastrow && c->S.nql == 0) return fail(c, DMC_ERR_INVALID, "the long-range Jastrow is off (numq = 0)");
+    c->sr_jas = opt_jastrow != 0;
+    c->sr_det = opt_det != 0;
+    c->srsum.release();
+    c->sr_count = 0;
+    return sr_buffers(c);
+}
+
 int dmc_sr_accumulate(dmc_ctx* c, int64_t* nsamples)
 {
     if (!c) return DMC_ERR_INVALID;
     int rc = sr_buffers(c);
     if (rc) return rc;
-    const int n = c->n, np = c->S.norb;
+    const int n = c->n, np = sr_nparm(c);
     if (n > 0) {
         StackBufs& s = c->st[c->istin];
         CK(c->sder.alloc((size_t)n * np));
-        if ((rc = derbcs_device(c, n, s.x.p, c->sder.p))) return rc;
+        if (c->sr_jas) {
+            CK(launch_jasder(c->P, c->jq.p, s.x.p, c->sder.p, n, c->grid, c->stream, np));
+            ++c->launches;
+        }
+        if (c->sr_det && (rc = derbcs_device(c, n, s.x.p, c->sder.p, np, c->sr_jas ? 2 : 0))) return rc;
         CK(launch_sr_sums(c->sder.p, s.d2psi.p, s.v.p, n, np, c->S.hbar, c->S.eunit, c->S.npart, c->srsum.p,
                           c->stream));
         ++c->launches;
@@ -1433,7 +1485,7 @@ int dmc_sr_get_sums(dmc_ctx* c, double* ovec, double* ovecw, double* pmat, doubl
     if (!c) return DMC_ERR_INVALID;
     int rc = sr_buffers(c);
     if (rc) return rc;
-    const size_t np = (size_t)c->S.norb, nout = np * np + 2 * np + 2;
+    const size_t np = (size_t)sr_nparm(c), nout = np * np + 2 * np + 2;
     std::vector<double> h(nout);
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemcpy(h.data(), c->srsum.p, nout * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1453,7 +1505,7 @@ int dmc_sr_zero(dmc_ctx* c)
     if (!c) return DMC_ERR_INVALID;
     int rc = sr_buffers(c);
     if (rc) return rc;
-    const size_t np = (size_t)c->S.norb, nout = np * np + 2 * np + 2;
+    const size_t np = (size_t)sr_nparm(c), nout = np * np + 2 * np + 2;
     CK(cudaMemsetAsync(c->srsum.p, 0, nout * sizeof(double), c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->sr_count = 0;
@@ -1494,7 +1546,7 @@ static bool host_inverse(int n, double* a)
 int dmc_sr_update(dmc_ctx* c, double delta0, double eps, double* newpars, double* eave, double* eerr)
 {
     if (!c) return DMC_ERR_INVALID;
-    const int np = c->S.norb;
+    const int np = sr_nparm(c);
     if (c->sr_count <= 0) return fail(c, DMC_ERR_INVALID, "no samples accumulated for the SR step");
     std::vector<double> ovec(np), ovecw(np), pmat((size_t)np * np), e(2);
     int64_t ns = 0;
@@ -1515,14 +1567,25 @@ int dmc_sr_update(dmc_ctx* c, double delta0, double eps, double* newpars, double
         pmat[i + (size_t)i * np] += eps;
     }
     if (!host_inverse(np, pmat.data())) return fail(c, DMC_ERR_INVALID, "singular SR matrix");
-    std::vector<double> vorb(c->S.vorb);
     for (int i = 0; i < np; ++i) {
         double sm = 0.0;
         for (int j = 0; j < np; ++j) sm += pmat[i + (size_t)j * np] * f[j];
         dpar[i] = delta0 * sm;
-        vorb[i] += dpar[i];
     }
-    if ((rc = dmc_set_vorb(c, vorb.data(), np))) return rc;
+    // params = params + newpars; setjasparam / setdetparam (optimizer.f90:163, 72-88)
+    if (c->sr_jas) {
+        c->S.set_jaslong(c->S.jbeta + dpar[0], c->S.jgamma + dpar[1]);
+        c->P.jbeta = c->S.jbeta;
+        c->P.jgamma = c->S.jgamma;
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaMemcpy(c->jq.p, c->S.jq.data(), c->S.jq.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (c->sr_det) {
+        const int off = c->sr_jas ? 2 : 0;
+        std::vector<double> vorb(c->S.vorb);
+        for (int i = 0; i < c->S.norb; ++i) vorb[i] += dpar[off + i];
+        if ((rc = dmc_set_vorb(c, vorb.data(), c->S.norb))) return rc;
+    }
     if ((rc = dmc_sr_zero(c))) return rc;
     if (newpars) std::copy(dpar.begin(), dpar.end(), newpars);
     if (eave) *eave = esum;

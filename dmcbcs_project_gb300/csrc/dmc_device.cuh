@@ -72,6 +72,8 @@ struct DevParams {
     int npart, nup, ndn, npair, nexup, nexdn, nd, nk, ncol, norb, ntab, nmax;
     int ieq, nobeta, cutdrift, fn, idmc, onebody, nest, nrand;
     int ntab0;            // last non-zero Jastrow grid point (healing distance)
+    int nql;              // long-range Jastrow q vectors (0: off)
+    double jbeta, jgamma; // its parameters
     int ldS, ldU;
     double el, eli, range, scale, rangeb, scaleb;
     double mass[2], sqm[2], imass[2], isqm[2];
@@ -127,6 +129,7 @@ struct KernelArgs {
     const unsigned long long* jumpA;   // LCG jump-ahead multipliers, [nrand+1]
     const unsigned long long* jumpC;   // LCG jump-ahead increments, [nrand+1]
     double* gscratch;            // per-CTA global scratch when the pair data do not fit on chip
+    const double* jq;            // long-range Jastrow q records, [nql][8]
     int* status;                 // per-walker status flags (bit 0: singular matrix)
 };
 

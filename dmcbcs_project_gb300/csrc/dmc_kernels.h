@@ -28,8 +28,12 @@ cudaError_t launch_bcsone(const DevParams& p, const KVecDev* kv, const TabUD* tu
 cudaError_t launch_getphione(const DevParams& p, const TabUD* tud, const TabSS* tss, const double* x,
                              const int* ipart, const double* drr, double* ratio, int nw, cudaStream_t st);
 size_t derbcs_smem_bytes(const DevParams& p);
+// dpsi[w*stride + off + shell]; stride < 0 means norb
 cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x, const double* smati, double* dpsi,
-                          int nw, int grid, cudaStream_t st);
+                          int nw, int grid, cudaStream_t st, int stride = -1, int off = 0);
+// getjasder: dpsi[w*stride + 0..1] = d U_long / d beta, d U_long / d gamma
+cudaError_t launch_jasder(const DevParams& p, const double* jq, const double* x, double* dpsi, int nw, int grid,
+                          cudaStream_t st, int stride);
 // adds the calder sums of n walkers (pop order) to sums[np*np + 2*np + 2]:
 // ovec, ovecw, pmat (column-major), esum, esum2
 cudaError_t launch_sr_sums(const double* der, const double* d2psi, const double* v, int n, int np, double hbar,

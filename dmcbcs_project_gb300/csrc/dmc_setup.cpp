@@ -283,9 +283,9 @@ int Setup::build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string&
         err = "bfact < 0 (beta table read from unit 80) is not supported";
         return DMC_ERR_UNSUPPORTED;
     }
-    if (sd.numq != 0) {
-        err = "the long-range Jastrow (numq > 0) is not built on the GPU path";
-        return DMC_ERR_UNSUPPORTED;
+    if (sd.numq < 0 || sd.numq > DMC_MAX_SHELLS) {
+        err = "numq out of range";
+        return DMC_ERR_INVALID;
     }
     npart = sd.nbin[0] + sd.nbin[1];
     ntab = sd.ntab;
@@ -354,6 +354,26 @@ int Setup::build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string&
     v0ex = sd.v0ex * 0.5;
     v0exjas = sd.v0exjas * v0ex;
     numq = sd.numq;
+    jbeta = sd.jbeta;
+    jgamma = sd.jgamma;
+    // setjaslong (jastrowlongrange.f90:10-20): the q vectors of numq shells
+    // (kstates3d, q = 0 excluded as getjaslong does) and their weights
+    // gamma exp(-beta |q|) / |q|
+    jq.clear();
+    nql = 0;
+    if (numq > 0) {
+        std::vector<KVec> kq;
+        std::vector<int> nsh;
+        int rc = k_shells(el, numq, kq, nsh, err);
+        if (rc) return rc;
+        for (size_t q = 1; q < kq.size(); ++q) {
+            const double qmod = std::sqrt(kq[q].k2);
+            const double rec[8] = {kq[q].k[0], kq[q].k[1], kq[q].k[2], kq[q].k2,
+                                   sd.jgamma * std::exp(-sd.jbeta * qmod) / qmod, 0.0, 0.0, 0.0};
+            jq.insert(jq.end(), rec, rec + 8);
+            ++nql;
+        }
+    }
     // setphi, coshpot.f90:14-143
     const double mu = mass[0] * mass[1] / (mass[0] + mass[1]);
     hbarp = 2.0 * (hbar / (2.0 * mu));
@@ -430,6 +450,17 @@ int Setup::build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string&
         dcut[s] = cutdrift ? sigma[s] * rd.dcut : 0.0;
     }
     return DMC_OK;
+}
+
+void Setup::set_jaslong(double beta, double gamma)
+{
+    jbeta = beta;
+    jgamma = gamma;
+    for (int q = 0; q < nql; ++q) {
+        double* rec = &jq[8 * (size_t)q];
+        const double qmod = std::sqrt(rec[3]);
+        rec[4] = gamma * std::exp(-beta * qmod) / qmod;
+    }
 }
 
 int Setup::set_vorb(const double* v, int n, std::string& err)

@@ -44,6 +44,11 @@ struct Setup {
     // one-body and long-range Jastrow
     double qex[3] = {0, 0, 0}, v0ex = 0, v0exjas = 0;
     int numq = 0;
+    // long-range Jastrow: nql q vectors, 8 doubles each (qx, qy, qz, q^2,
+    // gamma exp(-beta |q|)/|q|, 0, 0, 0)
+    int nql = 0;
+    std::vector<double> jq;
+    double jbeta = 0, jgamma = 0;
     // beta table (betafun.f90): swbtab, swdbtab, swd2btab on [0, L/2]
     bool nobeta = true;
     int ntabb = 0;
@@ -64,6 +69,9 @@ struct Setup {
     // Returns DMC_OK or an error code with a message in err.
     int build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string& err);
     int set_vorb(const double* v, int n, std::string& err);
+    // setjasparam (jastrowlongrange.f90:57-61): new beta, gamma; recomputes
+    // the q-vector weights
+    void set_jaslong(double beta, double gamma);
 };
 
 }  // namespace dmc

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kThreads) derbcs_kernel(const __grid_constant_
                                                          const KVecDev* __restrict__ kv,
                                                          const double* __restrict__ x,
                                                          const double* __restrict__ smati,
-                                                         double* __restrict__ dpsi, int nw)
+                                                         double* __restrict__ dpsi, int nw, int stride, int off)
 {
     extern __shared__ __align__(16) double sm[];
     const int nd = p.nd, nup = p.nup, ndn = p.ndn, P = p.npart, norb = p.norb;
@@ -134,7 +134,50 @@ __global__ void __launch_bounds__(kThreads) derbcs_kernel(const __grid_constant_
                 }
             __syncthreads();
         }
-        for (int t = threadIdx.x; t < norb; t += kThreads) dpsi[(size_t)w * norb + t] = dsh[t];
+        for (int t = threadIdx.x; t < norb; t += kThreads) dpsi[(size_t)w * stride + off + t] = dsh[t];
+        __syncthreads();
+    }
+}
+
+// getjasder (jastrowlongrange.f90:63-78) for one walker per CTA: the
+// long-range Jastrow at beta + dp, (beta + dp) - 2 dp and back, from the
+// densities rho_q; d/d beta by central differences as the reference takes
+// them, d/d gamma = U / gamma.  Writes dpsi[w*stride + 0..1].
+__global__ void __launch_bounds__(kThreads) jasder_kernel(const __grid_constant__ DevParams p,
+                                                         const double* __restrict__ jq,
+                                                         const double* __restrict__ x,
+                                                         double* __restrict__ dpsi, int nw, int stride)
+{
+    extern __shared__ __align__(16) double sm[];
+    const int P = p.npart;
+    double* r2 = sm;   // |rho_q|^2 - N per q
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
+        const double* xw = x + (size_t)w * 3 * P;
+        for (int q = threadIdx.x; q < p.nql; q += kThreads) {
+            const double* Q = jq + 8 * q;
+            double re = 0.0, im = 0.0;
+            for (int i = 0; i < P; ++i) {
+                double sn, cs;
+                sincos(Q[0] * xw[3 * i] + Q[1] * xw[3 * i + 1] + Q[2] * xw[3 * i + 2], &sn, &cs);
+                re += cs;
+                im += sn;
+            }
+            r2[q] = re * re + im * im - (double)P;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const double dp = 0.0001;
+            const double b1 = p.jbeta + dp, b2 = b1 - 2.0 * dp, b3 = b2 + dp;
+            double u1 = 0.0, u2 = 0.0, u3 = 0.0;
+            for (int q = 0; q < p.nql; ++q) {
+                const double qmod = sqrt(jq[8 * q + 3]);
+                u1 += p.jgamma * exp(-b1 * qmod) / qmod * r2[q];
+                u2 += p.jgamma * exp(-b2 * qmod) / qmod * r2[q];
+                u3 += p.jgamma * exp(-b3 * qmod) / qmod * r2[q];
+            }
+            dpsi[(size_t)w * stride] = (u1 - u2) / (2.0 * dp);
+            dpsi[(size_t)w * stride + 1] = u3 / p.jgamma;
+        }
         __syncthreads();
     }
 }
@@ -201,13 +244,23 @@ size_t derbcs_smem_bytes(const DevParams& p)
 }
 
 cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x, const double* smati, double* dpsi,
-                          int nw, int grid, cudaStream_t st)
+                          int nw, int grid, cudaStream_t st, int stride, int off)
 {
     if (nw <= 0) return cudaSuccess;
     const size_t smem = derbcs_smem_bytes(p);
     cudaError_t e = cudaFuncSetAttribute(derbcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    derbcs_kernel<<<grid < nw ? grid : nw, kThreads, smem, st>>>(p, kv, x, smati, dpsi, nw);
+    derbcs_kernel<<<grid < nw ? grid : nw, kThreads, smem, st>>>(p, kv, x, smati, dpsi, nw, stride < 0 ? p.norb : stride,
+                                                                 off);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_jasder(const DevParams& p, const double* jq, const double* x, double* dpsi, int nw, int grid,
+                          cudaStream_t st, int stride)
+{
+    if (nw <= 0) return cudaSuccess;
+    const size_t smem = sizeof(double) * (size_t)(p.nql > 0 ? p.nql : 1);
+    jasder_kernel<<<grid < nw ? grid : nw, kThreads, smem, st>>>(p, jq, x, dpsi, nw, stride);
     return cudaGetLastError();
 }
 

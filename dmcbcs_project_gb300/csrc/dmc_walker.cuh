@@ -1368,6 +1368,63 @@ __device__ void beta_drift_stage(const Ctx<R>& c)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Long-range Jastrow (getjaslong, jastrowlongrange.f90:22-46), FP64 on both
+// paths.  The reference's pair sum is evaluated through the densities
+// rho_q = sum_i e^{i q.x_i}:
+//   U    = sum_q f_q (|rho_q|^2 - N),          f_q = gamma e^{-beta|q|}/|q|,
+//   dU_i = -2 sum_q f_q q Im(e^{i q.x_i} conj(rho_q)),
+//   lap  = -2 sum_q f_q |q|^2 (|rho_q|^2 - N)  (before |dU|^2 is added),
+// O(N n_q) instead of O(N^2 n_q).  Leaves dU in sm[L.dg] (free until the
+// guide-function gradient is written) and uses the union region for rho_q.
+// ---------------------------------------------------------------------------
+__device__ inline void jaslong_stage(const DevParams& p, const KernelArgs& a, const SmemLayout& L, double* sm, double& ul,
+                              double& d2l)
+{
+    const double* x = sm + L.x;
+    double* rho = sm + L.R;
+    double* dl = sm + L.dg;
+    const int P = p.npart;
+    for (int q = threadIdx.x; q < p.nql; q += kThreads) {
+        const double* Q = a.jq + 8 * q;
+        double re = 0.0, im = 0.0;
+        for (int i = 0; i < P; ++i) {
+            double sn, cs;
+            sincos(Q[0] * x[3 * i] + Q[1] * x[3 * i + 1] + Q[2] * x[3 * i + 2], &sn, &cs);
+            re += cs;
+            im += sn;
+        }
+        rho[2 * q] = re;
+        rho[2 * q + 1] = im;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < P; i += kThreads) {
+        double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+        for (int q = 0; q < p.nql; ++q) {
+            const double* Q = a.jq + 8 * q;
+            double sn, cs;
+            sincos(Q[0] * x[3 * i] + Q[1] * x[3 * i + 1] + Q[2] * x[3 * i + 2], &sn, &cs);
+            const double f = -2.0 * Q[4] * (sn * rho[2 * q] - cs * rho[2 * q + 1]);
+            g0 = fma(f, Q[0], g0);
+            g1 = fma(f, Q[1], g1);
+            g2 = fma(f, Q[2], g2);
+        }
+        dl[3 * i] = g0;
+        dl[3 * i + 1] = g1;
+        dl[3 * i + 2] = g2;
+    }
+    double u = 0.0, d2 = 0.0;
+    for (int q = 0; q < p.nql; ++q) {
+        const double* Q = a.jq + 8 * q;
+        const double r2 = rho[2 * q] * rho[2 * q] + rho[2 * q + 1] * rho[2 * q + 1] - (double)P;
+        u += Q[4] * r2;
+        d2 += -2.0 * Q[4] * Q[3] * r2;
+    }
+    ul = u;
+    d2l = d2;
+    __syncthreads();
+}
+
 // Scalars of one evaluation.
 struct HRes {
     double psil, d2psi, v, vext, psigl, d2psig, u, d2u, logdet, d2phi;
@@ -1402,6 +1459,11 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         for (int i = threadIdx.x; i < n3; i += kThreads) du[i] = 0.0;
         __syncthreads();
     }
+    // long-range Jastrow: part of hpsi (getphilong, wavefunction.f90:148-159,173),
+    // not of getphi or bcs
+    const bool jl = p.nql > 0 && (mode == MODE_HPSI || mode == MODE_STEP);
+    double ulong = 0.0, d2long = 0.0;
+    if (jl) jaslong_stage(c.p, c.a, c.L, sm, ulong, d2long);
     double logdet = 0.0;
     int sgn = 1;
     bool ok = true;
@@ -1424,6 +1486,8 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     double sums[8] = {su, sv, sd2, 0.0, 0.0, 0.0, 0.0, 0.0};
     // sums[3]: sum lap/m (d2phi), [4]: |du|^2, [5]: du.dphi, [6]: one-body g, [7]: vext
     double g1 = 0.0, d2g = 0.0, dudg = 0.0;
+    double ll = 0.0, dudl = 0.0, dgdl = 0.0;   // |dUlong|^2, du.dUlong, dg.dUlong
+    const double* dl = sm + c.L.dg;
     for (int pt = threadIdx.x; pt < P; pt += kThreads) {
         const int sp = pt < p.nup ? 0 : 1;
         const double isq = p.isqm[sp], im = p.imass[sp];
@@ -1447,17 +1511,26 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         }
         double dtot[3];
         for (int k = 0; k < 3; ++k) dtot[k] = dj[k] + dg[k];
+        if (jl)
+            for (int k = 0; k < 3; ++k) {
+                const double l = dl[3 * pt + k];
+                ll += l * l;
+                dudl += dj[k] * l;
+                dgdl += dg[k] * l;
+                dtot[k] += l;
+            }
         sums[5] += dtot[0] * dph[0] + dtot[1] * dph[1] + dtot[2] * dph[2];
         // dpsi = dphi + du (+ dg)
         for (int k = 0; k < 3; ++k) acc[3 * pt + k] = dph[k] + dtot[k];
     }
     sums[6] = g1;
-    double more[2] = {d2g, dudg};
+    double more[5] = {d2g, dudg, ll, dudl, dgdl};
     block_sum<8>(sums, sm + c.L.red);
-    block_sum<2>(more, sm + c.L.red);
-    const double u = sums[0] + sums[6];
+    block_sum<5>(more, sm + c.L.red);
+    const double u = sums[0] + sums[6] + ulong;
     const double d2u_j = sums[2] + sums[4];                        // getphi d2u
-    const double d2u = d2u_j + more[0] + 2.0 * more[1];            // + one-body terms
+    // + one-body and long-range terms with their cross terms (wavefunction.f90:178-184)
+    const double d2u = d2u_j + more[0] + (d2long + more[2]) + 2.0 * (more[1] + more[3] + more[4]);
     h.u = u;
     h.d2u = mode == MODE_GETPHI ? d2u_j : d2u;
     h.v = sums[1] + sums[7];

@@ -147,7 +147,8 @@ int dmc_get_info(const dmc_ctx* ctx, dmc_info* out);
 /* Copy a setup table to host memory.  which: 0 utab, 1 dutab, 2 d2utab,
  * 3 vtab (each 2*(ntab+1) values, layout [ic][0..ntab] i.e. Fortran
  * (2,0:ntab) transposed), 4 swbtab, 5 swdbtab, 6 swd2btab (ntab+1 each),
- * 7 ak (3*nk), 8 ak2 (nk), 9 numsh (norb, as doubles), 10 vorb (norb). */
+ * 7 ak (3*nk), 8 ak2 (nk), 9 numsh (norb, as doubles), 10 vorb (norb),
+ * 11 (beta, gamma) of the long-range Jastrow. */
 int dmc_get_table(const dmc_ctx* ctx, int which, double* out, int n);
 
 /* Arithmetic of the walker kernel.  DMC_PREC_FP64 (the default) computes
@@ -217,18 +218,30 @@ int dmc_getphione_batch(dmc_ctx* ctx, int nw, const double* x, const int* ipart,
  * optbeta=.false.: d log|det| / d vorb(k), dpsi[nw][norb]. */
 int dmc_getderbcs_batch(dmc_ctx* ctx, int nw, const double* x, double* dpsi);
 
+/* Replaces getjasder (jastrowlongrange.f90:63-78): dpsi[nw][2] = d U / d beta
+ * (central differences with dp = 1e-4, as the reference takes them) and
+ * d U / d gamma of the long-range Jastrow; DMC_ERR_INVALID when numq = 0. */
+int dmc_getjasder_batch(dmc_ctx* ctx, int nw, const double* x, double* dpsi);
+
 /* ---- stochastic reconfiguration (optimizer.f90:90-169) ----------------- */
 
+/* Which parameters the SR step optimises, as iopt(1) and iopt(2) of the
+ * optimizer input: the long-range Jastrow's (beta, gamma), then vorb(norb).
+ * nparm = 2 opt_jastrow + norb opt_det; the default is (0, 1).  Clears the
+ * sums. */
+int dmc_sr_configure(dmc_ctx* ctx, int opt_jastrow, int opt_det);
+
 /* Replaces the calder loop of dmcbcs.f90:492-503 (optimizer.f90:90-116)
- * over the current population, in pop order: per walker d log|det|/d vorb
- * (getderbcs) and ene = (-hbar*d2psi + v)/eunit/npart from its stored
+ * over the current population, in pop order: per walker the parameter
+ * derivatives (getjasder, getderbcs) and ene = (-hbar*d2psi + v)/eunit/npart from its stored
  * evaluation are added to the context's sums ovec, ovecw, pmat, esum and
  * esum2; the walkers are left in reverse order, as that pop/push pass
  * leaves them.  *nsamples (may be NULL) receives the running count. */
 int dmc_sr_accumulate(dmc_ctx* ctx, int64_t* nsamples);
 
-/* The running sums: ovec[norb], ovecw[norb], pmat[norb*norb] (column-major),
- * e[2] = {esum, esum2} and the sample count; any pointer may be NULL. */
+/* The running sums: ovec[nparm], ovecw[nparm], pmat[nparm*nparm]
+ * (column-major), e[2] = {esum, esum2} and the sample count; any pointer may
+ * be NULL. */
 int dmc_sr_get_sums(dmc_ctx* ctx, double* ovec, double* ovecw, double* pmat, double* e, int64_t* nsamples);
 
 /* Clears the sums. */
@@ -237,8 +250,8 @@ int dmc_sr_zero(dmc_ctx* ctx);
 /* Replaces updatepar (optimizer.f90:118-169) on one process: normalises the
  * sums by the sample count, f = -2 ovecw + 2 ovec esum,
  * P = pmat - ovec ovec^T + eps I, newpars = delta0 P^-1 f; adds newpars to
- * vorb (the determinant parameters, as setdetparam does) and clears the
- * sums.  newpars[norb], eave and eerr may be NULL.  DMC_ERR_INVALID when no
+ * the parameters (setjasparam / setdetparam) and clears the sums.
+ * newpars[nparm], eave and eerr may be NULL.  DMC_ERR_INVALID when no
  * sample was accumulated. */
 int dmc_sr_update(dmc_ctx* ctx, double delta0, double eps, double* newpars, double* eave, double* eerr);
 

@@ -922,6 +922,28 @@ static void getjaslong(const orc_state* s, const double* x, double* u_, double* 
     *d2u_ = d2u + ss;
 }
 
+/* getjasder, jastrowlongrange.f90:63-78: d U / d beta by central
+ * differences with dp = 1e-4 (beta moved up, down, then back), d U / d gamma
+ * = U / gamma */
+void orc_getjasder(orc_state* s, const double* x, double* dpsi)
+{
+    const double dp = 0.0001;
+    double u, d2u, psi1, psi2;
+    double* du = (double*)malloc(sizeof(double) * 3 * s->npart);
+    dpsi[0] = dpsi[1] = 0.0;
+    s->jbeta = s->jbeta + dp;
+    getjaslong(s, x, &u, du, &d2u);
+    psi1 = u;
+    s->jbeta = s->jbeta - 2.0 * dp;
+    getjaslong(s, x, &u, du, &d2u);
+    psi2 = u;
+    s->jbeta = s->jbeta + dp;
+    getjaslong(s, x, &u, du, &d2u);
+    dpsi[0] = (psi1 - psi2) / (2.0 * dp);
+    dpsi[1] = u / s->jgamma;
+    free(du);
+}
+
 /* ------------------------------------------------------------------------ */
 /* dense inverse: rmatinv, matrixlapack.f90:13-41                           */
 /* ------------------------------------------------------------------------ */

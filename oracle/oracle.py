@@ -58,6 +58,7 @@ def lib():
         L.orc_bcsone.restype = C.c_double
         L.orc_bcsone.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp]
         L.orc_getderbcs.argtypes = [C.c_void_p, _dp, _dp]
+        L.orc_getjasder.argtypes = [C.c_void_p, _dp, _dp]
         L.orc_matinv.argtypes = [C.c_int, _dp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
         L.orc_hpsi_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_bcs_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, _dp, _dp, C.c_void_p]
@@ -196,6 +197,12 @@ class Oracle:
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(self.npart, 3)
         return lib().orc_bcsone(self._h, x, np.ascontiguousarray(dr, dtype=np.float64), int(i1),
                                 np.ascontiguousarray(smati, dtype=np.float64))
+
+    def getjasder(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(self.npart, 3)
+        d = np.zeros(2)
+        lib().orc_getjasder(self._h, x, d)
+        return d
 
     def getderbcs(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(self.npart, 3)

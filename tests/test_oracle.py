@@ -195,8 +195,8 @@ def _near_half_box(x, nup, el, ntab, cells=6):
     return bool(np.any(np.abs(r - 0.5 * el) < cells * 0.5 * el / ntab))
 
 
-def _walkers(name, nw, seed=11):
-    sysd, rund, _ = configs.workload(name, nwalk=nw, seed=seed)
+def _walkers(name, nw, seed=11, longrange=None):
+    sysd, rund, _ = configs.workload(name, nwalk=nw, seed=seed, longrange=longrange)
     o = oracle.Oracle(sysd, rund, threads=1)
     o.init_walkers()
     base = o.walkers()["x"]
@@ -211,11 +211,12 @@ def _walkers(name, nw, seed=11):
     return sysd, o, np.array(out)
 
 
-@pytest.mark.parametrize("name", ["n14", "p38_33"])
-def test_chkder_gradient_and_laplacian(name):
+@pytest.mark.parametrize("name,longrange", [("n14", None), ("p38_33", None), ("n14", (3, 1.0, 0.3))])
+def test_chkder_gradient_and_laplacian(name, longrange):
     """wavefunction.f90:289-321: central differences of log|Psi| give dpsi;
-    differences of dpsi*Psi give the Laplacian d2psi."""
-    sysd, o, x = _walkers(name, 1)
+    differences of dpsi*Psi give the Laplacian d2psi (also with the
+    long-range Jastrow of jastrowlongrange.f90 on)."""
+    sysd, o, x = _walkers(name, 1, longrange=longrange)
     x = x[0]
     h0 = o.hpsi(x[None])
     h = 1e-5
