@@ -27,7 +27,7 @@ EXPORTS = [
     "dmc_set_precision", "dmc_get_precision", "dmc_probe_peak", "dmc_sr_accumulate", "dmc_sr_get_sums",
     "dmc_sr_zero", "dmc_sr_update", "dmc_fort9_write", "dmc_fort9_read", "dmc_save_walkers", "dmc_restore_walkers",
     "dmc_set_operators", "dmc_zero_operators", "dmc_add_operators", "dmc_update_operators", "dmc_get_operators",
-    "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure",
+    "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure", "dmc_dfmath_eval",
 ]
 
 PREC_FP64 = 0
@@ -97,6 +97,7 @@ def load(path=LIB_PATH):
     L.dmc_put_walkers.argtypes = [vp, C.POINTER(Walkers)]
     L.dmc_set_precision.argtypes = [vp, C.c_int]
     L.dmc_probe_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.dmc_dfmath_eval.argtypes = [C.c_int, C.c_int, vp, vp]
     L.dmc_get_precision.argtypes = [vp, C.POINTER(C.c_int)]
     L.dmc_fort9_write.argtypes = [C.c_char_p, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.c_double]
     L.dmc_fort9_read.argtypes = [C.c_char_p, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.POINTER(C.c_int),
@@ -119,6 +120,21 @@ def load(path=LIB_PATH):
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
     _lib = L
     return L
+
+
+def dfmath_eval(fn, values):
+    """The mixed path's double-float sin/cos (fn 0: of pi a; fn 1: of 2 pi m 2^-48
+    for integers m) and log (fn 2), evaluated on the GPU; returns (n, 2) or (n,)."""
+    if fn == 1:
+        arr = np.ascontiguousarray(values, dtype=np.uint64)
+    else:
+        arr = np.ascontiguousarray(values, dtype=np.float64)
+    n = arr.shape[0]
+    out = np.zeros(n if fn == 2 else 2 * n)
+    st = load().dmc_dfmath_eval(int(fn), n, _opt(arr), _opt(out))
+    if st != abi.DMC_OK:
+        raise DMCError(st, "dfmath_eval")
+    return out if fn == 2 else out.reshape(n, 2)
 
 
 def fort9_write(path, x, weight, psil, psigl, irn, tau=0.0):
@@ -493,4 +509,5 @@ class Context:
         return ms.value
 
 
-__all__ = ["Context", "DMCError", "load", "EXPORTS", "LIB_PATH", "DMC_NEST_MAX", "fort9_write", "fort9_read"]
+__all__ = ["Context", "DMCError", "load", "EXPORTS", "LIB_PATH", "DMC_NEST_MAX", "fort9_write", "fort9_read",
+           "dfmath_eval"]

@@ -220,6 +220,7 @@ void fill_params(dmc_ctx* c)
     p.scaleb_df = from_double(S.scaleb);
     p.rangeb_df = from_double(S.rangeb);
     p.range_df = from_double(S.range);
+    p.eli2_df = from_double(2.0 * S.eli);
     p.eli_f = (float)S.eli;
     for (int i = 0; i < DMC_MAX_UNPAIRED; ++i) {
         for (int k = 0; k < 3; ++k) {
@@ -1681,6 +1682,23 @@ int dmc_get_precision(const dmc_ctx* c, int* precision)
     if (!c || !precision) return DMC_ERR_INVALID;
     *precision = c->precision;
     return DMC_OK;
+}
+
+int dmc_dfmath_eval(int fn, int n, const void* in, double* out)
+{
+    if (fn < 0 || fn > 2 || n < 0 || (n > 0 && (!in || !out))) return DMC_ERR_INVALID;
+    if (n == 0) return DMC_OK;
+    const size_t nin = (size_t)n * 8, nout = (size_t)n * 8 * (fn == 2 ? 1 : 2);
+    void* din = nullptr;
+    double* dout = nullptr;
+    cudaError_t e = cudaMalloc(&din, nin);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dout, nout);
+    if (e == cudaSuccess) e = cudaMemcpy(din, in, nin, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_dfmath_eval(fn, n, din, dout, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, nout, cudaMemcpyDeviceToHost);
+    cudaFree(din);
+    cudaFree(dout);
+    return e == cudaSuccess ? DMC_OK : DMC_ERR_CUDA;
 }
 
 int dmc_probe_peak(int kind, double* tflops)

@@ -82,6 +82,7 @@ struct DevParams {
     double qex[3], v0ex, v0exjas, vorb1;
     // double-float copies for the mixed-precision kernel
     df el_df, scaleb_df, rangeb_df, range_df;
+    df eli2_df;           // 2 / L: orbital base angle over pi
     float eli_f;
     double akup[DMC_MAX_UNPAIRED][3], ak2up[DMC_MAX_UNPAIRED];
     double akdn[DMC_MAX_UNPAIRED][3], ak2dn[DMC_MAX_UNPAIRED];
@@ -136,6 +137,8 @@ struct KernelArgs {
 // On-chip layout of one walker CTA, offsets in doubles.
 struct SmemLayout {
     int x, xr, xo, dx, drift, dg, kq, S, pb, R, U, D, E, acc, colk, red, total;
+    int ksoa;             // k-vector fields as arrays: kx, ky, kz, k^2, v [5][nk],
+                          // then the integer components n [3][nk]
     int S2;               // second nd x ldS buffer of the blocked inverse (-1: none)
     int pb_in_smem;
     int pb_size;          // doubles of pair data per walker
@@ -158,6 +161,7 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
     L.drift = take(n3);           // old drift (step)
     L.dg = take(n3);              // guide-function gradient when a2 != 0
     L.kq = take(p.nk * 8);        // k vector records
+    L.ksoa = take(p.nk * 7);      // the same fields as arrays (conflict-free reads across k)
     L.S = take(p.nd * p.ldS);     // pair matrix -> inverse
     L.colk = take(2 * p.nd + 2);  // pivot column of the unblocked Gauss-Jordan
     L.acc = take(p.npart * 8);    // per particle: drift(3), lap, du(3), spare

@@ -140,27 +140,34 @@ __device__ __forceinline__ df acc_value(const dfacc& a) { return fast_two_sum(a.
 
 // Dot products with a known bound on sum |x_j y_j|, after Rump, Ogita and
 // Oishi's ExtractScalar (Accurate floating-point summation part I, SIAM J.
-// Sci. Comput. 31(1), 2008).  With sigma = 2^k >= 4 sum |x_j y_j|,
-// t = fl(sigma + x*y) lies in [sigma/2, 2 sigma], so q = t - sigma is exact
-// and a multiple of 2^(k-24); the partial sums of the q stay below sigma/2
-// and are therefore exact in FP32.  The remainder x*y - q (one FMA, one
-// rounding) and the products with the low parts go into an FP32 tail.
-// 7 FP32 instructions per multiply-add (12 for dfacc); error of order
-// n 2^-48 sigma for n terms.
+// Sci. Comput. 31(1), 2008).  With sigma = 2^k >= 4 sum |x_j y_j|, the
+// running value T = sigma + (partial sum) stays in [3 sigma/4, 5 sigma/4]:
+// each step T' = fl(T + x*y) is one FMA, its change q = T' - T is exact by
+// Sterbenz's lemma, and the remainder x*y - q (one FMA, one rounding) goes
+// into an FP32 tail; the products with the low parts go into a second tail.
+// At the end T - sigma is exact.  6 FP32 instructions per multiply-add (12
+// for dfacc); error of order n 2^-48 sigma for n terms.
 struct bacc {
-    float hi, lo;
+    float t, e, c;
 };
-__device__ __forceinline__ void bacc_init(bacc& a) { a.hi = a.lo = 0.0f; }
-__device__ __forceinline__ void bacc_madd(bacc& a, df x, df y, float sigma)
+__device__ __forceinline__ void bacc_init(bacc& a, float sigma)
 {
-    const float t = fmaf(x.hi, y.hi, sigma);
-    const float q = __fsub_rn(t, sigma);
-    a.hi = __fadd_rn(a.hi, q);
-    a.lo += fmaf(x.hi, y.hi, -q);
-    a.lo = fmaf(x.hi, y.lo, a.lo);
-    a.lo = fmaf(x.lo, y.hi, a.lo);
+    a.t = sigma;
+    a.e = a.c = 0.0f;
 }
-__device__ __forceinline__ df bacc_value(const bacc& a) { return two_sum(a.hi, a.lo); }
+__device__ __forceinline__ void bacc_madd(bacc& a, df x, df y)
+{
+    const float t = fmaf(x.hi, y.hi, a.t);
+    const float q = __fsub_rn(t, a.t);
+    a.t = t;
+    a.e = __fadd_rn(a.e, fmaf(x.hi, y.hi, -q));
+    a.c = fmaf(x.hi, y.lo, a.c);
+    a.c = fmaf(x.lo, y.hi, a.c);
+}
+__device__ __forceinline__ df bacc_value(const bacc& a, float sigma)
+{
+    return two_sum(__fsub_rn(a.t, sigma), __fadd_rn(a.e, a.c));
+}
 // smallest power of two >= v for finite v > 0 (2^-100 for v = 0)
 __device__ __forceinline__ float pow2_ceil(float v)
 {

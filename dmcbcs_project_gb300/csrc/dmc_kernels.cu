@@ -34,6 +34,20 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
     const int P = p.npart, n3 = 3 * P;
     const double* kvsrc = reinterpret_cast<const double*>(walker::Prec<R>::kv(a));
     for (int i = threadIdx.x; i < p.nk * 8; i += kThreads) sm[L.kq + i] = kvsrc[i];
+    {
+        using KV = typename walker::Prec<R>::KV;
+        const KV* kg = walker::Prec<R>::kv(a);
+        R* ks = walker::at<R>(sm, L.ksoa);
+        for (int q = threadIdx.x; q < p.nk; q += kThreads) {
+            ks[q] = kg[q].k[0];
+            ks[p.nk + q] = kg[q].k[1];
+            ks[2 * p.nk + q] = kg[q].k[2];
+            ks[3 * p.nk + q] = kg[q].k2;
+            ks[4 * p.nk + q] = kg[q].v;
+            int* kn = reinterpret_cast<int*>(ks + 5 * p.nk);
+            for (int cc = 0; cc < 3; ++cc) kn[cc * p.nk + q] = kg[q].n[cc];
+        }
+    }
     double* pb = L.pb_in_smem ? sm + L.pb : a.gscratch + (size_t)blockIdx.x * L.pb_size;
     Ctx<R> c{p, a, L, sm, pb};
     __syncthreads();
@@ -54,16 +68,32 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
             // walker's stream, pair i uses draws 2i-1, 2i
             const int npairs = (n3 + 1) / 2;
             for (int q = threadIdx.x; q < npairs; q += kThreads) {
-                const double u1 = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 1));
-                const double u2 = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 2));
-                double sn, cs;
-                sincospi(2.0 * u1, &sn, &cs);
-                const double r = sqrt(-2.0 * log(u2));
-                if (2 * q + 1 < n3) {
-                    dxs[2 * q] = sn * r;
-                    dxs[2 * q + 1] = cs * r;
+                double gs, gc;   // r sin(2 pi u1), r cos(2 pi u1), r = sqrt(-2 log u2)
+                if constexpr (walker::is_df<R>::value) {
+                    // the same deviates in double-float on the FP32 pipe:
+                    // u = (state | 1) 2^-48 is exact there
+                    const unsigned long long m1 = lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 1) | 1ull;
+                    const unsigned long long m2 = lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 2) | 1ull;
+                    df sn, cs;
+                    dfm::sincos2pi_u48(m1, sn, cs);
+                    const df lg = dfm::log_df(dfm::u48(m2));
+                    const df r = dsqrt(df{-2.0f * lg.hi, -2.0f * lg.lo});
+                    gs = to_double(sn * r);
+                    gc = to_double(cs * r);
                 } else {
-                    dxs[2 * q] = cs * r;   // odd count: the last one uses cos (ran.f90:95-102)
+                    const double u1 = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 1));
+                    const double u2 = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 2));
+                    double sn, cs;
+                    sincospi(2.0 * u1, &sn, &cs);
+                    const double r = sqrt(-2.0 * log(u2));
+                    gs = sn * r;
+                    gc = cs * r;
+                }
+                if (2 * q + 1 < n3) {
+                    dxs[2 * q] = gs;
+                    dxs[2 * q + 1] = gc;
+                } else {
+                    dxs[2 * q] = gc;   // odd count: the last one uses cos (ran.f90:95-102)
                 }
             }
             __syncthreads();
@@ -588,6 +618,30 @@ __global__ void fma_probe_kernel(T* out, int iters, T a, T b)
 #pragma unroll
     for (int k = 0; k < 8; ++k) s += v[k];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void dfmath_eval_kernel(int fn, int n, const void* in, double* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    df s, c;
+    if (fn == 0) {
+        dfm::sincospi_df(from_double(static_cast<const double*>(in)[i]), s, c);
+    } else if (fn == 1) {
+        dfm::sincos2pi_u48(static_cast<const unsigned long long*>(in)[i], s, c);
+    } else {
+        out[i] = to_double(dfm::log_df(from_double(static_cast<const double*>(in)[i])));
+        return;
+    }
+    out[2 * i] = to_double(s);
+    out[2 * i + 1] = to_double(c);
+}
+
+cudaError_t launch_dfmath_eval(int fn, int n, const void* in, double* out, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    dfmath_eval_kernel<<<(n + 127) / 128, 128, 0, st>>>(fn, n, in, out);
+    return cudaGetLastError();
 }
 
 cudaError_t probe_fma_peak(int kind, int nsm, double* tflops)

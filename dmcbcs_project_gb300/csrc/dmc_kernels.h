@@ -55,4 +55,9 @@ cudaError_t launch_ops_reduce(const OpsDev& o, int n, const DevStack& s, const i
 // FMA throughput of the FP64 (kind 0) or FP32 (kind 1) pipe, TFLOP/s
 cudaError_t probe_fma_peak(int kind, int nsm, double* tflops);
 
+// The mixed path's double-float elementary functions on device arrays:
+// fn 0: sin(pi a), cos(pi a); fn 1: sin(2 pi u), cos(2 pi u) of u = m 2^-48
+// (in holds the integers m); fn 2: log x.  out[2i], out[2i+1] (fn 2: out[i]).
+cudaError_t launch_dfmath_eval(int fn, int n, const void* in, double* out, cudaStream_t st);
+
 }  // namespace dmc

@@ -25,6 +25,7 @@
 #include <math.h>
 
 #include "dmc_device.cuh"
+#include "dmc_dfmath.cuh"
 
 namespace dmc {
 namespace walker {
@@ -55,6 +56,36 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* red)
     if (threadIdx.x < NV) {
         double s = 0.0;
         for (int k = 0; k < kWarps; ++k) s += red[k * NV + threadIdx.x];
+        red[kWarps * NV + threadIdx.x] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = red[kWarps * NV + q];
+    __syncthreads();
+}
+
+// Deterministic block sum of NV values held by the first nw warps (the
+// other warps hold zeros and skip the shuffles), in the value type T
+// (double, or double-float on the FP32 pipe).  The result is returned in v
+// on every thread.
+__device__ __forceinline__ double wsum(double v) { return warp_sum(v); }
+__device__ __forceinline__ df wsum(df v) { return dfm::warp_sum(v); }
+template <int NV, class T>
+__device__ __forceinline__ void block_sum_t(T (&v)[NV], T* red, int nw = kWarps)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (w < nw) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q] = wsum(v[q]);
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) red[w * NV + q] = v[q];
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        T s = red[threadIdx.x];
+        for (int k = 1; k < nw; ++k) s = s + red[k * NV + threadIdx.x];
         red[kWarps * NV + threadIdx.x] = s;
     }
     __syncthreads();
@@ -236,11 +267,12 @@ __device__ __forceinline__ T* at(double* sm, int off) { return reinterpret_cast<
 // Up-down pairs are processed in row chunks; each pair stores its Jastrow
 // gradient vector g = dx * u'/r, whose row sums (up) and column sums (down)
 // are taken in a fixed order.  Writes S[i][j] = beta(r_ij) and the beta pair
-// terms (f'/r, lap f) to pb.  Accumulates per-thread sums of u, v and the
-// pair Laplacian part.
+// terms (f'/r, lap f) to pb.  Returns per-thread sums of u, v and the pair
+// Laplacian part: jt[] for the up-down pairs in the Jastrow type, ss[] for
+// the same-spin pairs (FP64 on both paths).
 // ---------------------------------------------------------------------------
 template <class R>
-__device__ void pair_stage(const Ctx<R>& c, double& su, double& sv, double& sd2)
+__device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double (&ss)[3])
 {
     using J = typename Prec<R>::J;
     const DevParams& p = c.p;
@@ -373,10 +405,13 @@ __device__ void pair_stage(const Ctx<R>& c, double& su, double& sv, double& sd2)
         }
         __syncthreads();
     }
-    su += to_double(tu);
-    sv += to_double(tv);
-    sd2 += to_double(td);
+    jt[0] = tu;
+    jt[1] = tv;
+    jt[2] = td;
     if (!p.ieq) return;
+    double& su = ss[0];
+    double& sv = ss[1];
+    double& sd2 = ss[2];
     // same-spin pairs (coshpot.f90:167 with cjas(2) != 0): up-up then down-down,
     // in FP64 on both paths (off the benchmark configurations)
     const double* xd = sm + c.L.x;
@@ -486,7 +521,6 @@ __device__ __forceinline__ void cmul(df ar, df ai, df br, df bi, df& cr, df& ci)
 template <class R>
 __device__ void orbital_stage(const Ctx<R>& c)
 {
-    using KV = typename Prec<R>::KV;
     const DevParams& p = c.p;
     double* sm = c.sm;
     const double* x = sm + c.L.x;
@@ -494,13 +528,16 @@ __device__ void orbital_stage(const Ctx<R>& c)
     R* D = at<R>(sm, c.L.D);
     R* E = at<R>(sm, c.L.E);
     R* S = at<R>(sm, c.L.S);
-    const KV* kq = reinterpret_cast<const KV*>(sm + c.L.kq);
     const int np1 = p.nmax + 1;
     // powers e^{i m theta_c}, m = 0..nmax, E[(p*3+c)*np1 + m] = (re, im)
     for (int t = threadIdx.x; t < 3 * p.npart; t += kThreads) {
-        double s1d, c1d;
-        sincospi(2.0 * x[t] * p.eli, &s1d, &c1d);
-        const R s1 = from_dbl<R>(s1d), c1 = from_dbl<R>(c1d);
+        R s1, c1;
+        if constexpr (is_df<R>::value) {
+            // base angle 2 pi x / L in double-float, off the FP64 pipe
+            dfm::sincospi_df(at<R>(sm, c.L.xr)[t] * p.eli2_df, s1, c1);
+        } else {
+            sincospi(2.0 * x[t] * p.eli, &s1, &c1);
+        }
         R* e = E + 2 * t * np1;
         e[0] = rone<R>();
         e[1] = rzero<R>();
@@ -521,23 +558,26 @@ __device__ void orbital_stage(const Ctx<R>& c)
     __syncthreads();
     // columns: (cos, sin) of k vector q at 2(q-1), 2(q-1)+1; the constant
     // term at 2 nq; zero padding up to ldU
-    const int nq = p.nk - 1;
+    const int nq = p.nk - 1, nk = p.nk;
+    // k-vector fields as arrays: lanes with consecutive k read consecutive words
+    const R* kv_v = at<R>(sm, c.L.ksoa) + 4 * nk;
+    const int* kn = reinterpret_cast<const int*>(at<R>(sm, c.L.ksoa) + 5 * nk);
     const int items = p.npart * (nq + 1);
     for (int t = threadIdx.x; t < items; t += kThreads) {
         const int part = t / (nq + 1), q = t % (nq + 1);
         const bool up = part < p.nup;
         R* row = up ? U + part * p.ldU : D + (part - p.nup) * p.ldU;
         if (q == 0) {
-            row[2 * nq] = up ? kq[0].v : rone<R>();
+            row[2 * nq] = up ? kv_v[0] : rone<R>();
             for (int z = 2 * nq + 1; z < p.ldU; ++z) row[z] = rzero<R>();
             continue;
         }
-        const KV& K = kq[q];
+        const R kvq = kv_v[q];
         R zr = rone<R>(), zi = rzero<R>();
         bool first = true;
 #pragma unroll
         for (int cc = 0; cc < 3; ++cc) {
-            const int n = K.n[cc];
+            const int n = kn[cc * nk + q];
             if (n == 0) continue;
             const R* e = E + 2 * ((part * 3 + cc) * np1 + (n < 0 ? -n : n));
             const R er = e[0], ei = n < 0 ? -e[1] : e[1];
@@ -553,8 +593,8 @@ __device__ void orbital_stage(const Ctx<R>& c)
             }
         }
         if (up) {
-            row[2 * q - 2] = K.v * zr;
-            row[2 * q - 1] = K.v * zi;
+            row[2 * q - 2] = kvq * zr;
+            row[2 * q - 1] = kvq * zi;
         } else {
             row[2 * q - 2] = zr;
             row[2 * q - 1] = zi;
@@ -652,6 +692,11 @@ __device__ __forceinline__ unsigned mag_lo(double v) { return (unsigned)(__doubl
 __device__ __forceinline__ unsigned mag_hi(df v) { return __float_as_uint(v.hi) & 0x7fffffffu; }
 __device__ __forceinline__ unsigned mag_lo(df) { return 0u; }
 __device__ __forceinline__ double shfl_r(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl_x(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ df shfl_x(df v, int o)
+{
+    return df{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
 __device__ __forceinline__ df shfl_r(df v, int src)
 {
     return df{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
@@ -733,27 +778,26 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
         const int win = (h1 > h0 || (h1 == h0 && (l1 > l0 || (l1 == l0 && r1 < r0)))) ? 1 : 0;
         if ((win ? h1 : h0) == 0u && (win ? l1 : l0) == 0u) return false;   // no non-zero candidate
         const int pr = (int)(win ? r1 : r0);
-        // pivot row, scaled; its column-c entry becomes 1/pivot
+        // Gauss-Jordan step with the unscaled pivot row p and multiplier
+        // m = a_c / p_c per row (m = -1/p_c for the pivot row itself):
+        //   a_c2 <- a_c2 - m p_c2   (pivot row: p_c2 / p_c),
+        //   a_c  <- -m              (pivot row: 1 / p_c)
+        // one multiply per row instead of scaling the pivot row on every thread
         R rr[B];
 #pragma unroll
         for (int c2 = 0; c2 < B; ++c2) rr[c2] = s_cand[buf][win][c2];
         const R pv = rr[c];
         const R pinv = rcp(pv);
 #pragma unroll
-        for (int c2 = 0; c2 < B; ++c2) rr[c2] = (c2 == c) ? pinv : rr[c2] * pinv;
-#pragma unroll
         for (int s = 0; s < RPL; ++s) {
-            const R m = v[s][c];
+            const bool isp = t + 64 * s == pr;
+            const R m = isp ? -pinv : v[s][c] * pinv;
 #pragma unroll
-            for (int c2 = 0; c2 < B; ++c2) v[s][c2] = fms(c2 == c ? rzero<R>() : v[s][c2], m, rr[c2]);
+            for (int c2 = 0; c2 < B; ++c2)
+                if (c2 != c) v[s][c2] = fms(isp ? rzero<R>() : v[s][c2], m, rr[c2]);
+            v[s][c] = -m;
+            if (isp) done[s] = true;
         }
-#pragma unroll
-        for (int s = 0; s < RPL; ++s)
-            if (t + 64 * s == pr) {
-#pragma unroll
-                for (int c2 = 0; c2 < B; ++c2) v[s][c2] = rr[c2];
-                done[s] = true;
-            }
         if (t == 0) {
             piv[k0 + c] = pr;
             pvals[k0 + c] = pv;
@@ -865,10 +909,18 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
         for (int q = threadIdx.x; q < n; q += kThreads)
             if (is_neg(pvals[q])) odd ^= 1;
         if (warp == 0) {
-            double ls = 0.0;
-            for (int q = lane; q < n; q += 32) ls += log(fabs(to_double(pvals[q])));
-            ls = warp_sum(ls);
-            if (lane == 0) s_logdet = ls;
+            if constexpr (is_df<R>::value) {
+                // double-float logarithms on the FP32 pipe
+                df ls = df{0.0f, 0.0f};
+                for (int q = lane; q < n; q += 32) ls = ls + dfm::log_df(dabs(pvals[q]));
+                ls = dfm::warp_sum(ls);
+                if (lane == 0) s_logdet = to_double(ls);
+            } else {
+                double ls = 0.0;
+                for (int q = lane; q < n; q += 32) ls += log(fabs(pvals[q]));
+                ls = warp_sum(ls);
+                if (lane == 0) s_logdet = ls;
+            }
         }
     }
     const int nodd = __syncthreads_count(odd);
@@ -1062,20 +1114,27 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
 //          G_{c,s} = sum_j D[j][c,s] Sinv[j][i]
 //  down j: sum_q k_q (H_s D_c - H_c D_s), lap -|k|^2 (H_c D_c + H_s D_s),
 //          H_{c,s} = sum_i Sinv[j][i] U[i][c,s]
-// Work items (particle, k vector) are split into contiguous per-thread
-// chunks; each thread sums its chunk per particle and the partial sums of a
-// particle are added in thread order.  Up and down items go to disjoint
-// warps (in proportion to the particle counts), so that no warp runs both
-// loop bodies one after the other.
+// Register-tiled: a task is one particle and kQT k vectors q = g, g + G,
+// g + 2G, ... (G = ceil(nq / kQT) groups per particle), so one Sinv load
+// feeds 2 kQT multiply-adds and a thread carries 2 kQT independent
+// accumulators; lanes of a warp read consecutive k vectors (no bank
+// conflicts).  Tasks are split into contiguous per-thread chunks; each
+// thread sums its chunk per particle and the partial sums of a particle are
+// added in thread order.  Up and down tasks go to disjoint warps (in
+// proportion to the particle counts), so that no warp runs both loop bodies
+// one after the other.
 // ---------------------------------------------------------------------------
+constexpr int kQT = 4;
+
 struct DriftSplit {
     int pbeg[2], np[2], tbeg[2], nth[2], chunk[2];
 };
 
 // Half 0 = up particles on the first warps, half 1 = down particles on the
-// rest.  A chunk must not span more than two particles (chunk <= nq); when a
-// split cannot guarantee that, half 0 takes every particle on all threads.
-__device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int nq)
+// rest.  A chunk must not span more than two particles (chunk <= ng, the
+// tasks per particle); when a split cannot guarantee that, half 0 takes
+// every particle on all threads.
+__device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int ng)
 {
     DriftSplit s;
     const int P = nup + ndn;
@@ -1092,13 +1151,13 @@ __device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int nq)
     s.nth[1] = kThreads - 32 * wu;
     bool ok = nup > 0 && ndn > 0;
     for (int h = 0; h < 2; ++h) {
-        s.chunk[h] = s.nth[h] > 0 ? (s.np[h] * nq + s.nth[h] - 1) / s.nth[h] : 0;
-        if (s.chunk[h] > nq) ok = false;
+        s.chunk[h] = s.nth[h] > 0 ? (s.np[h] * ng + s.nth[h] - 1) / s.nth[h] : 0;
+        if (s.chunk[h] > ng) ok = false;
     }
     if (!ok) {
         s.np[0] = P;
         s.nth[0] = kThreads;
-        s.chunk[0] = (P * nq + kThreads - 1) / kThreads;
+        s.chunk[0] = (P * ng + kThreads - 1) / kThreads;
         s.np[1] = 0;
         s.tbeg[1] = kThreads;
         s.nth[1] = 0;
@@ -1107,21 +1166,341 @@ __device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int nq)
     return s;
 }
 
+// one accumulator per (k vector, cos|sin) of a task
 template <class R>
-__device__ void drift_stage(const Ctx<R>& c)
+struct DriftAcc {
+    typename AccOf<R>::type a[2 * kQT];
+    __device__ __forceinline__ void init(const float*) {
+#pragma unroll
+        for (int m = 0; m < 2 * kQT; ++m) acc_init(a[m]);
+    }
+    __device__ __forceinline__ void madd(int m, R x, R y) { acc_madd(a[m], x, y); }
+    __device__ __forceinline__ R value(int m, const float*) const { return acc_value(a[m]); }
+};
+template <>
+struct DriftAcc<df> {
+    bacc a[2 * kQT];
+    __device__ __forceinline__ void init(const float* sig) {
+#pragma unroll
+        for (int m = 0; m < 2 * kQT; ++m) bacc_init(a[m], sig[m >> 1]);
+    }
+    __device__ __forceinline__ void madd(int m, df x, df y) { bacc_madd(a[m], x, y); }
+    __device__ __forceinline__ df value(int m, const float* sig) const { return bacc_value(a[m], sig[m >> 1]); }
+};
+
+// Warp-tiled form of stage 5 (the main path).  The contractions
+// G = Si^T D (up) and H = Si U (down) are GEMMs of nd x nd by nd x 2nq;
+// operand reads from shared memory bound them, so each lane keeps a
+// register tile of kTR particles x kTS k vectors (cos and sin: 2 kTR kTS
+// accumulators) and the lanes of a warp form a kTA x kTB grid: a warp tile
+// covers kTA kTR = 8 particles of one spin and kTB kTS = 40 k vectors, each
+// Sinv read feeds 2 kTS multiply-adds and each D/U read 2 kTR.  Warps 0-3
+// take the up tiles, warps 4-7 the down tiles.  Per particle, the lanes of
+// a tile that share it sum their k vectors with a fixed xor tree; particles
+// beyond the last full block of 8 are computed one (particle, k) item per
+// thread.  Partial sums go to shared memory and are added per particle in
+// a fixed order.  Returns false (nothing done) when the partial sums do not
+// fit the reduction area.
+constexpr int kTR = 2, kTS = 5, kTA = 4, kTB = 8;
+static_assert(kTA * kTB == 32, "one warp per tile");
+
+__device__ __forceinline__ float abs_hi(df v) { return fabsf(v.hi); }
+__device__ __forceinline__ float abs_hi(double v) { return (float)fabs(v); }
+
+// one (particle, k vector) item of the drift contraction: the 4 terms
+// (3 drift components, Laplacian) of k vector q (1-based) for particle pt
+template <class R>
+__device__ __forceinline__ void drift_item(const Ctx<R>& c, const float* bound, int pt, int q, R (&out)[4])
 {
-    using KV = typename Prec<R>::KV;
-    using Acc = typename AccOf<R>::type;
     const DevParams& p = c.p;
     double* sm = c.sm;
     const R* U = at<R>(sm, c.L.U);
     const R* D = at<R>(sm, c.L.D);
     const R* Si = at<R>(sm, c.L.S);
-    const KV* kq = reinterpret_cast<const KV*>(sm + c.L.kq);
+    const R* ks = at<R>(sm, c.L.ksoa);
+    const int nk = p.nk, ld = p.ldS, ldU = p.ldU, qc = 2 * q - 2;
+    typename AccOf<R>::type ac, as;
+    bacc bc, bs;
+    float sig = 0.0f;
+    const bool up = pt < p.nup;
+    if (up) {
+        if constexpr (is_df<R>::value) {
+            sig = pow2_ceil(4.0f * bound[pt]);
+            bacc_init(bc, sig);
+            bacc_init(bs, sig);
+        } else {
+            acc_init(ac);
+            acc_init(as);
+        }
+        for (int j = 0; j < p.ndn; ++j) {
+            const R sji = Si[j * ld + pt];
+            R dc, ds;
+            ld2(D + j * ldU + qc, dc, ds);
+            if constexpr (is_df<R>::value) {
+                bacc_madd(bc, dc, sji);
+                bacc_madd(bs, ds, sji);
+            } else {
+                acc_madd(ac, dc, sji);
+                acc_madd(as, ds, sji);
+            }
+        }
+    } else {
+        const int j = pt - p.nup;
+        if constexpr (is_df<R>::value) {
+            sig = pow2_ceil(4.0f * fabsf(ks[4 * nk + q].hi) * 1.001f * bound[p.nd + j]);
+            bacc_init(bc, sig);
+            bacc_init(bs, sig);
+        } else {
+            acc_init(ac);
+            acc_init(as);
+        }
+        for (int i = 0; i < p.nup; ++i) {
+            const R sji = Si[j * ld + i];
+            R uc, us;
+            ld2(U + i * ldU + qc, uc, us);
+            if constexpr (is_df<R>::value) {
+                bacc_madd(bc, sji, uc);
+                bacc_madd(bs, sji, us);
+            } else {
+                acc_madd(ac, sji, uc);
+                acc_madd(as, sji, us);
+            }
+        }
+    }
+    R vc, vs;
+    if constexpr (is_df<R>::value) {
+        vc = bacc_value(bc, sig);
+        vs = bacc_value(bs, sig);
+    } else {
+        vc = acc_value(ac);
+        vs = acc_value(as);
+    }
+    R t, l;
+    if (up) {
+        R uc, us;
+        ld2(U + pt * ldU + qc, uc, us);
+        t = uc * vs - us * vc;
+        l = uc * vc + us * vs;
+    } else {
+        R dc, ds;
+        ld2(D + (pt - p.nup) * ldU + qc, dc, ds);
+        t = vs * dc - vc * ds;
+        l = vc * dc + vs * ds;
+    }
+    out[0] = ks[q] * t;
+    out[1] = ks[nk + q] * t;
+    out[2] = ks[2 * nk + q] * t;
+    out[3] = -(ks[3 * nk + q] * l);
+}
+
+// one warp tile: particles blk*8 .. blk*8+7 of one spin (DOWN: the down
+// particles, contraction over up), k vectors of chunk qch; writes the
+// tile's per-particle sums to pbuf
+template <class R, bool DOWN>
+__device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, int blk, int qch, int nqc, R* pbuf)
+{
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const R* Si = at<R>(sm, c.L.S);
+    const R* ks = at<R>(sm, c.L.ksoa);
+    const R* B = at<R>(sm, DOWN ? c.L.U : c.L.D);     // contraction operand
+    const R* O = at<R>(sm, DOWN ? c.L.D : c.L.U);     // the particles' own orbital rows
+    const int nq = p.nk - 1, nk = p.nk, ld = p.ldS, ldU = p.ldU;
+    const int lane = threadIdx.x & 31, ai = lane & (kTA - 1), bi = lane / kTA;
+    const int nK = DOWN ? p.nup : p.ndn;
+    int pi[kTR];
+#pragma unroll
+    for (int k = 0; k < kTR; ++k) pi[k] = blk * kTA * kTR + ai + kTA * k;
+    int qo[kTS];       // offset of the (cos, sin) pair in an orbital row
+    bool okq[kTS];
+#pragma unroll
+    for (int m = 0; m < kTS; ++m) {
+        const int q = qch * kTB * kTS + bi + kTB * m;
+        okq[m] = q < nq;
+        qo[m] = 2 * (okq[m] ? q : 0);               // a missing k vector reads vector 1 and is dropped
+    }
+    // bound of the double-float dot products (|D| <= 1, |U[i][q]| <= |v_q|)
+    auto sigma = [&](int k, int m) {
+        return DOWN ? pow2_ceil(4.0f * abs_hi(ks[4 * nk + qo[m] / 2 + 1]) * 1.001f * bound[p.nd + pi[k]])
+                    : pow2_ceil(4.0f * bound[pi[k]]);
+    };
+    typename AccOf<R>::type a64[kTR][kTS][2];
+    bacc adf[kTR][kTS][2];
+#pragma unroll
+    for (int k = 0; k < kTR; ++k)
+#pragma unroll
+        for (int m = 0; m < kTS; ++m) {
+            if constexpr (is_df<R>::value) {
+                const float sg = sigma(k, m);
+                bacc_init(adf[k][m][0], sg);
+                bacc_init(adf[k][m][1], sg);
+            } else {
+                acc_init(a64[k][m][0]);
+                acc_init(a64[k][m][1]);
+            }
+        }
+    // up: G[i][q] = sum_j Si[j][i] D[j][q];  down: H[j][q] = sum_i Si[j][i] U[i][q]
+    const R* s0 = DOWN ? Si + pi[0] * ld : Si + pi[0];
+    const int sstride = DOWN ? 1 : ld;
+    for (int kk = 0; kk < nK; ++kk) {
+        R sv[kTR];
+#pragma unroll
+        for (int k = 0; k < kTR; ++k) sv[k] = s0[kk * sstride + (DOWN ? kTA * k * ld : kTA * k)];
+        const R* brow = B + kk * ldU;
+#pragma unroll
+        for (int m = 0; m < kTS; ++m) {
+            R bc, bs;
+            ld2(brow + qo[m], bc, bs);
+#pragma unroll
+            for (int k = 0; k < kTR; ++k) {
+                if constexpr (is_df<R>::value) {
+                    bacc_madd(adf[k][m][0], bc, sv[k]);
+                    bacc_madd(adf[k][m][1], bs, sv[k]);
+                } else {
+                    acc_madd(a64[k][m][0], bc, sv[k]);
+                    acc_madd(a64[k][m][1], bs, sv[k]);
+                }
+            }
+        }
+    }
+    // per particle: sum over this lane's k vectors
+    //   up:   t = U_c G_s - U_s G_c,  l = U_c G_c + U_s G_s
+    //   down: t = H_s D_c - H_c D_s,  l = H_c D_c + H_s D_s
+    R ts[kTR][4];
+#pragma unroll
+    for (int k = 0; k < kTR; ++k) {
+        typename AccOf<R>::type sx, sy, sz, sl;
+        acc_init(sx);
+        acc_init(sy);
+        acc_init(sz);
+        acc_init(sl);
+        const R* own = O + pi[k] * ldU;
+#pragma unroll
+        for (int m = 0; m < kTS; ++m) {
+            R vc, vs;
+            if constexpr (is_df<R>::value) {
+                const float sg = sigma(k, m);
+                vc = bacc_value(adf[k][m][0], sg);
+                vs = bacc_value(adf[k][m][1], sg);
+            } else {
+                vc = acc_value(a64[k][m][0]);
+                vs = acc_value(a64[k][m][1]);
+            }
+            if (!okq[m]) continue;
+            R oc, os;
+            ld2(own + qo[m], oc, os);
+            typename AccOf<R>::type at_, al_;
+            acc_init(at_);
+            acc_init(al_);
+            if (DOWN) {
+                acc_madd(at_, vs, oc);
+                acc_madd(at_, -vc, os);
+            } else {
+                acc_madd(at_, oc, vs);
+                acc_madd(at_, -os, vc);
+            }
+            acc_madd(al_, oc, vc);
+            acc_madd(al_, os, vs);
+            const R t = acc_value(at_), l = acc_value(al_);
+            const int q1 = qo[m] / 2 + 1;
+            acc_madd(sx, ks[q1], t);
+            acc_madd(sy, ks[nk + q1], t);
+            acc_madd(sz, ks[2 * nk + q1], t);
+            acc_madd(sl, -ks[3 * nk + q1], l);
+        }
+        ts[k][0] = acc_value(sx);
+        ts[k][1] = acc_value(sy);
+        ts[k][2] = acc_value(sz);
+        ts[k][3] = acc_value(sl);
+    }
+    // fixed xor tree over the lanes that share the particles (lane bits of bi)
+#pragma unroll
+    for (int o = kTA; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < kTR; ++k)
+#pragma unroll
+            for (int z = 0; z < 4; ++z) ts[k][z] = ts[k][z] + shfl_x(ts[k][z], o);
+    const int pbase = DOWN ? p.nup : 0;
+    if (bi == 0)
+#pragma unroll
+        for (int k = 0; k < kTR; ++k)
+#pragma unroll
+            for (int z = 0; z < 4; ++z) pbuf[((pbase + pi[k]) * nqc + qch) * 4 + z] = ts[k][z];
+}
+
+template <class R>
+__device__ bool drift_tiled(const Ctx<R>& c, const float* bound)
+{
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const int P = p.npart, nq = p.nk - 1;
+    const int nqc = (nq + kTB * kTS - 1) / (kTB * kTS);   // k-vector chunks of 40
+    const int tu = p.nup % (kTA * kTR), td = p.ndn % (kTA * kTR);
+    const int ntail = (tu + td) * nq;
+    if (p.nup == 0 || p.ndn == 0 || (P * nqc + ntail) * 4 > kThreads * 8) return false;
+    double* acc = sm + c.L.acc;
+    R* pbuf = at<R>(sm, c.L.red);              // [P][nqc][4], then tail items [ntail][4]
+    R* tbuf = pbuf + P * nqc * 4;
+    const int warp = threadIdx.x >> 5;
+    const int half = warp >= kWarps / 2 ? 1 : 0, hw = warp & (kWarps / 2 - 1);
+    const int n = half ? p.ndn : p.nup;        // particles of this spin
+    const int nb = n / (kTA * kTR);            // full blocks of 8
+    for (int tau = hw; tau < nb * nqc; tau += kWarps / 2) {
+        if (half)
+            drift_tile<R, true>(c, bound, tau / nqc, tau % nqc, nqc, pbuf);
+        else
+            drift_tile<R, false>(c, bound, tau / nqc, tau % nqc, nqc, pbuf);
+    }
+    // particles beyond the full blocks: one (particle, k vector) item per
+    // thread, spread over the warps
+    for (int r0 = 0; r0 < ntail; r0 += kThreads) {
+        // item r0 + i of a round goes to lane i / kWarps of warp i % kWarps
+        const int it = r0 + ((int)threadIdx.x & 31) * kWarps + ((int)threadIdx.x >> 5);
+        if (it >= ntail) continue;
+        const int pl = it / nq, q = it % nq + 1;
+        const int pt = pl < tu ? p.nup - tu + pl : p.nup + p.ndn - td + (pl - tu);
+        R o[4];
+        drift_item<R>(c, bound, pt, q, o);
+        for (int z = 0; z < 4; ++z) tbuf[it * 4 + z] = o[z];
+    }
+    __syncthreads();
+    for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+        const bool dn = pt >= p.nup;
+        const int pl = dn ? pt - p.nup : pt, nn = dn ? p.ndn : p.nup, tt = dn ? td : tu;
+        R r[4];
+        for (int z = 0; z < 4; ++z) r[z] = rzero<R>();
+        if (pl < nn - tt) {
+            for (int qch = 0; qch < nqc; ++qch)
+                for (int z = 0; z < 4; ++z) r[z] = r[z] + pbuf[(pt * nqc + qch) * 4 + z];
+        } else {
+            const int row = (dn ? tu + (pl - (nn - tt)) : pl - (nn - tt)) * nq;
+            for (int q = 0; q < nq; ++q)
+                for (int z = 0; z < 4; ++z) r[z] = r[z] + tbuf[(row + q) * 4 + z];
+        }
+        acc[3 * pt + 0] = to_double(r[0]);
+        acc[3 * pt + 1] = to_double(r[1]);
+        acc[3 * pt + 2] = to_double(r[2]);
+        acc[3 * P + pt] = to_double(r[3]);
+    }
+    __syncthreads();
+    return true;
+}
+
+template <class R>
+__device__ void drift_stage(const Ctx<R>& c)
+{
+    using KV = typename Prec<R>::KV;
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const R* U = at<R>(sm, c.L.U);
+    const R* D = at<R>(sm, c.L.D);
+    const R* Si = at<R>(sm, c.L.S);
+    const R* ks = at<R>(sm, c.L.ksoa);      // kx, ky, kz, k^2, v by k vector
     double* acc = sm + c.L.acc;             // drift [3N], lap [N]
     R* part = at<R>(sm, c.L.red);           // per thread: 2 segments x 4 sums
-    const int nq = p.nk - 1, P = p.npart, ld = p.ldS, ldU = p.ldU;
-    const DriftSplit sp = drift_split(p.nup, p.ndn, nq);
+    const int nq = p.nk - 1, nk = p.nk, P = p.npart, ld = p.ldS, ldU = p.ldU;
+    const int ng = (nq + kQT - 1) / kQT;    // tasks per particle
+    const DriftSplit sp = drift_split(p.nup, p.ndn, ng);
     // double-float path: abs column sums (bound[i], for G) and row sums
     // (bound[nd + j], for H) of the inverse bound the dot products
     float* bound = reinterpret_cast<float*>(sm + c.L.colk);
@@ -1136,109 +1515,107 @@ __device__ void drift_stage(const Ctx<R>& c)
         }
         __syncthreads();
     }
+    if (drift_tiled<R>(c, bound)) return;
     const int h = (int)threadIdx.x >= sp.tbeg[1] ? 1 : 0;
     const int lt = (int)threadIdx.x - sp.tbeg[h];
-    const int items = sp.np[h] * nq, chunk = sp.chunk[h], pbeg = sp.pbeg[h];
-    const int b = lt * chunk, e = min(items, b + chunk);
+    const int tasks = sp.np[h] * ng, chunk = sp.chunk[h], pbeg = sp.pbeg[h];
+    const int b = lt * chunk, e = min(tasks, b + chunk);
     R s0[4], s1[4];
     for (int k = 0; k < 4; ++k) s0[k] = s1[k] = rzero<R>();
-    const int first = b < e ? pbeg + b / nq : -1;
+    const int first = b < e ? pbeg + b / ng : -1;
     for (int it = b; it < e; ++it) {
-        const int pt = pbeg + it / nq, q = it % nq + 1;
-        const KV& K = kq[q];
-        const int qc = 2 * q - 2;   // (cos, sin) pair of k vector q
-        R t, l;
-        if (pt < p.nup) {
+        const int pt = pbeg + it / ng, g = it % ng;
+        // k vectors of the task (1-based records); a missing one (q > nq)
+        // reads vector g + 1 and is dropped
+        int qv[kQT];
+        bool ok[kQT];
+#pragma unroll
+        for (int m = 0; m < kQT; ++m) {
+            const int q = g + ng * m;
+            ok[m] = q < nq;
+            qv[m] = (ok[m] ? q : g) + 1;
+        }
+        R vc[kQT], vs[kQT];   // G or H of each k vector
+        float sig[kQT] = {};
+        DriftAcc<R> A;
+        const bool up = pt < p.nup;
+        if (up) {
             const int i = pt;
-            const R* dq = D + qc;
-            const R* sc = Si + i;
-            R vgc, vgs;
             if constexpr (is_df<R>::value) {
-                const float sig = pow2_ceil(4.0f * bound[i]);   // |D| <= 1
-                bacc gc, gs;
-                bacc_init(gc);
-                bacc_init(gs);
-                for (int j = 0; j < p.ndn; ++j) {
-                    const R sji = sc[j * ld];
-                    R dc_, ds_;
-                    ld2(dq + j * ldU, dc_, ds_);
-                    bacc_madd(gc, dc_, sji, sig);
-                    bacc_madd(gs, ds_, sji, sig);
-                }
-                vgc = bacc_value(gc);
-                vgs = bacc_value(gs);
-            } else {
-                Acc gc, gs;
-                acc_init(gc);
-                acc_init(gs);
-                for (int j = 0; j < p.ndn; ++j) {
-                    const R sji = sc[j * ld];
-                    R dc_, ds_;
-                    ld2(dq + j * ldU, dc_, ds_);
-                    acc_madd(gc, dc_, sji);
-                    acc_madd(gs, ds_, sji);
-                }
-                vgc = acc_value(gc);
-                vgs = acc_value(gs);
+                const float sg = pow2_ceil(4.0f * bound[i]);   // |D| <= 1
+#pragma unroll
+                for (int m = 0; m < kQT; ++m) sig[m] = sg;
             }
-            R uc, us;
-            ld2(U + i * ldU + qc, uc, us);
-            t = uc * vgs - us * vgc;
-            l = uc * vgc + us * vgs;
+            A.init(sig);
+            const R* sc = Si + i;
+            for (int j = 0; j < p.ndn; ++j) {
+                const R sji = sc[j * ld];
+                const R* dj = D + j * ldU;
+#pragma unroll
+                for (int m = 0; m < kQT; ++m) {
+                    R dc_, ds_;
+                    ld2(dj + 2 * qv[m] - 2, dc_, ds_);
+                    A.madd(2 * m, dc_, sji);
+                    A.madd(2 * m + 1, ds_, sji);
+                }
+            }
         } else {
             const int j = pt - p.nup;
-            const R* srow = Si + j * ld;
-            const R* uq = U + qc;
-            R vhc, vhs;
             if constexpr (is_df<R>::value) {
-                // |U[i][q]| <= |v_q|
-                const float sig = pow2_ceil(4.0f * fabsf(K.v.hi) * 1.001f * bound[p.nd + j]);
-                bacc hc, hs;
-                bacc_init(hc);
-                bacc_init(hs);
-                for (int i = 0; i < p.nup; ++i) {
-                    const R sji = srow[i];
-                    R uc_, us_;
-                    ld2(uq + i * ldU, uc_, us_);
-                    bacc_madd(hc, sji, uc_, sig);
-                    bacc_madd(hs, sji, us_, sig);
-                }
-                vhc = bacc_value(hc);
-                vhs = bacc_value(hs);
-            } else {
-                Acc hc, hs;
-                acc_init(hc);
-                acc_init(hs);
-                for (int i = 0; i < p.nup; ++i) {
-                    const R sji = srow[i];
-                    R uc_, us_;
-                    ld2(uq + i * ldU, uc_, us_);
-                    acc_madd(hc, sji, uc_);
-                    acc_madd(hs, sji, us_);
-                }
-                vhc = acc_value(hc);
-                vhs = acc_value(hs);
+#pragma unroll
+                for (int m = 0; m < kQT; ++m)   // |U[i][q]| <= |v_q|
+                    sig[m] = pow2_ceil(4.0f * fabsf(ks[4 * nk + qv[m]].hi) * 1.001f * bound[p.nd + j]);
             }
-            R dc, ds;
-            ld2(D + j * ldU + qc, dc, ds);
-            t = vhs * dc - vhc * ds;
-            l = vhc * dc + vhs * ds;
+            A.init(sig);
+            const R* srow = Si + j * ld;
+            for (int i = 0; i < p.nup; ++i) {
+                const R sji = srow[i];
+                const R* ui = U + i * ldU;
+#pragma unroll
+                for (int m = 0; m < kQT; ++m) {
+                    R uc_, us_;
+                    ld2(ui + 2 * qv[m] - 2, uc_, us_);
+                    A.madd(2 * m, sji, uc_);
+                    A.madd(2 * m + 1, sji, us_);
+                }
+            }
         }
-        const R lk = -(K.k2 * l);
+#pragma unroll
+        for (int m = 0; m < kQT; ++m) {
+            vc[m] = A.value(2 * m, sig);
+            vs[m] = A.value(2 * m + 1, sig);
+        }
+        R ts[4];
+        for (int k = 0; k < 4; ++k) ts[k] = rzero<R>();
+#pragma unroll
+        for (int m = 0; m < kQT; ++m) {
+            if (!ok[m]) continue;
+            const int qc = 2 * qv[m] - 2;   // (cos, sin) pair of the k vector
+            R t, l;
+            if (up) {
+                R uc, us;
+                ld2(U + pt * ldU + qc, uc, us);
+                t = uc * vs[m] - us * vc[m];
+                l = uc * vc[m] + us * vs[m];
+            } else {
+                R dc, ds;
+                ld2(D + (pt - p.nup) * ldU + qc, dc, ds);
+                t = vs[m] * dc - vc[m] * ds;
+                l = vc[m] * dc + vs[m] * ds;
+            }
+            ts[0] = fma(ks[qv[m]], t, ts[0]);
+            ts[1] = fma(ks[nk + qv[m]], t, ts[1]);
+            ts[2] = fma(ks[2 * nk + qv[m]], t, ts[2]);
+            ts[3] = ts[3] - ks[3 * nk + qv[m]] * l;
+        }
         if (pt == first) {
-            s0[0] = fma(K.k[0], t, s0[0]);
-            s0[1] = fma(K.k[1], t, s0[1]);
-            s0[2] = fma(K.k[2], t, s0[2]);
-            s0[3] = s0[3] + lk;
+            for (int k = 0; k < 4; ++k) s0[k] = s0[k] + ts[k];
         } else {
-            s1[0] = fma(K.k[0], t, s1[0]);
-            s1[1] = fma(K.k[1], t, s1[1]);
-            s1[2] = fma(K.k[2], t, s1[2]);
-            s1[3] = s1[3] + lk;
+            for (int k = 0; k < 4; ++k) s1[k] = s1[k] + ts[k];
         }
     }
     // publish the (at most two) particle segments of this thread's chunk;
-    // a chunk never spans more than two particles because chunk <= nq
+    // a chunk never spans more than two particles because chunk <= ng
     R* my = part + threadIdx.x * 8;
     for (int k = 0; k < 4; ++k) {
         my[k] = s0[k];
@@ -1246,18 +1623,18 @@ __device__ void drift_stage(const Ctx<R>& c)
     }
     __syncthreads();
     // particle pl of a half is covered by that half's local threads
-    // floor(pl*nq/chunk) .. floor((pl*nq+nq-1)/chunk)
+    // floor(pl*ng/chunk) .. floor((pl*ng+ng-1)/chunk)
     for (int pt = threadIdx.x; pt < P; pt += kThreads) {
         const int hh = (sp.nth[1] > 0 && pt >= sp.pbeg[1]) ? 1 : 0;
-        const int pl = pt - sp.pbeg[hh], ch = sp.chunk[hh], ni = sp.np[hh] * nq;
+        const int pl = pt - sp.pbeg[hh], ch = sp.chunk[hh], ni = sp.np[hh] * ng;
         R r[4];
         for (int k = 0; k < 4; ++k) r[k] = rzero<R>();
-        const int l0 = (pl * nq) / ch, l1 = (pl * nq + nq - 1) / ch;
+        const int l0 = (pl * ng) / ch, l1 = (pl * ng + ng - 1) / ch;
         for (int u = l0; u <= l1 && u < sp.nth[hh]; ++u) {
             const int tb = u * ch, te = min(ni, tb + ch);
             if (tb >= te) continue;
             const R* o = part + (sp.tbeg[hh] + u) * 8;
-            const int sl = (tb / nq == pl) ? 0 : (((te - 1) / nq == pl) ? 4 : -1);
+            const int sl = (tb / ng == pl) ? 0 : (((te - 1) / ng == pl) ? 4 : -1);
             if (sl < 0) continue;
             for (int k = 0; k < 4; ++k) r[k] = r[k] + o[sl + k];
         }
@@ -1452,12 +1829,27 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         __syncthreads();
     }
     HRes h;
+    using J = typename Prec<R>::J;
+    J jt[3] = {rzero<J>(), rzero<J>(), rzero<J>()};
+    double ss[3] = {0.0, 0.0, 0.0};
+    pair_stage<R>(c, jt, ss);   // also fills the beta part of S (needed by MODE_BCS too)
     double su = 0.0, sv = 0.0, sd2 = 0.0;
-    pair_stage<R>(c, su, sv, sd2);   // also fills the beta part of S (needed by MODE_BCS too)
     if (mode == MODE_BCS) {
-        su = sv = sd2 = 0.0;
         for (int i = threadIdx.x; i < n3; i += kThreads) du[i] = 0.0;
         __syncthreads();
+    } else {
+        // Jastrow, potential and pair-Laplacian sums in the Jastrow type
+        // (double-float on the mixed path: no FP64 shuffle tree)
+        block_sum_t<3>(jt, at<J>(sm, c.L.red));
+        su = to_double(jt[0]);
+        sv = to_double(jt[1]);
+        sd2 = to_double(jt[2]);
+        if (p.ieq) {
+            block_sum_t<3>(ss, sm + c.L.red);
+            su += ss[0];
+            sv += ss[1];
+            sd2 += ss[2];
+        }
     }
     // long-range Jastrow: part of hpsi (getphilong, wavefunction.f90:148-159,173),
     // not of getphi or bcs
@@ -1485,6 +1877,7 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     // one-body term (psislaterbcs.f90:378-395) and per-particle combination
     double sums[8] = {su, sv, sd2, 0.0, 0.0, 0.0, 0.0, 0.0};
     // sums[3]: sum lap/m (d2phi), [4]: |du|^2, [5]: du.dphi, [6]: one-body g, [7]: vext
+    const bool ob = p.onebody && (mode == MODE_HPSI || mode == MODE_STEP);
     double g1 = 0.0, d2g = 0.0, dudg = 0.0;
     double ll = 0.0, dudl = 0.0, dgdl = 0.0;   // |dUlong|^2, du.dUlong, dg.dUlong
     const double* dl = sm + c.L.dg;
@@ -1499,7 +1892,7 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         sums[3] += (ok ? acc[3 * P + pt] : 0.0) * im;
         sums[4] += dj[0] * dj[0] + dj[1] * dj[1] + dj[2] * dj[2];
         double dg[3] = {0.0, 0.0, 0.0};
-        if (p.onebody && (mode == MODE_HPSI || mode == MODE_STEP)) {
+        if (ob) {
             double s, co;
             sincos(p.qex[0] * x[3 * pt] + p.qex[1] * x[3 * pt + 1] + p.qex[2] * x[3 * pt + 2], &s, &co);
             sums[7] -= p.v0ex * co;
@@ -1524,9 +1917,24 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         for (int k = 0; k < 3; ++k) acc[3 * pt + k] = dph[k] + dtot[k];
     }
     sums[6] = g1;
+    // per-particle sums live on the first ceil(P/32) warps; the one-body
+    // and long-range terms are reduced only when present
+    const int pw = min(kWarps, (P + 31) / 32);
+    {
+        double ps[3] = {sums[3], sums[4], sums[5]};
+        block_sum_t<3>(ps, sm + c.L.red, pw);
+        sums[3] = ps[0];
+        sums[4] = ps[1];
+        sums[5] = ps[2];
+    }
     double more[5] = {d2g, dudg, ll, dudl, dgdl};
-    block_sum<8>(sums, sm + c.L.red);
-    block_sum<5>(more, sm + c.L.red);
+    if (ob || jl) {
+        double ex[7] = {sums[6], sums[7], more[0], more[1], more[2], more[3], more[4]};
+        block_sum_t<7>(ex, sm + c.L.red, pw);
+        sums[6] = ex[0];
+        sums[7] = ex[1];
+        for (int q = 0; q < 5; ++q) more[q] = ex[2 + q];
+    }
     const double u = sums[0] + sums[6] + ulong;
     const double d2u_j = sums[2] + sums[4];                        // getphi d2u
     // + one-body and long-range terms with their cross terms (wavefunction.f90:178-184)

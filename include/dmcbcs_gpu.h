@@ -167,6 +167,14 @@ int dmc_get_precision(const dmc_ctx* ctx, int* precision);
  * fractions; no counterpart in the reference. */
 int dmc_probe_peak(int kind, double* tflops);
 
+/* The mixed path's double-float elementary functions evaluated on the device
+ * for n host inputs (an accuracy check; no counterpart in the reference):
+ * fn 0: in = double a[n], out[2i], out[2i+1] = sin(pi a), cos(pi a);
+ * fn 1: in = uint64 m[n] (0 < m < 2^48), out = sin, cos of 2 pi m 2^-48, the
+ *       Box-Muller angle of ran.f90:74-104;
+ * fn 2: in = double x[n] > 0, out[i] = log x. */
+int dmc_dfmath_eval(int fn, int n, const void* in, double* out);
+
 /* Replaces setbcspar (psislaterbcs.f90:401-419) with optbeta=.false.:
  * new s-wave amplitudes vorb(1:norb). */
 int dmc_set_vorb(dmc_ctx* ctx, const double* vorb, int norb);
