@@ -451,15 +451,17 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
         dmc_destroy(c);
         return DMC_ERR_CUDA;
     }
-    // on-chip layout; two walker CTAs per SM when they fit
-    const int limit = std::min(optin, 227 * 1024) - 64;
+    // on-chip layout; two walker CTAs per SM when they fit (dynamic + static
+    // shared memory + the 1 KB the runtime reserves per block)
+    const int static_smem = std::max(0, walker_static_smem_bytes());
+    const int limit = std::min(optin, 227 * 1024) - 64 - static_smem;
     walker_smem_bytes(c->P, limit, &c->L);
     int per_sm = 1;
     {
         int regs_ok = 2;   // launch bounds give <= 128 registers at 256 threads
         int smem_sm = 0;
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
-        const int need = c->L.total * 8 + 1024;
+        const int need = c->L.total * 8 + static_smem + 1024;
         per_sm = std::max(1, std::min(regs_ok, smem_sm / need));
     }
     c->grid = c->nsm * per_sm;

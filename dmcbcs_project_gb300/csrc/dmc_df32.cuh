@@ -72,12 +72,14 @@ __device__ __forceinline__ df& operator-=(df& a, df b) { return a = a - b; }
 __device__ __forceinline__ df fma(df a, df b, df c) { return a * b + c; }
 using ::fma;   // keep the double overloads visible next to the double-float one
 
-// reciprocal: one Newton step from the FP32 reciprocal of the leading part
+// reciprocal: one Newton step from the FP32 reciprocal of the leading part.
+// For the correctly rounded y = 1/x.hi the residual 1 - x.hi*y is exact in
+// FP32 (one FMA); the low part contributes -x.lo*y.
 __device__ __forceinline__ df rcp(df x)
 {
     const float y = __frcp_rn(x.hi);
-    const df e = df{1.0f, 0.0f} - x * y;          // 1 - x*y, exact to double-float accuracy
-    return fast_two_sum(y, y * e.hi);
+    const float e = fmaf(-x.lo, y, fmaf(-x.hi, y, 1.0f));
+    return fast_two_sum(y, y * e);
 }
 __device__ __forceinline__ df operator/(df a, df b) { return a * rcp(b); }
 

@@ -50,6 +50,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
     }
     double* pb = L.pb_in_smem ? sm + L.pb : a.gscratch + (size_t)blockIdx.x * L.pb_size;
     Ctx<R> c{p, a, L, sm, pb};
+    __shared__ double s_old[9];
     __syncthreads();
     for (int w = blockIdx.x; w < a.nw; w += gridDim.x) {
         double* x = sm + L.x;
@@ -61,6 +62,23 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         if (a.mode == MODE_STEP) {
             // step.f90:59-74: wrap, gaussians, drift, proposal
             s0 = a.in.irn[src] & kMask48;
+            if (threadIdx.x >= kThreads - 32 && threadIdx.x < kThreads - 32 + 9) {
+                // the popped walker's scalars for the step decision (latency hidden behind the proposal)
+                const int k = threadIdx.x - (kThreads - 32);
+                double v;
+                switch (k) {
+                    case 0: v = a.in.psil[src]; break;
+                    case 1: v = a.in.psigl[src]; break;
+                    case 2: v = a.in.d2psi[src]; break;
+                    case 3: v = a.in.d2psig[src]; break;
+                    case 4: v = a.in.v[src]; break;
+                    case 5: v = a.in.vext[src]; break;
+                    case 6: v = a.in.weight[src]; break;
+                    case 7: v = (double)a.in.wt0[src]; break;
+                    default: v = (double)a.in.is[src]; break;
+                }
+                s_old[k] = v;
+            }
             const double* x1 = a.in.x + (size_t)src * n3;
             const double* g1 = a.in.dpsig + (size_t)src * n3;
             for (int e = threadIdx.x; e < n3; e += kThreads) xo[e] = min_image(x1[e], p);
@@ -150,14 +168,14 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         // ---- step1 decision (step.f90:76-226) ----
         __shared__ int s_take_new;
         const double hb = p.hbar;
-        const double* pin_psil = a.in.psil;
-        const double o_psil = pin_psil[src], o_psigl = a.in.psigl[src], o_d2psi = a.in.d2psi[src];
-        const double o_d2psig = a.in.d2psig[src], o_v = a.in.v[src], o_vext = a.in.vext[src];
-        const double o_weight = a.in.weight[src];
-        const float o_wt0 = a.in.wt0[src];
-        const int o_is = a.in.is[src];
-        const double eo = -hb * o_d2psi + o_v;
-        const double en = -hb * h.d2psi + h.v;
+        // the popped walker's scalars, fetched into shared memory before hpsi
+        const double o_psil = s_old[0], o_psigl = s_old[1], o_d2psi = s_old[2];
+        const double o_d2psig = s_old[3], o_v = s_old[4], o_vext = s_old[5];
+        const double o_weight = s_old[6];
+        const float o_wt0 = (float)s_old[7];
+        const int o_is = (int)s_old[8];
+        // psi/psi_G: exactly 1 when the guide function is psi itself (a2 = 0)
+        auto gratio = [](double l, double lg) { return l == lg ? 1.0 : exp(l - lg); };
         const int nr = p.nrand;
         unsigned long long irn_out = lcg_jump(s0, a.jumpA, a.jumpC, nr);
         double* est = a.est + (size_t)w * p.nest * 2;
@@ -201,6 +219,8 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         // scalars of the pushed walker
         const int k = w;   // push order = pop order
         if (threadIdx.x == 0) {
+            const double eo = -hb * o_d2psi + o_v;     // old and new local energies
+            const double en = -hb * h.d2psi + h.v;
             for (int q = 0; q < 2 * p.nest; ++q) est[q] = 0.0;
             auto add = [&](int i1, double val, double wt) {
                 est[2 * (i1 - 1)] = val;
@@ -242,14 +262,14 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                 } else {
                     add(5, 0.0, 1.0);
                 }
-                const double wtg = wt * exp(h.psil - h.psigl) * h.is * (double)o_wt0;
+                const double wtg = wt * gratio(h.psil, h.psigl) * h.is * (double)o_wt0;
                 if (a.opcomp) {
                     add(1, en * nfac, wtg);
                     add(2, (en - h.v) * nfac, wtg);
                     add(3, h.v * nfac, wtg);
                     add(4, h.vext * nfac, wtg);
                     add(6, 0.5 * (ego + egn) * nfac, 1.0);
-                    add(7, exp(h.psil - h.psigl), 1.0);
+                    add(7, gratio(h.psil, h.psigl), 1.0);
                     add(8, h.is * exp(h.psil), 1.0);
                     add(9, exp(h.psigl), 1.0);
                     add(10, 1.0 * h.is, 1.0);
@@ -271,12 +291,12 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                     } else {
                         add(4, 0.0, 1.0);
                     }
-                    const double wtg = wt * exp(h.psil - h.psigl) * h.is * (double)o_wt0;
+                    const double wtg = wt * gratio(h.psil, h.psigl) * h.is * (double)o_wt0;
                     if (a.opcomp) {
                         add(1, en * nfac, wtg);
                         add(2, (en - h.v) * nfac, wtg);
                         add(3, h.v * nfac, wtg);
-                        add(6, exp(h.psil - h.psigl), 1.0);
+                        add(6, gratio(h.psil, h.psigl), 1.0);
                         add(7, h.is * exp(h.psil), 1.0);
                         add(8, exp(h.psigl), 1.0);
                         add(9, 1.0 * h.is, 1.0);
@@ -288,13 +308,13 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                     add(5, 1.0, 1.0);
                 } else {
                     const double wt = exp(-(eo - p.etrial) * p.dt);
-                    const double wtg = wt * exp(o_psil - o_psigl) * o_is * (double)o_wt0;
+                    const double wtg = wt * gratio(o_psil, o_psigl) * o_is * (double)o_wt0;
                     wnew = fmin(p.wtcut, wt * o_weight);
                     if (a.opcomp) {
                         add(1, eo * nfac, wtg);
                         add(2, (eo - o_v) * nfac, wtg);
                         add(3, o_v * nfac, wtg);
-                        add(6, exp(o_psil - o_psigl), 1.0);
+                        add(6, gratio(o_psil, o_psigl), 1.0);
                         add(7, o_is * exp(o_psil), 1.0);
                         add(8, exp(o_psigl), 1.0);
                         add(9, 1.0 * o_is, 1.0);
@@ -471,6 +491,14 @@ int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout)
     SmemLayout L = make_layout(p, limit_bytes);
     if (Lout) *Lout = L;
     return L.total * 8;
+}
+
+int walker_static_smem_bytes()
+{
+    cudaFuncAttributes a64{}, amx{};
+    if (cudaFuncGetAttributes(&a64, walker_kernel<double>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&amx, walker_kernel<df>) != cudaSuccess) return -1;
+    return (int)(a64.sharedSizeBytes > amx.sharedSizeBytes ? a64.sharedSizeBytes : amx.sharedSizeBytes);
 }
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,

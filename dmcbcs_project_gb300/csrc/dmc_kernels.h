@@ -10,6 +10,8 @@ namespace dmc {
 // Bytes of dynamic shared memory of the walker kernel for these sizes; fills
 // the on-chip layout.  limit_bytes is the per-CTA budget.
 int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* L);
+// static shared memory of the walker kernels (the larger of the two), -1 on error
+int walker_static_smem_bytes();
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed = false);

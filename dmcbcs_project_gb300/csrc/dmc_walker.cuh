@@ -108,7 +108,20 @@ __device__ __forceinline__ double min_image(double d, const DevParams& p) { retu
 __device__ __forceinline__ df min_image(df d, const DevParams& p)
 {
     const float m = rintf(d.hi * p.eli_f);
-    return d - p.el_df * m;
+    // |m| <= 2 (positions in or next to the box): m L is exact in double-float
+    const df ml = fabsf(m) <= 2.0f ? df{p.el_df.hi * m, p.el_df.lo * m} : p.el_df * m;
+    return d - ml;
+}
+// |d|^2 of a displacement: one accumulator for the double-float path
+__device__ __forceinline__ double norm2(double a, double b, double c) { return a * a + b * b + c * c; }
+__device__ __forceinline__ df norm2(df a, df b, df c)
+{
+    dfacc s;
+    acc_init(s);
+    acc_madd(s, a, a);
+    acc_madd(s, b, b);
+    acc_madd(s, c, c);
+    return acc_value(s);
 }
 
 // ---- precision traits --------------------------------------------------------
@@ -201,7 +214,7 @@ __device__ __forceinline__ int grid_pos(df r, df scale, int ntab, df& frac)
 __device__ __forceinline__ Lagrange<df> lagrange_df(df t, int idx)
 {
     Lagrange<df> L;
-    const df tm1 = t - df{1.0f, 0.0f}, tm2 = t - df{2.0f, 0.0f}, tp1 = t + df{1.0f, 0.0f};
+    const df tm1 = dfm::add_f(t, -1.0f), tm2 = dfm::add_f(t, -2.0f), tp1 = dfm::add_f(t, 1.0f);
     const df sixth = df{0.16666667163372040f, -4.9670538e-09f};
     const df p = t * tm1, q = tp1 * tm2;
     L.idx = idx;
@@ -301,7 +314,7 @@ __device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double
             const R d0 = min_image(xi[0] - xj[0], p);
             const R d1 = min_image(xi[1] - xj[1], p);
             const R d2 = min_image(xi[2] - xj[2], p);
-            const R rb = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
+            const R rb = dsqrt(norm2(d0, d1, d2));
             const R rinv = rcp(rb);
             J g0 = rzero<J>(), g1 = rzero<J>(), g2 = rzero<J>();
             R f = rzero<R>(), dfr = rzero<R>(), d2f = rzero<R>();
@@ -562,42 +575,47 @@ __device__ void orbital_stage(const Ctx<R>& c)
     // k-vector fields as arrays: lanes with consecutive k read consecutive words
     const R* kv_v = at<R>(sm, c.L.ksoa) + 4 * nk;
     const int* kn = reinterpret_cast<const int*>(at<R>(sm, c.L.ksoa) + 5 * nk);
-    const int items = p.npart * (nq + 1);
+    // item t = part * (nq + 1) + q; (part, q) advance incrementally.  The
+    // product of the three component powers is taken branch-free: a zero
+    // component multiplies by e^0 = (1, 0), which is exact.
+    const int nq1 = nq + 1, items = p.npart * nq1;
+    const int dpart = kThreads / nq1, dq = kThreads % nq1;
+    int part = (int)threadIdx.x / nq1, q = (int)threadIdx.x % nq1;
     for (int t = threadIdx.x; t < items; t += kThreads) {
-        const int part = t / (nq + 1), q = t % (nq + 1);
         const bool up = part < p.nup;
         R* row = up ? U + part * p.ldU : D + (part - p.nup) * p.ldU;
         if (q == 0) {
             row[2 * nq] = up ? kv_v[0] : rone<R>();
             for (int z = 2 * nq + 1; z < p.ldU; ++z) row[z] = rzero<R>();
-            continue;
-        }
-        const R kvq = kv_v[q];
-        R zr = rone<R>(), zi = rzero<R>();
-        bool first = true;
+        } else {
+            const R* eb = E + 2 * (part * 3 * np1);
+            const int n0 = kn[q];
+            const R* e0 = eb + 2 * (n0 < 0 ? -n0 : n0);
+            R zr = e0[0], zi = n0 < 0 ? -e0[1] : e0[1];
 #pragma unroll
-        for (int cc = 0; cc < 3; ++cc) {
-            const int n = kn[cc * nk + q];
-            if (n == 0) continue;
-            const R* e = E + 2 * ((part * 3 + cc) * np1 + (n < 0 ? -n : n));
-            const R er = e[0], ei = n < 0 ? -e[1] : e[1];
-            if (first) {
-                zr = er;
-                zi = ei;
-                first = false;
-            } else {
+            for (int cc = 1; cc < 3; ++cc) {
+                const int n = kn[cc * nk + q];
+                const R* e = eb + 2 * (cc * np1 + (n < 0 ? -n : n));
+                const R er = e[0], ei = n < 0 ? -e[1] : e[1];
                 R nr, ni;
                 cmul(zr, zi, er, ei, nr, ni);
                 zr = nr;
                 zi = ni;
             }
+            if (up) {
+                const R kvq = kv_v[q];
+                row[2 * q - 2] = kvq * zr;
+                row[2 * q - 1] = kvq * zi;
+            } else {
+                row[2 * q - 2] = zr;
+                row[2 * q - 1] = zi;
+            }
         }
-        if (up) {
-            row[2 * q - 2] = kvq * zr;
-            row[2 * q - 1] = kvq * zi;
-        } else {
-            row[2 * q - 2] = zr;
-            row[2 * q - 1] = zi;
+        part += dpart;
+        q += dq;
+        if (q >= nq1) {
+            q -= nq1;
+            ++part;
         }
     }
     // unpaired plane waves: up columns ndn.., down rows nup.., zero corner
@@ -626,6 +644,12 @@ __device__ void orbital_stage(const Ctx<R>& c)
 }
 
 // Stage 3: S[i][j] = sum_q U[i][q] D[j][q] + beta (psislaterbcs.f90:278,289)
+// A task is one row i and up to kGJ columns j = g, g + ng, ... (ng groups
+// per row): one U read feeds kGJ multiply-adds, lanes with consecutive g
+// read consecutive D rows (conflict-free), and 33 x 7 tasks fill one round
+// of 256 threads at N = 66.  16-byte pair loads over the padded rows (the
+// padding is zero).
+constexpr int kGJ = 5;
 template <class R>
 __device__ void gemm_stage(const Ctx<R>& c)
 {
@@ -636,32 +660,38 @@ __device__ void gemm_stage(const Ctx<R>& c)
     const R* D = at<R>(sm, c.L.D);
     R* S = at<R>(sm, c.L.S);
     const int ldU = p.ldU;
-    // two outputs of one row per thread (shared U row); 16-byte pair loads
-    // over the padded rows (the padding is zero)
-    const int half = (p.ndn + 1) / 2;
-    for (int t = threadIdx.x; t < p.nup * half; t += kThreads) {
-        const int i = t / half, j0 = t % half, j1 = j0 + half;
+    const int ng = (p.ndn + kGJ - 1) / kGJ;
+    for (int t = threadIdx.x; t < p.nup * ng; t += kThreads) {
+        const int i = t / ng, g = t % ng;
         const R* u = U + i * ldU;
-        const R* d0 = D + j0 * ldU;
-        const bool two = j1 < p.ndn;
-        const R* d1 = D + (two ? j1 : j0) * ldU;
-        Acc a0, a1;
-        acc_init(a0);
-        acc_init(a1);
-#pragma unroll 2
-        for (int q = 0; q < ldU; q += 2) {
-            R ua, ub, xa, xb, ya, yb;
-            ld2(u + q, ua, ub);
-            ld2(d0 + q, xa, xb);
-            ld2(d1 + q, ya, yb);
-            acc_madd(a0, ua, xa);
-            acc_madd(a1, ua, ya);
-            acc_madd(a0, ub, xb);
-            acc_madd(a1, ub, yb);
+        const R* d[kGJ];
+        bool ok[kGJ];
+#pragma unroll
+        for (int m = 0; m < kGJ; ++m) {
+            const int j = g + ng * m;
+            ok[m] = j < p.ndn;
+            d[m] = D + (ok[m] ? j : g) * ldU;
         }
-        const R s0 = acc_value(a0), s1 = acc_value(a1);
-        S[i * p.ldS + j0] = s0 + S[i * p.ldS + j0];
-        if (two) S[i * p.ldS + j1] = s1 + S[i * p.ldS + j1];
+        Acc a[kGJ];
+#pragma unroll
+        for (int m = 0; m < kGJ; ++m) acc_init(a[m]);
+        for (int q = 0; q < ldU; q += 2) {
+            R ua, ub;
+            ld2(u + q, ua, ub);
+#pragma unroll
+            for (int m = 0; m < kGJ; ++m) {
+                R xa, xb;
+                ld2(d[m] + q, xa, xb);
+                acc_madd(a[m], ua, xa);
+                acc_madd(a[m], ub, xb);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < kGJ; ++m)
+            if (ok[m]) {
+                R* sij = S + i * p.ldS + g + ng * m;
+                *sij = acc_value(a[m]) + *sij;
+            }
     }
     __syncthreads();
 }
@@ -773,8 +803,15 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
             s_row[buf][pw] = wrow;
         }
         bar2_panel();
+        // keys and both candidate rows in one round of shared-memory reads
         const unsigned h0 = s_kh[buf][0], h1 = s_kh[buf][1], l0 = s_kl[buf][0], l1 = s_kl[buf][1];
         const unsigned r0 = s_row[buf][0], r1 = s_row[buf][1];
+        R ra[B], rb[B];
+#pragma unroll
+        for (int c2 = 0; c2 < B; ++c2) {
+            ra[c2] = s_cand[buf][0][c2];
+            rb[c2] = s_cand[buf][1][c2];
+        }
         const int win = (h1 > h0 || (h1 == h0 && (l1 > l0 || (l1 == l0 && r1 < r0)))) ? 1 : 0;
         if ((win ? h1 : h0) == 0u && (win ? l1 : l0) == 0u) return false;   // no non-zero candidate
         const int pr = (int)(win ? r1 : r0);
@@ -785,7 +822,7 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
         // one multiply per row instead of scaling the pivot row on every thread
         R rr[B];
 #pragma unroll
-        for (int c2 = 0; c2 < B; ++c2) rr[c2] = s_cand[buf][win][c2];
+        for (int c2 = 0; c2 < B; ++c2) rr[c2] = win ? rb[c2] : ra[c2];
         const R pv = rr[c];
         const R pinv = rcp(pv);
 #pragma unroll
@@ -1102,7 +1139,7 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
 {
     const int n = c.p.nd;
     if (c.L.S2 >= 0) {
-        if (n <= 64) return inverse_blocked<R, 1, 8>(c, logdet, sgn);
+        if (n <= 64) return inverse_blocked<R, 1, 6>(c, logdet, sgn);
         if (n <= 128) return inverse_blocked<R, 2, 8>(c, logdet, sgn);
     }
     return inverse_unblocked<R>(c, logdet, sgn);
@@ -1207,10 +1244,12 @@ static_assert(kTA * kTB == 32, "one warp per tile");
 __device__ __forceinline__ float abs_hi(df v) { return fabsf(v.hi); }
 __device__ __forceinline__ float abs_hi(double v) { return (float)fabs(v); }
 
-// one (particle, k vector) item of the drift contraction: the 4 terms
-// (3 drift components, Laplacian) of k vector q (1-based) for particle pt
+// partial contraction of one (particle, k vector) item over the terms
+// k0, k0 + kstep, ...: G (up particle) or H (down particle) for the cos and
+// sin parts of k vector q (1-based)
 template <class R>
-__device__ __forceinline__ void drift_item(const Ctx<R>& c, const float* bound, int pt, int q, R (&out)[4])
+__device__ __forceinline__ void drift_dots(const Ctx<R>& c, const float* bound, int pt, int q, int k0, int kstep,
+                                           R& vc, R& vs)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1219,55 +1258,32 @@ __device__ __forceinline__ void drift_item(const Ctx<R>& c, const float* bound, 
     const R* Si = at<R>(sm, c.L.S);
     const R* ks = at<R>(sm, c.L.ksoa);
     const int nk = p.nk, ld = p.ldS, ldU = p.ldU, qc = 2 * q - 2;
+    const bool up = pt < p.nup;
+    const int j = pt - p.nup;
     typename AccOf<R>::type ac, as;
     bacc bc, bs;
     float sig = 0.0f;
-    const bool up = pt < p.nup;
-    if (up) {
-        if constexpr (is_df<R>::value) {
-            sig = pow2_ceil(4.0f * bound[pt]);
-            bacc_init(bc, sig);
-            bacc_init(bs, sig);
-        } else {
-            acc_init(ac);
-            acc_init(as);
-        }
-        for (int j = 0; j < p.ndn; ++j) {
-            const R sji = Si[j * ld + pt];
-            R dc, ds;
-            ld2(D + j * ldU + qc, dc, ds);
-            if constexpr (is_df<R>::value) {
-                bacc_madd(bc, dc, sji);
-                bacc_madd(bs, ds, sji);
-            } else {
-                acc_madd(ac, dc, sji);
-                acc_madd(as, ds, sji);
-            }
-        }
+    if constexpr (is_df<R>::value) {
+        sig = up ? pow2_ceil(4.0f * bound[pt]) : pow2_ceil(4.0f * fabsf(ks[4 * nk + q].hi) * 1.001f * bound[p.nd + j]);
+        bacc_init(bc, sig);
+        bacc_init(bs, sig);
     } else {
-        const int j = pt - p.nup;
+        acc_init(ac);
+        acc_init(as);
+    }
+    const int nK = up ? p.ndn : p.nup;
+    for (int kk = k0; kk < nK; kk += kstep) {
+        const R sv = up ? Si[kk * ld + pt] : Si[j * ld + kk];
+        R bcv, bsv;
+        ld2((up ? D : U) + kk * ldU + qc, bcv, bsv);
         if constexpr (is_df<R>::value) {
-            sig = pow2_ceil(4.0f * fabsf(ks[4 * nk + q].hi) * 1.001f * bound[p.nd + j]);
-            bacc_init(bc, sig);
-            bacc_init(bs, sig);
+            bacc_madd(bc, bcv, sv);
+            bacc_madd(bs, bsv, sv);
         } else {
-            acc_init(ac);
-            acc_init(as);
-        }
-        for (int i = 0; i < p.nup; ++i) {
-            const R sji = Si[j * ld + i];
-            R uc, us;
-            ld2(U + i * ldU + qc, uc, us);
-            if constexpr (is_df<R>::value) {
-                bacc_madd(bc, sji, uc);
-                bacc_madd(bs, sji, us);
-            } else {
-                acc_madd(ac, sji, uc);
-                acc_madd(as, sji, us);
-            }
+            acc_madd(ac, bcv, sv);
+            acc_madd(as, bsv, sv);
         }
     }
-    R vc, vs;
     if constexpr (is_df<R>::value) {
         vc = bacc_value(bc, sig);
         vs = bacc_value(bs, sig);
@@ -1275,15 +1291,26 @@ __device__ __forceinline__ void drift_item(const Ctx<R>& c, const float* bound, 
         vc = acc_value(ac);
         vs = acc_value(as);
     }
+}
+
+// the 4 terms (3 drift components, Laplacian) of k vector q (1-based) for
+// particle pt from its contractions vc, vs
+template <class R>
+__device__ __forceinline__ void drift_terms(const Ctx<R>& c, int pt, int q, R vc, R vs, R (&out)[4])
+{
+    const DevParams& p = c.p;
+    double* sm = c.sm;
+    const R* ks = at<R>(sm, c.L.ksoa);
+    const int nk = p.nk, ldU = p.ldU, qc = 2 * q - 2;
     R t, l;
-    if (up) {
+    if (pt < p.nup) {
         R uc, us;
-        ld2(U + pt * ldU + qc, uc, us);
+        ld2(at<R>(sm, c.L.U) + pt * ldU + qc, uc, us);
         t = uc * vs - us * vc;
         l = uc * vc + us * vs;
     } else {
         R dc, ds;
-        ld2(D + (pt - p.nup) * ldU + qc, dc, ds);
+        ld2(at<R>(sm, c.L.D) + (pt - p.nup) * ldU + qc, dc, ds);
         t = vs * dc - vc * ds;
         l = vc * dc + vs * ds;
     }
@@ -1451,17 +1478,26 @@ __device__ bool drift_tiled(const Ctx<R>& c, const float* bound)
         else
             drift_tile<R, false>(c, bound, tau / nqc, tau % nqc, nqc, pbuf);
     }
-    // particles beyond the full blocks: one (particle, k vector) item per
-    // thread, spread over the warps
-    for (int r0 = 0; r0 < ntail; r0 += kThreads) {
-        // item r0 + i of a round goes to lane i / kWarps of warp i % kWarps
-        const int it = r0 + ((int)threadIdx.x & 31) * kWarps + ((int)threadIdx.x >> 5);
-        if (it >= ntail) continue;
-        const int pl = it / nq, q = it % nq + 1;
-        const int pt = pl < tu ? p.nup - tu + pl : p.nup + p.ndn - td + (pl - tu);
-        R o[4];
-        drift_item<R>(c, bound, pt, q, o);
-        for (int z = 0; z < 4; ++z) tbuf[it * 4 + z] = o[z];
+    // particles beyond the full blocks: (particle, k vector) items, 10 per
+    // warp, each contraction split over 3 lanes and added in lane order
+    {
+        const int lane = threadIdx.x & 31, grp = lane / 3, sub = lane % 3;
+        for (int r0 = 0; r0 < ntail; r0 += kWarps * 10) {
+            const int it = r0 + warp * 10 + grp;
+            const bool act = grp < 10 && it < ntail;
+            const int pl = act ? it / nq : 0, q = act ? it % nq + 1 : 1;
+            const int pt = pl < tu ? p.nup - tu + pl : p.nup + p.ndn - td + (pl - tu);
+            R vc = rzero<R>(), vs = rzero<R>();
+            if (act) drift_dots<R>(c, bound, pt, q, sub, 3, vc, vs);
+            const int l0 = min(grp, 9) * 3;
+            const R c1 = shfl_r(vc, l0 + 1), c2 = shfl_r(vc, l0 + 2);
+            const R s1 = shfl_r(vs, l0 + 1), s2 = shfl_r(vs, l0 + 2);
+            if (act && sub == 0) {
+                R o[4];
+                drift_terms<R>(c, pt, q, (vc + c1) + c2, (vs + s1) + s2, o);
+                for (int z = 0; z < 4; ++z) tbuf[it * 4 + z] = o[z];
+            }
+        }
     }
     __syncthreads();
     for (int pt = threadIdx.x; pt < P; pt += kThreads) {
@@ -1935,21 +1971,30 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         sums[7] = ex[1];
         for (int q = 0; q < 5; ++q) more[q] = ex[2 + q];
     }
-    const double u = sums[0] + sums[6] + ulong;
-    const double d2u_j = sums[2] + sums[4];                        // getphi d2u
-    // + one-body and long-range terms with their cross terms (wavefunction.f90:178-184)
-    const double d2u = d2u_j + more[0] + (d2long + more[2]) + 2.0 * (more[1] + more[3] + more[4]);
-    h.u = u;
-    h.d2u = mode == MODE_GETPHI ? d2u_j : d2u;
-    h.v = sums[1] + sums[7];
-    h.vext = sums[7];
-    h.logdet = ok ? logdet : DMC_MINUSHUGE;
-    h.d2phi = ok ? sums[3] : 0.0;
-    h.is = ok ? sgn : 1;
-    h.singular = !ok;
-    h.psil = h.logdet + u;
-    h.d2psi = h.d2phi + d2u + 2.0 * sums[5];
-    if (mode == MODE_GETPHI) h.psil = u;
+    // the scalar results in FP64 on warp 0 only (one FP64 warp instruction
+    // holds the sub-partition's FP64 pipe for ~64 cycles), then shared
+    __shared__ HRes s_h;
+    if (threadIdx.x < 32) {
+        const bool extra = ob || jl;
+        const double u = extra ? sums[0] + sums[6] + ulong : sums[0];
+        const double d2u_j = sums[2] + sums[4];                        // getphi d2u
+        // + one-body and long-range terms with their cross terms (wavefunction.f90:178-184)
+        const double d2u = extra ? d2u_j + more[0] + (d2long + more[2]) + 2.0 * (more[1] + more[3] + more[4]) : d2u_j;
+        h.u = u;
+        h.d2u = mode == MODE_GETPHI ? d2u_j : d2u;
+        h.v = extra ? sums[1] + sums[7] : sums[1];
+        h.vext = sums[7];
+        h.logdet = ok ? logdet : DMC_MINUSHUGE;
+        h.d2phi = ok ? sums[3] : 0.0;
+        h.is = ok ? sgn : 1;
+        h.singular = !ok;
+        h.psil = h.logdet + u;
+        h.d2psi = h.d2phi + d2u + 2.0 * sums[5];
+        if (mode == MODE_GETPHI) h.psil = u;
+        if (threadIdx.x == 0) s_h = h;
+    }
+    __syncthreads();
+    h = s_h;
     if (p.a2 == 0.0 || (mode != MODE_HPSI && mode != MODE_STEP)) {
         h.psigl = h.psil;
         h.d2psig = h.d2psi;
