@@ -857,6 +857,7 @@ template <class R, int B>
 __device__ __forceinline__ R gj_apply(const R* cur, int ld, int i, int j, int k0, int bw, const int (&prow)[B],
                                       const int* rowpos)
 {
+    if (bw == 0) return cur[i * ld + j];   // the first pass only copies
     typename AccOf<R>::type a;
     acc_init(a);
     const int rp = rowpos[i];
@@ -885,15 +886,16 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
     for (int i = threadIdx.x; i < n; i += kThreads) rowpos[i] = n;
     if (threadIdx.x == 0) s_sing = 0;
     __syncthreads();
-    if (warp < kPanelWarps && !gj_panel<R, RPL, B>(A0, ld, n, 0, min(B, n), piv, pvals, rowpos) &&
-        threadIdx.x == 0)
-        s_sing = 1;
-    __syncthreads();
+    // Pass 0 applies no block (it copies S into the second buffer) while the
+    // panel warps factor the first panel there; pass p > 0 applies block p-1
+    // and factors panel p.  One call site of the (unrolled) panel keeps the
+    // kernel's instruction footprint small.
     R* cur = A0;
     R* nxt = A1;
-    for (int k0 = 0; k0 < n; k0 += B) {
+    int k0 = 0, bw = 0;
+    for (;;) {
         if (s_sing) break;
-        const int bw = min(B, n - k0), k1 = k0 + bw, bw1 = min(B, n - k1);
+        const int k1 = k0 + bw, bw1 = min(B, n - k1);
         int prow[B];
 #pragma unroll
         for (int q = 0; q < B; ++q) prow[q] = q < bw ? piv[k0 + q] : 0;
@@ -932,6 +934,9 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
         R* t = cur;
         cur = nxt;
         nxt = t;
+        if (bw1 == 0) break;
+        k0 = k1;
+        bw = bw1;
     }
     const bool sing = s_sing != 0;
     // natural order, sign of the row permutation and of the pivots, log|det|
@@ -1320,21 +1325,25 @@ __device__ __forceinline__ void drift_terms(const Ctx<R>& c, int pt, int q, R vc
     out[3] = -(ks[3 * nk + q] * l);
 }
 
-// one warp tile: particles blk*8 .. blk*8+7 of one spin (DOWN: the down
-// particles, contraction over up), k vectors of chunk qch; writes the
-// tile's per-particle sums to pbuf
-template <class R, bool DOWN>
-__device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, int blk, int qch, int nqc, R* pbuf)
+// one warp tile: particles blk*8 .. blk*8+7 of one spin, k vectors of
+// chunk qch; writes the tile's per-particle sums to pbuf.  Both spins share
+// the code: up (down = false) contracts Sinv columns with D, down contracts
+// Sinv rows with U, and in both cases
+//   t = O_c V_s - O_s V_c,  l = O_c V_c + O_s V_s
+// with O the particle's own orbital row and V the contraction.
+template <class R>
+__device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, bool down, int blk, int qch, int nqc,
+                                           R* pbuf)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
     const R* Si = at<R>(sm, c.L.S);
     const R* ks = at<R>(sm, c.L.ksoa);
-    const R* B = at<R>(sm, DOWN ? c.L.U : c.L.D);     // contraction operand
-    const R* O = at<R>(sm, DOWN ? c.L.D : c.L.U);     // the particles' own orbital rows
+    const R* B = at<R>(sm, down ? c.L.U : c.L.D);     // contraction operand
+    const R* O = at<R>(sm, down ? c.L.D : c.L.U);     // the particles' own orbital rows
     const int nq = p.nk - 1, nk = p.nk, ld = p.ldS, ldU = p.ldU;
     const int lane = threadIdx.x & 31, ai = lane & (kTA - 1), bi = lane / kTA;
-    const int nK = DOWN ? p.nup : p.ndn;
+    const int nK = down ? p.nup : p.ndn;
     int pi[kTR];
 #pragma unroll
     for (int k = 0; k < kTR; ++k) pi[k] = blk * kTA * kTR + ai + kTA * k;
@@ -1348,7 +1357,7 @@ __device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, 
     }
     // bound of the double-float dot products (|D| <= 1, |U[i][q]| <= |v_q|)
     auto sigma = [&](int k, int m) {
-        return DOWN ? pow2_ceil(4.0f * abs_hi(ks[4 * nk + qo[m] / 2 + 1]) * 1.001f * bound[p.nd + pi[k]])
+        return down ? pow2_ceil(4.0f * abs_hi(ks[4 * nk + qo[m] / 2 + 1]) * 1.001f * bound[p.nd + pi[k]])
                     : pow2_ceil(4.0f * bound[pi[k]]);
     };
     typename AccOf<R>::type a64[kTR][kTS][2];
@@ -1367,12 +1376,13 @@ __device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, 
             }
         }
     // up: G[i][q] = sum_j Si[j][i] D[j][q];  down: H[j][q] = sum_i Si[j][i] U[i][q]
-    const R* s0 = DOWN ? Si + pi[0] * ld : Si + pi[0];
-    const int sstride = DOWN ? 1 : ld;
+    // Sinv element (particle pi[k], term kk) at s0 + kk * sstep + k * kTA * pstep
+    const int sstep = down ? 1 : ld, pstep = down ? ld : 1;
+    const R* s0 = Si + pi[0] * pstep;
     for (int kk = 0; kk < nK; ++kk) {
         R sv[kTR];
 #pragma unroll
-        for (int k = 0; k < kTR; ++k) sv[k] = s0[kk * sstride + (DOWN ? kTA * k * ld : kTA * k)];
+        for (int k = 0; k < kTR; ++k) sv[k] = s0[kk * sstep + k * kTA * pstep];
         const R* brow = B + kk * ldU;
 #pragma unroll
         for (int m = 0; m < kTS; ++m) {
@@ -1391,8 +1401,6 @@ __device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, 
         }
     }
     // per particle: sum over this lane's k vectors
-    //   up:   t = U_c G_s - U_s G_c,  l = U_c G_c + U_s G_s
-    //   down: t = H_s D_c - H_c D_s,  l = H_c D_c + H_s D_s
     R ts[kTR][4];
 #pragma unroll
     for (int k = 0; k < kTR; ++k) {
@@ -1419,13 +1427,8 @@ __device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, 
             typename AccOf<R>::type at_, al_;
             acc_init(at_);
             acc_init(al_);
-            if (DOWN) {
-                acc_madd(at_, vs, oc);
-                acc_madd(at_, -vc, os);
-            } else {
-                acc_madd(at_, oc, vs);
-                acc_madd(at_, -os, vc);
-            }
+            acc_madd(at_, oc, vs);
+            acc_madd(at_, -os, vc);
             acc_madd(al_, oc, vc);
             acc_madd(al_, os, vs);
             const R t = acc_value(at_), l = acc_value(al_);
@@ -1447,7 +1450,7 @@ __device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, 
         for (int k = 0; k < kTR; ++k)
 #pragma unroll
             for (int z = 0; z < 4; ++z) ts[k][z] = ts[k][z] + shfl_x(ts[k][z], o);
-    const int pbase = DOWN ? p.nup : 0;
+    const int pbase = down ? p.nup : 0;
     if (bi == 0)
 #pragma unroll
         for (int k = 0; k < kTR; ++k)
@@ -1472,12 +1475,8 @@ __device__ bool drift_tiled(const Ctx<R>& c, const float* bound)
     const int half = warp >= kWarps / 2 ? 1 : 0, hw = warp & (kWarps / 2 - 1);
     const int n = half ? p.ndn : p.nup;        // particles of this spin
     const int nb = n / (kTA * kTR);            // full blocks of 8
-    for (int tau = hw; tau < nb * nqc; tau += kWarps / 2) {
-        if (half)
-            drift_tile<R, true>(c, bound, tau / nqc, tau % nqc, nqc, pbuf);
-        else
-            drift_tile<R, false>(c, bound, tau / nqc, tau % nqc, nqc, pbuf);
-    }
+    for (int tau = hw; tau < nb * nqc; tau += kWarps / 2)
+        drift_tile<R>(c, bound, half != 0, tau / nqc, tau % nqc, nqc, pbuf);
     // particles beyond the full blocks: (particle, k vector) items, 10 per
     // warp, each contraction split over 3 lanes and added in lane order
     {
@@ -1877,9 +1876,11 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         // Jastrow, potential and pair-Laplacian sums in the Jastrow type
         // (double-float on the mixed path: no FP64 shuffle tree)
         block_sum_t<3>(jt, at<J>(sm, c.L.red));
-        su = to_double(jt[0]);
-        sv = to_double(jt[1]);
-        sd2 = to_double(jt[2]);
+        if (threadIdx.x < 32) {   // only warp 0 assembles the scalar results
+            su = to_double(jt[0]);
+            sv = to_double(jt[1]);
+            sd2 = to_double(jt[2]);
+        }
         if (p.ieq) {
             block_sum_t<3>(ss, sm + c.L.red);
             su += ss[0];
