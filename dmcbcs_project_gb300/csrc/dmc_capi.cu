@@ -896,11 +896,15 @@ int dmc_step(dmc_ctx* c, int opcomp)
     a.in = c->st[c->istin].view();
     a.out = c->st[1 - c->istin].view();
     a.est = c->est.p;
+    // DMC without Metropolis keeps every proposal: the weights and estimator
+    // records are computed one thread per walker after the walker kernel
+    a.defer = (c->P.idmc == 1 || c->P.idmc == -2) ? 1 : 0;
     CK(cudaEventRecord(c->ev0, c->stream));
     CK(launch_walker(c->P, a, c->L, grid_for(c, n), c->stream, c->precision == DMC_PREC_MIXED));
+    if (a.defer) CK(launch_step_decide(c->P, a, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2.p, c->wb.p, c->stream));
-    c->launches += 2;
+    c->launches += a.defer ? 3 : 2;
     c->istin = 1 - c->istin;
     return DMC_OK;
 }

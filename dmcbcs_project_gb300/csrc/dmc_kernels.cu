@@ -23,6 +23,133 @@ using walker::warp_sum;
 
 constexpr unsigned long long kMask48 = walker::kMask48;
 
+// Scalar part of one DMC/VMC move (step.f90:76-226): the estimator record
+// est[nest][2] of the pushed walker, its new weight and sign weight.  nn and
+// ol are the proposed and the old walker; take_new is the Metropolis
+// decision (always true for idmc = 1, -2); ejfd = sum |dpsi|^2/m of the
+// pushed walker (idmc = -1, 0).
+struct StepScalars {
+    double psil, psigl, d2psi, d2psig, v, vext;
+    int is;
+};
+__device__ inline void step_decision(const DevParams& p, int opcomp, const StepScalars& nn, const StepScalars& ol,
+                                     double o_weight, float o_wt0, bool take_new, double ejfd, double* est,
+                                     double& wnew_out, float& wt0_out)
+{
+    const double hb = p.hbar;
+    // psi/psi_G: exactly 1 when the guide function is psi itself (a2 = 0)
+    auto gratio = [](double l, double lg) { return l == lg ? 1.0 : exp(l - lg); };
+    const double eo = -hb * ol.d2psi + ol.v;     // old and new local energies
+    const double en = -hb * nn.d2psi + nn.v;
+    for (int q = 0; q < 2 * p.nest; ++q) est[q] = 0.0;
+    auto add = [&](int i1, double val, double wt) {
+        est[2 * (i1 - 1)] = val;
+        est[2 * (i1 - 1) + 1] = wt;
+    };
+    const double nfac = p.nfac;
+    double wnew = o_weight;
+    float wt0new = o_wt0;
+    if (p.idmc == -1 || p.idmc == 0) {
+        if (take_new) {
+            const double ejf = -0.5 * hb * (nn.d2psi - ejfd) + nn.v;
+            add(1, en * nfac, o_weight);
+            add(2, (en - nn.v) * nfac, o_weight);
+            add(3, nn.v * nfac, o_weight);
+            add(4, nn.vext * nfac, o_weight);
+            add(5, ejf * nfac, o_weight);
+            add(6, 1.0, 1.0);
+            wt0new = (float)nn.is;
+        } else {
+            const double ejf = -0.5 * hb * (ol.d2psi - ejfd) + ol.v;
+            add(1, eo * nfac, o_weight);
+            add(2, (eo - ol.v) * nfac, o_weight);
+            add(3, ol.v * nfac, o_weight);
+            add(4, ol.vext * nfac, o_weight);
+            add(5, ejf * nfac, o_weight);
+            add(6, 0.0, 1.0);
+        }
+    } else if (p.idmc == 1 || p.idmc == -2) {
+        const double ego = -hb * ol.d2psig + ol.v;
+        const double egn = -hb * nn.d2psig + nn.v;
+        double wt = exp(-(0.5 * (ego + egn) - p.etrial) * p.dt);
+        wnew = fmin(p.wtcut, wt);
+        if (nn.is != ol.is) {
+            if (p.fn) {
+                wnew = 0.0;
+                wt = 0.0;
+            }
+            add(5, 1.0, 1.0);
+        } else {
+            add(5, 0.0, 1.0);
+        }
+        const double wtg = wt * gratio(nn.psil, nn.psigl) * nn.is * (double)o_wt0;
+        if (opcomp) {
+            add(1, en * nfac, wtg);
+            add(2, (en - nn.v) * nfac, wtg);
+            add(3, nn.v * nfac, wtg);
+            add(4, nn.vext * nfac, wtg);
+            add(6, 0.5 * (ego + egn) * nfac, 1.0);
+            add(7, gratio(nn.psil, nn.psigl), 1.0);
+            add(8, nn.is * exp(nn.psil), 1.0);
+            add(9, exp(nn.psigl), 1.0);
+            add(10, 1.0 * nn.is, 1.0);
+            add(11, wt, 1.0);
+            add(12, wtg, 1.0);
+            add(13, copysign(1.0, wtg), 1.0);
+            add(14, copysign(1.0, wtg), wtg);
+        }
+    } else {   // idmc == 2
+        if (take_new) {
+            double wt = exp(-(0.5 * (eo + en) - p.etrial) * p.dt);
+            wnew = fmin(p.wtcut, wt);
+            if (nn.is != ol.is) {
+                if (p.fn) {
+                    wnew = 0.0;
+                    wt = 0.0;
+                }
+                add(4, 1.0, 1.0);
+            } else {
+                add(4, 0.0, 1.0);
+            }
+            const double wtg = wt * gratio(nn.psil, nn.psigl) * nn.is * (double)o_wt0;
+            if (opcomp) {
+                add(1, en * nfac, wtg);
+                add(2, (en - nn.v) * nfac, wtg);
+                add(3, nn.v * nfac, wtg);
+                add(6, gratio(nn.psil, nn.psigl), 1.0);
+                add(7, nn.is * exp(nn.psil), 1.0);
+                add(8, exp(nn.psigl), 1.0);
+                add(9, 1.0 * nn.is, 1.0);
+                add(10, wt, 1.0);
+                add(11, wtg, 1.0);
+                add(12, copysign(1.0, wtg), 1.0);
+                add(13, copysign(1.0, wtg), wtg);
+            }
+            add(5, 1.0, 1.0);
+        } else {
+            const double wt = exp(-(eo - p.etrial) * p.dt);
+            const double wtg = wt * gratio(ol.psil, ol.psigl) * ol.is * (double)o_wt0;
+            wnew = fmin(p.wtcut, wt * o_weight);
+            if (opcomp) {
+                add(1, eo * nfac, wtg);
+                add(2, (eo - ol.v) * nfac, wtg);
+                add(3, ol.v * nfac, wtg);
+                add(6, gratio(ol.psil, ol.psigl), 1.0);
+                add(7, ol.is * exp(ol.psil), 1.0);
+                add(8, exp(ol.psigl), 1.0);
+                add(9, 1.0 * ol.is, 1.0);
+                add(10, wt, 1.0);
+                add(11, wtg, 1.0);
+                add(12, copysign(1.0, wtg), 1.0);
+                add(13, copysign(1.0, wtg), wtg);
+            }
+            add(5, 0.0, 1.0);
+        }
+    }
+    wnew_out = wnew;
+    wt0_out = wt0new;
+}
+
 // ---------------------------------------------------------------------------
 // The walker kernel: persistent CTAs, one walker per CTA per iteration.
 // ---------------------------------------------------------------------------
@@ -167,15 +294,12 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         }
         // ---- step1 decision (step.f90:76-226) ----
         __shared__ int s_take_new;
-        const double hb = p.hbar;
         // the popped walker's scalars, fetched into shared memory before hpsi
         const double o_psil = s_old[0], o_psigl = s_old[1], o_d2psi = s_old[2];
         const double o_d2psig = s_old[3], o_v = s_old[4], o_vext = s_old[5];
         const double o_weight = s_old[6];
         const float o_wt0 = (float)s_old[7];
         const int o_is = (int)s_old[8];
-        // psi/psi_G: exactly 1 when the guide function is psi itself (a2 = 0)
-        auto gratio = [](double l, double lg) { return l == lg ? 1.0 : exp(l - lg); };
         const int nr = p.nrand;
         unsigned long long irn_out = lcg_jump(s0, a.jumpA, a.jumpC, nr);
         double* est = a.est + (size_t)w * p.nest * 2;
@@ -201,11 +325,8 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
             }
             irn_out = lcg_jump(s0, a.jumpA, a.jumpC, nr + 1);
             __syncthreads();
-        } else if (threadIdx.x == 0) {
-            s_take_new = 1;
         }
-        __syncthreads();
-        const bool take_new = s_take_new != 0;
+        const bool take_new = metro ? s_take_new != 0 : true;
         // sum |dpsi|^2/m of the pushed walker for the Jackson-Feenberg energy
         double ejfd[1] = {0.0};
         if (p.idmc == -1 || p.idmc == 0) {
@@ -219,113 +340,14 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         // scalars of the pushed walker
         const int k = w;   // push order = pop order
         if (threadIdx.x == 0) {
-            const double eo = -hb * o_d2psi + o_v;     // old and new local energies
-            const double en = -hb * h.d2psi + h.v;
-            for (int q = 0; q < 2 * p.nest; ++q) est[q] = 0.0;
-            auto add = [&](int i1, double val, double wt) {
-                est[2 * (i1 - 1)] = val;
-                est[2 * (i1 - 1) + 1] = wt;
-            };
-            const double nfac = p.nfac;
+            const StepScalars nn{h.psil, h.psigl, h.d2psi, h.d2psig, h.v, h.vext, h.is};
+            const StepScalars ol{o_psil, o_psigl, o_d2psi, o_d2psig, o_v, o_vext, o_is};
             double wnew = o_weight;
             float wt0new = o_wt0;
-            if (p.idmc == -1 || p.idmc == 0) {
-                if (take_new) {
-                    const double ejf = -0.5 * hb * (h.d2psi - ejfd[0]) + h.v;
-                    add(1, en * nfac, o_weight);
-                    add(2, (en - h.v) * nfac, o_weight);
-                    add(3, h.v * nfac, o_weight);
-                    add(4, h.vext * nfac, o_weight);
-                    add(5, ejf * nfac, o_weight);
-                    add(6, 1.0, 1.0);
-                    wt0new = (float)h.is;
-                } else {
-                    const double ejf = -0.5 * hb * (o_d2psi - ejfd[0]) + o_v;
-                    add(1, eo * nfac, o_weight);
-                    add(2, (eo - o_v) * nfac, o_weight);
-                    add(3, o_v * nfac, o_weight);
-                    add(4, o_vext * nfac, o_weight);
-                    add(5, ejf * nfac, o_weight);
-                    add(6, 0.0, 1.0);
-                }
-            } else if (p.idmc == 1 || p.idmc == -2) {
-                const double ego = -hb * o_d2psig + o_v;
-                const double egn = -hb * h.d2psig + h.v;
-                double wt = exp(-(0.5 * (ego + egn) - p.etrial) * p.dt);
-                wnew = fmin(p.wtcut, wt);
-                if (h.is != o_is) {
-                    if (p.fn) {
-                        wnew = 0.0;
-                        wt = 0.0;
-                    }
-                    add(5, 1.0, 1.0);
-                } else {
-                    add(5, 0.0, 1.0);
-                }
-                const double wtg = wt * gratio(h.psil, h.psigl) * h.is * (double)o_wt0;
-                if (a.opcomp) {
-                    add(1, en * nfac, wtg);
-                    add(2, (en - h.v) * nfac, wtg);
-                    add(3, h.v * nfac, wtg);
-                    add(4, h.vext * nfac, wtg);
-                    add(6, 0.5 * (ego + egn) * nfac, 1.0);
-                    add(7, gratio(h.psil, h.psigl), 1.0);
-                    add(8, h.is * exp(h.psil), 1.0);
-                    add(9, exp(h.psigl), 1.0);
-                    add(10, 1.0 * h.is, 1.0);
-                    add(11, wt, 1.0);
-                    add(12, wtg, 1.0);
-                    add(13, copysign(1.0, wtg), 1.0);
-                    add(14, copysign(1.0, wtg), wtg);
-                }
-            } else {   // idmc == 2
-                if (take_new) {
-                    double wt = exp(-(0.5 * (eo + en) - p.etrial) * p.dt);
-                    wnew = fmin(p.wtcut, wt);
-                    if (h.is != o_is) {
-                        if (p.fn) {
-                            wnew = 0.0;
-                            wt = 0.0;
-                        }
-                        add(4, 1.0, 1.0);
-                    } else {
-                        add(4, 0.0, 1.0);
-                    }
-                    const double wtg = wt * gratio(h.psil, h.psigl) * h.is * (double)o_wt0;
-                    if (a.opcomp) {
-                        add(1, en * nfac, wtg);
-                        add(2, (en - h.v) * nfac, wtg);
-                        add(3, h.v * nfac, wtg);
-                        add(6, gratio(h.psil, h.psigl), 1.0);
-                        add(7, h.is * exp(h.psil), 1.0);
-                        add(8, exp(h.psigl), 1.0);
-                        add(9, 1.0 * h.is, 1.0);
-                        add(10, wt, 1.0);
-                        add(11, wtg, 1.0);
-                        add(12, copysign(1.0, wtg), 1.0);
-                        add(13, copysign(1.0, wtg), wtg);
-                    }
-                    add(5, 1.0, 1.0);
-                } else {
-                    const double wt = exp(-(eo - p.etrial) * p.dt);
-                    const double wtg = wt * gratio(o_psil, o_psigl) * o_is * (double)o_wt0;
-                    wnew = fmin(p.wtcut, wt * o_weight);
-                    if (a.opcomp) {
-                        add(1, eo * nfac, wtg);
-                        add(2, (eo - o_v) * nfac, wtg);
-                        add(3, o_v * nfac, wtg);
-                        add(6, gratio(o_psil, o_psigl), 1.0);
-                        add(7, o_is * exp(o_psil), 1.0);
-                        add(8, exp(o_psigl), 1.0);
-                        add(9, 1.0 * o_is, 1.0);
-                        add(10, wt, 1.0);
-                        add(11, wtg, 1.0);
-                        add(12, copysign(1.0, wtg), 1.0);
-                        add(13, copysign(1.0, wtg), wtg);
-                    }
-                    add(5, 0.0, 1.0);
-                }
-            }
+            // idmc = 1, -2: weights and estimators in step_decide_kernel, one
+            // thread per walker after this kernel
+            if (!a.defer)
+                step_decision(p, a.opcomp, nn, ol, o_weight, o_wt0, take_new, ejfd[0], est, wnew, wt0new);
             DevStack o = a.out;
             if (take_new) {
                 o.psil[k] = h.psil;
@@ -344,8 +366,10 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                 o.vext[k] = o_vext;
                 o.is[k] = o_is;
             }
-            o.weight[k] = wnew;
-            o.wt0[k] = wt0new;
+            if (!a.defer) {
+                o.weight[k] = wnew;
+                o.wt0[k] = wt0new;
+            }
             o.irn[k] = irn_out;
             o.psil0[k] = a.in.psil0[src];
             o.psigl0[k] = a.in.psigl0[src];
@@ -365,6 +389,36 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         }
         __syncthreads();
     }
+}
+
+// ---------------------------------------------------------------------------
+// Deferred step decision for idmc = 1, -2 (every proposal is kept): one
+// thread per pushed walker k computes its weight, sign weight and estimator
+// record from its new scalars (written by the walker kernel) and the popped
+// walker's old ones.
+// ---------------------------------------------------------------------------
+__global__ void step_decide_kernel(const __grid_constant__ DevParams p, const __grid_constant__ KernelArgs a)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.nw) return;
+    const int src = a.nw - 1 - k;
+    const StepScalars nn{a.out.psil[k], a.out.psigl[k], a.out.d2psi[k], a.out.d2psig[k], a.out.v[k], a.out.vext[k],
+                         a.out.is[k]};
+    const StepScalars ol{a.in.psil[src], a.in.psigl[src], a.in.d2psi[src], a.in.d2psig[src], a.in.v[src],
+                         a.in.vext[src], a.in.is[src]};
+    double wnew;
+    float wt0new;
+    step_decision(p, a.opcomp, nn, ol, a.in.weight[src], a.in.wt0[src], true, 0.0, a.est + (size_t)k * p.nest * 2,
+                  wnew, wt0new);
+    a.out.weight[k] = wnew;
+    a.out.wt0[k] = wt0new;
+}
+
+cudaError_t launch_step_decide(const DevParams& p, const KernelArgs& a, cudaStream_t st)
+{
+    if (a.nw <= 0) return cudaSuccess;
+    step_decide_kernel<<<(a.nw + 127) / 128, 128, 0, st>>>(p, a);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

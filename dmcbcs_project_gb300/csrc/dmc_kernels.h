@@ -54,6 +54,10 @@ cudaError_t launch_ops_enk(const DevParams& p, const OpsDev& o, const KVecDev* k
 cudaError_t launch_ops_reduce(const OpsDev& o, int n, const DevStack& s, const int* hg, const int* hd,
                               const double* sv, const double* tk, double* sums, cudaStream_t st);
 
+// deferred step decision (idmc = 1, -2): weights and estimator records of
+// the pushed walkers after a MODE_STEP walker launch with a.defer set
+cudaError_t launch_step_decide(const DevParams& p, const KernelArgs& a, cudaStream_t st);
+
 // FMA throughput of the FP64 (kind 0) or FP32 (kind 1) pipe, TFLOP/s
 cudaError_t probe_fma_peak(int kind, int nsm, double* tflops);
 
