@@ -122,6 +122,21 @@ struct dmc_ctx {
     StackBufs st[2];
     int istin = 0;
     int n = 0;
+    // walker count on the device during generations: pop = {n slot 0, n slot 1,
+    // error flags (bit 0 died out, bit 1 overflow), population-control flag};
+    // popf = {population-control factor}; psteps counts walker-steps
+    DevBuf<int> pop;
+    DevBuf<double> popf;
+    DevBuf<unsigned long long> psteps;
+    int pcur = 0;          // slot of the current count
+    bool n_stale = false;  // the device count leads (host n out of date)
+    // captured generations by (stack, count slot) parity, valid while the
+    // parameters, launch arguments and precision match the capture
+    cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int gnl[2][2] = {{0, 0}, {0, 0}};
+    DevParams gP;
+    KernelArgs gA;
+    int gprec = -1;
     DevBuf<double> est;
     DevBuf<int> counts, offs, status;
     DevBuf<unsigned long long> irn1, wtisto;
@@ -157,6 +172,25 @@ int fail(dmc_ctx* c, int code, const std::string& msg)
 {
     if (c) c->err = msg;
     return code;
+}
+
+// Bring the host walker count up to date after generations that counted on
+// the device; reports a population that died out or overflowed the stack.
+int sync_n(dmc_ctx* c)
+{
+    if (!c->n_stale) return DMC_OK;
+    int h[4] = {0, 0, 0, 0};
+    if (cudaMemcpyAsync(h, c->pop.p, sizeof h, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return fail(c, DMC_ERR_CUDA, "walker count");
+    c->n = h[c->pcur];
+    c->n_stale = false;
+    if (h[2]) {
+        cudaMemsetAsync(c->pop.p + 2, 0, sizeof(int), c->stream);
+        if (h[2] & 2) return fail(c, DMC_ERR_OVERFLOW, "stack overflow in branch");
+        return fail(c, DMC_ERR_EMPTY, "population died out");
+    }
+    return DMC_OK;
 }
 
 int cuda_fail(dmc_ctx* c, cudaError_t e, const char* where)
@@ -482,7 +516,8 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     if (c->st[0].alloc(c->cap, c->n3) || c->st[1].alloc(c->cap, c->n3) || c->est.alloc((size_t)c->cap * nest * 2) ||
         c->counts.alloc(c->cap) || c->offs.alloc(c->cap + 1) || c->irn1.alloc(c->cap) ||
         c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(DMC_NEST_MAX) || c->vb2.alloc(DMC_NEST_MAX) ||
-        c->wb.alloc(DMC_NEST_MAX) || c->status.alloc(1)) {
+        c->wb.alloc(DMC_NEST_MAX) || c->status.alloc(1) || c->pop.alloc(4) || c->popf.alloc(1) ||
+        c->psteps.alloc(1)) {
         dmc_destroy(c);
         return DMC_ERR_NOMEM;
     }
@@ -491,7 +526,10 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     cudaMemset(c->vb2.p, 0, DMC_NEST_MAX * sizeof(double));
     cudaMemset(c->wb.p, 0, DMC_NEST_MAX * sizeof(double));
     cudaMemset(c->status.p, 0, sizeof(int));
-    e = cudaDeviceSynchronize();
+    cudaMemset(c->pop.p, 0, 4 * sizeof(int));
+    cudaMemset(c->psteps.p, 0, sizeof(unsigned long long));
+    e = prepare_walker(c->L);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         dmc_destroy(c);
         return DMC_ERR_CUDA;
@@ -511,6 +549,9 @@ int dmc_destroy(dmc_ctx* c)
     c->vb2.release(); c->wb.release(); c->bx.release(); c->bpsil.release(); c->bdpsi.release();
     c->bd2psi.release(); c->bv.release(); c->bvext.release(); c->bpsigl.release(); c->bdpsig.release();
     c->bd2psig.release(); c->bsinv.release(); c->bis.release(); c->flush.release();
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+            if (c->gexec[i][j]) cudaGraphExecDestroy(c->gexec[i][j]);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -679,6 +720,7 @@ int dmc_init_walkers(dmc_ctx* c)
     CK(cudaMemcpy(s.psigl0.p, Z.data(), nw * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(s.irn.p, irn.data(), nw * sizeof(unsigned long long), cudaMemcpyHostToDevice));
     c->n = nw;
+    c->n_stale = false;
     return DMC_OK;
 }
 
@@ -697,12 +739,17 @@ int dmc_load_walkers(dmc_ctx* c, const dmc_walkers* w)
     for (int k = 0; k < n; ++k) irn[k] = (unsigned long long)w->irn[k];
     CK(cudaMemcpy(s.irn.p, irn.data(), n * sizeof(unsigned long long), cudaMemcpyHostToDevice));
     c->n = n;
+    c->n_stale = false;
     return DMC_OK;
 }
 
 int dmc_save_walkers(dmc_ctx* c, const char* path, double tau)
 {
     if (!c || !path) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     const int n = c->n;
     const size_t n3 = (size_t)c->n3;
     std::vector<double> x(std::max<size_t>(1, n * n3)), w(n + 1), pl(n + 1), pg(n + 1);
@@ -763,6 +810,10 @@ int dmc_restore_walkers(dmc_ctx* c, const char* path, double* tau)
 int dmc_num_walkers(dmc_ctx* c, int* n)
 {
     if (!c || !n) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     *n = c->n;
     return DMC_OK;
 }
@@ -770,6 +821,10 @@ int dmc_num_walkers(dmc_ctx* c, int* n)
 int dmc_get_walkers(dmc_ctx* c, dmc_walkers* w)
 {
     if (!c || !w) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     if (w->n < c->n) {
         w->n = c->n;
         return fail(c, DMC_ERR_INVALID, "walker arrays too small");
@@ -818,6 +873,10 @@ static int reverse_stacks(dmc_ctx* c)
 int dmc_initial_eval(dmc_ctx* c, double* sums)
 {
     if (!c) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     const int n = c->n;
     StackBufs& s = c->st[c->istin];
     int rc = run_eval(c, MODE_HPSI, n, s.x.p, s.psil.p, s.is.p, s.dpsi.p, s.d2psi.p, s.v.p, s.vext.p, s.psigl.p,
@@ -887,6 +946,10 @@ int dmc_initial_eval(dmc_ctx* c, double* sums)
 int dmc_step(dmc_ctx* c, int opcomp)
 {
     if (!c) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     const int n = c->n;
     if (n == 0) return fail(c, DMC_ERR_EMPTY, "no walkers");
     KernelArgs a = base_args(c);
@@ -922,6 +985,10 @@ int dmc_last_step_ms(dmc_ctx* c, double* ms)
 int dmc_branch(dmc_ctx* c, double factor)
 {
     if (!c) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     const int n = c->n;
     StackBufs& in = c->st[c->istin];
     StackBufs& out = c->st[1 - c->istin];
@@ -936,31 +1003,88 @@ int dmc_branch(dmc_ctx* c, double factor)
     c->istin = 1 - c->istin;
     if (total > c->cap) {
         c->n = c->cap;
+        c->n_stale = false;
         return fail(c, DMC_ERR_OVERFLOW, "stack overflow in branch");
     }
     c->n = total;
+    c->n_stale = false;
+    return DMC_OK;
+}
+
+// One generation enqueued with the walker count on the device (no host
+// round trip): the move of every walker, its weights and estimator sums,
+// the branch (DMC) and the population control of dmcbcs.f90 as a
+// conditional second pass.  The stack and count slots swap a fixed number
+// of times, so the same launch sequence can be captured as a graph.
+static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch)
+{
+    if (!c->n_stale) {   // the host count is current: hand it to the device
+        CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->n_stale = true;
+    }
+    int nl = 0;
+    KernelArgs a = base_args(c);
+    a.mode = MODE_STEP;
+    a.nw = c->cap;                    // bound; the count is read from a.pn
+    a.pn = c->pop.p + c->pcur;
+    a.opcomp = opcomp ? 1 : 0;
+    a.in = c->st[c->istin].view();
+    a.out = c->st[1 - c->istin].view();
+    a.est = c->est.p;
+    a.defer = (c->P.idmc == 1 || c->P.idmc == -2) ? 1 : 0;
+    // the move itself, for dmc_last_step_ms (in a capture the records become
+    // external event nodes of the graph)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(c->stream, &cap));
+    const unsigned evflags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    CK(cudaEventRecordWithFlags(c->ev0, c->stream, evflags));
+    CK(launch_walker(c->P, a, c->L, c->grid, c->stream, c->precision == DMC_PREC_MIXED));
+    ++nl;
+    if (a.defer) {
+        CK(launch_step_decide(c->P, a, c->stream));
+        ++nl;
+    }
+    CK(cudaEventRecordWithFlags(c->ev1, c->stream, evflags));
+    CK(launch_estimators(c->est.p, 0, c->P.nest, c->vb.p, c->vb2.p, c->wb.p, c->stream, a.pn, c->psteps.p));
+    ++nl;
+    c->istin = 1 - c->istin;
+    int* pop = c->pop.p;
+    auto branch = [&](const int* need, const double* fac) -> int {
+        CK(launch_branch_dev(c->st[c->istin].view(), c->st[1 - c->istin].view(), pop + c->pcur, pop + (1 - c->pcur),
+                             need, fac, pop + 2, c->n3, c->cap, c->nsm, c->counts.p, c->offs.p, c->irn1.p,
+                             c->wtisto.p, c->stream));
+        nl += need ? 4 : 3;
+        if (!need) c->istin = 1 - c->istin;   // the conditional pass leaves the walkers in place
+        c->pcur = 1 - c->pcur;
+        return DMC_OK;
+    };
+    const int idmc = c->rd.idmc;
+    if (idmc > 0 || idmc == -2) {
+        const int rc = branch(nullptr, nullptr);
+        if (rc) return rc;
+    }
+    CK(launch_popctl(pop + c->pcur, (double)c->rd.nwalk, c->rd.popup, c->rd.popdn, pop + 3, c->popf.p, pop + 2,
+                     c->stream));
+    ++nl;
+    const int rc = branch(pop + 3, c->popf.p);
+    if (rc) return rc;
+    c->launches += nl;
+    if (nlaunch) *nlaunch = nl;
     return DMC_OK;
 }
 
 int dmc_generation(dmc_ctx* c, int opcomp, int* nt)
 {
     if (!c) return DMC_ERR_INVALID;
-    int rc = dmc_step(c, opcomp);
+    int rc = gen_async(c, opcomp, nullptr);
     if (rc) return rc;
-    const int idmc = c->rd.idmc;
-    if (idmc > 0 || idmc == -2) {
-        rc = dmc_branch(c, 1.0);
-        if (rc) return rc;
+    // the count (and any error of the generation) comes back only on request
+    if (nt) {
+        rc = sync_n(c);
+        *nt = c->n;
     }
-    const int n = c->n;
-    const double nw = c->rd.nwalk;
-    if (n > c->rd.popup * nw || n < c->rd.popdn * nw) {
-        if (n == 0) return fail(c, DMC_ERR_EMPTY, "population died out");
-        rc = dmc_branch(c, 1.0 * c->rd.nwalk / n);
-        if (rc) return rc;
-    }
-    if (nt) *nt = c->n;
-    return DMC_OK;
+    return rc;
 }
 
 int dmc_zero_estimators(dmc_ctx* c)
@@ -1248,6 +1372,10 @@ int dmc_zero_operators(dmc_ctx* c)
 int dmc_add_operators(dmc_ctx* c)
 {
     if (!c) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     auto& O = c->ops;
     if (!O.on) return fail(c, DMC_ERR_INVALID, "operators are not set up");
     const int n = c->n;
@@ -1464,6 +1592,10 @@ int dmc_sr_configure(dmc_ctx* c, int opt_jastrow, int opt_det)
 int dmc_sr_accumulate(dmc_ctx* c, int64_t* nsamples)
 {
     if (!c) return DMC_ERR_INVALID;
+    if (c) {
+        const int rs = sync_n(c);
+        if (rs) return rs;
+    }
     int rc = sr_buffers(c);
     if (rc) return rc;
     const int n = c->n, np = sr_nparm(c);
@@ -1604,35 +1736,97 @@ int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, i
                           double* device_ms, int64_t* launches)
 {
     if (!c || ngen < 0) return DMC_ERR_INVALID;
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    int rc = sync_n(c);
+    if (rc) return rc;
+    if (c->n == 0) return fail(c, DMC_ERR_EMPTY, "no walkers");
     if (flush_l2) {
         int l2 = 0;
         cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
         const size_t fb = std::max<size_t>((size_t)2 * l2, 64u << 20);
         CK(c->flush.alloc(fb));
     }
-    double total = 0.0;
-    int64_t steps = 0, l0 = 0, lsum = 0;
-    int rc = DMC_OK;
+    CK(cudaMemsetAsync(c->psteps.p, 0, sizeof(unsigned long long), c->stream));
+    // Each generation is a captured graph, one per (stack, count-slot)
+    // parity at its start; the timed region of generation g lies between
+    // events ev[2g] and ev[2g+1] (the L2 flush before it is not timed).
+    std::vector<cudaEvent_t> ev(2 * (size_t)ngen, nullptr);
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    {
+        // drop the captured generations when anything they baked in changed
+        const KernelArgs A = base_args(c);
+        if (c->gprec != c->precision || std::memcmp(&c->gP, &c->P, sizeof c->P) != 0 ||
+            std::memcmp(&c->gA, &A, sizeof A) != 0) {
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    if (c->gexec[i][j]) {
+                        cudaGraphExecDestroy(c->gexec[i][j]);
+                        c->gexec[i][j] = nullptr;
+                    }
+            std::memcpy(&c->gP, &c->P, sizeof c->P);
+            std::memcpy(&c->gA, &A, sizeof A);
+            c->gprec = c->precision;
+        }
+    }
+    int64_t lsum = 0;
+    // the host count goes to the device once, before any capture
+    CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->n_stale = true;
     for (int g = 0; g < ngen && rc == DMC_OK; ++g) {
         if (flush_l2) CK(cudaMemsetAsync(c->flush.p, g & 0xff, c->flush.n, c->stream));
-        steps += c->n;
-        l0 = c->launches;
-        CK(cudaEventRecord(e0, c->stream));
-        int nt = 0;
-        rc = dmc_generation(c, (g == ngen - 1) ? opcomp_last : 0, &nt);
-        CK(cudaEventRecord(e1, c->stream));
-        CK(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
-        total += ms;
-        lsum += c->launches - l0;
+        const bool last = (g == ngen - 1) && opcomp_last;
+        if (last) {
+            // estimator-complete generation: launched directly
+            CK(cudaEventRecord(ev[2 * g], c->stream));
+            int nl = 0;
+            rc = gen_async(c, opcomp_last, &nl);
+            lsum += nl;
+            CK(cudaEventRecord(ev[2 * g + 1], c->stream));
+            continue;
+        }
+        const int pi = c->istin, pc = c->pcur;
+        if (!c->gexec[pi][pc]) {
+            cudaGraph_t graph = nullptr;
+            const int64_t l0 = c->launches;
+            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            int nl = 0;
+            rc = gen_async(c, 0, &nl);
+            cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+            if (rc == DMC_OK && ce != cudaSuccess) rc = DMC_ERR_CUDA;
+            if (rc == DMC_OK && cudaGraphInstantiate(&c->gexec[pi][pc], graph, 0) != cudaSuccess) rc = DMC_ERR_CUDA;
+            if (graph) cudaGraphDestroy(graph);
+            // the capture only recorded the launches: restore the parities
+            c->istin = pi;
+            c->pcur = pc;
+            c->launches = l0;
+            c->gnl[pi][pc] = nl;
+            if (rc) break;
+        }
+        CK(cudaEventRecord(ev[2 * g], c->stream));
+        CK(cudaGraphLaunch(c->gexec[pi][pc], c->stream));
+        CK(cudaEventRecord(ev[2 * g + 1], c->stream));
+        // the parity changes of one generation, as in gen_async: the move and
+        // the DMC branch swap the stacks, both branch passes swap the count slots
+        const int idmc = c->rd.idmc;
+        const int nbr = (idmc > 0 || idmc == -2) ? 1 : 0;
+        c->istin = (pi + 1 + nbr) & 1;
+        c->pcur = (pc + nbr + 1) & 1;
+        c->launches += c->gnl[pi][pc];
+        lsum += c->gnl[pi][pc];
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (walker_steps) *walker_steps = steps;
+    CK(cudaStreamSynchronize(c->stream));
+    double total = 0.0;
+    for (int g = 0; g < ngen && rc == DMC_OK; ++g) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ev[2 * g], ev[2 * g + 1]));
+        total += ms;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    unsigned long long steps = 0;
+    CK(cudaMemcpy(&steps, c->psteps.p, sizeof steps, cudaMemcpyDeviceToHost));
+    const int rs = sync_n(c);
+    if (rc == DMC_OK) rc = rs;
+    if (walker_steps) *walker_steps = (int64_t)steps;
     if (device_ms) *device_ms = total;
     if (launches) *launches = lsum;
     return rc;
@@ -1670,6 +1864,7 @@ int dmc_put_walkers(dmc_ctx* c, const dmc_walkers* w)
     CK(H(s.wt0.p, t.data(), n * sizeof(float)));
     CK(cudaStreamSynchronize(c->stream));
     c->n = n;
+    c->n_stale = false;
     return DMC_OK;
 }
 

@@ -117,6 +117,7 @@ struct KernelArgs {
     int nw;
     int opcomp;
     int defer;                   // MODE_STEP: weights and estimators left to step_decide_kernel
+    const int* pn;               // MODE_STEP: walker count on the device (nullptr: nw)
     const double* xin;
     double *o_psil, *o_dpsi, *o_d2psi, *o_v, *o_vext, *o_psigl, *o_dpsig, *o_d2psig, *o_sinv;
     int* o_is;

@@ -179,12 +179,13 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
     Ctx<R> c{p, a, L, sm, pb};
     __shared__ double s_old[9];
     __syncthreads();
-    for (int w = blockIdx.x; w < a.nw; w += gridDim.x) {
+    const int nw = a.pn ? *a.pn : a.nw;   // the population is counted on the device in a generation
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
         double* x = sm + L.x;
         double* xo = sm + L.xo;
         double* dxs = sm + L.dx;
         double* drift = sm + L.drift;
-        const int src = a.nw - 1 - w;   // MODE_STEP pops from the top
+        const int src = nw - 1 - w;   // MODE_STEP pops from the top
         unsigned long long s0 = 0;
         if (a.mode == MODE_STEP) {
             // step.f90:59-74: wrap, gaussians, drift, proposal
@@ -399,9 +400,10 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
 // ---------------------------------------------------------------------------
 __global__ void step_decide_kernel(const __grid_constant__ DevParams p, const __grid_constant__ KernelArgs a)
 {
+    const int nw = a.pn ? *a.pn : a.nw;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.nw) return;
-    const int src = a.nw - 1 - k;
+    if (k >= nw) return;
+    const int src = nw - 1 - k;
     const StepScalars nn{a.out.psil[k], a.out.psigl[k], a.out.d2psi[k], a.out.d2psig[k], a.out.v[k], a.out.vext[k],
                          a.out.is[k]};
     const StepScalars ol{a.in.psil[src], a.in.psigl[src], a.in.d2psi[src], a.in.d2psig[src], a.in.v[src],
@@ -416,7 +418,7 @@ __global__ void step_decide_kernel(const __grid_constant__ DevParams p, const __
 
 cudaError_t launch_step_decide(const DevParams& p, const KernelArgs& a, cudaStream_t st)
 {
-    if (a.nw <= 0) return cudaSuccess;
+    if (a.nw <= 0) return cudaSuccess;   // with a.pn, a.nw is the capacity
     step_decide_kernel<<<(a.nw + 127) / 128, 128, 0, st>>>(p, a);
     return cudaGetLastError();
 }
@@ -425,9 +427,12 @@ cudaError_t launch_step_decide(const DevParams& p, const KernelArgs& a, cudaStre
 // Estimator block sums (estimator.f90:72-82): est[n][nest][2] -> valblk,
 // valblk2, wtblk (accumulated), fixed-order tree per estimator.
 // ---------------------------------------------------------------------------
-__global__ void estimator_kernel(const double* est, int n, int nest, double* valblk, double* valblk2, double* wtblk)
+__global__ void estimator_kernel(const double* est, int n, const int* pn, int nest, double* valblk, double* valblk2,
+                                 double* wtblk, unsigned long long* steps)
 {
+    if (pn) n = *pn;
     const int e = blockIdx.x;
+    if (steps && e == 0 && threadIdx.x == 0) *steps += (unsigned long long)n;   // walker-steps of the generation
     double s[3] = {0.0, 0.0, 0.0};
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         const double v = est[((size_t)k * nest + e) * 2], wt = est[((size_t)k * nest + e) * 2 + 1];
@@ -455,11 +460,28 @@ __global__ void estimator_kernel(const double* est, int n, int nest, double* val
 // branch (step.f90:287-315), three passes: copy counts, scan, scatter.
 // The input stack is popped from the top: pop index m = n-1-j.
 // ---------------------------------------------------------------------------
+// Device-count form (BranchDev): n from *pn; with a condition flag the pass
+// branches only when *need is set (population control) and otherwise copies
+// every walker unchanged in place.
+struct BranchDev {
+    const int* pn;          // walkers in the input stack
+    int* pn_out;            // walkers in the output stack (written by the scan)
+    const int* need;        // nullptr: always branch
+    const double* factor;   // weight factor when need is set
+    int* flags;             // bit 1: the output stack overflowed
+};
+
 __global__ void branch_count_kernel(DevStack in, int n, double factor, int* counts,
-                                    unsigned long long* irn1, unsigned long long* wtisto)
+                                    unsigned long long* irn1, unsigned long long* wtisto, BranchDev bd)
 {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= n) return;
+    if (bd.pn) {
+        n = *bd.pn;
+        if (bd.need) {
+            if (!*bd.need) return;   // plain copy pass
+            factor = *bd.factor;
+        }
+    }
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
     const int j = n - 1 - m;
     const double wt = in.weight[j] * factor;
     // ran1 on the walker's own state
@@ -470,12 +492,20 @@ __global__ void branch_count_kernel(DevStack in, int n, double factor, int* coun
     counts[m] = iwt > 0 ? iwt : 0;
     irn1[m] = s1;
     if (iwt >= 0 && iwt < DMC_WTISTO) atomicAdd(&wtisto[iwt], 1ull);
+    }
 }
 
 // single-CTA exclusive scan of counts[0..n) -> offs, total in offs[n]
-__global__ void scan_kernel(const int* counts, int n, int* offs)
+__global__ void scan_kernel(const int* counts, int n, int* offs, int cap, BranchDev bd)
 {
     __shared__ int part[1024];
+    if (bd.pn) {
+        n = *bd.pn;
+        if (bd.need && !*bd.need) {
+            if (threadIdx.x == 0) *bd.pn_out = n;   // plain copy pass
+            return;
+        }
+    }
     const int t = threadIdx.x, T = blockDim.x;
     const int chunk = (n + T - 1) / T;
     const int b = t * chunk, e = min(n, b + chunk);
@@ -495,17 +525,28 @@ __global__ void scan_kernel(const int* counts, int n, int* offs)
         offs[i] = run;
         run += counts[i];
     }
-    if (t == T - 1) offs[n] = part[T - 1];
+    if (t == T - 1) {
+        offs[n] = part[T - 1];
+        if (bd.pn_out) {
+            *bd.pn_out = min(part[T - 1], cap);
+            if (part[T - 1] > cap) atomicOr(bd.flags, 2);
+        }
+    }
 }
 
 // one warp per source walker; copy c (1-based) advanced by c ran2 steps
 __global__ void branch_scatter_kernel(DevStack in, DevStack out, int n, int n3, int cap, const int* counts,
-                                      const int* offs, const unsigned long long* irn1)
+                                      const int* offs, const unsigned long long* irn1, BranchDev bd)
 {
-    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (m >= n) return;
+    if (bd.pn) {
+        n = *bd.pn;
+        if (bd.need && !*bd.need) return;   // no population control this generation
+    }
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < n; m += nwarps) {
     const int j = n - 1 - m;
+
     const int cnt = counts[m];
     const int o0 = offs[m];
     unsigned long long s = irn1[m];
@@ -513,7 +554,7 @@ __global__ void branch_scatter_kernel(DevStack in, DevStack out, int n, int n3, 
     for (int cp = 0; cp < cnt; ++cp) {
         s = (34522712143931ull * s + 55789347517ull) & kMask48;   // ran2 (ran.f90:29-48)
         const int d = o0 + cp;
-        if (d >= cap) return;
+        if (d >= cap) break;
         for (int e = lane; e < n3; e += 32) {
             out.x[(size_t)d * n3 + e] = in.x[(size_t)j * n3 + e];
             out.dpsi[(size_t)d * n3 + e] = in.dpsi[(size_t)j * n3 + e];
@@ -534,6 +575,53 @@ __global__ void branch_scatter_kernel(DevStack in, DevStack out, int n, int n3, 
             out.irn[d] = s;
         }
     }
+    }
+}
+
+// Population-control pass, second half: the branched stack back into the
+// input stack (same order), so the pass leaves the walkers where they were
+// whether or not it branched
+__global__ void stack_copy_kernel(DevStack from, DevStack to, const int* pn, const int* need, int n3)
+{
+    if (!*need) return;
+    const int n = *pn;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += nwarps) {
+        for (int e = lane; e < n3; e += 32) {
+            to.x[(size_t)j * n3 + e] = from.x[(size_t)j * n3 + e];
+            to.dpsi[(size_t)j * n3 + e] = from.dpsi[(size_t)j * n3 + e];
+            to.dpsig[(size_t)j * n3 + e] = from.dpsig[(size_t)j * n3 + e];
+        }
+        if (lane == 0) {
+            to.psil[j] = from.psil[j];
+            to.psigl[j] = from.psigl[j];
+            to.d2psi[j] = from.d2psi[j];
+            to.d2psig[j] = from.d2psig[j];
+            to.v[j] = from.v[j];
+            to.vext[j] = from.vext[j];
+            to.weight[j] = from.weight[j];
+            to.psil0[j] = from.psil0[j];
+            to.psigl0[j] = from.psigl0[j];
+            to.wt0[j] = from.wt0[j];
+            to.is[j] = from.is[j];
+            to.irn[j] = from.irn[j];
+        }
+    }
+}
+
+// Population control of dmcbcs.f90 (after the branch of a generation): a
+// second branch with factor nwalk/n when n left [popdn, popup] * nwalk.
+// One thread: sets *need and *factor for the conditional branch pass;
+// flags bit 0 when the population died out.
+__global__ void popctl_kernel(const int* pn, double nwalk, double popup, double popdn, int* need, double* factor,
+                              int* flags)
+{
+    const int n = *pn;
+    const bool out = n > popup * nwalk || n < popdn * nwalk;
+    if (n == 0) atomicOr(flags, 1);
+    *need = (out && n > 0) ? 1 : 0;
+    *factor = n > 0 ? nwalk / n : 1.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -555,27 +643,52 @@ int walker_static_smem_bytes()
     return (int)(a64.sharedSizeBytes > amx.sharedSizeBytes ? a64.sharedSizeBytes : amx.sharedSizeBytes);
 }
 
+static int g_smem_set_mixed = -1, g_smem_set_fp64 = -1;
+
+cudaError_t prepare_walker(const SmemLayout& L)
+{
+    const int smem = L.total * 8;
+    if (g_smem_set_mixed < smem) {
+        const cudaError_t e = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        g_smem_set_mixed = smem;
+    }
+    if (g_smem_set_fp64 < smem) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        g_smem_set_fp64 = smem;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed)
 {
     const size_t smem = (size_t)L.total * 8;
-    cudaError_t e;
-    if (mixed) {
-        e = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the shared-memory opt-in is set once per size (prepare_walker sets it
+    // before any graph capture)
+    int& have = mixed ? g_smem_set_mixed : g_smem_set_fp64;
+    if (have < (int)smem) {
+        const cudaError_t e = mixed ? cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                           (int)smem)
+                                    : cudaFuncSetAttribute(walker_kernel<double>,
+                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        walker_kernel<df><<<grid, kThreads, smem, st>>>(p, a, L);
-    } else {
-        e = cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        walker_kernel<double><<<grid, kThreads, smem, st>>>(p, a, L);
+        have = (int)smem;
     }
+    if (mixed)
+        walker_kernel<df><<<grid, kThreads, smem, st>>>(p, a, L);
+    else
+        walker_kernel<double><<<grid, kThreads, smem, st>>>(p, a, L);
     return cudaGetLastError();
 }
 
-cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, cudaStream_t st)
+cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, cudaStream_t st,
+                              const int* pn, unsigned long long* steps)
 {
-    if (n <= 0) return cudaSuccess;
-    estimator_kernel<<<nest, 256, 0, st>>>(est, n, nest, vb, vb2, wb);
+    if (n <= 0 && !pn) return cudaSuccess;
+    estimator_kernel<<<nest, 256, 0, st>>>(est, n, pn, nest, vb, vb2, wb, steps);
     return cudaGetLastError();
 }
 
@@ -583,10 +696,30 @@ cudaError_t launch_branch(const DevStack& in, const DevStack& out, int n, int n3
                           int* offs, unsigned long long* irn1, unsigned long long* wtisto, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    branch_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, factor, counts, irn1, wtisto);
-    scan_kernel<<<1, 1024, 0, st>>>(counts, n, offs);
+    const BranchDev none{nullptr, nullptr, nullptr, nullptr, nullptr};
+    branch_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, factor, counts, irn1, wtisto, none);
+    scan_kernel<<<1, 1024, 0, st>>>(counts, n, offs, cap, none);
     const int warps = n;
-    branch_scatter_kernel<<<(warps * 32 + 255) / 256, 256, 0, st>>>(in, out, n, n3, cap, counts, offs, irn1);
+    branch_scatter_kernel<<<(warps * 32 + 255) / 256, 256, 0, st>>>(in, out, n, n3, cap, counts, offs, irn1, none);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_branch_dev(const DevStack& in, const DevStack& out, const int* pn, int* pn_out, const int* need,
+                              const double* dfactor, int* flags, int n3, int cap, int nsm, int* counts, int* offs,
+                              unsigned long long* irn1, unsigned long long* wtisto, cudaStream_t st)
+{
+    const BranchDev bd{pn, pn_out, need, dfactor, flags};
+    branch_count_kernel<<<nsm * 4, 256, 0, st>>>(in, 0, 1.0, counts, irn1, wtisto, bd);
+    scan_kernel<<<1, 1024, 0, st>>>(counts, 0, offs, cap, bd);
+    branch_scatter_kernel<<<nsm * 16, 256, 0, st>>>(in, out, 0, n3, cap, counts, offs, irn1, bd);
+    if (need) stack_copy_kernel<<<nsm * 16, 256, 0, st>>>(out, in, pn_out, need, n3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_popctl(const int* pn, double nwalk, double popup, double popdn, int* need, double* factor,
+                          int* flags, cudaStream_t st)
+{
+    popctl_kernel<<<1, 1, 0, st>>>(pn, nwalk, popup, popdn, need, factor, flags);
     return cudaGetLastError();
 }
 

@@ -10,18 +10,32 @@ namespace dmc {
 // Bytes of dynamic shared memory of the walker kernel for these sizes; fills
 // the on-chip layout.  limit_bytes is the per-CTA budget.
 int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* L);
+// dynamic shared-memory opt-in of both walker kernels for layout L (once,
+// before any graph capture)
+cudaError_t prepare_walker(const SmemLayout& L);
 // static shared memory of the walker kernels (the larger of the two), -1 on error
 int walker_static_smem_bytes();
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed = false);
 
-cudaError_t launch_estimators(const double* est, int n, int nest, double* valblk, double* valblk2, double* wtblk,
-                              cudaStream_t st);
+cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, cudaStream_t st,
+                              const int* pn = nullptr, unsigned long long* steps = nullptr);
 
 cudaError_t launch_branch(const DevStack& in, const DevStack& out, int n, int n3, int cap, double factor,
                           int* counts, int* offs, unsigned long long* irn1, unsigned long long* wtisto,
                           cudaStream_t st);
+// the same with the walker count on the device: *pn walkers in, the count
+// out to *pn_out; with need != nullptr a population-control pass that
+// branches with *dfactor only when *need is set and then copies the result
+// back into `in` (the walkers stay in `in` either way); overflow sets bit 1
+// of *flags
+cudaError_t launch_branch_dev(const DevStack& in, const DevStack& out, const int* pn, int* pn_out, const int* need,
+                              const double* dfactor, int* flags, int n3, int cap, int nsm, int* counts, int* offs,
+                              unsigned long long* irn1, unsigned long long* wtisto, cudaStream_t st);
+// population control decision (dmcbcs.f90): *need, *factor for the next pass
+cudaError_t launch_popctl(const int* pn, double nwalk, double popup, double popdn, int* need, double* factor,
+                          int* flags, cudaStream_t st);
 
 // Single-particle ratios and parameter derivatives (dmc_single.cu)
 cudaError_t launch_bcsone(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x,

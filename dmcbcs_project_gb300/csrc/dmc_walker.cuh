@@ -764,81 +764,93 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
 #pragma unroll
         for (int c = 0; c < B; ++c) v[s][c] = (ok && c < bw) ? A[r * ld + k0 + c] : rzero<R>();
     }
-#pragma unroll
+    // Column steps.  The registers rotate by one column per step, so the
+    // active column is always v[.][0] and the step body is compiled once (a
+    // rolled loop keeps the kernel's instruction footprint small); after B
+    // steps the columns are back in order.
+#pragma unroll 1
     for (int c = 0; c < B; ++c) {
-        if (c >= bw) break;
-        const int buf = c & 1;
-        // this warp's largest |a| among rows not yet pivoted; smallest row on ties
-        unsigned kh[RPL], mh = 0u;
+        if (c < bw) {
+            const int buf = c & 1;
+            // this warp's largest |a| among rows not yet pivoted; smallest row on ties
+            unsigned kh[RPL], mh = 0u;
 #pragma unroll
-        for (int s = 0; s < RPL; ++s) {
-            kh[s] = done[s] ? 0u : mag_hi(v[s][c]);
-            mh = kh[s] > mh ? kh[s] : mh;
-        }
-        const unsigned gh = __reduce_max_sync(0xffffffffu, mh);
-        unsigned gl = 0u;
-        if constexpr (!is_df<R>::value) {
-            unsigned ml = 0u;
+            for (int s = 0; s < RPL; ++s) {
+                kh[s] = done[s] ? 0u : mag_hi(v[s][0]);
+                mh = kh[s] > mh ? kh[s] : mh;
+            }
+            const unsigned gh = __reduce_max_sync(0xffffffffu, mh);
+            unsigned gl = 0u;
+            if constexpr (!is_df<R>::value) {
+                unsigned ml = 0u;
+#pragma unroll
+                for (int s = 0; s < RPL; ++s)
+                    if (!done[s] && kh[s] == gh) {
+                        const unsigned l = mag_lo(v[s][0]);
+                        ml = l > ml ? l : ml;
+                    }
+                gl = __reduce_max_sync(0xffffffffu, ml);
+            }
+            unsigned mine = 0xffffffffu;
+#pragma unroll
+            for (int s = RPL - 1; s >= 0; --s)
+                if (!done[s] && kh[s] == gh && mag_lo(v[s][0]) == gl) mine = (unsigned)(t + 64 * s);
+            const unsigned wrow = __reduce_min_sync(0xffffffffu, mine);
 #pragma unroll
             for (int s = 0; s < RPL; ++s)
-                if (!done[s] && kh[s] == gh) {
-                    const unsigned l = mag_lo(v[s][c]);
-                    ml = l > ml ? l : ml;
-                }
-            gl = __reduce_max_sync(0xffffffffu, ml);
+                if ((unsigned)(t + 64 * s) == wrow)
+#pragma unroll
+                    for (int c2 = 0; c2 < B; ++c2) s_cand[buf][pw][c2] = v[s][c2];
+            if ((t & 31) == 0) {
+                s_kh[buf][pw] = gh;
+                s_kl[buf][pw] = gl;
+                s_row[buf][pw] = wrow;
+            }
+            bar2_panel();
+            // keys and both candidate rows in one round of shared-memory reads
+            const unsigned h0 = s_kh[buf][0], h1 = s_kh[buf][1], l0 = s_kl[buf][0], l1 = s_kl[buf][1];
+            const unsigned r0 = s_row[buf][0], r1 = s_row[buf][1];
+            R ra[B], rb[B];
+#pragma unroll
+            for (int c2 = 0; c2 < B; ++c2) {
+                ra[c2] = s_cand[buf][0][c2];
+                rb[c2] = s_cand[buf][1][c2];
+            }
+            const int win = (h1 > h0 || (h1 == h0 && (l1 > l0 || (l1 == l0 && r1 < r0)))) ? 1 : 0;
+            if ((win ? h1 : h0) == 0u && (win ? l1 : l0) == 0u) return false;   // no non-zero candidate
+            const int pr = (int)(win ? r1 : r0);
+            // Gauss-Jordan step with the unscaled pivot row p and multiplier
+            // m = a_c / p_c per row (m = -1/p_c for the pivot row itself):
+            //   a_c2 <- a_c2 - m p_c2   (pivot row: p_c2 / p_c),
+            //   a_c  <- -m              (pivot row: 1 / p_c)
+            // one multiply per row instead of scaling the pivot row on every thread
+            R rr[B];
+#pragma unroll
+            for (int c2 = 0; c2 < B; ++c2) rr[c2] = win ? rb[c2] : ra[c2];
+            const R pv = rr[0];
+            const R pinv = rcp(pv);
+#pragma unroll
+            for (int s = 0; s < RPL; ++s) {
+                const bool isp = t + 64 * s == pr;
+                const R m = isp ? -pinv : v[s][0] * pinv;
+#pragma unroll
+                for (int c2 = 1; c2 < B; ++c2) v[s][c2] = fms(isp ? rzero<R>() : v[s][c2], m, rr[c2]);
+                v[s][0] = -m;
+                if (isp) done[s] = true;
+            }
+            if (t == 0) {
+                piv[k0 + c] = pr;
+                pvals[k0 + c] = pv;
+                rowpos[pr] = k0 + c;
+            }
         }
-        unsigned mine = 0xffffffffu;
-#pragma unroll
-        for (int s = RPL - 1; s >= 0; --s)
-            if (!done[s] && kh[s] == gh && mag_lo(v[s][c]) == gl) mine = (unsigned)(t + 64 * s);
-        const unsigned wrow = __reduce_min_sync(0xffffffffu, mine);
-#pragma unroll
-        for (int s = 0; s < RPL; ++s)
-            if ((unsigned)(t + 64 * s) == wrow)
-#pragma unroll
-                for (int c2 = 0; c2 < B; ++c2) s_cand[buf][pw][c2] = v[s][c2];
-        if ((t & 31) == 0) {
-            s_kh[buf][pw] = gh;
-            s_kl[buf][pw] = gl;
-            s_row[buf][pw] = wrow;
-        }
-        bar2_panel();
-        // keys and both candidate rows in one round of shared-memory reads
-        const unsigned h0 = s_kh[buf][0], h1 = s_kh[buf][1], l0 = s_kl[buf][0], l1 = s_kl[buf][1];
-        const unsigned r0 = s_row[buf][0], r1 = s_row[buf][1];
-        R ra[B], rb[B];
-#pragma unroll
-        for (int c2 = 0; c2 < B; ++c2) {
-            ra[c2] = s_cand[buf][0][c2];
-            rb[c2] = s_cand[buf][1][c2];
-        }
-        const int win = (h1 > h0 || (h1 == h0 && (l1 > l0 || (l1 == l0 && r1 < r0)))) ? 1 : 0;
-        if ((win ? h1 : h0) == 0u && (win ? l1 : l0) == 0u) return false;   // no non-zero candidate
-        const int pr = (int)(win ? r1 : r0);
-        // Gauss-Jordan step with the unscaled pivot row p and multiplier
-        // m = a_c / p_c per row (m = -1/p_c for the pivot row itself):
-        //   a_c2 <- a_c2 - m p_c2   (pivot row: p_c2 / p_c),
-        //   a_c  <- -m              (pivot row: 1 / p_c)
-        // one multiply per row instead of scaling the pivot row on every thread
-        R rr[B];
-#pragma unroll
-        for (int c2 = 0; c2 < B; ++c2) rr[c2] = win ? rb[c2] : ra[c2];
-        const R pv = rr[c];
-        const R pinv = rcp(pv);
+        // rotate: the next column becomes v[.][0]
 #pragma unroll
         for (int s = 0; s < RPL; ++s) {
-            const bool isp = t + 64 * s == pr;
-            const R m = isp ? -pinv : v[s][c] * pinv;
+            const R f = v[s][0];
 #pragma unroll
-            for (int c2 = 0; c2 < B; ++c2)
-                if (c2 != c) v[s][c2] = fms(isp ? rzero<R>() : v[s][c2], m, rr[c2]);
-            v[s][c] = -m;
-            if (isp) done[s] = true;
-        }
-        if (t == 0) {
-            piv[k0 + c] = pr;
-            pvals[k0 + c] = pv;
-            rowpos[pr] = k0 + c;
+            for (int c2 = 0; c2 < B - 1; ++c2) v[s][c2] = v[s][c2 + 1];
+            v[s][B - 1] = f;
         }
     }
 #pragma unroll
