@@ -347,6 +347,31 @@ def run_gpu(args):
 
     acc = accuracy_vs_fp64(ctxs["mixed"], ctxs["fp64"], sysd.hbar) if len(ctxs) == 2 and rank == 0 else None
 
+    # The N = 132 (66 up / 66 down) system of the mixed-precision benchmark
+    # configuration, 8192 walkers: both paths over a short run (not the
+    # headline; reported beside it)
+    n132 = None
+    if len(ctxs) == 2 and args.n132_steps > 0:
+        s132, r132, _ = configs.workload("n132", nwalk=8192)
+        r132.seed = 17 + 1000003 * rank
+        sub, c132 = {}, {}
+        sub_args = argparse.Namespace(**vars(args))
+        sub_args.steps = args.n132_steps
+        for prec in ("mixed", "fp64"):
+            cx = capi.Context(s132, r132, precision=prec)
+            cx.init_walkers()
+            cx.initial_eval()
+            t = time_path(cx, sub_args, world, local, barrier)
+            sub[prec] = {"value": t["value"], "ms_per_step": t["ms_per_step"], "avg_walkers": t["avg_n"],
+                         "clocks": t["clocks"]}
+            c132[prec] = cx
+        n132 = {"workload": "dmc_n132_66u66d", "walkers": 8192, "steps": args.n132_steps, "unit": UNIT,
+                "mixed": sub["mixed"], "fp64": sub["fp64"], "speedup_vs_fp64": sub["mixed"]["value"] / sub["fp64"]["value"],
+                "accuracy_vs_fp64": accuracy_vs_fp64(c132["mixed"], c132["fp64"], s132.hbar, nmax=256)
+                if rank == 0 else None}
+        for cx in c132.values():
+            cx.close()
+
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -378,6 +403,8 @@ def run_gpu(args):
                                  "clocks": f["clocks"], "roofline": roofline("fp64")}
             line["speedup_vs_fp64"] = r["value"] / f["value"]
             line["accuracy_vs_fp64"] = acc
+        if n132:
+            line["n132"] = n132
         print(json.dumps(line), flush=True)
     for c in ctxs.values():
         c.close()
@@ -400,6 +427,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-walkers", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n132-steps", type=int, default=20,
+                    help="generations of the N = 132, 8192-walker side measurement (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

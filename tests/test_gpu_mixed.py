@@ -26,7 +26,7 @@ def walkers(name, nw, seed):
     return sysd, rund, orc, x
 
 
-@pytest.mark.parametrize("name,nw", [("n14", 64), ("n66", 128), ("p33_30", 32), ("p38_33", 32)])
+@pytest.mark.parametrize("name,nw", [("n14", 64), ("n66", 128), ("p33_30", 32), ("p38_33", 32), ("n132", 16)])
 def test_mixed_hpsi_against_fp64_oracle(name, nw):
     sysd, rund, orc, x = walkers(name, nw, 21)
     ref = orc.hpsi(x)
