@@ -510,6 +510,26 @@ __device__ __forceinline__ void cmul(double ar, double ai, double br, double bi,
     cr = ar * br - ai * bi;
     ci = ar * bi + ai * br;
 }
+// product of two unit-modulus complex numbers (|a|, |b| <= 1 up to rounding):
+// every partial product is below 1 in magnitude, so the bounded accumulator
+// with sigma = 4 applies (6 instead of 12 FP32 instructions per term)
+__device__ __forceinline__ void cmul_unit(double ar, double ai, double br, double bi, double& cr, double& ci)
+{
+    cr = ar * br - ai * bi;
+    ci = ar * bi + ai * br;
+}
+__device__ __forceinline__ void cmul_unit(df ar, df ai, df br, df bi, df& cr, df& ci)
+{
+    bacc r, i;
+    bacc_init(r, 4.0f);
+    bacc_init(i, 4.0f);
+    bacc_madd(r, ar, br);
+    bacc_madd(r, -ai, bi);
+    bacc_madd(i, ar, bi);
+    bacc_madd(i, ai, br);
+    cr = bacc_value(r, 4.0f);
+    ci = bacc_value(i, 4.0f);
+}
 __device__ __forceinline__ void cmul(df ar, df ai, df br, df bi, df& cr, df& ci)
 {
     dfacc r, i;
@@ -561,7 +581,7 @@ __device__ void orbital_stage(const Ctx<R>& c)
         R cr = c1, ci = s1;
         for (int m = 2; m <= p.nmax; ++m) {
             R nr, ni;
-            cmul(cr, ci, c1, s1, nr, ni);
+            cmul_unit(cr, ci, c1, s1, nr, ni);
             cr = nr;
             ci = ni;
             e[2 * m] = cr;
@@ -598,7 +618,7 @@ __device__ void orbital_stage(const Ctx<R>& c)
                 const R* e = eb + 2 * (cc * np1 + (n < 0 ? -n : n));
                 const R er = e[0], ei = n < 0 ? -e[1] : e[1];
                 R nr, ni;
-                cmul(zr, zi, er, ei, nr, ni);
+                cmul_unit(zr, zi, er, ei, nr, ni);
                 zr = nr;
                 zi = ni;
             }
