@@ -224,16 +224,20 @@ __device__ __forceinline__ Lagrange<df> lagrange_df(df t, int idx)
     L.c4 = (p * tp1) * sixth;
     return L;
 }
-// 4-point combination c1 a0 + c2 a1 + c3 a2 + c4 a3 with one lazy accumulator
+// 4-point combination c1 a0 + c2 a1 + c3 a2 + c4 a3: the cubic Lagrange
+// weights on [0, 1) are at most 1.1 in magnitude, so 1.1 sum |a_k| bounds
+// the terms of the bounded accumulator
 __device__ __forceinline__ df lag4(const Lagrange<df>& W, df a0, df a1, df a2, df a3)
 {
-    dfacc s;
-    acc_init(s);
-    acc_madd(s, W.c1, a0);
-    acc_madd(s, W.c2, a1);
-    acc_madd(s, W.c3, a2);
-    acc_madd(s, W.c4, a3);
-    return acc_value(s);
+    const float b = (fabsf(a0.hi) + fabsf(a1.hi)) + (fabsf(a2.hi) + fabsf(a3.hi));
+    const float sg = pow2_ceil(4.0f * 1.13f * b);
+    bacc s;
+    bacc_init(s, sg);
+    bacc_madd(s, W.c1, a0);
+    bacc_madd(s, W.c2, a1);
+    bacc_madd(s, W.c3, a2);
+    bacc_madd(s, W.c4, a3);
+    return bacc_value(s, sg);
 }
 __device__ __forceinline__ Lagrange<float> lagrange_f(float t, int idx)
 {
@@ -1490,14 +1494,33 @@ __device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, 
             if (!okq[m]) continue;
             R oc, os;
             ld2(own + qo[m], oc, os);
-            typename AccOf<R>::type at_, al_;
-            acc_init(at_);
-            acc_init(al_);
-            acc_madd(at_, oc, vs);
-            acc_madd(at_, -os, vc);
-            acc_madd(al_, oc, vc);
-            acc_madd(al_, os, vs);
-            const R t = acc_value(at_), l = acc_value(al_);
+            R t, l;
+            if constexpr (is_df<R>::value) {
+                // |t|, |l| <= |own (cos, sin)| |(vc, vs)|: up |v_q| * colsum,
+                // down 1 * |v_q| * rowsum
+                const float vq = abs_hi(ks[4 * nk + qo[m] / 2 + 1]) * 1.001f;
+                const float sg = down ? sigma(k, m)
+                                      : pow2_ceil(4.0f * fmaxf(1.0f, vq) * bound[pi[k]]);
+                bacc at_, al_;
+                bacc_init(at_, sg);
+                bacc_init(al_, sg);
+                bacc_madd(at_, oc, vs);
+                bacc_madd(at_, -os, vc);
+                bacc_madd(al_, oc, vc);
+                bacc_madd(al_, os, vs);
+                t = bacc_value(at_, sg);
+                l = bacc_value(al_, sg);
+            } else {
+                typename AccOf<R>::type at_, al_;
+                acc_init(at_);
+                acc_init(al_);
+                acc_madd(at_, oc, vs);
+                acc_madd(at_, -os, vc);
+                acc_madd(al_, oc, vc);
+                acc_madd(al_, os, vs);
+                t = acc_value(at_);
+                l = acc_value(al_);
+            }
             const int q1 = qo[m] / 2 + 1;
             acc_madd(sx, ks[q1], t);
             acc_madd(sy, ks[nk + q1], t);
