@@ -278,6 +278,54 @@ def accuracy_vs_fp64(ctx_mixed, ctx_fp64, hbar, nmax=512):
             "drift_rel_err_max": float(dr.max()), "log_psi_abs_err_max": float(np.max(np.abs(a["psil"] - b["psil"])))}
 
 
+# The uneven batch: six systems (N up / N down) in one generation graph,
+# 16384 walkers split over them by seeded weights, plain FP64
+BATCH_SYSTEMS = ["n14", "n38", "n66", "p33_30", "p38_33", "n132"]
+BATCH_WALKERS = 16384
+
+
+def uneven_batch(args, rank):
+    """Batched generations of the six systems with the tuned CTA split, then
+    the same contexts one after another (dmc_timed_generations each), both
+    with the L2 flushed before every generation."""
+    from dmcbcs_project_gb300 import capi, configs
+
+    rng = np.random.default_rng(2024)
+    w = rng.uniform(0.5, 1.5, len(BATCH_SYSTEMS))
+    nws = np.floor(BATCH_WALKERS * w / w.sum()).astype(int)
+    nws[-1] += BATCH_WALKERS - int(nws.sum())
+    ctxs, systems = [], []
+    for i, (name, nw) in enumerate(zip(BATCH_SYSTEMS, nws)):
+        s, r, meta = configs.workload(name, nwalk=int(nw), seed=1234 + i)
+        r.seed = 17 + 1000003 * rank + 7919 * i
+        c = capi.Context(s, r, precision="fp64")
+        c.init_walkers()
+        c.initial_eval()
+        ctxs.append(c)
+        systems.append(f"{meta['nup']}/{meta['ndn']}:{int(nw)}")
+    gens = args.batch_steps
+    with capi.Batch(ctxs) as b:
+        initial = b.grids.tolist()
+        grids, tune_ms = b.tune(3)
+        b.generations(max(args.warmup, 3), opcomp_last=False, flush_l2=True)
+        steps, ms, nl = b.generations(gens, opcomp_last=True, flush_l2=True)
+    seq_steps, seq_ms = 0, 0.0
+    for c in ctxs:
+        c.timed_generations(max(args.warmup, 3), opcomp_last=False, flush_l2=True)
+        st, m, _ = c.timed_generations(gens, opcomp_last=True, flush_l2=True)
+        seq_steps += st
+        seq_ms += m
+    for c in ctxs:
+        c.close()
+    value = steps / (ms * 1e-3)
+    seq = seq_steps / (seq_ms * 1e-3)
+    return {"workload": "uneven_batch_6_systems", "systems": systems, "walkers": BATCH_WALKERS, "precision": "fp64",
+            "steps": gens, "unit": UNIT, "value": value, "ms_per_step": ms / max(gens, 1), "gpu_launches": nl,
+            "grids_tuned": [int(g) for g in grids], "grids_initial": initial, "tune_pass_ms": tune_ms,
+            "sequential": {"value": seq, "ms_per_step": seq_ms / max(gens, 1)},
+            "speedup_vs_sequential": value / seq}
+
+
 def run_gpu(args):
     import torch
 
@@ -372,6 +420,8 @@ def run_gpu(args):
         for cx in c132.values():
             cx.close()
 
+    batch = uneven_batch(args, rank) if args.batch_steps > 0 else None
+
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -405,6 +455,8 @@ def run_gpu(args):
             line["accuracy_vs_fp64"] = acc
         if n132:
             line["n132"] = n132
+        if batch:
+            line["uneven_batch"] = batch
         print(json.dumps(line), flush=True)
     for c in ctxs.values():
         c.close()
@@ -429,6 +481,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n132-steps", type=int, default=20,
                     help="generations of the N = 132, 8192-walker side measurement (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=20,
+                    help="generations of the six-system uneven batch side measurement (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -28,6 +28,8 @@ EXPORTS = [
     "dmc_sr_zero", "dmc_sr_update", "dmc_fort9_write", "dmc_fort9_read", "dmc_save_walkers", "dmc_restore_walkers",
     "dmc_set_operators", "dmc_zero_operators", "dmc_add_operators", "dmc_update_operators", "dmc_get_operators",
     "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure", "dmc_dfmath_eval",
+    "dmc_batch_create", "dmc_batch_destroy", "dmc_batch_last_error", "dmc_batch_set_grids", "dmc_batch_get_grids",
+    "dmc_batch_plan", "dmc_batch_tune", "dmc_batch_generations",
 ]
 
 PREC_FP64 = 0
@@ -118,6 +120,16 @@ def load(path=LIB_PATH):
     L.dmc_sr_update.argtypes = [vp, C.c_double, C.c_double, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.dmc_branch_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(abi.DevStack),
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
+    L.dmc_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
+    L.dmc_batch_destroy.argtypes = [vp]
+    L.dmc_batch_last_error.restype = C.c_char_p
+    L.dmc_batch_last_error.argtypes = [vp]
+    L.dmc_batch_set_grids.argtypes = [vp, _ip]
+    L.dmc_batch_get_grids.argtypes = [vp, _ip]
+    L.dmc_batch_plan.argtypes = [C.c_int, _dp, _ip, _ip, _ip, C.c_int, _ip]
+    L.dmc_batch_tune.argtypes = [vp, C.c_int, _ip, C.POINTER(C.c_double)]
+    L.dmc_batch_generations.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     _lib = L
     return L
 
@@ -509,5 +521,74 @@ class Context:
         return ms.value
 
 
-__all__ = ["Context", "DMCError", "load", "EXPORTS", "LIB_PATH", "DMC_NEST_MAX", "fort9_write", "fort9_read",
-           "dfmath_eval"]
+def batch_plan(tau, nw, per_sm, maxgrid, nsm):
+    """The batch tuner's host-only split (dmc_batch_plan): CTAs per system."""
+    ns = len(tau)
+    grids = np.zeros(ns, dtype=np.int32)
+    st = load().dmc_batch_plan(ns, np.ascontiguousarray(tau, dtype=np.float64),
+                               np.ascontiguousarray(nw, dtype=np.int32), np.ascontiguousarray(per_sm, dtype=np.int32),
+                               np.ascontiguousarray(maxgrid, dtype=np.int32), int(nsm), grids)
+    if st != abi.DMC_OK:
+        raise DMCError(st, "dmc_batch_plan")
+    return grids
+
+
+class Batch:
+    """Several contexts (systems of uneven size) advanced together, one CUDA
+    graph per generation (``dmc_batch_create``)."""
+
+    def __init__(self, contexts):
+        L = load()
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c._h.value for c in self.contexts])
+        h = C.c_void_p()
+        st = L.dmc_batch_create(arr, len(self.contexts), C.byref(h))
+        if st != abi.DMC_OK:
+            raise DMCError(st, "dmc_batch_create failed")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().dmc_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st):
+        if st != abi.DMC_OK:
+            msg = load().dmc_batch_last_error(self._h)
+            raise DMCError(st, msg.decode() if msg else "")
+
+    @property
+    def grids(self):
+        g = np.zeros(len(self.contexts), dtype=np.int32)
+        self._check(load().dmc_batch_get_grids(self._h, g))
+        return g
+
+    @grids.setter
+    def grids(self, values):
+        self._check(load().dmc_batch_set_grids(self._h, np.ascontiguousarray(values, dtype=np.int32)))
+
+    def tune(self, rounds=3):
+        """Autotune the CTA split; returns (grids, pass_ms)."""
+        g = np.zeros(len(self.contexts), dtype=np.int32)
+        ms = C.c_double()
+        self._check(load().dmc_batch_tune(self._h, int(rounds), g, C.byref(ms)))
+        return g, ms.value
+
+    def generations(self, ngen, opcomp_last=True, flush_l2=False):
+        """ngen batched generations; returns (walker_steps, device_ms, kernel_launches)."""
+        st, ms, nl = C.c_int64(), C.c_double(), C.c_int64()
+        self._check(load().dmc_batch_generations(self._h, int(ngen), int(bool(opcomp_last)), int(bool(flush_l2)),
+                                                 C.byref(st), C.byref(ms), C.byref(nl)))
+        return st.value, ms.value, nl.value
+
+
+__all__ = ["Context", "Batch", "DMCError", "load", "EXPORTS", "LIB_PATH", "DMC_NEST_MAX", "fort9_write",
+           "fort9_read", "dfmath_eval", "batch_plan"]

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -1016,6 +1017,16 @@ int dmc_branch(dmc_ctx* c, double factor)
 // the branch (DMC) and the population control of dmcbcs.f90 as a
 // conditional second pass.  The stack and count slots swap a fixed number
 // of times, so the same launch sequence can be captured as a graph.
+// The parity changes of one generation, as gen_async makes them: the move
+// and the DMC branch swap the stacks, both branch passes swap the count slots.
+static void advance_parities(dmc_ctx* c)
+{
+    const int idmc = c->rd.idmc;
+    const int nbr = (idmc > 0 || idmc == -2) ? 1 : 0;
+    c->istin = (c->istin + 1 + nbr) & 1;
+    c->pcur = (c->pcur + nbr + 1) & 1;
+}
+
 static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch)
 {
     if (!c->n_stale) {   // the host count is current: hand it to the device
@@ -1805,12 +1816,7 @@ int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, i
         CK(cudaEventRecord(ev[2 * g], c->stream));
         CK(cudaGraphLaunch(c->gexec[pi][pc], c->stream));
         CK(cudaEventRecord(ev[2 * g + 1], c->stream));
-        // the parity changes of one generation, as in gen_async: the move and
-        // the DMC branch swap the stacks, both branch passes swap the count slots
-        const int idmc = c->rd.idmc;
-        const int nbr = (idmc > 0 || idmc == -2) ? 1 : 0;
-        c->istin = (pi + 1 + nbr) & 1;
-        c->pcur = (pc + nbr + 1) & 1;
+        advance_parities(c);
         c->launches += c->gnl[pi][pc];
         lsum += c->gnl[pi][pc];
     }
@@ -1909,6 +1915,475 @@ int dmc_probe_peak(int kind, double* tflops)
     if (cudaGetDevice(&dev) != cudaSuccess) return DMC_ERR_CUDA;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DMC_ERR_CUDA;
     return probe_fma_peak(kind, nsm, tflops) == cudaSuccess ? DMC_OK : DMC_ERR_CUDA;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches of systems of uneven size: one graph per generation, each system's
+// generation on its own stream (fork/join through events on the batch stream)
+// ---------------------------------------------------------------------------
+struct dmc_batch {
+    std::vector<dmc_ctx*> sys;
+    std::vector<int> grid;            // walker-kernel CTAs per system
+    std::vector<int> order;           // launch order: longest walker first
+    cudaStream_t stream = nullptr;    // fork/join stream
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join, done;
+    // captured generations keyed by opcomp and every system's (stack, count
+    // slot) parities; valid while each system's parameters, launch arguments,
+    // precision and grid match the snapshot taken at capture
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        int nl = 0;                 // kernels in the graph
+        std::vector<int> nls;       // of which per system
+    };
+    std::map<uint64_t, Graph> graphs;
+    std::vector<DevParams> gP;
+    std::vector<KernelArgs> gA;
+    std::vector<int> gprec, ggrid;
+    DevBuf<unsigned char> flush;
+    std::string err;
+};
+
+namespace {
+
+int bfail(dmc_batch* b, int code, const std::string& msg)
+{
+    b->err = msg;
+    return code;
+}
+
+#define CKB(expr)                                                                            \
+    do {                                                                                     \
+        cudaError_t _e = (expr);                                                             \
+        if (_e != cudaSuccess) return bfail(b, DMC_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+// algorithmic flops of one walker-step (pair-matrix products, inverse,
+// contractions, pair loop, beta lookups, move): the tuner's first cost guess
+double flops_per_walker(const dmc_ctx* c)
+{
+    const double nu = c->S.nup, nd_ = c->S.ndn, nd = c->S.nd, K = 2.0 * c->S.nk - 1.0, N = c->S.npart;
+    return 10.0 * nu * nd_ * K + 2.0 * nd * nd * nd + 8.0 * nd * (nu + nd_) + 30.0 * N * (N - 1) + 40.0 * nu * nd_ +
+           30.0 * N;
+}
+
+int per_sm_of(const dmc_ctx* c) { return std::max(1, c->grid / std::max(1, c->nsm)); }
+
+// launch order of the systems: decreasing time per walker, so that systems
+// with short walkers fill the tail of the long ones
+void set_order(dmc_batch* b, const std::vector<double>& tau)
+{
+    b->order.resize(b->sys.size());
+    for (size_t s = 0; s < b->order.size(); ++s) b->order[s] = (int)s;
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return tau[x] > tau[y]; });
+}
+
+void drop_graphs(dmc_batch* b)
+{
+    for (auto& kv : b->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    b->graphs.clear();
+}
+
+// hand each system's host count to the device (outside any capture)
+int push_counts(dmc_batch* b)
+{
+    for (dmc_ctx* c : b->sys) {
+        int rc = sync_n(c);
+        if (rc) return bfail(b, rc, c->err);
+        if (c->n == 0) return bfail(b, DMC_ERR_EMPTY, "a system of the batch has no walkers");
+        CKB(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        CKB(cudaStreamSynchronize(c->stream));
+        c->n_stale = true;
+    }
+    return DMC_OK;
+}
+
+// one generation of every system, forked from and joined to the batch stream
+int batch_gen_async(dmc_batch* b, int opcomp, int* nlaunch, std::vector<int>& nls)
+{
+    CKB(cudaEventRecord(b->fork, b->stream));
+    int nl = 0;
+    nls.assign(b->sys.size(), 0);
+    for (const int s : b->order) {
+        dmc_ctx* c = b->sys[s];
+        CKB(cudaStreamWaitEvent(c->stream, b->fork, 0));
+        const int g0 = c->grid;
+        c->grid = b->grid[s];
+        int k = 0;
+        const int rc = gen_async(c, opcomp, &k);
+        c->grid = g0;
+        if (rc) return bfail(b, rc, c->err);
+        nl += k;
+        nls[s] = k;
+        CKB(cudaEventRecord(b->join[s], c->stream));
+        CKB(cudaStreamWaitEvent(b->stream, b->join[s], 0));
+    }
+    if (nlaunch) *nlaunch = nl;
+    return DMC_OK;
+}
+
+// one wavefunction evaluation of every system's current walkers, each on its
+// own stream with grids[s] CTAs (no walker state changes); ms[s] = time from
+// the fork to the end of system s, returns the time to the join in *total
+int batch_eval_pass(dmc_batch* b, const std::vector<int>& grids, bool concurrent, std::vector<double>& ms,
+                    double* total)
+{
+    const size_t ns = b->sys.size();
+    ms.assign(ns, 0.0);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CKB(cudaEventCreate(&e0));
+    CKB(cudaEventCreate(&e1));
+    int rc = DMC_OK;
+    double tsum = 0.0;
+    for (size_t i = 0; i < ns && rc == DMC_OK; ++i) {
+        const int s = b->order[i];
+        if (!concurrent || i == 0) {
+            if (cudaEventRecord(e0, b->stream) != cudaSuccess) rc = DMC_ERR_CUDA;
+        }
+        dmc_ctx* c = b->sys[s];
+        if (rc == DMC_OK && cudaStreamWaitEvent(c->stream, e0, 0) != cudaSuccess) rc = DMC_ERR_CUDA;
+        if (rc == DMC_OK) {
+            KernelArgs a = base_args(c);
+            a.mode = MODE_HPSI;
+            a.nw = c->n;
+            a.xin = c->st[c->istin].x.p;
+            a.status = nullptr;
+            if (launch_walker(c->P, a, c->L, std::max(1, std::min(grids[s], c->n)), c->stream,
+                              c->precision == DMC_PREC_MIXED) != cudaSuccess)
+                rc = DMC_ERR_CUDA;
+        }
+        if (rc == DMC_OK && cudaEventRecord(b->done[s], c->stream) != cudaSuccess) rc = DMC_ERR_CUDA;
+        if (rc == DMC_OK && cudaStreamWaitEvent(b->stream, b->done[s], 0) != cudaSuccess) rc = DMC_ERR_CUDA;
+        if (rc == DMC_OK && !concurrent) {
+            float t = 0.f;
+            // (in order: e0 was recorded after the previous system ended)
+            if (cudaEventSynchronize(b->done[s]) != cudaSuccess ||
+                cudaEventElapsedTime(&t, e0, b->done[s]) != cudaSuccess)
+                rc = DMC_ERR_CUDA;
+            ms[s] = t;
+            tsum += t;
+        }
+    }
+    if (rc == DMC_OK && concurrent) {
+        if (cudaEventRecord(e1, b->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) rc = DMC_ERR_CUDA;
+        for (size_t s = 0; s < ns && rc == DMC_OK; ++s) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, e0, b->done[s]) != cudaSuccess) rc = DMC_ERR_CUDA;
+            ms[s] = t;
+        }
+        float t = 0.f;
+        if (rc == DMC_OK && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) rc = DMC_ERR_CUDA;
+        tsum = t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return bfail(b, rc, "tuning pass");
+    if (total) *total = tsum;
+    return DMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmc_batch_plan(int nsys, const double* tau, const int* nw, const int* per_sm, const int* maxgrid, int nsm,
+                   int* grids)
+{
+    if (nsys < 1 || nsys > DMC_BATCH_MAX || !tau || !nw || !per_sm || !maxgrid || !grids || nsm < 1)
+        return DMC_ERR_INVALID;
+    int units = 2 * nsm;   // half-SM slots
+    std::vector<int> unit(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        if (!(tau[s] > 0.0) || nw[s] < 1 || (per_sm[s] != 1 && per_sm[s] != 2) || maxgrid[s] < 1)
+            return DMC_ERR_INVALID;
+        unit[s] = 2 / per_sm[s];
+        grids[s] = 1;
+        units -= unit[s];
+    }
+    if (units < 0) return DMC_ERR_INVALID;
+    auto waves = [&](int s, int g) { return (nw[s] + g - 1) / g; };
+    // the smallest grid that takes one wave of walkers off system s (0: none)
+    auto next_grid = [&](int s) {
+        const int w = waves(s, grids[s]);
+        if (w <= 1) return 0;
+        const int g = (nw[s] + w - 2) / (w - 1);
+        return g <= maxgrid[s] && (g - grids[s]) * unit[s] <= units ? g : 0;
+    };
+    for (;;) {
+        int best = -1;
+        double tb = -1.0;
+        for (int s = 0; s < nsys; ++s) {
+            if (!next_grid(s)) continue;
+            const double t = waves(s, grids[s]) * tau[s];
+            if (t > tb) {
+                tb = t;
+                best = s;
+            }
+        }
+        if (best < 0) break;
+        const int g = next_grid(best);
+        units -= (g - grids[best]) * unit[best];
+        grids[best] = g;
+    }
+    return DMC_OK;
+}
+
+int dmc_batch_create(dmc_ctx* const* ctxs, int nsys, dmc_batch** out)
+{
+    if (!ctxs || !out || nsys < 1 || nsys > DMC_BATCH_MAX) return DMC_ERR_INVALID;
+    *out = nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return DMC_ERR_CUDA;
+    for (int s = 0; s < nsys; ++s) {
+        if (!ctxs[s] || ctxs[s]->device != dev) return DMC_ERR_INVALID;
+        for (int t = 0; t < s; ++t)
+            if (ctxs[t] == ctxs[s]) return DMC_ERR_INVALID;
+    }
+    dmc_batch* b = new (std::nothrow) dmc_batch();
+    if (!b) return DMC_ERR_NOMEM;
+    b->sys.assign(ctxs, ctxs + nsys);
+    b->join.assign(nsys, nullptr);
+    b->done.assign(nsys, nullptr);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int s = 0; s < nsys && e == cudaSuccess; ++s) {
+        e = cudaEventCreateWithFlags(&b->join[s], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreate(&b->done[s]);
+    }
+    if (e != cudaSuccess) {
+        dmc_batch_destroy(b);
+        return DMC_ERR_CUDA;
+    }
+    // first split: every system on its whole persistent grid, launched in
+    // decreasing order of algorithmic flops per walker-step
+    std::vector<double> tau(nsys);
+    b->grid.resize(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        tau[s] = flops_per_walker(ctxs[s]);
+        b->grid[s] = ctxs[s]->grid;
+    }
+    set_order(b, tau);
+    *out = b;
+    return DMC_OK;
+}
+
+int dmc_batch_destroy(dmc_batch* b)
+{
+    if (!b) return DMC_ERR_INVALID;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graphs(b);
+    for (cudaEvent_t e : b->join)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->done)
+        if (e) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return DMC_OK;
+}
+
+const char* dmc_batch_last_error(const dmc_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int dmc_batch_set_grids(dmc_batch* b, const int* grids)
+{
+    if (!b || !grids) return DMC_ERR_INVALID;
+    for (size_t s = 0; s < b->sys.size(); ++s)
+        if (grids[s] < 1 || grids[s] > b->sys[s]->grid) return bfail(b, DMC_ERR_INVALID, "grid out of range");
+    b->grid.assign(grids, grids + b->sys.size());
+    return DMC_OK;
+}
+
+int dmc_batch_get_grids(const dmc_batch* b, int* grids)
+{
+    if (!b || !grids) return DMC_ERR_INVALID;
+    std::copy(b->grid.begin(), b->grid.end(), grids);
+    return DMC_OK;
+}
+
+int dmc_batch_tune(dmc_batch* b, int rounds, int* grids, double* ms)
+{
+    if (!b || rounds < 0) return DMC_ERR_INVALID;
+    const int ns = (int)b->sys.size();
+    for (dmc_ctx* c : b->sys) {
+        const int rc = sync_n(c);
+        if (rc) return bfail(b, rc, c->err);
+        if (c->n == 0) return bfail(b, DMC_ERR_EMPTY, "a system of the batch has no walkers");
+        CKB(cudaStreamSynchronize(c->stream));
+    }
+    std::vector<int> nw(ns), psm(ns), mg(ns), full(ns);
+    for (int s = 0; s < ns; ++s) {
+        const dmc_ctx* c = b->sys[s];
+        nw[s] = c->n;
+        psm[s] = std::min(2, per_sm_of(c));
+        mg[s] = c->grid;
+        full[s] = c->grid;
+    }
+    // each system alone on the whole GPU (after one warm-up pass)
+    std::vector<double> t;
+    double tot = 0.0;
+    int rc = batch_eval_pass(b, full, false, t, &tot);
+    if (!rc) rc = batch_eval_pass(b, full, false, t, &tot);
+    if (rc) return rc;
+    std::vector<double> tau(ns);
+    for (int s = 0; s < ns; ++s) {
+        const int g = std::min(full[s], nw[s]);
+        tau[s] = std::max(1e-6, t[s]) / ((nw[s] + g - 1) / g);
+    }
+    const std::vector<int> order0 = b->order;
+    set_order(b, tau);
+    std::vector<int> cur(ns), best = b->grid;
+    double best_ms = 0.0;
+    {
+        // the split in use, as the reference point
+        std::vector<double> tt;
+        rc = batch_eval_pass(b, best, true, tt, &best_ms);
+        if (rc) return rc;
+        // every system on its whole persistent grid: the CTA scheduler then
+        // starts each system's CTAs as the previous system's CTAs retire
+        double pass = 0.0;
+        rc = batch_eval_pass(b, full, true, tt, &pass);
+        if (rc) return rc;
+        if (pass < best_ms) {
+            best_ms = pass;
+            best = full;
+        }
+    }
+    for (int r = 0; r <= rounds; ++r) {
+        rc = dmc_batch_plan(ns, tau.data(), nw.data(), psm.data(), mg.data(), b->sys[0]->nsm, cur.data());
+        if (rc) return bfail(b, rc, "plan");
+        std::vector<double> ts;
+        double pass = 0.0;
+        rc = batch_eval_pass(b, cur, true, ts, &pass);
+        if (rc) return rc;
+        if (pass < best_ms) {
+            best_ms = pass;
+            best = cur;
+        }
+        // per-walker times seen with the other systems resident
+        for (int s = 0; s < ns; ++s) {
+            const int g = std::min(cur[s], nw[s]);
+            tau[s] = std::max(1e-6, ts[s]) / ((nw[s] + g - 1) / g);
+        }
+    }
+    if (best != b->grid || b->order != order0) drop_graphs(b);
+    b->grid = best;
+    if (grids) std::copy(best.begin(), best.end(), grids);
+    if (ms) *ms = best_ms;
+    return DMC_OK;
+}
+
+int dmc_batch_generations(dmc_batch* b, int ngen, int opcomp_last, int flush_l2, int64_t* walker_steps,
+                          double* device_ms, int64_t* launches)
+{
+    if (!b || ngen < 0) return DMC_ERR_INVALID;
+    const int ns = (int)b->sys.size();
+    int rc = DMC_OK;
+    for (dmc_ctx* c : b->sys) {
+        rc = sync_n(c);
+        if (rc) return bfail(b, rc, c->err);
+        if (c->n == 0) return bfail(b, DMC_ERR_EMPTY, "a system of the batch has no walkers");
+    }
+    if (flush_l2) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, b->sys[0]->device);
+        const size_t fb = std::max<size_t>((size_t)2 * l2, 64u << 20);
+        CKB(b->flush.alloc(fb));
+    }
+    // drop the captured generations when anything they baked in changed
+    {
+        bool same = (int)b->gP.size() == ns && b->ggrid == b->grid;
+        for (int s = 0; s < ns && same; ++s) {
+            dmc_ctx* c = b->sys[s];
+            const KernelArgs A = base_args(c);
+            same = b->gprec[s] == c->precision && std::memcmp(&b->gP[s], &c->P, sizeof c->P) == 0 &&
+                   std::memcmp(&b->gA[s], &A, sizeof A) == 0;
+        }
+        if (!same) {
+            drop_graphs(b);
+            b->gP.resize(ns);
+            b->gA.resize(ns);
+            b->gprec.resize(ns);
+            for (int s = 0; s < ns; ++s) {
+                dmc_ctx* c = b->sys[s];
+                const KernelArgs A = base_args(c);
+                std::memcpy(&b->gP[s], &c->P, sizeof c->P);
+                std::memcpy(&b->gA[s], &A, sizeof A);
+                b->gprec[s] = c->precision;
+            }
+            b->ggrid = b->grid;
+        }
+    }
+    for (dmc_ctx* c : b->sys) CKB(cudaMemsetAsync(c->psteps.p, 0, sizeof(unsigned long long), c->stream));
+    rc = push_counts(b);
+    if (rc) return rc;
+    std::vector<cudaEvent_t> ev(2 * (size_t)ngen, nullptr);
+    for (auto& e : ev) CKB(cudaEventCreate(&e));
+    int64_t lsum = 0;
+    for (int g = 0; g < ngen && rc == DMC_OK; ++g) {
+        if (flush_l2) CKB(cudaMemsetAsync(b->flush.p, g & 0xff, b->flush.n, b->stream));
+        const int op = (g == ngen - 1) && opcomp_last ? 1 : 0;
+        uint64_t key = (uint64_t)op;
+        for (int s = 0; s < ns; ++s)
+            key |= (uint64_t)(b->sys[s]->istin | (b->sys[s]->pcur << 1)) << (1 + 2 * s);
+        auto it = b->graphs.find(key);
+        if (it == b->graphs.end()) {
+            std::vector<int> pi(ns), pc(ns);
+            std::vector<int64_t> l0(ns);
+            for (int s = 0; s < ns; ++s) {
+                pi[s] = b->sys[s]->istin;
+                pc[s] = b->sys[s]->pcur;
+                l0[s] = b->sys[s]->launches;
+            }
+            cudaGraph_t graph = nullptr;
+            dmc_batch::Graph G;
+            CKB(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            rc = batch_gen_async(b, op, &G.nl, G.nls);
+            const cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+            if (rc == DMC_OK && ce != cudaSuccess) rc = bfail(b, DMC_ERR_CUDA, "batch capture");
+            if (rc == DMC_OK && cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess)
+                rc = bfail(b, DMC_ERR_CUDA, "batch graph instantiate");
+            if (graph) cudaGraphDestroy(graph);
+            // the capture only recorded the launches: restore the parities
+            for (int s = 0; s < ns; ++s) {
+                b->sys[s]->istin = pi[s];
+                b->sys[s]->pcur = pc[s];
+                b->sys[s]->launches = l0[s];
+            }
+            if (rc) break;
+            it = b->graphs.emplace(key, G).first;
+        }
+        CKB(cudaEventRecord(ev[2 * g], b->stream));
+        CKB(cudaGraphLaunch(it->second.exec, b->stream));
+        CKB(cudaEventRecord(ev[2 * g + 1], b->stream));
+        for (int s = 0; s < ns; ++s) {
+            advance_parities(b->sys[s]);
+            b->sys[s]->launches += it->second.nls[s];
+        }
+        lsum += it->second.nl;
+    }
+    if (rc == DMC_OK) CKB(cudaStreamSynchronize(b->stream));
+    double total = 0.0;
+    for (int g = 0; g < ngen && rc == DMC_OK; ++g) {
+        float ms = 0.f;
+        CKB(cudaEventElapsedTime(&ms, ev[2 * g], ev[2 * g + 1]));
+        total += ms;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    int64_t steps = 0;
+    for (dmc_ctx* c : b->sys) {
+        unsigned long long st = 0;
+        CKB(cudaMemcpy(&st, c->psteps.p, sizeof st, cudaMemcpyDeviceToHost));
+        steps += (int64_t)st;
+        const int rs = sync_n(c);
+        if (rc == DMC_OK && rs) rc = bfail(b, rs, c->err);
+    }
+    if (walker_steps) *walker_steps = steps;
+    if (device_ms) *device_ms = total;
+    if (launches) *launches = lsum;
+    return rc;
 }
 
 }  // extern "C"

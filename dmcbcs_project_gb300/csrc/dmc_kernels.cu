@@ -648,6 +648,18 @@ static int g_smem_set_mixed = -1, g_smem_set_fp64 = -1;
 cudaError_t prepare_walker(const SmemLayout& L)
 {
     const int smem = L.total * 8;
+    // every launch asks for the largest shared-memory carveout, so CTAs of
+    // launches with different layouts (systems of a batch) can share an SM
+    static bool carveout = false;
+    if (!carveout) {
+        cudaError_t e = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        carveout = true;
+    }
     if (g_smem_set_mixed < smem) {
         const cudaError_t e = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;

@@ -445,6 +445,68 @@ typedef struct dmc_dev_stack {
 int dmc_branch_noalloc(int n, int npart, int cap, double factor, const dmc_dev_stack* in,
                        const dmc_dev_stack* out, uint64_t* wtisto, int* nout, void* stream);
 
+/* ---- Batches of systems of uneven size ----
+ * No counterpart in the reference, where one MPI job runs one system: a
+ * batch advances several contexts (one system each: its own N, polarisation,
+ * wavefunction, walkers, trial energy and estimators) generation by
+ * generation on one GPU.  Each batched generation is one CUDA graph: the
+ * generation of every system (dmcbcs.f90:435-449 as in dmc_generation) on
+ * its own stream, forked from and joined to the batch's stream, so that the
+ * systems' walker kernels run concurrently.  grids[s] CTAs run system s's
+ * walker kernel; the split and the launch order are what the batch tunes.  Each system's
+ * walkers, random streams, estimators and populations come out exactly as
+ * from dmc_generation on that context alone.  A context belongs to at most
+ * one batch and must not be used on its own while a batched call runs. */
+#define DMC_BATCH_MAX 16
+
+typedef struct dmc_batch dmc_batch;
+
+/* Group nsys contexts on the current device (DMC_ERR_INVALID if they are on
+ * different devices, repeated or more than DMC_BATCH_MAX).  Initially every
+ * system runs on its whole persistent grid: the CTA scheduler then starts a
+ * system's CTAs as those of the systems launched before it retire.  Systems
+ * are launched in decreasing order of cost per walker (algorithmic flops
+ * until dmc_batch_tune measures them), so short walkers fill the tails. */
+int dmc_batch_create(dmc_ctx* const* ctxs, int nsys, dmc_batch** out);
+int dmc_batch_destroy(dmc_batch* b);
+const char* dmc_batch_last_error(const dmc_batch* b);
+
+/* The walker-kernel CTAs of each system in a batched generation:
+ * 1 <= grids[s] <= the context's own persistent grid. */
+int dmc_batch_set_grids(dmc_batch* b, const int* grids);
+int dmc_batch_get_grids(const dmc_batch* b, int* grids);
+
+/* Host-only planning step of the tuner (no GPU work): split the SMs over
+ * nsys systems to minimise the predicted longest system.  System s has nw[s]
+ * walkers, tau[s] seconds per walker on one of its CTAs, per_sm[s] of its
+ * CTAs fit on one SM (1 or 2) and at most maxgrid[s] CTAs; a CTA takes
+ * 2 / per_sm[s] of the 2 * nsm half-SM slots.  Predicted time of s:
+ * ceil(nw[s] / grids[s]) * tau[s].  Starting from one CTA per system, one
+ * CTA at a time goes to the system with the longest predicted time among
+ * those that can still take one.  DMC_ERR_INVALID if the systems do not get
+ * one CTA each. */
+int dmc_batch_plan(int nsys, const double* tau, const int* nw, const int* per_sm, const int* maxgrid, int nsm,
+                   int* grids);
+
+/* Autotuner: time each system's walker kernel alone on its current walkers
+ * (a wavefunction evaluation, which leaves every walker as it was) and order
+ * the launches by the measured time per walker.  Then time concurrent
+ * passes of all systems with the split in use, with every system on its
+ * whole grid, and with `rounds` + 1 partitions from dmc_batch_plan (each
+ * re-planned from the per-system times of the pass before); keep the split
+ * with the shortest measured pass.  grids (optional, [nsys]) receives it,
+ * ms (optional) its pass time in milliseconds. */
+int dmc_batch_tune(dmc_batch* b, int rounds, int* grids, double* ms);
+
+/* ngen batched generations, the last one with opcomp (estimators) when
+ * opcomp_last is set; each generation is bracketed by CUDA events on the
+ * batch's stream and, with flush_l2, preceded by an untimed write of a
+ * buffer twice the L2 size.  Returns the summed device milliseconds, the
+ * walker-steps of all systems and the kernels launched in the timed
+ * intervals (each optional). */
+int dmc_batch_generations(dmc_batch* b, int ngen, int opcomp_last, int flush_l2, int64_t* walker_steps,
+                          double* device_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

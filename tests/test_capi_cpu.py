@@ -136,3 +136,59 @@ def test_reference_decks_parse(name):
         pytest.skip("reference decks not present")
     s, r, e = deck.load_deck(open(path).read())
     assert s.norb == 10
+
+
+def _plan_units(grids, per_sm):
+    return sum(g * (2 // p) for g, p in zip(grids, per_sm))
+
+
+def test_batch_plan_balances_and_fits(lib):
+    """dmc_batch_plan (host only): the split fits the SMs, every system gets a
+    CTA, no system gets more CTAs than walkers or its own grid, and the
+    predicted longest system cannot be shortened by moving one CTA."""
+    import numpy as np
+
+    nsm = 152
+    nw = [2731, 2712, 2745, 2698, 2760, 2738]
+    tau = [1.0, 4.0, 21.0, 19.0, 26.0, 150.0]
+    per_sm = [2, 2, 2, 2, 2, 1]
+    maxg = [304, 304, 304, 304, 304, 152]
+    g = capi.batch_plan(tau, nw, per_sm, maxg, nsm)
+    assert g.min() >= 1 and all(g[s] <= min(maxg[s], nw[s]) for s in range(6))
+    assert _plan_units(g, per_sm) <= 2 * nsm
+    pred = [-(-nw[s] // g[s]) * tau[s] for s in range(6)]
+    worst = int(np.argmax(pred))
+    # taking one CTA from any other system and giving it to the worst one does
+    # not shorten the makespan
+    for s in range(6):
+        if s == worst or g[s] == 1:
+            continue
+        g2 = g.copy()
+        g2[s] -= 1
+        free = 2 * nsm - _plan_units(g2, per_sm)
+        add = free // (2 // per_sm[worst])
+        g2[worst] = min(maxg[worst], g2[worst] + add)
+        pred2 = [-(-nw[k] // g2[k]) * tau[k] for k in range(6)]
+        assert max(pred2) >= max(pred) * (1 - 1e-12)
+
+
+def test_batch_plan_small_and_invalid(lib):
+    import numpy as np
+
+    # fewer walkers than SMs: never more CTAs than walkers
+    g = capi.batch_plan([1.0, 1.0], [3, 5], [2, 2], [304, 304], 152)
+    assert list(g) == [3, 5]
+    # equal systems: the makespan of the even split (14 waves of 76 CTAs)
+    g = capi.batch_plan([1.0] * 4, [1000] * 4, [2] * 4, [304] * 4, 152)
+    assert max(-(-1000 // int(x)) for x in g) == 14 and sum(g) <= 304
+    # one-per-SM systems take two slots per CTA
+    g = capi.batch_plan([1.0, 1.0], [1000, 1000], [1, 2], [152, 304], 152)
+    assert _plan_units(g, [1, 2]) <= 304 and g[0] * 2 + g[1] >= 300
+    for bad in (dict(tau=[0.0]), dict(nw=[0]), dict(per_sm=[3]), dict(maxgrid=[0])):
+        args = dict(tau=[1.0], nw=[10], per_sm=[2], maxgrid=[10])
+        args.update(bad)
+        with pytest.raises(capi.DMCError):
+            capi.batch_plan(args["tau"], args["nw"], args["per_sm"], args["maxgrid"], 152)
+    with pytest.raises(capi.DMCError):   # more systems than slots
+        capi.batch_plan([1.0] * 3, [10] * 3, [1] * 3, [10] * 3, 1)
+    assert np.all(capi.batch_plan([2.0], [100], [1], [152], 152) == 100)
