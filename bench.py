@@ -326,6 +326,31 @@ def uneven_batch(args, rank):
             "speedup_vs_sequential": value / seq}
 
 
+def param_gradients(args, rank):
+    """dmc_param_grad (adjoint d log Psi / d theta and d E_L / d theta for
+    theta = vorb(1..7), bfact) on 8192 walkers of the N = 66 system, through
+    the C ABI with host buffers; median of three calls after one warm-up."""
+    from dmcbcs_project_gb300 import capi, configs
+
+    s, r, _ = configs.workload(WORKLOAD, nwalk=args.pgrad_walkers, idmc=-1)
+    r.seed = 17 + 1000003 * rank
+    with capi.Context(s, r) as c:
+        c.init_walkers()
+        x = c.walkers()["x"]
+        c.param_grad(x[:64])
+        times = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            dl, de = c.param_grad(x)
+            times.append(time.perf_counter() - t0)
+        np_ = c.param_count()
+    t = float(np.median(times))
+    return {"workload": "param_grad_n66_33u33d", "walkers": int(x.shape[0]), "parameters": np_,
+            "seconds_per_call": t, "walkers_per_s": x.shape[0] / t,
+            "includes": "host-to-device copy of x, FP64 wavefunction and determinant evaluation, adjoint kernel, "
+                        "device-to-host copy of both gradients"}
+
+
 def run_gpu(args):
     import torch
 
@@ -421,6 +446,7 @@ def run_gpu(args):
             cx.close()
 
     batch = uneven_batch(args, rank) if args.batch_steps > 0 else None
+    pgrad = param_gradients(args, rank) if args.pgrad_walkers > 0 else None
 
     if rank == 0:
         cpu = None
@@ -457,6 +483,8 @@ def run_gpu(args):
             line["n132"] = n132
         if batch:
             line["uneven_batch"] = batch
+        if pgrad:
+            line["param_grad"] = pgrad
         print(json.dumps(line), flush=True)
     for c in ctxs.values():
         c.close()
@@ -481,6 +509,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n132-steps", type=int, default=20,
                     help="generations of the N = 132, 8192-walker side measurement (0: skip)")
+    ap.add_argument("--pgrad-walkers", type=int, default=8192,
+                    help="walkers of the adjoint parameter-gradient side measurement (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=20,
                     help="generations of the six-system uneven batch side measurement (0: skip)")
     args = ap.parse_args()

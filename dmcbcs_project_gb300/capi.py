@@ -29,7 +29,7 @@ EXPORTS = [
     "dmc_set_operators", "dmc_zero_operators", "dmc_add_operators", "dmc_update_operators", "dmc_get_operators",
     "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure", "dmc_dfmath_eval",
     "dmc_batch_create", "dmc_batch_destroy", "dmc_batch_last_error", "dmc_batch_set_grids", "dmc_batch_get_grids",
-    "dmc_batch_plan", "dmc_batch_tune", "dmc_batch_generations",
+    "dmc_batch_plan", "dmc_batch_tune", "dmc_batch_generations", "dmc_param_count", "dmc_param_grad",
 ]
 
 PREC_FP64 = 0
@@ -120,6 +120,8 @@ def load(path=LIB_PATH):
     L.dmc_sr_update.argtypes = [vp, C.c_double, C.c_double, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.dmc_branch_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(abi.DevStack),
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
+    L.dmc_param_count.argtypes = [vp, C.POINTER(C.c_int)]
+    L.dmc_param_grad.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.dmc_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
     L.dmc_batch_destroy.argtypes = [vp]
     L.dmc_batch_last_error.restype = C.c_char_p
@@ -369,6 +371,21 @@ class Context:
 
     def write_operators(self, directory, tau=0.0):
         self._check(load().dmc_write_operators(self._h, os.fsencode(str(directory)), float(tau)))
+
+    def param_count(self):
+        n = C.c_int()
+        self._check(load().dmc_param_count(self._h, C.byref(n)))
+        return n.value
+
+    def param_grad(self, x):
+        """Adjoint gradients for theta = (vorb(1..norb)[, bfact]): returns
+        (d log|Psi|/d theta, d E_L/d theta), each (nw, np)."""
+        x = self._x(x)
+        nw, np_ = x.shape[0], self.param_count()
+        dl = np.zeros((nw, np_))
+        de = np.zeros((nw, np_))
+        self._check(load().dmc_param_grad(self._h, nw, x.reshape(-1), dl.reshape(-1), de.reshape(-1)))
+        return dl, de
 
     def getjasder(self, x):
         """d U_long / d beta, d U_long / d gamma per walker, shape [nw, 2]."""

@@ -148,6 +148,7 @@ struct dmc_ctx {
     DevBuf<unsigned char> flush;
     // single-particle moves and parameter derivatives
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
+    DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
     DevBuf<int> sip;
     int64_t sr_count = 0;
     bool sr_jas = false, sr_det = true;   // iopt(1), iopt(2) of the optimizer deck
@@ -1226,6 +1227,58 @@ int dmc_getjasder_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)
     CK(launch_jasder(c->P, c->jq.p, c->sx.p, c->sder.p, nw, c->grid, c->stream, 2));
     ++c->launches;
     CK(cudaMemcpyAsync(dpsi, c->sder.p, 2 * nw * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
+static int pgrad_np(const dmc_ctx* c) { return c->S.norb + (c->P.nobeta ? 0 : 1); }
+
+int dmc_param_count(const dmc_ctx* c, int* np)
+{
+    if (!c || !np) return DMC_ERR_INVALID;
+    *np = pgrad_np(c);
+    return DMC_OK;
+}
+
+int dmc_param_grad(dmc_ctx* c, int nw, const double* x, double* dlogpsi, double* deloc)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (nw < 0 || (nw > 0 && (!x || !dlogpsi || !deloc))) return fail(c, DMC_ERR_INVALID, "bad param_grad arguments");
+    if (nw == 0) return DMC_OK;
+    const size_t n3 = (size_t)c->n3, nd2 = (size_t)c->S.nd * c->S.nd;
+    const int np = pgrad_np(c);
+    CK(c->sx.alloc(nw * n3));
+    CK(c->pg_dpsi.alloc(nw * n3));
+    CK(c->pg_dphi.alloc(nw * n3));
+    CK(c->ssinv.alloc(nw * nd2));
+    CK(c->pg_dlog.alloc((size_t)nw * np));
+    CK(c->pg_del.alloc((size_t)nw * np));
+    CK(cudaMemcpyAsync(c->sx.p, x, nw * n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    // the total drift and the determinant's drift and inverse, in FP64
+    const int prec = c->precision;
+    c->precision = DMC_PREC_FP64;
+    int rc = run_eval(c, MODE_HPSI, nw, c->sx.p, nullptr, nullptr, c->pg_dpsi.p, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, c->stream);
+    if (rc == DMC_OK)
+        rc = run_eval(c, MODE_BCS, nw, c->sx.p, nullptr, nullptr, c->pg_dphi.p, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, c->ssinv.p, c->stream);
+    c->precision = prec;
+    if (rc) return rc;
+    c->launches += 2;
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    const size_t need = pgrad_doubles(c->P);
+    const int grid = std::max(1, std::min(nw, 2 * c->nsm));
+    double* scr = nullptr;
+    if (need * 8 > (size_t)optin) {
+        CK(c->pg_scr.alloc((size_t)grid * need));
+        scr = c->pg_scr.p;
+    }
+    CK(launch_pgrad(c->P, c->kv.p, c->tud.p, c->sx.p, c->ssinv.p, c->pg_dpsi.p, c->pg_dphi.p, c->pg_dlog.p,
+                    c->pg_del.p, nw, np, c->sd.bfact, grid, scr, optin, c->stream));
+    ++c->launches;
+    CK(cudaMemcpyAsync(dlogpsi, c->pg_dlog.p, (size_t)nw * np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(deloc, c->pg_del.p, (size_t)nw * np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return DMC_OK;
 }

@@ -44,6 +44,12 @@ cudaError_t launch_bcsone(const DevParams& p, const KVecDev* kv, const TabUD* tu
 cudaError_t launch_getphione(const DevParams& p, const TabUD* tud, const TabSS* tss, const double* x,
                              const int* ipart, const double* drr, double* ratio, int nw, cudaStream_t st);
 size_t derbcs_smem_bytes(const DevParams& p);
+// adjoint parameter gradients (dmc_single.cu): doubles of one CTA's working
+// set; on chip when it fits in smem_limit bytes, else in gscr (grid x that)
+size_t pgrad_doubles(const DevParams& p);
+cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x, const double* sinv,
+                         const double* dpsi, const double* dphi, double* dlog, double* deloc, int nw, int np,
+                         double bfact, int grid, double* gscr, int smem_limit, cudaStream_t st);
 // dpsi[w*stride + off + shell]; stride < 0 means norb
 cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x, const double* smati, double* dpsi,
                           int nw, int grid, cudaStream_t st, int stride = -1, int off = 0);

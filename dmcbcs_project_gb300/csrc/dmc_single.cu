@@ -7,7 +7,10 @@
 //  - getderbcs (psislaterbcs.f90:449-524, optsw on, optbeta off):
 //    d log|det| / d vorb(shell) = tr(S^-1 dS/dvorb);
 //  - the sums that calder (optimizer.f90:90-116) accumulates over a walker
-//    population for the stochastic-reconfiguration step.
+//    population for the stochastic-reconfiguration step;
+//  - the adjoint parameter gradients d log Psi / d theta and d E_L / d theta
+//    for theta = (vorb(1..norb), bfact), the amplitudes the pair function
+//    phi (psislaterbcs.f90:249-293) is linear in.
 // One warp per walker for the ratios (a few hundred flops each); one CTA per
 // walker for the derivatives, which contract the whole inverse.
 #include <cuda_runtime.h>
@@ -139,6 +142,233 @@ __global__ void __launch_bounds__(kThreads) derbcs_kernel(const __grid_constant_
     }
 }
 
+// beta(r) with its radial derivative and Laplacian (radialfun,
+// betafun.f90:173-194); zero beyond the range
+__device__ __forceinline__ void beta_all(const DevParams& p, const TabUD* tud, double r, double& f, double& df,
+                                         double& d2f)
+{
+    f = df = d2f = 0.0;
+    if (p.nobeta || r > p.rangeb) return;
+    const walker::Lagrange<double> W = walker::lagrange(r, p.scaleb, p.ntab);
+    const TabUD* T = tud + (W.idx - 1);
+    f = W.c1 * T[0].b + W.c2 * T[1].b + W.c3 * T[2].b + W.c4 * T[3].b;
+    df = W.c1 * T[0].db + W.c2 * T[1].db + W.c3 * T[2].db + W.c4 * T[3].db;
+    d2f = W.c1 * T[0].d2b + W.c2 * T[1].d2b + W.c3 * T[2].d2b + W.c4 * T[3].d2b;
+}
+
+__device__ double block_sum1(double v, double* red)
+{
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int h = kThreads / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    const double t = red[0];
+    __syncthreads();
+    return t;
+}
+
+// Adjoint parameter gradients, one walker per CTA (FP64).
+//
+// The determinant's share of the kinetic term of E_L = -hbar d2psi + v is
+//   Q = sum_p (1/m_p) [ lap_p Phi / Phi + 2 grad_p log Phi . grad_p J ]
+//     = tr(S^-1 M),   M_ij = sum over the particles p that entry (i,j) of the
+//                     pair matrix depends on of (1/m_p) lap_p S_ij
+//                     + 2 grad_p S_ij . w_p,   w_p = grad_p J / m_p,
+// because S is linear in each particle's row or column (psislaterbcs.f90:
+// 209-223).  J (Jastrow, one-body and long-range terms) and v do not depend
+// on theta, so with S' = dS/dtheta and M' = dM/dtheta
+//   d log Psi / d theta = tr(S^-1 S')
+//   d Q / d theta       = tr(S^-1 M') - tr(T S'),   T = S^-1 M S^-1
+// and d E_L / d theta = -hbar dQ/dtheta: one extra pair of nd^3 products per
+// walker gives every parameter.  Only the up-down block depends on theta:
+// phi = vorb(1) + sum_k 2 vorb(shell k) cos(k.r) + beta(r) with beta linear
+// in bfact.  Inputs per walker: x, the inverse (column-major as smati), the
+// total and determinant drifts (grad / sqrt m) whose difference is grad J.
+// Outputs dlog[w*np + t], deloc[w*np + t] for t = vorb(1..norb), then bfact.
+__global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__ DevParams p,
+                                                         const KVecDev* __restrict__ kv,
+                                                         const TabUD* __restrict__ tud, const double* __restrict__ x,
+                                                         const double* __restrict__ sinv,
+                                                         const double* __restrict__ dpsi,
+                                                         const double* __restrict__ dphi, double* __restrict__ dlog,
+                                                         double* __restrict__ deloc, int nw, int np, double bfact,
+                                                         double* gscr, size_t per_cta)
+{
+    extern __shared__ __align__(16) double smp[];
+    double* base = gscr ? gscr + (size_t)blockIdx.x * per_cta : smp;
+    const int nd = p.nd, nup = p.nup, ndn = p.ndn, P = p.npart, nq = p.nk - 1, norb = p.norb;
+    const size_t nd2 = (size_t)nd * nd;
+    double* Si = base;                 // (S^-1)_{rc} = Si[r + c nd]
+    double* M = Si + nd2;              // M, later T
+    double* B = M + nd2;               // M S^-1
+    double* xs = B + nd2;              // [P][3]
+    double* w = xs + 3 * P;            // [P][3]: grad J / m
+    double* cs = w + 3 * P;            // [nq][P][2]: cos, sin of k_q . x_p
+    double* red = cs + 2 * (size_t)P * (nq > 0 ? nq : 1);
+    double* res = red + kThreads;      // [2][norb + 1]
+    int* sh0 = reinterpret_cast<int*>(res + 2 * (norb + 1));   // first k of each shell, [norb + 1]
+    const double imu = p.imass[0], imd = p.imass[1], ims = imu + imd;
+    if (threadIdx.x == 0) {
+        // k vectors are sorted by shell; shell 1 is k = 0
+        int q = 1;
+        for (int sh = 2; sh <= norb; ++sh) {
+            sh0[sh - 2] = q;
+            while (q < p.nk && kv[q].shell == sh) ++q;
+        }
+        sh0[norb - 1] = q;
+    }
+    for (int wk = blockIdx.x; wk < nw; wk += gridDim.x) {
+        for (size_t t = threadIdx.x; t < nd2; t += kThreads) Si[t] = sinv[(size_t)wk * nd2 + t];
+        for (int t = threadIdx.x; t < 3 * P; t += kThreads) {
+            const size_t g = (size_t)wk * 3 * P + t;
+            xs[t] = x[g];
+            const int sp = (t / 3) < nup ? 0 : 1;
+            w[t] = (dpsi[g] - dphi[g]) * p.isqm[sp];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < nq * P; t += kThreads) {
+            const int q = t / P + 1, pp = t % P;
+            const KVecDev& K = kv[q];
+            double sn, c;
+            sincos(K.k[0] * xs[3 * pp] + K.k[1] * xs[3 * pp + 1] + K.k[2] * xs[3 * pp + 2], &sn, &c);
+            cs[2 * t] = c;
+            cs[2 * t + 1] = sn;
+        }
+        __syncthreads();
+        // M (psislaterbcs.f90:171-206, 249-293 for the entries and their derivatives)
+        for (size_t t = threadIdx.x; t < nd2; t += kThreads) {
+            const int i = (int)(t % nd), j = (int)(t / nd);
+            double m = 0.0;
+            if (i < nup && j < ndn) {
+                const int pj = nup + j;
+                double l = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
+                for (int q = 1; q <= nq; ++q) {
+                    const KVecDev& K = kv[q];
+                    const double* ci = cs + 2 * ((size_t)(q - 1) * P + i);
+                    const double* cj = cs + 2 * ((size_t)(q - 1) * P + pj);
+                    const double co = ci[0] * cj[0] + ci[1] * cj[1];
+                    const double si = ci[1] * cj[0] - ci[0] * cj[1];
+                    l -= K.v * K.k2 * co;
+                    const double vs = K.v * si;
+                    g0 -= vs * K.k[0];
+                    g1 -= vs * K.k[1];
+                    g2 -= vs * K.k[2];
+                }
+                if (!p.nobeta) {
+                    double d[3];
+                    for (int cc = 0; cc < 3; ++cc) d[cc] = walker::min_image(xs[3 * i + cc] - xs[3 * pj + cc], p);
+                    const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                    double f, df, d2f;
+                    beta_all(p, tud, r, f, df, d2f);
+                    if (r > 0.0) {
+                        const double dr = df / r;
+                        g0 += dr * d[0];
+                        g1 += dr * d[1];
+                        g2 += dr * d[2];
+                    }
+                    l += d2f;
+                }
+                m = l * ims + 2.0 * (g0 * (w[3 * i] - w[3 * pj]) + g1 * (w[3 * i + 1] - w[3 * pj + 1]) +
+                                     g2 * (w[3 * i + 2] - w[3 * pj + 2]));
+            } else if (i < nup) {
+                // unpaired up plane wave in column j (depends on up particle i)
+                const int u = j - ndn;
+                const double* k = p.akup[u];
+                double sn, c;
+                sincos(k[0] * xs[3 * i] + k[1] * xs[3 * i + 1] + k[2] * xs[3 * i + 2], &sn, &c);
+                const double a = p.sinup[u] ? c : -sn;        // d/d(k.x) of the entry
+                const double e = p.sinup[u] ? sn : c;
+                m = -p.ak2up[u] * e * imu + 2.0 * a * (k[0] * w[3 * i] + k[1] * w[3 * i + 1] + k[2] * w[3 * i + 2]);
+            } else if (j < ndn) {
+                // unpaired down plane wave in row i (depends on down particle j)
+                const int u = i - nup, pj = nup + j;
+                const double* k = p.akdn[u];
+                double sn, c;
+                sincos(k[0] * xs[3 * pj] + k[1] * xs[3 * pj + 1] + k[2] * xs[3 * pj + 2], &sn, &c);
+                const double a = p.sindn[u] ? c : -sn;
+                const double e = p.sindn[u] ? sn : c;
+                m = -p.ak2dn[u] * e * imd + 2.0 * a * (k[0] * w[3 * pj] + k[1] * w[3 * pj + 1] + k[2] * w[3 * pj + 2]);
+            }
+            M[t] = m;
+        }
+        __syncthreads();
+        // B = M S^-1, then T = S^-1 B (into M)
+        for (size_t t = threadIdx.x; t < nd2; t += kThreads) {
+            const int i = (int)(t % nd), j = (int)(t / nd);
+            double s = 0.0;
+            for (int k = 0; k < nd; ++k) s = fma(M[i + (size_t)k * nd], Si[k + (size_t)j * nd], s);
+            B[t] = s;
+        }
+        __syncthreads();
+        for (size_t t = threadIdx.x; t < nd2; t += kThreads) {
+            const int i = (int)(t % nd), j = (int)(t / nd);
+            double s = 0.0;
+            for (int k = 0; k < nd; ++k) s = fma(Si[i + (size_t)k * nd], B[k + (size_t)j * nd], s);
+            M[t] = s;
+        }
+        __syncthreads();
+        // per parameter: sums over the up-down pairs of S^-1_ji S'_ij and
+        // S^-1_ji M'_ij - T_ji S'_ij
+        const int npairs = nup * ndn;
+        for (int th = 0; th < np; ++th) {
+            double sl = 0.0, sq = 0.0;
+            for (int t = threadIdx.x; t < npairs; t += kThreads) {
+                const int i = t / ndn, j = t % ndn, pj = nup + j;
+                const double a = Si[j + (size_t)i * nd], tt = M[j + (size_t)i * nd];
+                if (th == 0) {   // vorb(1): S' = 1
+                    sl += a;
+                    sq -= tt;
+                } else if (th < norb) {
+                    const int q0 = sh0[th - 1], q1 = sh0[th];
+                    double ds = 0.0, dl = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
+                    for (int q = q0; q < q1; ++q) {
+                        const KVecDev& K = kv[q];
+                        const double* ci = cs + 2 * ((size_t)(q - 1) * P + i);
+                        const double* cj = cs + 2 * ((size_t)(q - 1) * P + pj);
+                        const double co = ci[0] * cj[0] + ci[1] * cj[1];
+                        const double si = ci[1] * cj[0] - ci[0] * cj[1];
+                        ds += 2.0 * co;
+                        dl -= 2.0 * K.k2 * co;
+                        g0 -= 2.0 * si * K.k[0];
+                        g1 -= 2.0 * si * K.k[1];
+                        g2 -= 2.0 * si * K.k[2];
+                    }
+                    const double dm = dl * ims + 2.0 * (g0 * (w[3 * i] - w[3 * pj]) + g1 * (w[3 * i + 1] - w[3 * pj + 1]) +
+                                                        g2 * (w[3 * i + 2] - w[3 * pj + 2]));
+                    sl += a * ds;
+                    sq += a * dm - tt * ds;
+                } else {   // bfact: beta / bfact
+                    double d[3];
+                    for (int cc = 0; cc < 3; ++cc) d[cc] = walker::min_image(xs[3 * i + cc] - xs[3 * pj + cc], p);
+                    const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                    double f, df, d2f;
+                    beta_all(p, tud, r, f, df, d2f);
+                    const double ib = 1.0 / bfact;
+                    const double dr = r > 0.0 ? df / r : 0.0;
+                    const double dm = d2f * ims + 2.0 * dr * (d[0] * (w[3 * i] - w[3 * pj]) + d[1] * (w[3 * i + 1] - w[3 * pj + 1]) +
+                                                              d[2] * (w[3 * i + 2] - w[3 * pj + 2]));
+                    sl += a * f * ib;
+                    sq += (a * dm - tt * f) * ib;
+                }
+            }
+            sl = block_sum1(sl, red);
+            sq = block_sum1(sq, red);
+            if (threadIdx.x == 0) {
+                res[th] = sl;
+                res[norb + 1 + th] = sq;
+            }
+        }
+        __syncthreads();
+        for (int th = threadIdx.x; th < np; th += kThreads) {
+            dlog[(size_t)wk * np + th] = res[th];
+            deloc[(size_t)wk * np + th] = -p.hbar * res[norb + 1 + th];
+        }
+        __syncthreads();
+    }
+}
+
 // getjasder (jastrowlongrange.f90:63-78) for one walker per CTA: the
 // long-range Jastrow at beta + dp, (beta + dp) - 2 dp and back, from the
 // densities rho_q; d/d beta by central differences as the reference takes
@@ -252,6 +482,35 @@ cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x
     if (e != cudaSuccess) return e;
     derbcs_kernel<<<grid < nw ? grid : nw, kThreads, smem, st>>>(p, kv, x, smati, dpsi, nw, stride < 0 ? p.norb : stride,
                                                                  off);
+    return cudaGetLastError();
+}
+
+// Layout of one pgrad CTA, in doubles: inverse, M, product buffer (nd^2
+// each), positions and Jastrow gradient (3 npart each), cos/sin of every
+// k vector at every particle (2 npart (nk-1)), reduction buffer, results.
+size_t pgrad_doubles(const DevParams& p)
+{
+    const size_t nd2 = (size_t)p.nd * p.nd;
+    return 3 * nd2 + 6 * (size_t)p.npart + 2 * (size_t)p.npart * (p.nk > 1 ? p.nk - 1 : 1) + kThreads +
+           2 * (size_t)(p.norb + 1) + (size_t)(p.norb + 2);
+}
+
+cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x, const double* sinv,
+                         const double* dpsi, const double* dphi, double* dlog, double* deloc, int nw, int np,
+                         double bfact, int grid, double* gscr, int smem_limit, cudaStream_t st)
+{
+    if (nw <= 0) return cudaSuccess;
+    const size_t need = pgrad_doubles(p);
+    const bool on_chip = need * 8 <= (size_t)smem_limit;
+    const size_t smem = on_chip ? need * 8 : 0;
+    if (on_chip) {
+        cudaError_t e = cudaFuncSetAttribute(pgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    } else if (!gscr) {
+        return cudaErrorInvalidValue;
+    }
+    pgrad_kernel<<<grid < nw ? grid : nw, kThreads, smem, st>>>(p, kv, tud, x, sinv, dpsi, dphi, dlog, deloc, nw, np,
+                                                                bfact, on_chip ? nullptr : gscr, need);
     return cudaGetLastError();
 }
 

@@ -226,6 +226,19 @@ int dmc_getphione_batch(dmc_ctx* ctx, int nw, const double* x, const int* ipart,
  * optbeta=.false.: d log|det| / d vorb(k), dpsi[nw][norb]. */
 int dmc_getderbcs_batch(dmc_ctx* ctx, int nw, const double* x, double* dpsi);
 
+/* No counterpart in the reference (its optimizer uses d log Psi only):
+ * per-walker gradients with respect to the amplitudes the pair function is
+ * linear in, theta = (vorb(1), ..., vorb(norb), bfact) -- bfact only when
+ * the beta function is on (bfact != 0); dmc_param_count gives their number
+ * np.  dlogpsi[nw][np] = d log|Psi| / d theta (the vorb part equals
+ * getderbcs, psislaterbcs.f90:449-524) and deloc[nw][np] = d E_L / d theta
+ * with E_L = -hbar d2psi + v in the units of v (step.f90:62,76), by the
+ * adjoint of the determinant's kinetic terms: one extra pair of nd^3
+ * products per walker for all parameters.  FP64 whatever the context's
+ * precision. */
+int dmc_param_count(const dmc_ctx* ctx, int* np);
+int dmc_param_grad(dmc_ctx* ctx, int nw, const double* x, double* dlogpsi, double* deloc);
+
 /* Replaces getjasder (jastrowlongrange.f90:63-78): dpsi[nw][2] = d U / d beta
  * (central differences with dp = 1e-4, as the reference takes them) and
  * d U / d gamma of the long-range Jastrow; DMC_ERR_INVALID when numq = 0. */
