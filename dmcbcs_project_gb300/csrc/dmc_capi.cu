@@ -499,6 +499,17 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
         const int need = c->L.total * 8 + static_smem + 1024;
         per_sm = std::max(1, std::min(regs_ok, smem_sm / need));
+        if (per_sm < regs_ok) {
+            // two CTAs per SM when the beta pair data move to global scratch
+            // (L2-resident, written by the pair stage and read once by the
+            // beta drift terms) and the rest of the layout fits twice
+            SmemLayout L2;
+            walker_smem_bytes(c->P, smem_sm / regs_ok - static_smem - 1024, &L2);
+            if (L2.total * 8 + static_smem + 1024 <= smem_sm / regs_ok) {
+                c->L = L2;
+                per_sm = regs_ok;
+            }
+        }
     }
     c->grid = c->nsm * per_sm;
     if (!c->L.pb_in_smem) {
