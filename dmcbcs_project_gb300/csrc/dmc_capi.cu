@@ -131,10 +131,11 @@ struct dmc_ctx {
     DevBuf<unsigned long long> psteps;
     int pcur = 0;          // slot of the current count
     bool n_stale = false;  // the device count leads (host n out of date)
-    // captured generations by (stack, count slot) parity, valid while the
-    // parameters, launch arguments and precision match the capture
-    cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    int gnl[2][2] = {{0, 0}, {0, 0}};
+    // captured generations by (opcomp, stack parity, count-slot parity),
+    // valid while the parameters, launch arguments and precision match the
+    // capture
+    cudaGraphExec_t gexec[2][2][2] = {};
+    int gnl[2][2][2] = {};
     DevParams gP;
     KernelArgs gA;
     int gprec = -1;
@@ -149,6 +150,10 @@ struct dmc_ctx {
     // single-particle moves and parameter derivatives
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
     DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
+    // device views of the caller's walker arrays from the last put/get call
+    void* hw_key[15] = {};
+    HostWalkers hw_view{};
+    bool hw_ok = false;
     DevBuf<int> sip;
     int64_t sr_count = 0;
     bool sr_jas = false, sr_det = true;   // iopt(1), iopt(2) of the optimizer deck
@@ -562,9 +567,10 @@ int dmc_destroy(dmc_ctx* c)
     c->vb2.release(); c->wb.release(); c->bx.release(); c->bpsil.release(); c->bdpsi.release();
     c->bd2psi.release(); c->bv.release(); c->bvext.release(); c->bpsigl.release(); c->bdpsig.release();
     c->bd2psig.release(); c->bsinv.release(); c->bis.release(); c->flush.release();
-    for (int i = 0; i < 2; ++i)
-        for (int j = 0; j < 2; ++j)
-            if (c->gexec[i][j]) cudaGraphExecDestroy(c->gexec[i][j]);
+    for (auto& a : c->gexec)
+        for (auto& b : a)
+            for (auto& g : b)
+                if (g) cudaGraphExecDestroy(g);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -831,6 +837,49 @@ int dmc_num_walkers(dmc_ctx* c, int* n)
     return DMC_OK;
 }
 
+// The device-side address of a caller's host array: pinned memory (mapped
+// into the device's address space), managed or device memory.  nullptr
+// for pageable memory, which then goes through cudaMemcpy.
+static void* device_view(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if (a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeDevice) return const_cast<void*>(p);
+    return nullptr;
+}
+
+// Device views of every non-null field of w (cached for the last set of
+// arrays); false when one of them is not addressable from the device.
+static bool host_views(dmc_ctx* c, const dmc_walkers* w, HostWalkers* h)
+{
+    void* key[15] = {w->x, w->dpsi, w->dpsig, w->psil, w->psigl, w->d2psi, w->d2psig, w->v, w->vext, w->weight,
+                     w->psil0, w->psigl0, w->wt0, w->is, w->irn};
+    if (std::memcmp(key, c->hw_key, sizeof key) != 0) {
+        void* view[15];
+        bool ok = true;
+        for (int k = 0; k < 15 && ok; ++k) {
+            view[k] = key[k] ? device_view(key[k]) : nullptr;
+            if (key[k] && !view[k]) ok = false;
+        }
+        std::memcpy(c->hw_key, key, sizeof key);
+        c->hw_ok = ok;
+        if (ok) {
+            HostWalkers& v = c->hw_view;
+            double** d[13] = {&v.x, &v.dpsi, &v.dpsig, &v.psil, &v.psigl, &v.d2psi, &v.d2psig, &v.v, &v.vext,
+                              &v.weight, &v.psil0, &v.psigl0, &v.wt0};
+            for (int k = 0; k < 13; ++k) *d[k] = static_cast<double*>(view[k]);
+            v.is = static_cast<int*>(view[13]);
+            v.irn = static_cast<long long*>(view[14]);
+        }
+    }
+    if (c->hw_ok) *h = c->hw_view;
+    return c->hw_ok;
+}
+
 int dmc_get_walkers(dmc_ctx* c, dmc_walkers* w)
 {
     if (!c || !w) return DMC_ERR_INVALID;
@@ -845,6 +894,14 @@ int dmc_get_walkers(dmc_ctx* c, dmc_walkers* w)
     const int n = c->n;
     const size_t n3 = (size_t)c->n3;
     StackBufs& s = c->st[c->istin];
+    HostWalkers hv;
+    if (n > 0 && host_views(c, w, &hv)) {
+        // one launch writes every field into the caller's mapped arrays
+        CK(launch_walkers_get(s.view(), hv, n, (int)n3, 8 * c->nsm, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        w->n = n;
+        return DMC_OK;
+    }
     CK(cudaStreamSynchronize(c->stream));
     auto D = [&](void* h, const void* d, size_t bytes) {
         return h ? cudaMemcpy(h, d, bytes, cudaMemcpyDeviceToHost) : cudaSuccess;
@@ -1097,10 +1154,68 @@ static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch)
     return DMC_OK;
 }
 
+// Drop the captured generations when anything they baked in changed.
+static void check_graphs(dmc_ctx* c)
+{
+    const KernelArgs A = base_args(c);
+    if (c->gprec == c->precision && std::memcmp(&c->gP, &c->P, sizeof c->P) == 0 &&
+        std::memcmp(&c->gA, &A, sizeof A) == 0)
+        return;
+    for (auto& a : c->gexec)
+        for (auto& b : a)
+            for (auto& g : b)
+                if (g) {
+                    cudaGraphExecDestroy(g);
+                    g = nullptr;
+                }
+    std::memcpy(&c->gP, &c->P, sizeof c->P);
+    std::memcpy(&c->gA, &A, sizeof A);
+    c->gprec = c->precision;
+}
+
+// One generation as a captured graph, one per (opcomp, stack parity,
+// count-slot parity) at its start, captured on first use.
+static int gen_graph(dmc_ctx* c, int opcomp, int* nlaunch)
+{
+    if (!c->n_stale) {   // the host count is current: hand it to the device
+        CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->n_stale = true;
+    }
+    check_graphs(c);
+    const int op = opcomp ? 1 : 0, pi = c->istin, pc = c->pcur;
+    cudaGraphExec_t& ex = c->gexec[op][pi][pc];
+    if (!ex) {
+        cudaGraph_t graph = nullptr;
+        const int64_t l0 = c->launches;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int nl = 0;
+        int rc = gen_async(c, op, &nl);
+        const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        if (rc == DMC_OK && ce != cudaSuccess) rc = cuda_fail(c, ce, "generation capture");
+        if (rc == DMC_OK) {
+            const cudaError_t ie = cudaGraphInstantiate(&ex, graph, 0);
+            if (ie != cudaSuccess) rc = cuda_fail(c, ie, "generation graph");
+        }
+        if (graph) cudaGraphDestroy(graph);
+        // the capture only recorded the launches: restore the parities
+        c->istin = pi;
+        c->pcur = pc;
+        c->launches = l0;
+        c->gnl[op][pi][pc] = nl;
+        if (rc) return rc;
+    }
+    CK(cudaGraphLaunch(ex, c->stream));
+    advance_parities(c);
+    c->launches += c->gnl[op][pi][pc];
+    if (nlaunch) *nlaunch = c->gnl[op][pi][pc];
+    return DMC_OK;
+}
+
 int dmc_generation(dmc_ctx* c, int opcomp, int* nt)
 {
     if (!c) return DMC_ERR_INVALID;
-    int rc = gen_async(c, opcomp, nullptr);
+    int rc = gen_graph(c, opcomp, nullptr);
     if (rc) return rc;
     // the count (and any error of the generation) comes back only on request
     if (nt) {
@@ -1826,22 +1941,6 @@ int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, i
     // events ev[2g] and ev[2g+1] (the L2 flush before it is not timed).
     std::vector<cudaEvent_t> ev(2 * (size_t)ngen, nullptr);
     for (auto& e : ev) CK(cudaEventCreate(&e));
-    {
-        // drop the captured generations when anything they baked in changed
-        const KernelArgs A = base_args(c);
-        if (c->gprec != c->precision || std::memcmp(&c->gP, &c->P, sizeof c->P) != 0 ||
-            std::memcmp(&c->gA, &A, sizeof A) != 0) {
-            for (int i = 0; i < 2; ++i)
-                for (int j = 0; j < 2; ++j)
-                    if (c->gexec[i][j]) {
-                        cudaGraphExecDestroy(c->gexec[i][j]);
-                        c->gexec[i][j] = nullptr;
-                    }
-            std::memcpy(&c->gP, &c->P, sizeof c->P);
-            std::memcpy(&c->gA, &A, sizeof A);
-            c->gprec = c->precision;
-        }
-    }
     int64_t lsum = 0;
     // the host count goes to the device once, before any capture
     CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -1850,39 +1949,12 @@ int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, i
     for (int g = 0; g < ngen && rc == DMC_OK; ++g) {
         if (flush_l2) CK(cudaMemsetAsync(c->flush.p, g & 0xff, c->flush.n, c->stream));
         const bool last = (g == ngen - 1) && opcomp_last;
-        if (last) {
-            // estimator-complete generation: launched directly
-            CK(cudaEventRecord(ev[2 * g], c->stream));
-            int nl = 0;
-            rc = gen_async(c, opcomp_last, &nl);
-            lsum += nl;
-            CK(cudaEventRecord(ev[2 * g + 1], c->stream));
-            continue;
-        }
-        const int pi = c->istin, pc = c->pcur;
-        if (!c->gexec[pi][pc]) {
-            cudaGraph_t graph = nullptr;
-            const int64_t l0 = c->launches;
-            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            int nl = 0;
-            rc = gen_async(c, 0, &nl);
-            cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
-            if (rc == DMC_OK && ce != cudaSuccess) rc = DMC_ERR_CUDA;
-            if (rc == DMC_OK && cudaGraphInstantiate(&c->gexec[pi][pc], graph, 0) != cudaSuccess) rc = DMC_ERR_CUDA;
-            if (graph) cudaGraphDestroy(graph);
-            // the capture only recorded the launches: restore the parities
-            c->istin = pi;
-            c->pcur = pc;
-            c->launches = l0;
-            c->gnl[pi][pc] = nl;
-            if (rc) break;
-        }
         CK(cudaEventRecord(ev[2 * g], c->stream));
-        CK(cudaGraphLaunch(c->gexec[pi][pc], c->stream));
+        int nl = 0;
+        rc = gen_graph(c, last ? 1 : 0, &nl);
+        if (rc) break;
+        lsum += nl;
         CK(cudaEventRecord(ev[2 * g + 1], c->stream));
-        advance_parities(c);
-        c->launches += c->gnl[pi][pc];
-        lsum += c->gnl[pi][pc];
     }
     CK(cudaStreamSynchronize(c->stream));
     double total = 0.0;
@@ -1912,6 +1984,17 @@ int dmc_put_walkers(dmc_ctx* c, const dmc_walkers* w)
         return fail(c, DMC_ERR_INVALID, "dmc_put_walkers needs every field");
     StackBufs& s = c->st[c->istin];
     const size_t n3 = (size_t)c->n3;
+    HostWalkers hv;
+    if (n > 0 && host_views(c, w, &hv)) {
+        // one launch reads every field from the caller's mapped arrays and
+        // leaves the count in the device count slot for the next generation
+        CK(cudaStreamSynchronize(c->stream));
+        CK(launch_walkers_put(hv, s.view(), n, (int)n3, c->pop.p + c->pcur, 8 * c->nsm, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->n = n;
+        c->n_stale = true;
+        return DMC_OK;
+    }
     auto H = [&](void* d, const void* h, size_t bytes) {
         return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream);
     };

@@ -728,6 +728,78 @@ cudaError_t launch_branch_dev(const DevStack& in, const DevStack& out, const int
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Whole walker stacks to and from the caller's host arrays in one launch each
+// (dmc_put_walkers / dmc_get_walkers), reading and writing mapped host memory
+// directly; the reference's single-precision wt0 (stack.f90:12) is converted
+// here.  put also leaves the walker count in the device count slot.
+// ---------------------------------------------------------------------------
+__global__ void walkers_put_kernel(HostWalkers h, DevStack d, int n, int n3, int* pn)
+{
+    const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (size_t)gridDim.x * blockDim.x;
+    const size_t nb = (size_t)n * n3;
+    for (size_t e = t0; e < nb; e += nt) {
+        d.x[e] = h.x[e];
+        d.dpsi[e] = h.dpsi[e];
+        d.dpsig[e] = h.dpsig[e];
+    }
+    for (size_t k = t0; k < (size_t)n; k += nt) {
+        d.psil[k] = h.psil[k];
+        d.psigl[k] = h.psigl[k];
+        d.d2psi[k] = h.d2psi[k];
+        d.d2psig[k] = h.d2psig[k];
+        d.v[k] = h.v[k];
+        d.vext[k] = h.vext[k];
+        d.weight[k] = h.weight[k];
+        d.psil0[k] = h.psil0[k];
+        d.psigl0[k] = h.psigl0[k];
+        d.wt0[k] = (float)h.wt0[k];
+        d.is[k] = h.is[k];
+        d.irn[k] = (unsigned long long)h.irn[k];
+    }
+    if (t0 == 0 && pn) *pn = n;
+}
+
+// absent (null) host fields are skipped
+__global__ void walkers_get_kernel(DevStack d, HostWalkers h, int n, int n3)
+{
+    const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (size_t)gridDim.x * blockDim.x;
+    const size_t nb = (size_t)n * n3;
+    for (size_t e = t0; e < nb; e += nt) {
+        if (h.x) h.x[e] = d.x[e];
+        if (h.dpsi) h.dpsi[e] = d.dpsi[e];
+        if (h.dpsig) h.dpsig[e] = d.dpsig[e];
+    }
+    for (size_t k = t0; k < (size_t)n; k += nt) {
+        if (h.psil) h.psil[k] = d.psil[k];
+        if (h.psigl) h.psigl[k] = d.psigl[k];
+        if (h.d2psi) h.d2psi[k] = d.d2psi[k];
+        if (h.d2psig) h.d2psig[k] = d.d2psig[k];
+        if (h.v) h.v[k] = d.v[k];
+        if (h.vext) h.vext[k] = d.vext[k];
+        if (h.weight) h.weight[k] = d.weight[k];
+        if (h.psil0) h.psil0[k] = d.psil0[k];
+        if (h.psigl0) h.psigl0[k] = d.psigl0[k];
+        if (h.wt0) h.wt0[k] = (double)d.wt0[k];
+        if (h.is) h.is[k] = d.is[k];
+        if (h.irn) h.irn[k] = (long long)d.irn[k];
+    }
+}
+
+cudaError_t launch_walkers_put(const HostWalkers& h, const DevStack& d, int n, int n3, int* pn, int grid,
+                               cudaStream_t st)
+{
+    walkers_put_kernel<<<grid, 256, 0, st>>>(h, d, n, n3, pn);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_walkers_get(const DevStack& d, const HostWalkers& h, int n, int n3, int grid, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    walkers_get_kernel<<<grid, 256, 0, st>>>(d, h, n, n3);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_popctl(const int* pn, double nwalk, double popup, double popdn, int* need, double* factor,
                           int* flags, cudaStream_t st)
 {

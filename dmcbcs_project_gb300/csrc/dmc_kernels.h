@@ -43,6 +43,16 @@ cudaError_t launch_bcsone(const DevParams& p, const KVecDev* kv, const TabUD* tu
                           cudaStream_t st);
 cudaError_t launch_getphione(const DevParams& p, const TabUD* tud, const TabSS* tss, const double* x,
                              const int* ipart, const double* drr, double* ratio, int nw, cudaStream_t st);
+// walker arrays in host memory the device addresses directly (pinned and
+// mapped, or managed), laid out as dmc_walkers
+struct HostWalkers {
+    double *x, *dpsi, *dpsig, *psil, *psigl, *d2psi, *d2psig, *v, *vext, *weight, *psil0, *psigl0, *wt0;
+    int* is;
+    long long* irn;
+};
+cudaError_t launch_walkers_put(const HostWalkers& h, const DevStack& d, int n, int n3, int* pn, int grid,
+                               cudaStream_t st);
+cudaError_t launch_walkers_get(const DevStack& d, const HostWalkers& h, int n, int n3, int grid, cudaStream_t st);
 size_t derbcs_smem_bytes(const DevParams& p);
 // adjoint parameter gradients (dmc_single.cu): doubles of one CTA's working
 // set; on chip when it fits in smem_limit bytes, else in gscr (grid x that)
