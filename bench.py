@@ -221,9 +221,11 @@ def time_path(ctx, args, world, local, barrier):
 
 
 def e2e_rate(ctx, info, args, world, barrier):
-    """The same generations through the C ABI with the walker state in pinned
-    host memory: dmc_put_walkers, dmc_generation, dmc_get_walkers and the
-    estimator sums every generation."""
+    """The same generations through the C ABI with the walker population in
+    pinned host memory, as a host that keeps its own stacks holds it:
+    dmc_generation_host every generation (the walker kernel reads each
+    walker's state from the host arrays, one kernel writes the new
+    population back) and the estimator sums."""
     import torch
 
     cap = info.capacity
@@ -235,22 +237,25 @@ def e2e_rate(ctx, info, args, world, barrier):
     host["irn"] = pin((cap,), torch.int64)
     host["cap"] = cap
     n_cur = ctx.get_walkers_into(host)
-    per_walker = 3 * 3 * info.npart * 8 + 10 * 8 + 8 + 4 + 8     # x, dpsi, dpsig, 10 doubles, wt0, is, irn
+    n3b = 3 * info.npart * 8
+    # read per walker: x, dpsig, 11 doubles, is, irn (dpsi only for rejected
+    # moves: none with idmc = 1); written: every field
+    per_in = 2 * n3b + 11 * 8 + 4 + 8
+    per_out = 3 * n3b + 10 * 8 + 8 + 4 + 8
     nsteps = max(1, min(args.steps, args.e2e_steps))
-    h2d = d2h = 0
+    h2d = d2h = total = 0
     barrier()
     t0 = time.perf_counter()
     for g in range(nsteps):
-        ctx.put_walkers(dict(host, n=n_cur))
-        h2d += n_cur * per_walker
-        ctx.generation(g == nsteps - 1)
-        n_new = ctx.get_walkers_into(host)
-        d2h += n_new * per_walker + 3 * info.nest * 8
+        n_new = ctx.generation_host(dict(host, n=n_cur), host, g == nsteps - 1)
+        total += n_cur
+        h2d += n_cur * per_in + 4
+        d2h += n_new * per_out + 16
         ctx.estimators()
+        d2h += 3 * info.nest * 8
         n_cur = n_new
     barrier()
     t = time.perf_counter() - t0
-    total = h2d // per_walker                  # walkers entering each generation
     rate = total / t
     if world > 1:
         tt = torch.tensor([t], device="cuda", dtype=torch.float64)
@@ -260,7 +265,7 @@ def e2e_rate(ctx, info, args, world, barrier):
         rate = float(s_t.item()) / float(tt.item())
     return {"value": rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d / nsteps),
             "d2h_bytes_per_step": int(d2h / nsteps), "steps": nsteps,
-            "path": "dmc_put_walkers + dmc_generation + dmc_get_walkers + dmc_get_estimators, pinned host"}
+            "path": "dmc_generation_host (population in pinned host arrays) + dmc_get_estimators"}
 
 
 def accuracy_vs_fp64(ctx_mixed, ctx_fp64, hbar, nmax=512):

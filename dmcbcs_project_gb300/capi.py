@@ -30,6 +30,7 @@ EXPORTS = [
     "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure", "dmc_dfmath_eval",
     "dmc_batch_create", "dmc_batch_destroy", "dmc_batch_last_error", "dmc_batch_set_grids", "dmc_batch_get_grids",
     "dmc_batch_plan", "dmc_batch_tune", "dmc_batch_generations", "dmc_param_count", "dmc_param_grad",
+    "dmc_generation_host",
 ]
 
 PREC_FP64 = 0
@@ -120,6 +121,7 @@ def load(path=LIB_PATH):
     L.dmc_sr_update.argtypes = [vp, C.c_double, C.c_double, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.dmc_branch_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(abi.DevStack),
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
+    L.dmc_generation_host.argtypes = [vp, C.POINTER(Walkers), C.POINTER(Walkers), C.c_int]
     L.dmc_param_count.argtypes = [vp, C.POINTER(C.c_int)]
     L.dmc_param_grad.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.dmc_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
@@ -525,6 +527,14 @@ class Context:
 
     def put_walkers(self, arrs):
         self._check(load().dmc_put_walkers(self._h, C.byref(self.walker_struct(arrs))))
+
+    def generation_host(self, arrs_in, arrs_out, opcomp):
+        """One generation on a population held in host arrays (dicts as for
+        put_walkers; arrs_out['cap'] is its capacity); returns the new count."""
+        wi = self.walker_struct(arrs_in)
+        wo = self.walker_struct(dict(arrs_out, n=arrs_out["cap"]))
+        self._check(load().dmc_generation_host(self._h, C.byref(wi), C.byref(wo), int(bool(opcomp))))
+        return wo.n
 
     def get_walkers_into(self, arrs):
         """dmc_get_walkers into caller-owned arrays (capacity arrs['cap']); returns n."""

@@ -151,9 +151,9 @@ struct dmc_ctx {
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
     DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
     // device views of the caller's walker arrays from the last put/get call
-    void* hw_key[15] = {};
-    HostWalkers hw_view{};
-    bool hw_ok = false;
+    void* hw_key[2][15] = {};
+    HostWalkers hw_view[2] = {};
+    bool hw_ok[2] = {false, false};
     DevBuf<int> sip;
     int64_t sr_count = 0;
     bool sr_jas = false, sr_det = true;   // iopt(1), iopt(2) of the optimizer deck
@@ -854,21 +854,21 @@ static void* device_view(const void* p)
 
 // Device views of every non-null field of w (cached for the last set of
 // arrays); false when one of them is not addressable from the device.
-static bool host_views(dmc_ctx* c, const dmc_walkers* w, HostWalkers* h)
+static bool host_views(dmc_ctx* c, const dmc_walkers* w, HostWalkers* h, int slot = 0)
 {
     void* key[15] = {w->x, w->dpsi, w->dpsig, w->psil, w->psigl, w->d2psi, w->d2psig, w->v, w->vext, w->weight,
                      w->psil0, w->psigl0, w->wt0, w->is, w->irn};
-    if (std::memcmp(key, c->hw_key, sizeof key) != 0) {
+    if (std::memcmp(key, c->hw_key[slot], sizeof key) != 0) {
         void* view[15];
         bool ok = true;
         for (int k = 0; k < 15 && ok; ++k) {
             view[k] = key[k] ? device_view(key[k]) : nullptr;
             if (key[k] && !view[k]) ok = false;
         }
-        std::memcpy(c->hw_key, key, sizeof key);
-        c->hw_ok = ok;
+        std::memcpy(c->hw_key[slot], key, sizeof key);
+        c->hw_ok[slot] = ok;
         if (ok) {
-            HostWalkers& v = c->hw_view;
+            HostWalkers& v = c->hw_view[slot];
             double** d[13] = {&v.x, &v.dpsi, &v.dpsig, &v.psil, &v.psigl, &v.d2psi, &v.d2psig, &v.v, &v.vext,
                               &v.weight, &v.psil0, &v.psigl0, &v.wt0};
             for (int k = 0; k < 13; ++k) *d[k] = static_cast<double*>(view[k]);
@@ -876,8 +876,8 @@ static bool host_views(dmc_ctx* c, const dmc_walkers* w, HostWalkers* h)
             v.irn = static_cast<long long*>(view[14]);
         }
     }
-    if (c->hw_ok) *h = c->hw_view;
-    return c->hw_ok;
+    if (c->hw_ok[slot]) *h = c->hw_view[slot];
+    return c->hw_ok[slot];
 }
 
 int dmc_get_walkers(dmc_ctx* c, dmc_walkers* w)
@@ -1096,7 +1096,8 @@ static void advance_parities(dmc_ctx* c)
     c->pcur = (c->pcur + nbr + 1) & 1;
 }
 
-static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch)
+static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch, const DevStack* in_host = nullptr,
+                     const double* wt0_host = nullptr)
 {
     if (!c->n_stale) {   // the host count is current: hand it to the device
         CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -1109,7 +1110,8 @@ static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch)
     a.nw = c->cap;                    // bound; the count is read from a.pn
     a.pn = c->pop.p + c->pcur;
     a.opcomp = opcomp ? 1 : 0;
-    a.in = c->st[c->istin].view();
+    a.in = in_host ? *in_host : c->st[c->istin].view();
+    a.in_wt0d = wt0_host;
     a.out = c->st[1 - c->istin].view();
     a.est = c->est.p;
     a.defer = (c->P.idmc == 1 || c->P.idmc == -2) ? 1 : 0;
@@ -1223,6 +1225,46 @@ int dmc_generation(dmc_ctx* c, int opcomp, int* nt)
         *nt = c->n;
     }
     return rc;
+}
+
+int dmc_generation_host(dmc_ctx* c, const dmc_walkers* in, dmc_walkers* out, int opcomp)
+{
+    if (!c || !in || !out || in->n < 0 || out->n < 0) return DMC_ERR_INVALID;
+    const int n = in->n;
+    if (n == 0) return fail(c, DMC_ERR_EMPTY, "no walkers");
+    if (n > c->cap) return fail(c, DMC_ERR_OVERFLOW, "more walkers than the stack capacity");
+    if (!in->x || !in->dpsi || !in->dpsig || !in->psil || !in->psigl || !in->d2psi || !in->d2psig || !in->v ||
+        !in->vext || !in->weight || !in->psil0 || !in->psigl0 || !in->wt0 || !in->is || !in->irn)
+        return fail(c, DMC_ERR_INVALID, "dmc_generation_host needs every input field");
+    HostWalkers hi, ho;
+    if (!host_views(c, in, &hi, 0) || !host_views(c, out, &ho, 1)) {
+        // arrays the device cannot address: hand the population over by copies
+        int rc = dmc_put_walkers(c, in);
+        if (rc == DMC_OK) rc = dmc_generation(c, opcomp, nullptr);
+        if (rc == DMC_OK) rc = dmc_get_walkers(c, out);
+        return rc;
+    }
+    // the walker kernel pops the caller's population directly (device views
+    // of the host arrays; wt0 converted to single precision on the device)
+    const DevStack hs{hi.x, hi.dpsi, hi.dpsig, hi.psil, hi.psigl, hi.d2psi, hi.d2psig, hi.v, hi.vext, hi.weight,
+                      hi.psil0, hi.psigl0, nullptr, hi.is, reinterpret_cast<unsigned long long*>(hi.irn)};
+    CK(cudaStreamSynchronize(c->stream));
+    c->n = n;
+    CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    c->n_stale = true;
+    int rc = gen_async(c, opcomp, nullptr, &hs, hi.wt0);
+    if (rc) return rc;
+    // the new population into the caller's arrays, its count read on the device
+    CK(launch_walkers_get(c->st[c->istin].view(), ho, 0, c->n3, 8 * c->nsm, c->stream, c->pop.p + c->pcur, out->n));
+    ++c->launches;
+    rc = sync_n(c);
+    if (rc) return rc;
+    if (c->n > out->n) {
+        out->n = c->n;
+        return fail(c, DMC_ERR_INVALID, "walker arrays too small");
+    }
+    out->n = c->n;
+    return DMC_OK;
 }
 
 int dmc_zero_estimators(dmc_ctx* c)

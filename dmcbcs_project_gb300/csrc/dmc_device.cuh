@@ -134,6 +134,8 @@ struct KernelArgs {
     double* gscratch;            // per-CTA global scratch when the pair data do not fit on chip
     const double* jq;            // long-range Jastrow q records, [nql][8]
     int* status;                 // per-walker status flags (bit 0: singular matrix)
+    const double* in_wt0d;       // MODE_STEP: the old wt0 in double precision (input stack in the
+                                 // caller's host arrays), else nullptr: in.wt0
 };
 
 // On-chip layout of one walker CTA, offsets in doubles.

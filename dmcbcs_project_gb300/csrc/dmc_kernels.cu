@@ -202,7 +202,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                     case 4: v = a.in.v[src]; break;
                     case 5: v = a.in.vext[src]; break;
                     case 6: v = a.in.weight[src]; break;
-                    case 7: v = (double)a.in.wt0[src]; break;
+                    case 7: v = a.in_wt0d ? (double)(float)a.in_wt0d[src] : (double)a.in.wt0[src]; break;
                     default: v = (double)a.in.is[src]; break;
                 }
                 s_old[k] = v;
@@ -410,8 +410,8 @@ __global__ void step_decide_kernel(const __grid_constant__ DevParams p, const __
                          a.in.vext[src], a.in.is[src]};
     double wnew;
     float wt0new;
-    step_decision(p, a.opcomp, nn, ol, a.in.weight[src], a.in.wt0[src], true, 0.0, a.est + (size_t)k * p.nest * 2,
-                  wnew, wt0new);
+    const float wt0 = a.in_wt0d ? (float)a.in_wt0d[src] : a.in.wt0[src];
+    step_decision(p, a.opcomp, nn, ol, a.in.weight[src], wt0, true, 0.0, a.est + (size_t)k * p.nest * 2, wnew, wt0new);
     a.out.weight[k] = wnew;
     a.out.wt0[k] = wt0new;
 }
@@ -760,9 +760,11 @@ __global__ void walkers_put_kernel(HostWalkers h, DevStack d, int n, int n3, int
     if (t0 == 0 && pn) *pn = n;
 }
 
-// absent (null) host fields are skipped
-__global__ void walkers_get_kernel(DevStack d, HostWalkers h, int n, int n3)
+// absent (null) host fields are skipped; with pn the count is read on the
+// device and at most cap walkers are written
+__global__ void walkers_get_kernel(DevStack d, HostWalkers h, int n, const int* pn, int cap, int n3)
 {
+    if (pn) n = min(*pn, cap);
     const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (size_t)gridDim.x * blockDim.x;
     const size_t nb = (size_t)n * n3;
     for (size_t e = t0; e < nb; e += nt) {
@@ -793,10 +795,11 @@ cudaError_t launch_walkers_put(const HostWalkers& h, const DevStack& d, int n, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_walkers_get(const DevStack& d, const HostWalkers& h, int n, int n3, int grid, cudaStream_t st)
+cudaError_t launch_walkers_get(const DevStack& d, const HostWalkers& h, int n, int n3, int grid, cudaStream_t st,
+                               const int* pn, int cap)
 {
-    if (n <= 0) return cudaSuccess;
-    walkers_get_kernel<<<grid, 256, 0, st>>>(d, h, n, n3);
+    if (!pn && n <= 0) return cudaSuccess;
+    walkers_get_kernel<<<grid, 256, 0, st>>>(d, h, n, pn, cap, n3);
     return cudaGetLastError();
 }
 

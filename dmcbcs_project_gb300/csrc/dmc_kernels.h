@@ -52,7 +52,9 @@ struct HostWalkers {
 };
 cudaError_t launch_walkers_put(const HostWalkers& h, const DevStack& d, int n, int n3, int* pn, int grid,
                                cudaStream_t st);
-cudaError_t launch_walkers_get(const DevStack& d, const HostWalkers& h, int n, int n3, int grid, cudaStream_t st);
+// with pn: the count is read on the device, at most cap walkers written
+cudaError_t launch_walkers_get(const DevStack& d, const HostWalkers& h, int n, int n3, int grid, cudaStream_t st,
+                               const int* pn = nullptr, int cap = 0);
 size_t derbcs_smem_bytes(const DevParams& p);
 // adjoint parameter gradients (dmc_single.cu): doubles of one CTA's working
 // set; on chip when it fits in smem_limit bytes, else in gscr (grid x that)

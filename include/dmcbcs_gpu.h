@@ -417,6 +417,19 @@ int dmc_last_step_ms(dmc_ctx* ctx, double* ms);
 int dmc_timed_generations(dmc_ctx* ctx, int ngen, int opcomp_last, int flush_l2, int64_t* walker_steps,
                           double* device_ms, int64_t* launches);
 
+/* One generation (dmcbcs.f90:436-448, as dmc_generation) for a host that
+ * keeps its walker stacks in its own memory (stack.f90:82-110): the
+ * population in->n walkers with every field set is read, the new population
+ * is written to out (out->n: its capacity on entry, the new count on
+ * return; out may be the same arrays as in).  With pinned (page-locked,
+ * mapped) host arrays the walker kernel reads each walker's state directly
+ * from them and one kernel writes the new population back, so the call
+ * makes one round trip; other memory goes through dmc_put_walkers,
+ * dmc_generation and dmc_get_walkers.  DMC_ERR_INVALID with out->n set to
+ * the count needed when out is too small (the first out->n walkers are
+ * written). */
+int dmc_generation_host(dmc_ctx* ctx, const dmc_walkers* in, dmc_walkers* out, int opcomp);
+
 /* Replace the current stack by w->n walkers with their full state (all
  * fields of dmc_walkers must be set): the inverse of dmc_get_walkers, for
  * hosts that keep the walker stacks in their own memory (stack.f90:82-110)
