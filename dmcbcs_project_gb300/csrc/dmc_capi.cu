@@ -142,7 +142,10 @@ struct dmc_ctx {
     DevBuf<double> est;
     DevBuf<int> counts, offs, status;
     DevBuf<unsigned long long> irn1, wtisto;
-    DevBuf<double> vb, vb2, wb;
+    // estimator block sums valblk, valblk2, wtblk: one buffer of
+    // 3 DMC_NEST_MAX doubles (vb2 and wb point into it), read with one copy
+    DevBuf<double> vb;
+    double *vb2 = nullptr, *wb = nullptr;
     // batch staging
     DevBuf<double> bx, bpsil, bdpsi, bd2psi, bv, bvext, bpsigl, bdpsig, bd2psig, bsinv;
     DevBuf<int> bis;
@@ -533,16 +536,16 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     const int nest = c->P.nest;
     if (c->st[0].alloc(c->cap, c->n3) || c->st[1].alloc(c->cap, c->n3) || c->est.alloc((size_t)c->cap * nest * 2) ||
         c->counts.alloc(c->cap) || c->offs.alloc(c->cap + 1) || c->irn1.alloc(c->cap) ||
-        c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(DMC_NEST_MAX) || c->vb2.alloc(DMC_NEST_MAX) ||
-        c->wb.alloc(DMC_NEST_MAX) || c->status.alloc(1) || c->pop.alloc(4) || c->popf.alloc(1) ||
+        c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(3 * DMC_NEST_MAX) || c->status.alloc(1) ||
+        c->pop.alloc(4) || c->popf.alloc(1) ||
         c->psteps.alloc(1)) {
         dmc_destroy(c);
         return DMC_ERR_NOMEM;
     }
     cudaMemset(c->wtisto.p, 0, DMC_WTISTO * sizeof(unsigned long long));
-    cudaMemset(c->vb.p, 0, DMC_NEST_MAX * sizeof(double));
-    cudaMemset(c->vb2.p, 0, DMC_NEST_MAX * sizeof(double));
-    cudaMemset(c->wb.p, 0, DMC_NEST_MAX * sizeof(double));
+    c->vb2 = c->vb.p + DMC_NEST_MAX;
+    c->wb = c->vb.p + 2 * DMC_NEST_MAX;
+    cudaMemset(c->vb.p, 0, 3 * DMC_NEST_MAX * sizeof(double));
     cudaMemset(c->status.p, 0, sizeof(int));
     cudaMemset(c->pop.p, 0, 4 * sizeof(int));
     cudaMemset(c->psteps.p, 0, sizeof(unsigned long long));
@@ -564,7 +567,7 @@ int dmc_destroy(dmc_ctx* c)
     c->tss_mp.release(); c->jumpA.release(); c->jumpC.release(); c->jq.release();
     c->gscratch.release(); c->st[0].release(); c->st[1].release(); c->est.release(); c->counts.release();
     c->offs.release(); c->status.release(); c->irn1.release(); c->wtisto.release(); c->vb.release();
-    c->vb2.release(); c->wb.release(); c->bx.release(); c->bpsil.release(); c->bdpsi.release();
+    c->bx.release(); c->bpsil.release(); c->bdpsi.release();
     c->bd2psi.release(); c->bv.release(); c->bvext.release(); c->bpsigl.release(); c->bdpsig.release();
     c->bd2psig.release(); c->bsinv.release(); c->bis.release(); c->flush.release();
     for (auto& a : c->gexec)
@@ -1006,9 +1009,7 @@ int dmc_initial_eval(dmc_ctx* c, double* sums)
         rc = reverse_stacks(c);
         if (rc) return rc;
     }
-    CK(cudaMemsetAsync(c->vb.p, 0, DMC_NEST_MAX * 8, c->stream));
-    CK(cudaMemsetAsync(c->vb2.p, 0, DMC_NEST_MAX * 8, c->stream));
-    CK(cudaMemsetAsync(c->wb.p, 0, DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->vb.p, 0, 3 * DMC_NEST_MAX * 8, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return DMC_OK;
 }
@@ -1036,7 +1037,7 @@ int dmc_step(dmc_ctx* c, int opcomp)
     CK(launch_walker(c->P, a, c->L, grid_for(c, n), c->stream, c->precision == DMC_PREC_MIXED));
     if (a.defer) CK(launch_step_decide(c->P, a, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
-    CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2.p, c->wb.p, c->stream));
+    CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2, c->wb, c->stream));
     c->launches += a.defer ? 3 : 2;
     c->istin = 1 - c->istin;
     return DMC_OK;
@@ -1128,7 +1129,7 @@ static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch, const DevStack* in_ho
         ++nl;
     }
     CK(cudaEventRecordWithFlags(c->ev1, c->stream, evflags));
-    CK(launch_estimators(c->est.p, 0, c->P.nest, c->vb.p, c->vb2.p, c->wb.p, c->stream, a.pn, c->psteps.p));
+    CK(launch_estimators(c->est.p, 0, c->P.nest, c->vb.p, c->vb2, c->wb, c->stream, a.pn, c->psteps.p));
     ++nl;
     c->istin = 1 - c->istin;
     int* pop = c->pop.p;
@@ -1248,8 +1249,7 @@ int dmc_generation_host(dmc_ctx* c, const dmc_walkers* in, dmc_walkers* out, int
     // of the host arrays; wt0 converted to single precision on the device)
     const DevStack hs{hi.x, hi.dpsi, hi.dpsig, hi.psil, hi.psigl, hi.d2psi, hi.d2psig, hi.v, hi.vext, hi.weight,
                       hi.psil0, hi.psigl0, nullptr, hi.is, reinterpret_cast<unsigned long long*>(hi.irn)};
-    CK(cudaStreamSynchronize(c->stream));
-    c->n = n;
+    c->n = n;   // staged by the copy below before it returns (pageable source)
     CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     c->n_stale = true;
     int rc = gen_async(c, opcomp, nullptr, &hs, hi.wt0);
@@ -1270,9 +1270,7 @@ int dmc_generation_host(dmc_ctx* c, const dmc_walkers* in, dmc_walkers* out, int
 int dmc_zero_estimators(dmc_ctx* c)
 {
     if (!c) return DMC_ERR_INVALID;
-    CK(cudaMemsetAsync(c->vb.p, 0, DMC_NEST_MAX * 8, c->stream));
-    CK(cudaMemsetAsync(c->vb2.p, 0, DMC_NEST_MAX * 8, c->stream));
-    CK(cudaMemsetAsync(c->wb.p, 0, DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->vb.p, 0, 3 * DMC_NEST_MAX * 8, c->stream));
     return DMC_OK;
 }
 
@@ -1280,10 +1278,12 @@ int dmc_get_estimators(dmc_ctx* c, double* valblk, double* valblk2, double* wtbl
 {
     if (!c || !valblk || !valblk2 || !wtblk) return DMC_ERR_INVALID;
     const int ne = c->P.nest;
+    double h[3 * DMC_NEST_MAX];
+    CK(cudaMemcpyAsync(h, c->vb.p, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    CK(cudaMemcpy(valblk, c->vb.p, ne * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(valblk2, c->vb2.p, ne * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(wtblk, c->wb.p, ne * 8, cudaMemcpyDeviceToHost));
+    std::memcpy(valblk, h, ne * 8);
+    std::memcpy(valblk2, h + DMC_NEST_MAX, ne * 8);
+    std::memcpy(wtblk, h + 2 * DMC_NEST_MAX, ne * 8);
     return DMC_OK;
 }
 
