@@ -153,10 +153,6 @@ struct dmc_ctx {
     // single-particle moves and parameter derivatives
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
     DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
-    // device views of the caller's walker arrays from the last put/get call
-    void* hw_key[2][15] = {};
-    HostWalkers hw_view[2] = {};
-    bool hw_ok[2] = {false, false};
     DevBuf<int> sip;
     int64_t sr_count = 0;
     bool sr_jas = false, sr_det = true;   // iopt(1), iopt(2) of the optimizer deck
@@ -855,32 +851,24 @@ static void* device_view(const void* p)
     return nullptr;
 }
 
-// Device views of every non-null field of w (cached for the last set of
-// arrays); false when one of them is not addressable from the device.
-static bool host_views(dmc_ctx* c, const dmc_walkers* w, HostWalkers* h, int slot = 0)
+// Device views of every non-null field of w; false when one of them is not
+// addressable from the device.  Looked up on every call: memory freed and
+// allocated again at the same address may be of another kind.
+static bool host_views(dmc_ctx*, const dmc_walkers* w, HostWalkers* h)
 {
     void* key[15] = {w->x, w->dpsi, w->dpsig, w->psil, w->psigl, w->d2psi, w->d2psig, w->v, w->vext, w->weight,
                      w->psil0, w->psigl0, w->wt0, w->is, w->irn};
-    if (std::memcmp(key, c->hw_key[slot], sizeof key) != 0) {
-        void* view[15];
-        bool ok = true;
-        for (int k = 0; k < 15 && ok; ++k) {
-            view[k] = key[k] ? device_view(key[k]) : nullptr;
-            if (key[k] && !view[k]) ok = false;
-        }
-        std::memcpy(c->hw_key[slot], key, sizeof key);
-        c->hw_ok[slot] = ok;
-        if (ok) {
-            HostWalkers& v = c->hw_view[slot];
-            double** d[13] = {&v.x, &v.dpsi, &v.dpsig, &v.psil, &v.psigl, &v.d2psi, &v.d2psig, &v.v, &v.vext,
-                              &v.weight, &v.psil0, &v.psigl0, &v.wt0};
-            for (int k = 0; k < 13; ++k) *d[k] = static_cast<double*>(view[k]);
-            v.is = static_cast<int*>(view[13]);
-            v.irn = static_cast<long long*>(view[14]);
-        }
+    void* view[15];
+    for (int k = 0; k < 15; ++k) {
+        view[k] = key[k] ? device_view(key[k]) : nullptr;
+        if (key[k] && !view[k]) return false;
     }
-    if (c->hw_ok[slot]) *h = c->hw_view[slot];
-    return c->hw_ok[slot];
+    double** d[13] = {&h->x, &h->dpsi, &h->dpsig, &h->psil, &h->psigl, &h->d2psi, &h->d2psig, &h->v, &h->vext,
+                      &h->weight, &h->psil0, &h->psigl0, &h->wt0};
+    for (int k = 0; k < 13; ++k) *d[k] = static_cast<double*>(view[k]);
+    h->is = static_cast<int*>(view[13]);
+    h->irn = static_cast<long long*>(view[14]);
+    return true;
 }
 
 int dmc_get_walkers(dmc_ctx* c, dmc_walkers* w)
@@ -1238,7 +1226,7 @@ int dmc_generation_host(dmc_ctx* c, const dmc_walkers* in, dmc_walkers* out, int
         !in->vext || !in->weight || !in->psil0 || !in->psigl0 || !in->wt0 || !in->is || !in->irn)
         return fail(c, DMC_ERR_INVALID, "dmc_generation_host needs every input field");
     HostWalkers hi, ho;
-    if (!host_views(c, in, &hi, 0) || !host_views(c, out, &ho, 1)) {
+    if (!host_views(c, in, &hi) || !host_views(c, out, &ho)) {
         // arrays the device cannot address: hand the population over by copies
         int rc = dmc_put_walkers(c, in);
         if (rc == DMC_OK) rc = dmc_generation(c, opcomp, nullptr);
