@@ -104,6 +104,15 @@ __device__ __forceinline__ unsigned long long lcg_jump(unsigned long long s0, co
 __device__ __forceinline__ double lcg_uniform(unsigned long long s) { return (double)(s | 1ull) * kTwoM48; }
 
 // minimum-image separation component
+// Division of loop indices by a runtime divisor d >= 1 with one multiply-high:
+// q = umulhi(e, m), m = floor((2^32 - 1) / d) + 1, is e / d for every
+// e * d < 2^32 (here e <= 256^2 and d <= 256); the divider is built once per loop.
+struct UDiv {
+    unsigned d, m;
+    __device__ __forceinline__ explicit UDiv(int dd) : d((unsigned)dd), m(dd > 1 ? 0xffffffffu / (unsigned)dd + 1u : 0u) {}
+    __device__ __forceinline__ int quo(int e) const { return d > 1 ? (int)__umulhi((unsigned)e, m) : e; }
+};
+
 __device__ __forceinline__ double min_image(double d, const DevParams& p) { return d - p.el * rint(d * p.eli); }
 __device__ __forceinline__ df min_image(df d, const DevParams& p)
 {
@@ -311,8 +320,10 @@ __device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double
     for (int r0 = 0; r0 < nup; r0 += c.L.rows_jas) {
         const int r1 = min(nup, r0 + c.L.rows_jas);
         const int npc = (r1 - r0) * ndn;
+        const UDiv dv(ndn);
         for (int q = threadIdx.x; q < npc; q += kThreads) {
-            const int i = r0 + q / ndn, j = q % ndn;
+            const int qi = dv.quo(q);
+            const int i = r0 + qi, j = q - qi * ndn;
             const R* xi = x + 3 * i;
             const R* xj = x + 3 * (nup + j);
             const R d0 = min_image(xi[0] - xj[0], p);
@@ -696,8 +707,9 @@ __device__ void gemm_stage(const Ctx<R>& c)
         for (int q = 1; q < p.nk; ++q) sv += 2.0f * fabsf(kv[q].hi);
         sig = pow2_ceil(4.0f * 1.001f * sv);
     }
+    const UDiv dg(ng);
     for (int t = threadIdx.x; t < p.nup * ng; t += kThreads) {
-        const int i = t / ng, g = t % ng;
+        const int i = dg.quo(t), g = t - i * ng;
         const R* u = U + i * ldU;
         const R* d[kGJ];
         bool ok[kGJ];
@@ -973,8 +985,9 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
         const bool scatter = (bw1 == 0) && (nxt == A0);
         if (bw1 > 0) {
             // columns of the next panel first, by everyone
+            const UDiv db(bw1);
             for (int e = threadIdx.x; e < n * bw1; e += kThreads) {
-                const int i = e / bw1, j = k1 + e % bw1;
+                const int i = db.quo(e), j = k1 + e - i * bw1;
                 nxt[i * ld + j] = gj_apply<R, B>(cur, ld, i, j, k0, bw, prow, rowpos);
             }
             if (warp < kPanelWarps) {
@@ -989,8 +1002,9 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
             const int nt = bw1 > 0 ? kThreads - 32 * kPanelWarps : kThreads;
             const int t0 = bw1 > 0 ? (int)threadIdx.x - 32 * kPanelWarps : (int)threadIdx.x;
             const int nc = n - bw1;
+            const UDiv dc(nc);
             for (int e = t0; e < n * nc; e += nt) {
-                const int i = e / nc, jj = e % nc;
+                const int i = dc.quo(e), jj = e - i * nc;
                 const int j = jj < k1 ? jj : jj + bw1;
                 // the block's own (factored) columns pass through unchanged
                 const R val = (j >= k0 && j < k1) ? cur[i * ld + j] : gj_apply<R, B>(cur, ld, i, j, k0, bw, prow, rowpos);
@@ -1013,8 +1027,9 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
     int odd = 0;
     if (!sing) {
         const bool copy = (cur == A1);
+        const UDiv dn(n);
         for (int e = threadIdx.x; e < n * n; e += kThreads) {
-            const int a = e / n, b = e % n;
+            const int a = dn.quo(e), b = e - a * n;
             if (copy) A0[a * ld + b] = A1[piv[a] * ld + rowpos[b]];
             if (a < b && piv[a] > piv[b]) odd ^= 1;
         }
@@ -1791,8 +1806,10 @@ __device__ void beta_drift_stage(const Ctx<R>& c)
         for (int r0 = 0; r0 < nup; r0 += c.L.rows_beta) {
             const int r1 = min(nup, r0 + c.L.rows_beta);
             const int npc = (r1 - r0) * ndn;
+            const UDiv dv(ndn);
             for (int q = threadIdx.x; q < npc; q += kThreads) {
-                const int i = r0 + q / ndn, j = q % ndn;
+                const int qi = dv.quo(q);
+                const int i = r0 + qi, j = q - qi * ndn;
                 const R* xi = xr + 3 * i;
                 const R* xj = xr + 3 * (nup + j);
                 const R* pbq = pb + 2 * (i * ndn + j);
