@@ -802,33 +802,29 @@ __device__ __forceinline__ df shfl_r(df v, int src)
     return df{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
 }
 
-// Named barrier 1 over the whole CTA: the panel warps wait, the others only
-// arrive.  Named barrier 2 pairs the two panel warps.
+// Named barrier 1 over the whole CTA: the panel warp waits, the others only
+// arrive.
 __device__ __forceinline__ void bar1_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
 __device__ __forceinline__ void bar1_arrive() { asm volatile("bar.arrive 1, %0;" ::"n"(kThreads) : "memory"); }
-__device__ __forceinline__ void bar2_panel() { asm volatile("bar.sync 2, 64;" ::: "memory"); }
 
-constexpr int kPanelWarps = 2;
+constexpr int kPanelWarps = 1;
 
 // Factor columns k0..k0+bw-1 of A (all n rows, rows pivoted in earlier
 // blocks excluded from the pivot search) by Gauss-Jordan steps restricted
-// to the panel.  Called by warps 0 and 1 (threads 0..63); thread t holds rows
-// t + 64 s in registers.  Each warp finds its best candidate with REDUX
-// max/min and publishes key, row and the candidate's panel row in shared
-// memory (double-buffered by step parity); after the pair barrier both
-// warps pick the same winner.  Records piv[k], pvals[k] and
-// rowpos[piv[k]] = k.  Returns false on a zero pivot.
+// to the panel.  Called by warp 0; lane t holds rows t + 32 s (s < RPL) in
+// registers, so the pivot search is a warp reduction (REDUX max of the
+// magnitude keys, then min of the rows that reach it: the first maximum, as
+// idamax) and the pivot row reaches every lane by shuffles.  Records piv[k],
+// pvals[k] and rowpos[piv[k]] = k.  Returns false on a zero pivot.
 template <class R, int RPL, int B>
 __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, int* piv, R* pvals, int* rowpos)
 {
-    __shared__ unsigned s_kh[2][kPanelWarps], s_kl[2][kPanelWarps], s_row[2][kPanelWarps];
-    __shared__ R s_cand[2][kPanelWarps][B];
-    const int t = threadIdx.x, pw = t >> 5;
+    const int t = threadIdx.x;
     R v[RPL][B];
     bool done[RPL];
 #pragma unroll
     for (int s = 0; s < RPL; ++s) {
-        const int r = t + 64 * s;
+        const int r = t + 32 * s;
         const bool ok = r < n;
         done[s] = !ok || rowpos[r] < k0;
 #pragma unroll
@@ -841,8 +837,7 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
 #pragma unroll 1
     for (int c = 0; c < B; ++c) {
         if (c < bw) {
-            const int buf = c & 1;
-            // this warp's largest |a| among rows not yet pivoted; smallest row on ties
+            // largest |a| among rows not yet pivoted; smallest row on ties
             unsigned kh[RPL], mh = 0u;
 #pragma unroll
             for (int s = 0; s < RPL; ++s) {
@@ -861,47 +856,33 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
                     }
                 gl = __reduce_max_sync(0xffffffffu, ml);
             }
+            if (gh == 0u && gl == 0u) return false;   // no non-zero candidate
             unsigned mine = 0xffffffffu;
 #pragma unroll
             for (int s = RPL - 1; s >= 0; --s)
-                if (!done[s] && kh[s] == gh && mag_lo(v[s][0]) == gl) mine = (unsigned)(t + 64 * s);
-            const unsigned wrow = __reduce_min_sync(0xffffffffu, mine);
-#pragma unroll
-            for (int s = 0; s < RPL; ++s)
-                if ((unsigned)(t + 64 * s) == wrow)
-#pragma unroll
-                    for (int c2 = 0; c2 < B; ++c2) s_cand[buf][pw][c2] = v[s][c2];
-            if ((t & 31) == 0) {
-                s_kh[buf][pw] = gh;
-                s_kl[buf][pw] = gl;
-                s_row[buf][pw] = wrow;
-            }
-            bar2_panel();
-            // keys and both candidate rows in one round of shared-memory reads
-            const unsigned h0 = s_kh[buf][0], h1 = s_kh[buf][1], l0 = s_kl[buf][0], l1 = s_kl[buf][1];
-            const unsigned r0 = s_row[buf][0], r1 = s_row[buf][1];
-            R ra[B], rb[B];
+                if (!done[s] && kh[s] == gh && mag_lo(v[s][0]) == gl) mine = (unsigned)(t + 32 * s);
+            const int pr = (int)__reduce_min_sync(0xffffffffu, mine);
+            // the pivot row from its lane (slot pr / 32 is the same on every lane)
+            const int ps = pr >> 5, pl = pr & 31;
+            R rr[B];
 #pragma unroll
             for (int c2 = 0; c2 < B; ++c2) {
-                ra[c2] = s_cand[buf][0][c2];
-                rb[c2] = s_cand[buf][1][c2];
+                R own = v[0][c2];
+#pragma unroll
+                for (int s = 1; s < RPL; ++s)
+                    if (ps == s) own = v[s][c2];
+                rr[c2] = shfl_r(own, pl);
             }
-            const int win = (h1 > h0 || (h1 == h0 && (l1 > l0 || (l1 == l0 && r1 < r0)))) ? 1 : 0;
-            if ((win ? h1 : h0) == 0u && (win ? l1 : l0) == 0u) return false;   // no non-zero candidate
-            const int pr = (int)(win ? r1 : r0);
             // Gauss-Jordan step with the unscaled pivot row p and multiplier
             // m = a_c / p_c per row (m = -1/p_c for the pivot row itself):
             //   a_c2 <- a_c2 - m p_c2   (pivot row: p_c2 / p_c),
             //   a_c  <- -m              (pivot row: 1 / p_c)
-            // one multiply per row instead of scaling the pivot row on every thread
-            R rr[B];
-#pragma unroll
-            for (int c2 = 0; c2 < B; ++c2) rr[c2] = win ? rb[c2] : ra[c2];
+            // one multiply per row instead of scaling the pivot row on every lane
             const R pv = rr[0];
             const R pinv = rcp(pv);
 #pragma unroll
             for (int s = 0; s < RPL; ++s) {
-                const bool isp = t + 64 * s == pr;
+                const bool isp = t + 32 * s == pr;
                 const R m = isp ? -pinv : v[s][0] * pinv;
 #pragma unroll
                 for (int c2 = 1; c2 < B; ++c2) v[s][c2] = fms(isp ? rzero<R>() : v[s][c2], m, rr[c2]);
@@ -925,7 +906,7 @@ __device__ __forceinline__ bool gj_panel(R* A, int ld, int n, int k0, int bw, in
     }
 #pragma unroll
     for (int s = 0; s < RPL; ++s) {
-        const int r = t + 64 * s;
+        const int r = t + 32 * s;
         if (r < n)
 #pragma unroll
             for (int c = 0; c < B; ++c)
@@ -1229,8 +1210,8 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
 {
     const int n = c.p.nd;
     if (c.L.S2 >= 0) {
-        if (n <= 64) return inverse_blocked<R, 1, 6>(c, logdet, sgn);
-        if (n <= 128) return inverse_blocked<R, 2, 8>(c, logdet, sgn);
+        if (n <= 64) return inverse_blocked<R, 2, 6>(c, logdet, sgn);
+        if (n <= 128) return inverse_blocked<R, 4, 8>(c, logdet, sgn);
     }
     return inverse_unblocked<R>(c, logdet, sgn);
 }
