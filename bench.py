@@ -37,12 +37,12 @@ WORKLOAD = "n66"
 # one step launch over 1024 walkers, ncu): FP64 walker kernel 4.14 MB,
 # mixed walker kernel 4.20 MB (profiles/walker_kernel_n66_fp64.md,
 # profiles/walker_kernel_n66_mixed.md).
-NCU_TRAFFIC_BYTES_PER_WALKER = {"fp64": 4044.5, "mixed": 4099.5}
+NCU_TRAFFIC_BYTES_PER_WALKER = {"fp64": 4045.0, "mixed": 4104.2}
 
 # FP32 flops (FFMA = 2, FADD/FMUL = 1) executed per walker-step by the mixed
 # walker kernel, from the instruction counters of the same capture:
-# 5.475e9 over 1024 walkers.
-MIXED_FP32_FLOPS_PER_WALKER = 5.347e6
+# 5.463e9 over 1024 walkers.
+MIXED_FP32_FLOPS_PER_WALKER = 5.335e6
 
 
 def algorithmic_flops(nup, ndn, nd, K, npart):
