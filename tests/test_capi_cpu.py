@@ -192,3 +192,30 @@ def test_batch_plan_small_and_invalid(lib):
     with pytest.raises(capi.DMCError):   # more systems than slots
         capi.batch_plan([1.0] * 3, [10] * 3, [1] * 3, [10] * 3, 1)
     assert np.all(capi.batch_plan([2.0], [100], [1], [152], 152) == 100)
+
+
+def test_new_entry_points_reject_bad_arguments(lib):
+    """Argument checks of the batch, gradient and host-generation entry
+    points (no context, no GPU work)."""
+    c_int, vp = ctypes.c_int, ctypes.c_void_p
+    lib.dmc_batch_create.argtypes = [vp, c_int, vp]
+    lib.dmc_batch_destroy.argtypes = [vp]
+    lib.dmc_batch_tune.argtypes = [vp, c_int, vp, vp]
+    lib.dmc_batch_generations.argtypes = [vp, c_int, c_int, c_int, vp, vp, vp]
+    lib.dmc_batch_set_grids.argtypes = [vp, vp]
+    lib.dmc_param_count.argtypes = [vp, vp]
+    lib.dmc_param_grad.argtypes = [vp, c_int, vp, vp, vp]
+    lib.dmc_generation_host.argtypes = [vp, vp, vp, c_int]
+    out = vp()
+    assert lib.dmc_batch_create(None, 1, ctypes.byref(out)) == abi.DMC_ERR_INVALID
+    assert lib.dmc_batch_create(None, 0, ctypes.byref(out)) == abi.DMC_ERR_INVALID
+    arr = (vp * 17)()
+    assert lib.dmc_batch_create(arr, 17, ctypes.byref(out)) == abi.DMC_ERR_INVALID   # more than DMC_BATCH_MAX
+    assert lib.dmc_batch_destroy(None) == abi.DMC_ERR_INVALID
+    assert lib.dmc_batch_tune(None, 1, None, None) == abi.DMC_ERR_INVALID
+    assert lib.dmc_batch_generations(None, 1, 1, 0, None, None, None) == abi.DMC_ERR_INVALID
+    assert lib.dmc_batch_set_grids(None, None) == abi.DMC_ERR_INVALID
+    n = c_int()
+    assert lib.dmc_param_count(None, ctypes.byref(n)) == abi.DMC_ERR_INVALID
+    assert lib.dmc_param_grad(None, 1, None, None, None) == abi.DMC_ERR_INVALID
+    assert lib.dmc_generation_host(None, None, None, 0) == abi.DMC_ERR_INVALID
