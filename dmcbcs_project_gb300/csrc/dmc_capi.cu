@@ -98,6 +98,18 @@ struct StackBufs {
 
 }  // namespace
 
+// CUDA events owned for the length of a call (destroyed on every return path)
+struct EventVec {
+    std::vector<cudaEvent_t> v;
+    explicit EventVec(size_t n) : v(n, nullptr) {}
+    ~EventVec()
+    {
+        for (cudaEvent_t e : v)
+            if (e) cudaEventDestroy(e);
+    }
+    cudaEvent_t& operator[](size_t i) { return v[i]; }
+};
+
 struct dmc_ctx {
     Setup S;
     dmc_system_desc sd;
@@ -1969,8 +1981,8 @@ int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, i
     // Each generation is a captured graph, one per (stack, count-slot)
     // parity at its start; the timed region of generation g lies between
     // events ev[2g] and ev[2g+1] (the L2 flush before it is not timed).
-    std::vector<cudaEvent_t> ev(2 * (size_t)ngen, nullptr);
-    for (auto& e : ev) CK(cudaEventCreate(&e));
+    EventVec ev(2 * (size_t)ngen);
+    for (auto& e : ev.v) CK(cudaEventCreate(&e));
     int64_t lsum = 0;
     // the host count goes to the device once, before any capture
     CK(cudaMemcpyAsync(c->pop.p + c->pcur, &c->n, sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -1993,7 +2005,6 @@ int dmc_timed_generations(dmc_ctx* c, int ngen, int opcomp_last, int flush_l2, i
         CK(cudaEventElapsedTime(&ms, ev[2 * g], ev[2 * g + 1]));
         total += ms;
     }
-    for (auto& e : ev) cudaEventDestroy(e);
     unsigned long long steps = 0;
     CK(cudaMemcpy(&steps, c->psteps.p, sizeof steps, cudaMemcpyDeviceToHost));
     const int rs = sync_n(c);
@@ -2496,8 +2507,8 @@ int dmc_batch_generations(dmc_batch* b, int ngen, int opcomp_last, int flush_l2,
     for (dmc_ctx* c : b->sys) CKB(cudaMemsetAsync(c->psteps.p, 0, sizeof(unsigned long long), c->stream));
     rc = push_counts(b);
     if (rc) return rc;
-    std::vector<cudaEvent_t> ev(2 * (size_t)ngen, nullptr);
-    for (auto& e : ev) CKB(cudaEventCreate(&e));
+    EventVec ev(2 * (size_t)ngen);
+    for (auto& e : ev.v) CKB(cudaEventCreate(&e));
     int64_t lsum = 0;
     for (int g = 0; g < ngen && rc == DMC_OK; ++g) {
         if (flush_l2) CKB(cudaMemsetAsync(b->flush.p, g & 0xff, b->flush.n, b->stream));
@@ -2548,7 +2559,6 @@ int dmc_batch_generations(dmc_batch* b, int ngen, int opcomp_last, int flush_l2,
         CKB(cudaEventElapsedTime(&ms, ev[2 * g], ev[2 * g + 1]));
         total += ms;
     }
-    for (auto& e : ev) cudaEventDestroy(e);
     int64_t steps = 0;
     for (dmc_ctx* c : b->sys) {
         unsigned long long st = 0;
