@@ -356,6 +356,39 @@ def param_gradients(args, rank):
                         "device-to-host copy of both gradients"}
 
 
+def energy_agreement(args, rank, neq=20, nblocks=10, nstep=20):
+    """DMC energy of the mixed and the FP64 path from the same seed: neq
+    generations of equilibration, then nblocks blocks of nstep generations
+    with the estimators on every generation (dmcbcs.f90:426-449); energy per
+    particle in free-gas units with the error of the block averages."""
+    from dmcbcs_project_gb300 import capi, configs
+
+    out = {}
+    for prec in ("mixed", "fp64"):
+        s, r, _ = configs.workload(WORKLOAD, nwalk=args.walkers or configs.WORKLOADS[WORKLOAD][3])
+        r.seed = 17 + 1000003 * rank
+        with capi.Context(s, r, precision=prec) as c:
+            c.init_walkers()
+            c.initial_eval()
+            for _ in range(neq):
+                c.generation(False)
+            c.zero_estimators()
+            blocks = []
+            for _ in range(nblocks):
+                for j in range(nstep):
+                    c.generation(True)
+                val, _ = c.block_update()
+                blocks.append(float(val[0]))
+        b = np.array(blocks)
+        out[prec] = {"energy": float(b.mean()), "error": float(b.std(ddof=1) / np.sqrt(len(b)))}
+    d = out["mixed"]["energy"] - out["fp64"]["energy"]
+    sig = float(np.hypot(out["mixed"]["error"], out["fp64"]["error"]))
+    return {"unit": "E / (N E_FG)", "generations": neq + nblocks * nstep, "blocks": nblocks,
+            "mixed": out["mixed"], "fp64": out["fp64"], "delta": d, "sigma": sig,
+            "delta_over_sigma": abs(d) / sig if sig > 0 else None,
+            "note": "same seed and random streams for both paths, so the two runs are correlated"}
+
+
 def run_gpu(args):
     import torch
 
@@ -424,6 +457,8 @@ def run_gpu(args):
                 "peak_source": "FFMA throughput probe measured in this run (no FP32 figure in the measured-peaks file)"}
 
     acc = accuracy_vs_fp64(ctxs["mixed"], ctxs["fp64"], sysd.hbar) if len(ctxs) == 2 and rank == 0 else None
+    if acc is not None and args.energy_blocks > 0:
+        acc["dmc_energy"] = energy_agreement(args, rank, nblocks=args.energy_blocks)
 
     # The N = 132 (66 up / 66 down) system of the mixed-precision benchmark
     # configuration, 8192 walkers: both paths over a short run (not the
@@ -514,6 +549,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n132-steps", type=int, default=20,
                     help="generations of the N = 132, 8192-walker side measurement (0: skip)")
+    ap.add_argument("--energy-blocks", type=int, default=10,
+                    help="blocks of 20 generations of the mixed-vs-FP64 DMC energy comparison (0: skip)")
     ap.add_argument("--pgrad-walkers", type=int, default=8192,
                     help="walkers of the adjoint parameter-gradient side measurement (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=20,
