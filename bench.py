@@ -243,6 +243,7 @@ def e2e_rate(ctx, info, args, world, barrier):
     per_in = 2 * n3b + 11 * 8 + 4 + 8
     per_out = 3 * n3b + 10 * 8 + 8 + 4 + 8
     nsteps = max(1, min(args.steps, args.e2e_steps))
+    n_cur = ctx.generation_host(dict(host, n=n_cur), host, False)   # warm-up, untimed
     h2d = d2h = total = 0
     barrier()
     t0 = time.perf_counter()
@@ -542,7 +543,7 @@ def main():
     ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"],
                     help="both: the mixed path is the headline, the FP64 path is timed beside it")
     ap.add_argument("--walkers", type=int, default=None)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-walkers", type=int, default=512)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-walkers", type=int, default=1024)
