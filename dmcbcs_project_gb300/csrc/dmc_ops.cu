@@ -105,16 +105,37 @@ __global__ void __launch_bounds__(kThreads) ops_enk_kernel(const __grid_constant
                                                           const double* __restrict__ x,
                                                           const unsigned long long* __restrict__ irn,
                                                           const double* __restrict__ sinv, int n,
-                                                          double* __restrict__ tk)
+                                                          double* __restrict__ tk, int tab)
 {
     extern __shared__ __align__(16) double osm[];
     const int P = p.npart, nd = p.nd, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nct = o.nnk + 1;
+    const int nct = o.nnk + 1, nq = p.nk - 1;
     double* xs = osm;
     double* accv = xs + 3 * P;   // [kWarps][nkv]
+    // with tab: (cos, sin) of every k vector at every particle, [nq][P], and
+    // at each warp's moved particle, [kWarps][nq]
+    // (16-byte aligned: the offset from the aligned start is rounded up to an even count)
+    double2* cs = reinterpret_cast<double2*>(osm + ((3 * P + kWarps * o.nkv + 1) & ~1));
+    double2* csn = cs + (size_t)nq * P + (size_t)warp * nq;
+    // with tab: each particle's Jastrow sum at its current position, [P]
+    double* uold = reinterpret_cast<double*>(cs + (size_t)nq * P + (size_t)kWarps * nq);
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         for (int t = threadIdx.x; t < 3 * P; t += kThreads) xs[t] = x[(size_t)w * 3 * P + t];
         for (int t = threadIdx.x; t < kWarps * o.nkv; t += kThreads) accv[t] = 0.0;
+        __syncthreads();
+        if (tab)
+            for (int t = threadIdx.x; t < nq * P; t += kThreads) {
+                const int k = t / P + 1, j = t - (k - 1) * P;
+                double sn, c;
+                sincos(kv[k].k[0] * xs[3 * j] + kv[k].k[1] * xs[3 * j + 1] + kv[k].k[2] * xs[3 * j + 2], &sn, &c);
+                cs[t] = make_double2(c, sn);
+            }
+        if (tab)
+            for (int i = warp; i < P; i += kWarps) {
+                const double r[3] = {xs[3 * i], xs[3 * i + 1], xs[3 * i + 2]};
+                const double u = single::warp_jastrow_sum(p, tud, tss, xs, i, r);
+                if (lane == 0) uold[i] = u;
+            }
         __syncthreads();
         const unsigned long long s0 = irn[w];
         const double* S = sinv + (size_t)w * nd * nd;
@@ -128,8 +149,22 @@ __global__ void __launch_bounds__(kThreads) ops_enk_kernel(const __grid_constant
                 drr[c] = -dx[c];
                 xi[c] = xs[3 * i + c] + dx[c];
             }
-            const double rat1 = single::warp_getphione(p, tud, tss, xs, i, drr);
-            const double rat2 = single::warp_bcsone(p, kv, tud, xs, S, i, xi);
+            double rat1, rat2;
+            if (tab) {
+                // getphione as exp(U(x_i') - U(x_i)) with U(x_i) computed once per walker
+                rat1 = exp(single::warp_jastrow_sum(p, tud, tss, xs, i, xi) - uold[i]);
+                for (int k = lane; k < nq; k += 32) {
+                    double sn, c;
+                    sincos(kv[k + 1].k[0] * xi[0] + kv[k + 1].k[1] * xi[1] + kv[k + 1].k[2] * xi[2], &sn, &c);
+                    csn[k] = make_double2(c, sn);
+                }
+                __syncwarp();
+                rat2 = single::warp_bcsone_tab(p, kv, tud, xs, S, i, xi, cs, csn);
+                __syncwarp();
+            } else {
+                rat1 = single::warp_getphione(p, tud, tss, xs, i, drr);
+                rat2 = single::warp_bcsone(p, kv, tud, xs, S, i, xi);
+            }
             const double psirat = rat1 * rat2;
             // cos(dk m dx_c) for m = 0..nnk, c = 0..2, one per lane
             double ct = 1.0;
@@ -225,10 +260,17 @@ cudaError_t launch_ops_enk(const DevParams& p, const OpsDev& o, const KVecDev* k
                            int n, double* tk, int grid, cudaStream_t st)
 {
     if (n <= 0 || o.nkv <= 0) return cudaSuccess;
-    const size_t smem = sizeof(double) * (3 * (size_t)p.npart + (size_t)kWarps * o.nkv);
+    const size_t base = sizeof(double) * ((3 * (size_t)p.npart + (size_t)kWarps * o.nkv + 1) & ~(size_t)1);
+    const size_t nq = p.nk > 1 ? p.nk - 1 : 1;
+    const size_t with_tab = base + sizeof(double2) * nq * ((size_t)p.npart + kWarps) + sizeof(double) * p.npart;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const int tab = with_tab <= (size_t)optin ? 1 : 0;   // plane-wave tables on chip when they fit
+    const size_t smem = tab ? with_tab : base;
     cudaError_t e = cudaFuncSetAttribute(ops_enk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    ops_enk_kernel<<<grid < n ? grid : n, kThreads, smem, st>>>(p, o, kv, tud, tss, x, irn, sinv, n, tk);
+    ops_enk_kernel<<<grid < n ? grid : n, kThreads, smem, st>>>(p, o, kv, tud, tss, x, irn, sinv, n, tk, tab);
     return cudaGetLastError();
 }
 

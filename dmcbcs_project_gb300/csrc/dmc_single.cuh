@@ -76,6 +76,49 @@ __device__ __forceinline__ double warp_bcsone(const DevParams& p, const KVecDev*
     return walker::warp_sum(acc);
 }
 
+// The same ratio with the plane waves from tables: cs[(k-1) npart + j] holds
+// (cos, sin) of k.x_j for every particle j and k = 1..nk-1, csn[k-1] the
+// same at the moved particle's new position, so each pair-function entry is
+// sum_k v_k (cos k.r' cos k.r_j + sin k.r' sin k.r_j) = sum_k v_k cos k.(r' - r_j)
+// with two multiply-adds per k instead of a cosine.
+__device__ __forceinline__ double warp_bcsone_tab(const DevParams& p, const KVecDev* __restrict__ kv,
+                                                  const TabUD* __restrict__ tud, const double* xw, const double* S,
+                                                  int i, const double (&xi)[3], const double2* cs,
+                                                  const double2* csn)
+{
+    const int lane = threadIdx.x & 31, nd = p.nd, P = p.npart, nq = p.nk - 1;
+    const bool isup = i < p.nup;
+    const int nloop = isup ? p.npair + p.nexdn : p.npair + p.nexup;
+    double acc = 0.0;
+    for (int q = lane; q < nd; q += 32) {
+        double ph;
+        if (q < nloop) {
+            const int jj = isup ? q + p.npair + p.nexup : q;
+            double d[3];
+            for (int c = 0; c < 3; ++c) {
+                d[c] = xi[c] - xw[3 * jj + c];
+                d[c] = d[c] - p.el * fnint(d[c] / p.el);
+            }
+            ph = kv[0].v;
+            const double2* cj = cs + jj;
+            for (int k = 0; k < nq; ++k) {
+                const double2 a = csn[k], b = cj[(size_t)k * P];
+                ph = fma(kv[k + 1].v, fma(a.x, b.x, a.y * b.y), ph);
+            }
+            ph += beta_value(p, tud, sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+        } else {
+            const int j = q - nloop;
+            const double* a = isup ? p.akup[j] : p.akdn[j];
+            const int sn = isup ? p.sinup[j] : p.sindn[j];
+            const double arg = a[0] * xi[0] + a[1] * xi[1] + a[2] * xi[2];
+            ph = sn ? sin(arg) : cos(arg);
+        }
+        const double s = isup ? S[q + (size_t)i * nd] : S[(i - p.nup) + (size_t)q * nd];
+        acc = fma(s, ph, acc);
+    }
+    return walker::warp_sum(acc);
+}
+
 // getphione (coshpot.f90:207-264): exp(U' - U) for particle i (0-based)
 // displaced by -drr.  Called by a whole warp; every lane returns the ratio.
 __device__ __forceinline__ double warp_getphione(const DevParams& p, const TabUD* __restrict__ tud,
@@ -102,6 +145,31 @@ __device__ __forceinline__ double warp_getphione(const DevParams& p, const TabUD
         }
     }
     return exp(walker::warp_sum(u));
+}
+
+// sum over the other particles j of u(|r - x_j|) for particle i (0-based) at
+// position r, with the pair rules of getphione (coshpot.f90:218-250); a
+// whole warp calls it and every lane returns the sum
+__device__ __forceinline__ double warp_jastrow_sum(const DevParams& p, const TabUD* __restrict__ tud,
+                                                   const TabSS* __restrict__ tss, const double* xw, int i,
+                                                   const double (&r)[3])
+{
+    const int lane = threadIdx.x & 31, P = p.npart;
+    const bool upi = i < p.nup;
+    double u = 0.0;
+    for (int j = lane; j < P; j += 32) {
+        if (j == i) continue;
+        const bool opposite = upi != (j < p.nup);
+        if (!opposite && !p.ieq) continue;
+        double d[3];
+        for (int c = 0; c < 3; ++c) {
+            d[c] = r[c] - xw[3 * j + c];
+            d[c] = d[c] - p.el * fnint(d[c] * p.eli);
+        }
+        const double rr = fmax(sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), 1.0e-14);
+        u += jastrow_u(p, tud, tss, opposite, rr);
+    }
+    return walker::warp_sum(u);
 }
 
 }  // namespace single
