@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -30,10 +31,15 @@ constexpr unsigned long long kMask48 = (1ull << 48) - 1ull;
 constexpr unsigned long long kMult1 = 44485709377909ull, kAdd1 = 96309754297ull;
 constexpr unsigned long long kMult2 = 34522712143931ull, kAdd2 = 55789347517ull;
 
+// Device array owned by its holder: freed by release() or on destruction.
 template <class T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
     cudaError_t alloc(size_t cnt)
     {
         if (cnt <= n && p) return cudaSuccess;
@@ -174,7 +180,7 @@ struct dmc_ctx {
         OpsDev dev{};
         std::vector<double> akq;
         std::vector<int> ik, indk, nkk, numshq;
-        DevBuf<double> akq_d, sv, tk, sums;
+        DevBuf<double> akq_d, sv, tk, sums, wts;
         DevBuf<int> ik_d, indk_d, nkk_d, hg, hd;
         DevBuf<unsigned long long> jA, jC;
         std::vector<double> val[4], err[4];   // after the last update: g, density, S(q), n(k)
@@ -1490,7 +1496,9 @@ int dmc_set_operators(dmc_ctx* c, int ntabg, int ntabq, int ntabk)
     if (ntabg < 0 || ntabq < 0 || ntabk < 0 || ntabg > 100000) return fail(c, DMC_ERR_INVALID, "bad operator table sizes");
     if (ntabk > 80) return fail(c, DMC_ERR_UNSUPPORTED, "n(k) is built for |ik|^2 <= 80");
     auto& O = c->ops;
-    O = dmc_ctx::Ops();
+    // a fresh operator state; the old one's device buffers are freed
+    O.~Ops();
+    new (&O) dmc_ctx::Ops();
     OpsDev& o = O.dev;
     std::memset(&o, 0, sizeof o);
     const Setup& S = c->S;
@@ -1638,8 +1646,9 @@ int dmc_add_operators(dmc_ctx* c)
                               c->stream));
             ++c->launches;
         }
-        CK(launch_ops_reduce(o, n, s.view(), O.hg.p, O.hd.p, O.sv.p, O.tk.p, O.sums.p, c->stream));
-        ++c->launches;
+        CK(O.wts.alloc((size_t)n));
+        CK(launch_ops_reduce(o, n, s.view(), O.hg.p, O.hd.p, O.sv.p, O.tk.p, O.sums.p, O.wts.p, c->stream));
+        c->launches += 2;
         int rc = reverse_stacks(c);   // the pop/push pass of dmcbcs.f90:465-473
         if (rc) return rc;
         ++c->launches;

@@ -83,8 +83,9 @@ cudaError_t launch_ops_walker(const DevParams& p, const OpsDev& o, const double*
 cudaError_t launch_ops_enk(const DevParams& p, const OpsDev& o, const KVecDev* kv, const TabUD* tud,
                            const TabSS* tss, const double* x, const unsigned long long* irn, const double* sinv,
                            int n, double* tk, int grid, cudaStream_t st);
+// wts: scratch of n doubles for the walker weights
 cudaError_t launch_ops_reduce(const OpsDev& o, int n, const DevStack& s, const int* hg, const int* hd,
-                              const double* sv, const double* tk, double* sums, cudaStream_t st);
+                              const double* sv, const double* tk, double* sums, double* wts, cudaStream_t st);
 
 // deferred step decision (idmc = 1, -2): weights and estimator records of
 // the pushed walkers after a MODE_STEP walker launch with a.defer set

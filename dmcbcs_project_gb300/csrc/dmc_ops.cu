@@ -193,12 +193,21 @@ __global__ void __launch_bounds__(kThreads) ops_enk_kernel(const __grid_constant
     }
 }
 
+// Weight of each walker for the operator sums: weight * exp(psil - psigl) *
+// is * wt0 (operators.f90:103), once per walker.
+__global__ void ops_weight_kernel(DevStack s, int n, double* __restrict__ wt)
+{
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
+        wt[w] = s.weight[w] * exp(s.psil[w] - s.psigl[w]) * s.is[w] * (double)s.wt0[w];
+}
+
 // The weighted sums (addgofr/addsofq/addenk accumulation), walkers in pop
-// order (index n-1 first), one thread per running sum.  Weight of a walker:
-// weight * exp(psil - psigl) * is * wt0 (operators.f90:103).
-__global__ void ops_reduce_kernel(const __grid_constant__ OpsDev o, int n, DevStack s, const int* __restrict__ hg,
-                                  const int* __restrict__ hd, const double* __restrict__ sv,
-                                  const double* __restrict__ tk, double* __restrict__ sums)
+// order (index n-1 first), one thread per running sum, with the walker
+// weights of ops_weight_kernel.
+__global__ void ops_reduce_kernel(const __grid_constant__ OpsDev o, int n, const double* __restrict__ wts,
+                                  const int* __restrict__ hg, const int* __restrict__ hd,
+                                  const double* __restrict__ sv, const double* __restrict__ tk,
+                                  double* __restrict__ sums)
 {
     const int ng = o.ntabg > 0 ? 3 * (o.ntabg + 1) : 0, ndh = o.ntabg > 0 ? 6 * (2 * o.ntabg + 1) : 0;
     const int nq = 3 * o.nqtot, nk = o.nkv > 0 ? o.ntabk + 1 : 0;
@@ -207,7 +216,7 @@ __global__ void ops_reduce_kernel(const __grid_constant__ OpsDev o, int n, DevSt
         double acc = sums[t];
         int u = t;
         for (int w = n - 1; w >= 0; --w) {
-            const double wt = s.weight[w] * exp(s.psil[w] - s.psigl[w]) * s.is[w] * (double)s.wt0[w];
+            const double wt = wts[w];
             double add;
             if (u < 2 * ng) {
                 const int b = u % ng;
@@ -275,10 +284,11 @@ cudaError_t launch_ops_enk(const DevParams& p, const OpsDev& o, const KVecDev* k
 }
 
 cudaError_t launch_ops_reduce(const OpsDev& o, int n, const DevStack& s, const int* hg, const int* hd,
-                              const double* sv, const double* tk, double* sums, cudaStream_t st)
+                              const double* sv, const double* tk, double* sums, double* wts, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    ops_reduce_kernel<<<1, 1024, 0, st>>>(o, n, s, hg, hd, sv, tk, sums);
+    ops_weight_kernel<<<(n + 255) / 256, 256, 0, st>>>(s, n, wts);
+    ops_reduce_kernel<<<1, 1024, 0, st>>>(o, n, wts, hg, hd, sv, tk, sums);
     return cudaGetLastError();
 }
 
