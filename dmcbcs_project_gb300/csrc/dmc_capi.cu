@@ -169,7 +169,7 @@ struct dmc_ctx {
     DevBuf<int> bis;
     DevBuf<unsigned char> flush;
     // single-particle moves and parameter derivatives
-    DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum;
+    DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum, srene;
     DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
     DevBuf<int> sip;
     int64_t sr_count = 0;
@@ -1848,9 +1848,10 @@ int dmc_sr_accumulate(dmc_ctx* c, int64_t* nsamples)
             ++c->launches;
         }
         if (c->sr_det && (rc = derbcs_device(c, n, s.x.p, c->sder.p, np, c->sr_jas ? 2 : 0))) return rc;
+        CK(c->srene.alloc((size_t)n));   // the walkers' local energies
         CK(launch_sr_sums(c->sder.p, s.d2psi.p, s.v.p, n, np, c->S.hbar, c->S.eunit, c->S.npart, c->srsum.p,
-                          c->stream));
-        ++c->launches;
+                          c->srene.p, c->stream));
+        c->launches += 2;
         if ((rc = reverse_stacks(c))) return rc;
         ++c->launches;
         c->sr_count += n;

@@ -69,9 +69,9 @@ cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x
 cudaError_t launch_jasder(const DevParams& p, const double* jq, const double* x, double* dpsi, int nw, int grid,
                           cudaStream_t st, int stride);
 // adds the calder sums of n walkers (pop order) to sums[np*np + 2*np + 2]:
-// ovec, ovecw, pmat (column-major), esum, esum2
+// ovec, ovecw, pmat (column-major), esum, esum2; ene: scratch of n doubles
 cudaError_t launch_sr_sums(const double* der, const double* d2psi, const double* v, int n, int np, double hbar,
-                           double eunit, int npart, double* sums, cudaStream_t st);
+                           double eunit, int npart, double* sums, double* ene, cudaStream_t st);
 
 // Operators (dmc_ops.cu): per-walker histograms and S(q) values, n(k) per
 // walker, and the weighted sums over the population in pop order.  sums:

@@ -417,16 +417,22 @@ __global__ void __launch_bounds__(kThreads) jasder_kernel(const __grid_constant_
 // esum += e, esum2 += e^2 with e = E_L / eunit / npart.  One thread per
 // output, so every sum runs over the walkers in the same order as the
 // reference's loop; products are rounded before the add (no contraction).
-__global__ void sr_sums_kernel(const double* __restrict__ der, const double* __restrict__ d2psi,
-                               const double* __restrict__ v, int n, int np, double hbar, double eunit,
-                               double npart, double* __restrict__ sums)
+// ene = (-hbar*d2psi + v)/eunit/npart (dmcbcs.f90:497), once per walker
+__global__ void sr_energy_kernel(const double* __restrict__ d2psi, const double* __restrict__ v, int n,
+                                 double hbar, double eunit, double npart, double* __restrict__ ene)
+{
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
+        ene[w] = __ddiv_rn(__ddiv_rn(__dadd_rn(__dmul_rn(-hbar, d2psi[w]), v[w]), eunit), npart);
+}
+
+__global__ void sr_sums_kernel(const double* __restrict__ der, const double* __restrict__ ene, int n, int np,
+                               double* __restrict__ sums)
 {
     const int nout = np * np + 2 * np + 2;
     for (int t = threadIdx.x; t < nout; t += blockDim.x) {
         double s = sums[t];
         for (int w = n - 1; w >= 0; --w) {
-            // ene = (-hbar*d2psi + v)/eunit/npart (dmcbcs.f90:497)
-            const double e = __ddiv_rn(__ddiv_rn(__dadd_rn(__dmul_rn(-hbar, d2psi[w]), v[w]), eunit), npart);
+            const double e = ene[w];
             const double* d = der + (size_t)w * np;
             double term;
             if (t < np)
@@ -524,10 +530,11 @@ cudaError_t launch_jasder(const DevParams& p, const double* jq, const double* x,
 }
 
 cudaError_t launch_sr_sums(const double* der, const double* d2psi, const double* v, int n, int np, double hbar,
-                           double eunit, int npart, double* sums, cudaStream_t st)
+                           double eunit, int npart, double* sums, double* ene, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    sr_sums_kernel<<<1, 1024, 0, st>>>(der, d2psi, v, n, np, hbar, eunit, (double)npart, sums);
+    sr_energy_kernel<<<(n + 255) / 256, 256, 0, st>>>(d2psi, v, n, hbar, eunit, (double)npart, ene);
+    sr_sums_kernel<<<1, 1024, 0, st>>>(der, ene, n, np, sums);
     return cudaGetLastError();
 }
 
