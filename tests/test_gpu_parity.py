@@ -136,3 +136,54 @@ def test_generation_parity(name, nw, idmc, gens):
         assert rel_each(vb_g, vb_o) < 1e-9
         assert rel_each(wb_g, wb_o) < 1e-9
         assert np.array_equal(ctx.wtisto(), orc.wtisto())
+
+
+@pytest.mark.parametrize("name,nw,idmc", [("n14", 48, 1), ("n14", 32, 0), ("p33_30", 16, 2)])
+def test_step_and_branch_calls(name, nw, idmc):
+    """The separate drop-ins for step1 (step.f90:43) and branch (step.f90:287),
+    called the way the reference's loop calls them, against the oracle."""
+    sysd, rund, _ = configs.workload(name, nwalk=nw, idmc=idmc)
+    orc = oracle.Oracle(sysd, rund)
+    with capi.Context(sysd, rund) as ctx:
+        ctx.init_walkers()
+        orc.init_walkers()
+        ctx.initial_eval()
+        orc.initial_eval()
+        for g in range(3):
+            op = g == 2
+            ctx.step(op)
+            orc.step(op)
+            if idmc > 0:
+                ctx.branch(1.0)
+                orc.branch(1.0)
+            assert ctx.num_walkers() == orc.num_walkers()
+        wg, wo = ctx.walkers(), orc.walkers()
+        assert np.array_equal(wg["irn"], wo["irn"])
+        assert np.array_equal(wg["is_"], wo["is_"])
+        assert rel(wg["x"], wo["x"]) < 1e-10
+        for k in ("psil", "d2psi", "v", "weight"):
+            assert rel_each(wg[k], wo[k]) < TOL, k
+        vb_g, _, wb_g = ctx.estimators()
+        vb_o, _, wb_o = orc.estimators()
+        assert rel_each(vb_g, vb_o) < 1e-9 and rel_each(wb_g, wb_o) < 1e-9
+
+
+def test_timed_generations_equal_generations():
+    """dmc_timed_generations (graph replay with events) gives the same walkers
+    as the same number of dmc_generation calls."""
+    sysd, rund, _ = configs.workload("n66", nwalk=64, idmc=1)
+    with capi.Context(sysd, rund) as a, capi.Context(sysd, rund) as b:
+        for c in (a, b):
+            c.init_walkers()
+            c.initial_eval()
+        steps, ms, nl = a.timed_generations(4, opcomp_last=True, flush_l2=True)
+        n_in = []
+        for g in range(4):
+            n_in.append(b.num_walkers())
+            b.generation(g == 3)
+        assert steps == sum(n_in) and ms > 0 and nl > 0
+        wa, wb = a.walkers(), b.walkers()
+        for k in ("x", "irn", "weight", "psil", "d2psi"):
+            assert np.array_equal(wa[k], wb[k]), k
+        for ea, eb in zip(a.estimators(), b.estimators()):
+            assert np.array_equal(ea, eb)
