@@ -953,8 +953,12 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
     // panel warps factor the first panel there; pass p > 0 applies block p-1
     // and factors panel p.  One call site of the (unrolled) panel keeps the
     // kernel's instruction footprint small.
+    // With an even number of panels the first pass works in place (the copy
+    // writes every element onto itself), so that the last pass lands in S
+    // and writes the natural order directly: no final copy.
+    const bool inplace = ((n + B - 1) / B) % 2 == 0;
     R* cur = A0;
-    R* nxt = A1;
+    R* nxt = inplace ? A0 : A1;
     int k0 = 0, bw = 0;
     for (;;) {
         if (s_sing) break;
@@ -998,7 +1002,7 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
         __syncthreads();
         R* t = cur;
         cur = nxt;
-        nxt = t;
+        nxt = (t == cur) ? (cur == A0 ? A1 : A0) : t;
         if (bw1 == 0) break;
         k0 = k1;
         bw = bw1;
