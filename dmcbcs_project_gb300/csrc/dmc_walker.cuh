@@ -1215,6 +1215,7 @@ __device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
     const int n = c.p.nd;
     if (c.L.S2 >= 0) {
         if (n <= 64) return inverse_blocked<R, 2, 6>(c, logdet, sgn);
+        if (n <= 96) return inverse_blocked<R, 3, 8>(c, logdet, sgn);
         if (n <= 128) return inverse_blocked<R, 4, 8>(c, logdet, sgn);
     }
     return inverse_unblocked<R>(c, logdet, sgn);
