@@ -37,7 +37,7 @@ WORKLOAD = "n66"
 # one step launch over 1024 walkers, ncu): FP64 walker kernel 4.14 MB,
 # mixed walker kernel 4.20 MB (profiles/walker_kernel_n66_fp64.md,
 # profiles/walker_kernel_n66_mixed.md).
-NCU_TRAFFIC_BYTES_PER_WALKER = {"fp64": 4046.5, "mixed": 4103.5}
+NCU_TRAFFIC_BYTES_PER_WALKER = {"fp64": 4045.5, "mixed": 4102.5}
 
 # FP32 flops (FFMA = 2, FADD/FMUL = 1) executed per walker-step by the mixed
 # walker kernel, from the instruction counters of the same capture:
