@@ -160,6 +160,28 @@ def dist_setup():
     return world, rank, local
 
 
+def replica_seed(rank):
+    """Random-number seed of the replica on one rank (independent walkers per GPU)."""
+    return 17 + 1000003 * rank
+
+
+def reduce_over_ranks(t, count, world):
+    """The longest timed interval and the summed work over the ranks (each
+    rank runs an independent replica); the identity on one rank.  Works on
+    both backends: CUDA tensors for NCCL, CPU tensors for gloo."""
+    if world <= 1:
+        return t, count
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tt = torch.tensor([float(t)], device=dev, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    ct = torch.tensor([float(count)], device=dev, dtype=torch.float64)
+    dist.all_reduce(ct)
+    return float(tt.item()), int(round(ct.item()))
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -207,14 +229,7 @@ def time_path(ctx, args, world, local, barrier):
         kern_ms += ctx.last_step_ms()
     barrier()
     clocks = sampler.stop()
-    t_max, steps_all = dev_ms, steps
-    if world > 1:
-        t = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-        s_t = torch.tensor([steps], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(s_t)
-        steps_all = int(s_t.item())
+    t_max, steps_all = reduce_over_ranks(dev_ms, steps, world)
     return {"value": steps_all / (t_max * 1e-3), "ms_per_step": t_max / max(args.steps, 1), "steps": steps,
             "kern_ms": kern_ms / max(args.steps, 1), "avg_n": steps / max(args.steps, 1), "launches": launches,
             "clocks": clocks}
@@ -257,13 +272,8 @@ def e2e_rate(ctx, info, args, world, barrier):
         n_cur = n_new
     barrier()
     t = time.perf_counter() - t0
-    rate = total / t
-    if world > 1:
-        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        s_t = torch.tensor([total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(s_t)
-        rate = float(s_t.item()) / float(tt.item())
+    t_all, total_all = reduce_over_ranks(t, total, world)
+    rate = total_all / t_all
     return {"value": rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d / nsteps),
             "d2h_bytes_per_step": int(d2h / nsteps), "steps": nsteps,
             "path": "dmc_generation_host (population in pinned host arrays) + dmc_get_estimators"}
@@ -303,7 +313,7 @@ def uneven_batch(args, rank):
     ctxs, systems = [], []
     for i, (name, nw) in enumerate(zip(BATCH_SYSTEMS, nws)):
         s, r, meta = configs.workload(name, nwalk=int(nw), seed=1234 + i)
-        r.seed = 17 + 1000003 * rank + 7919 * i
+        r.seed = replica_seed(rank) + 7919 * i
         c = capi.Context(s, r, precision="fp64")
         c.init_walkers()
         c.initial_eval()
@@ -339,7 +349,7 @@ def param_gradients(args, rank):
     from dmcbcs_project_gb300 import capi, configs
 
     s, r, _ = configs.workload(WORKLOAD, nwalk=args.pgrad_walkers, idmc=-1)
-    r.seed = 17 + 1000003 * rank
+    r.seed = replica_seed(rank)
     with capi.Context(s, r) as c:
         c.init_walkers()
         x = c.walkers()["x"]
@@ -367,7 +377,7 @@ def energy_agreement(args, rank, neq=20, nblocks=10, nstep=20):
     out = {}
     for prec in ("mixed", "fp64"):
         s, r, _ = configs.workload(WORKLOAD, nwalk=args.walkers or configs.WORKLOADS[WORKLOAD][3])
-        r.seed = 17 + 1000003 * rank
+        r.seed = replica_seed(rank)
         with capi.Context(s, r, precision=prec) as c:
             c.init_walkers()
             c.initial_eval()
@@ -412,7 +422,7 @@ def run_gpu(args):
     nup, ndn, norb, nwalk, dt, _ = configs.WORKLOADS[WORKLOAD]
     nwalk = args.walkers or nwalk
     sysd, rund, _ = configs.workload(WORKLOAD, nwalk=nwalk)
-    rund.seed = 17 + 1000003 * rank                     # independent replica per GPU
+    rund.seed = replica_seed(rank)                      # independent replica per GPU
     precisions = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
     ctxs, res = {}, {}
     for prec in precisions:
@@ -467,7 +477,7 @@ def run_gpu(args):
     n132 = None
     if len(ctxs) == 2 and args.n132_steps > 0:
         s132, r132, _ = configs.workload("n132", nwalk=8192)
-        r132.seed = 17 + 1000003 * rank
+        r132.seed = replica_seed(rank)
         sub, c132 = {}, {}
         sub_args = argparse.Namespace(**vars(args))
         sub_args.steps = args.n132_steps
