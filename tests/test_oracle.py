@@ -420,3 +420,54 @@ def test_oracle_nofk_against_python_loop():
     assert np.allclose(e, tmp / nk * wt, rtol=1e-10, atol=1e-12)
     assert np.allclose(e2, (tmp / nk) ** 2 * wt, rtol=1e-10, atol=1e-12)
     assert abs(ws - 10 * wt) < 1e-12
+
+
+def _custom_walker(extra, nbin=(7, 7), ikup=(), ikdn=(), seed=13):
+    from dmcbcs_project_gb300.abi import make_run, make_system
+
+    nup, ndn = nbin
+    sp = configs.system_params(max(nup, ndn), max(nup, ndn), 5, seed=seed)
+    sp.update(nbin=[nup, ndn], nexup=len(ikup), ikup=[list(k) for k in ikup], nexdn=len(ikdn),
+              ikdn=[list(k) for k in ikdn])
+    sp.update(extra)
+    sysd = make_system(sp)
+    o = oracle.Oracle(sysd, make_run(configs.run_params(4, 0.002)), threads=1)
+    o.init_walkers()
+    rng = np.random.default_rng(seed)
+    while True:
+        x = o.walkers()["x"][0] + rng.normal(scale=0.2, size=(o.npart, 3))
+        if not _near_half_box(x, o.info.nup, o.info.el, o.info.ntab):
+            return o, x
+
+
+@pytest.mark.parametrize("label,extra,nbin,ikup,ikdn", [
+    ("one-body", dict(v0ex=0.5, v0exjas=0.3, nqex=[1, 0, 0]), (7, 7), (), ()),
+    ("guide", dict(a2=0.05), (7, 7), (), ()),
+    ("unpaired down", {}, (7, 8), (), ((0, 0, 0),)),
+    ("unpaired both", {}, (9, 10), ((0, 0, 0),), ((1, 0, 0), (-1, 0, 0))),
+])
+def test_chkder_optional_terms(label, extra, nbin, ikup, ikdn):
+    """chkder (wavefunction.f90:289-321) for the hpsi terms and determinant
+    rows the benchmark systems leave off: the one-body potential and Jastrow,
+    the guiding function (its gradient and Laplacian checked the same way
+    against psi_G) and unpaired down states."""
+    o, x = _custom_walker(extra, nbin, ikup, ikdn)
+    h0 = o.hpsi(x[None])
+    h = 1e-5
+    d2num = d2gnum = 0.0
+    for i in range(o.npart):
+        for c in range(3):
+            xp = x.copy(); xp[i, c] += h
+            xm = x.copy(); xm[i, c] -= h
+            hp, hm = o.hpsi(xp[None]), o.hpsi(xm[None])
+            for lg, dg in (("psil", "dpsi"), ("psigl", "dpsig")):
+                dnum = (hp[lg][0] - hm[lg][0]) / (2 * h)
+                assert abs(h0[dg][0, i, c] - dnum) < 1e-5 * max(1.0, abs(dnum)), (label, dg, i, c)
+            gp = hp["dpsi"][0, i, c] * np.exp(hp["psil"][0] - h0["psil"][0])
+            gm = hm["dpsi"][0, i, c] * np.exp(hm["psil"][0] - h0["psil"][0])
+            d2num += (gp - gm) / (2 * h)
+            gp = hp["dpsig"][0, i, c] * np.exp(hp["psigl"][0] - h0["psigl"][0])
+            gm = hm["dpsig"][0, i, c] * np.exp(hm["psigl"][0] - h0["psigl"][0])
+            d2gnum += (gp - gm) / (2 * h)
+    assert abs(d2num - h0["d2psi"][0]) < 1e-4 * max(1.0, abs(h0["d2psi"][0])), label
+    assert abs(d2gnum - h0["d2psig"][0]) < 1e-4 * max(1.0, abs(h0["d2psig"][0])), label
