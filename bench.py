@@ -471,30 +471,35 @@ def run_gpu(args):
     if acc is not None and args.energy_blocks > 0:
         acc["dmc_energy"] = energy_agreement(args, rank, nblocks=args.energy_blocks)
 
-    # The N = 132 (66 up / 66 down) system of the mixed-precision benchmark
-    # configuration, 8192 walkers: both paths over a short run (not the
-    # headline; reported beside it)
-    n132 = None
-    if len(ctxs) == 2 and args.n132_steps > 0:
-        s132, r132, _ = configs.workload("n132", nwalk=8192)
-        r132.seed = replica_seed(rank)
-        sub, c132 = {}, {}
+    # The mixed-precision benchmark configuration, 8192 walkers: N = 132 (66 up
+    # / 66 down) and N = 66, both paths over a short run (not the headline;
+    # reported beside it)
+    def mixed_config(name, workload):
+        s_, r_, _ = configs.workload(name, nwalk=8192)
+        r_.seed = replica_seed(rank)
+        sub, cs = {}, {}
         sub_args = argparse.Namespace(**vars(args))
         sub_args.steps = args.n132_steps
         for prec in ("mixed", "fp64"):
-            cx = capi.Context(s132, r132, precision=prec)
+            cx = capi.Context(s_, r_, precision=prec)
             cx.init_walkers()
             cx.initial_eval()
             t = time_path(cx, sub_args, world, local, barrier)
             sub[prec] = {"value": t["value"], "ms_per_step": t["ms_per_step"], "avg_walkers": t["avg_n"],
                          "clocks": t["clocks"]}
-            c132[prec] = cx
-        n132 = {"workload": "dmc_n132_66u66d", "walkers": 8192, "steps": args.n132_steps, "unit": UNIT,
-                "mixed": sub["mixed"], "fp64": sub["fp64"], "speedup_vs_fp64": sub["mixed"]["value"] / sub["fp64"]["value"],
-                "accuracy_vs_fp64": accuracy_vs_fp64(c132["mixed"], c132["fp64"], s132.hbar, nmax=256)
-                if rank == 0 else None}
-        for cx in c132.values():
+            cs[prec] = cx
+        out = {"workload": workload, "walkers": 8192, "steps": args.n132_steps, "unit": UNIT,
+               "mixed": sub["mixed"], "fp64": sub["fp64"], "speedup_vs_fp64": sub["mixed"]["value"] / sub["fp64"]["value"],
+               "accuracy_vs_fp64": accuracy_vs_fp64(cs["mixed"], cs["fp64"], s_.hbar, nmax=256)
+               if rank == 0 else None}
+        for cx in cs.values():
             cx.close()
+        return out
+
+    n132 = n66_8192 = None
+    if len(ctxs) == 2 and args.n132_steps > 0:
+        n132 = mixed_config("n132", "dmc_n132_66u66d")
+        n66_8192 = mixed_config("n66", "dmc_n66_33u33d_8192")
 
     batch = uneven_batch(args, rank) if args.batch_steps > 0 else None
     pgrad = param_gradients(args, rank) if args.pgrad_walkers > 0 else None
@@ -532,6 +537,8 @@ def run_gpu(args):
             line["accuracy_vs_fp64"] = acc
         if n132:
             line["n132"] = n132
+        if n66_8192:
+            line["n66_8192"] = n66_8192
         if batch:
             line["uneven_batch"] = batch
         if pgrad:
@@ -559,7 +566,7 @@ def main():
     ap.add_argument("--ref-walkers", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n132-steps", type=int, default=20,
-                    help="generations of the N = 132, 8192-walker side measurement (0: skip)")
+                    help="generations of the 8192-walker side measurements at N = 132 and N = 66 (0: skip)")
     ap.add_argument("--energy-blocks", type=int, default=10,
                     help="blocks of 20 generations of the mixed-vs-FP64 DMC energy comparison (0: skip)")
     ap.add_argument("--pgrad-walkers", type=int, default=8192,
