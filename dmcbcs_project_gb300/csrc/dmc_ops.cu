@@ -156,7 +156,8 @@ __global__ void __launch_bounds__(kThreads) ops_enk_kernel(const __grid_constant
                 for (int k = lane; k < nq; k += 32) {
                     double sn, c;
                     sincos(kv[k + 1].k[0] * xi[0] + kv[k + 1].k[1] * xi[1] + kv[k + 1].k[2] * xi[2], &sn, &c);
-                    csn[k] = make_double2(c, sn);
+                    const double v = kv[k + 1].v;   // the shell amplitude 2 vorb, applied once per move
+                    csn[k] = make_double2(v * c, v * sn);
                 }
                 __syncwarp();
                 rat2 = single::warp_bcsone_tab(p, kv, tud, xs, S, i, xi, cs, csn);

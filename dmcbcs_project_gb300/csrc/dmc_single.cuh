@@ -77,10 +77,10 @@ __device__ __forceinline__ double warp_bcsone(const DevParams& p, const KVecDev*
 }
 
 // The same ratio with the plane waves from tables: cs[(k-1) npart + j] holds
-// (cos, sin) of k.x_j for every particle j and k = 1..nk-1, csn[k-1] the
-// same at the moved particle's new position, so each pair-function entry is
-// sum_k v_k (cos k.r' cos k.r_j + sin k.r' sin k.r_j) = sum_k v_k cos k.(r' - r_j)
-// with two multiply-adds per k instead of a cosine.
+// (cos, sin) of k.x_j for every particle j and k = 1..nk-1, csn[k-1] holds
+// v_k (cos, sin) of k.r' at the moved particle's new position, so each
+// pair-function entry is sum_k v_k (cos k.r' cos k.r_j + sin k.r' sin k.r_j)
+// = sum_k v_k cos k.(r' - r_j) with two multiply-adds per k instead of a cosine.
 __device__ __forceinline__ double warp_bcsone_tab(const DevParams& p, const KVecDev* __restrict__ kv,
                                                   const TabUD* __restrict__ tud, const double* xw, const double* S,
                                                   int i, const double (&xi)[3], const double2* cs,
@@ -103,7 +103,7 @@ __device__ __forceinline__ double warp_bcsone_tab(const DevParams& p, const KVec
             const double2* cj = cs + jj;
             for (int k = 0; k < nq; ++k) {
                 const double2 a = csn[k], b = cj[(size_t)k * P];
-                ph = fma(kv[k + 1].v, fma(a.x, b.x, a.y * b.y), ph);
+                ph = fma(a.x, b.x, fma(a.y, b.y, ph));
             }
             ph += beta_value(p, tud, sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
         } else {
