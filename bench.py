@@ -34,15 +34,25 @@ UNIT = "walker-steps/s"
 WORKLOAD = "n66"
 
 # DRAM bytes per walker-step (dram__bytes_read.sum + dram__bytes_write.sum of
-# one step launch over 1024 walkers, ncu): FP64 walker kernel 4.14 MB,
-# mixed walker kernel 4.20 MB (profiles/walker_kernel_n66_fp64.md,
-# profiles/walker_kernel_n66_mixed.md).
+# one step launch over 1024 walkers, one ncu capture of each walker kernel):
+# FP64 walker kernel 4.14 MB, mixed walker kernel 4.20 MB.
 NCU_TRAFFIC_BYTES_PER_WALKER = {"fp64": 4045.5, "mixed": 4102.5}
 
 # FP32 flops (FFMA = 2, FADD/FMUL = 1) executed per walker-step by the mixed
 # walker kernel, from the instruction counters of the same capture:
-# 5.463e9 over 1024 walkers.
+# 5.463e9 over 1024 walkers.  Reported beside the roofline, not in it: the
+# double-float arithmetic executes ~4.7 FP32 flops per algorithmic flop.
 MIXED_FP32_FLOPS_PER_WALKER = 5.335e6
+
+
+def measured_peaks():
+    """The machine's measured peaks (HBM copy GB/s, cuBLAS bf16 TFLOP/s), if the
+    file is present next to this script."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def algorithmic_flops(nup, ndn, nd, K, npart):
@@ -190,7 +200,8 @@ def run_reference(args):
     from dmcbcs_project_gb300 import configs
 
     nup, ndn, norb, nwalk, dt, _ = configs.WORKLOADS[WORKLOAD]
-    nsample = args.ref_walkers
+    nwalk = args.walkers or nwalk
+    nsample = args.ref_walkers or nwalk
     # warm-up generations, then K timed generations of the sampled population
     rate_w, _, _, _ = cpu_reference_rate(nsample, 0.0, threads, gens_max=max(1, args.warmup))
     rate, steps, gens, el = cpu_reference_rate(nsample, 1e9, threads, gens_max=args.steps)
@@ -198,8 +209,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / max(gens, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "dmc_n66_33u33d", "walkers": nsample, "target_walkers": nwalk, "idmc": 1,
-                   "dt_efg": dt, "shells": norb},
+        "config": {"workload": "dmc_n66_33u33d", "walkers": nsample, "idmc": 1, "dt_efg": dt, "shells": norb,
+                   "precision": "f64", "parallelism": "host threads"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{gens} DMC generations of {nsample} walkers (N=66) on {threads} host threads; "
                                    "the reference Fortran/MPI/MKL build is not possible here, so the C "
@@ -367,37 +378,78 @@ def param_gradients(args, rank):
                         "device-to-host copy of both gradients"}
 
 
-def energy_agreement(args, rank, neq=20, nblocks=10, nstep=20):
-    """DMC energy of the mixed and the FP64 path from the same seed: neq
-    generations of equilibration, then nblocks blocks of nstep generations
-    with the estimators on every generation (dmcbcs.f90:426-449); energy per
-    particle in free-gas units with the error of the block averages."""
-    from dmcbcs_project_gb300 import capi, configs
+def deck_system(name, nwalk, idmc=None, dt=None):
+    """System and run descriptors of one of the reference's production decks
+    (the committed parse in tests/golden/decks.json)."""
+    from dmcbcs_project_gb300 import abi
 
+    with open(os.path.join(ROOT, "tests", "golden", "decks.json")) as f:
+        d = json.load(f)[name]
+    r = dict(d["run"], nwalk=nwalk)
+    if idmc is not None:
+        r["idmc"] = idmc
+    if dt is not None:
+        r["dt"] = dt
+    return abi.make_system(d["system"]), abi.make_run(r)
+
+
+def energy_agreement(args, rank):
+    """DMC energy of the mixed and the FP64 path on the reference's N = 66
+    production deck (dmcbcs.dat: 10 fitted shells, beta b = 0.5, d = 5,
+    dt = 5e-5).  Each precision runs R independent replicas (own seeds: no
+    random stream is shared between replicas or precisions).  A replica:
+    eq VMC generations at dt_eq from random walkers, eq_dmc DMC generations
+    at the deck's dt, then nblocks blocks of nstep generations with the
+    estimators on every generation; its energy is the mean of its block
+    averages.  At dt = 5e-5 successive blocks are strongly correlated, so the
+    error of a precision's energy is the standard error over its replicas
+    (which also carries the spread of the starting walkers), not the block
+    error."""
+    from dmcbcs_project_gb300 import capi
+
+    nw = args.energy_walkers
     out = {}
-    for prec in ("mixed", "fp64"):
-        s, r, _ = configs.workload(WORKLOAD, nwalk=args.walkers or configs.WORKLOADS[WORKLOAD][3])
-        r.seed = replica_seed(rank)
-        with capi.Context(s, r, precision=prec) as c:
-            c.init_walkers()
-            c.initial_eval()
-            for _ in range(neq):
-                c.generation(False)
-            c.zero_estimators()
-            blocks = []
-            for _ in range(nblocks):
-                for j in range(nstep):
-                    c.generation(True)
-                val, _ = c.block_update()
-                blocks.append(float(val[0]))
-        b = np.array(blocks)
-        out[prec] = {"energy": float(b.mean()), "error": float(b.std(ddof=1) / np.sqrt(len(b)))}
+    for k, prec in enumerate(("mixed", "fp64")):
+        reps = []
+        for rep in range(args.energy_replicas):
+            seed = replica_seed(rank) + 104729 * (1 + k * args.energy_replicas + rep)
+            s, r = deck_system("dmcbcs.dat", nw, idmc=0, dt=args.energy_dt_eq)
+            r.seed = seed
+            with capi.Context(s, r, precision=prec) as v:
+                v.init_walkers()
+                v.initial_eval()
+                for _ in range(args.energy_eq):
+                    v.generation(False)
+                w = v.walkers()
+            s, r = deck_system("dmcbcs.dat", nw)
+            r.seed = seed
+            with capi.Context(s, r, precision=prec) as c:
+                c.load_walkers(w["x"], w["irn"])
+                c.initial_eval()
+                for _ in range(args.energy_eq_dmc):
+                    c.generation(False)
+                c.zero_estimators()
+                blocks = []
+                for _ in range(args.energy_blocks):
+                    for _ in range(args.energy_steps):
+                        c.generation(True)
+                    val, _ = c.block_update()
+                    blocks.append(float(val[0]))
+            reps.append(float(np.mean(blocks)))
+        e = np.array(reps)
+        out[prec] = {"energy": float(e.mean()), "error": float(e.std(ddof=1) / np.sqrt(len(e))),
+                     "replicas": [round(v, 6) for v in reps]}
     d = out["mixed"]["energy"] - out["fp64"]["energy"]
     sig = float(np.hypot(out["mixed"]["error"], out["fp64"]["error"]))
-    return {"unit": "E / (N E_FG)", "generations": neq + nblocks * nstep, "blocks": nblocks,
-            "mixed": out["mixed"], "fp64": out["fp64"], "delta": d, "sigma": sig,
-            "delta_over_sigma": abs(d) / sig if sig > 0 else None,
-            "note": "same seed and random streams for both paths, so the two runs are correlated"}
+    e = abs(out["fp64"]["energy"])
+    return {"unit": "E / (N E_FG)", "system": "dmcbcs.dat (N = 66, 10 shells, dt = 5e-5)",
+            "walkers_per_replica": nw, "replicas_per_precision": args.energy_replicas,
+            "vmc_equilibration": {"generations": args.energy_eq, "dt": args.energy_dt_eq},
+            "dmc_equilibration": args.energy_eq_dmc, "blocks": args.energy_blocks,
+            "generations_per_block": args.energy_steps, "mixed": out["mixed"], "fp64": out["fp64"],
+            "delta": d, "sigma": sig, "delta_over_sigma": abs(d) / sig if sig > 0 else None,
+            "sigma_over_energy": sig / e if e > 0 else None,
+            "note": "independent seeds for every replica of both precisions; errors from the spread over replicas"}
 
 
 def run_gpu(args):
@@ -441,6 +493,7 @@ def run_gpu(args):
     peak64 = capi.probe_peak("fp64") if rank == 0 else None
     peak32 = capi.probe_peak("fp32") if rank == 0 else None
     dgemm = fp64_peak_tflops(torch) if rank == 0 else None
+    peaks = measured_peaks()
 
     def roofline(prec):
         r = res[prec]
@@ -455,21 +508,30 @@ def run_gpu(args):
                     "executed_achieved": flops_exe * r["avg_n"] / (kms * 1e-3) / 1e12,
                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the measured-peaks "
                                    "file); DFMA probe " + (f"{peak64:.3f}" if peak64 else "-") + " TFLOP/s"}
+        # achieved = the reference algorithm's flops (not the double-float
+        # instructions executed) per launch / the walker kernel's event time
         ex = MIXED_FP32_FLOPS_PER_WALKER
-        return {"bound": "fp32", "achieved": (ex * r["avg_n"] / (kms * 1e-3) / 1e12) if ex else None,
-                "peak": peak32, "unit": "TFLOP/s",
-                "frac": (ex * r["avg_n"] / (kms * 1e-3) / 1e12 / peak32) if (ex and peak32) else None,
+        bf16 = peaks.get("bf16_tflops")
+        return {"bound": "fp32", "achieved": alg, "peak": peak32, "unit": "TFLOP/s",
+                "frac": alg / peak32 if peak32 else None,
                 "traffic": NCU_TRAFFIC_BYTES_PER_WALKER["mixed"] * r["avg_n"],
                 "kernel": "walker_kernel<df>", "kernel_ms_per_launch": kms, "walkers_per_launch": r["avg_n"],
-                "executed_fp32_flops_per_walker_step": ex,
-                "fp64_equivalent": {"achieved": alg, "peak": dgemm,
-                                    "frac": alg / dgemm if dgemm else None,
-                                    "algorithmic_flops_per_walker_step": flops_alg},
-                "peak_source": "FFMA throughput probe measured in this run (no FP32 figure in the measured-peaks file)"}
+                "algorithmic_flops_per_walker_step": flops_alg,
+                "peak_source": "FFMA throughput probe measured in this run (the measured-peaks file has no FP32 "
+                               "figure)",
+                "of_measured_bf16_tensor_peak": {"peak": bf16, "frac": alg / bf16 if bf16 else None,
+                                                 "source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 burst)"},
+                "of_measured_dgemm": {"peak": dgemm, "frac": alg / dgemm if dgemm else None},
+                "executed": {"fp32_flops_per_walker_step": ex,
+                             "achieved": ex * r["avg_n"] / (kms * 1e-3) / 1e12,
+                             "frac_of_ffma_probe": (ex * r["avg_n"] / (kms * 1e-3) / 1e12 / peak32) if peak32
+                             else None,
+                             "note": "FP32 instructions of the double-float arithmetic (ncu counters); pipe "
+                                     "busyness, not useful work"}}
 
     acc = accuracy_vs_fp64(ctxs["mixed"], ctxs["fp64"], sysd.hbar) if len(ctxs) == 2 and rank == 0 else None
     if acc is not None and args.energy_blocks > 0:
-        acc["dmc_energy"] = energy_agreement(args, rank, nblocks=args.energy_blocks)
+        acc["dmc_energy"] = energy_agreement(args, rank)
 
     # The mixed-precision benchmark configuration, 8192 walkers: N = 132 (66 up
     # / 66 down) and N = 66, both paths over a short run (not the headline;
@@ -563,12 +625,19 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-walkers", type=int, default=512)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--ref-walkers", type=int, default=1024)
+    ap.add_argument("--ref-walkers", type=int, default=None,
+                    help="walkers of the reference arm (default: the GPU arm's workload, 4096)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n132-steps", type=int, default=20,
                     help="generations of the 8192-walker side measurements at N = 132 and N = 66 (0: skip)")
     ap.add_argument("--energy-blocks", type=int, default=10,
-                    help="blocks of 20 generations of the mixed-vs-FP64 DMC energy comparison (0: skip)")
+                    help="blocks of the mixed-vs-FP64 DMC energy comparison on the dmcbcs.dat deck (0: skip)")
+    ap.add_argument("--energy-steps", type=int, default=20, help="generations per energy block")
+    ap.add_argument("--energy-walkers", type=int, default=1024, help="walkers per energy replica")
+    ap.add_argument("--energy-replicas", type=int, default=8, help="independent replicas per precision")
+    ap.add_argument("--energy-eq", type=int, default=200, help="VMC equilibration generations")
+    ap.add_argument("--energy-dt-eq", type=float, default=5e-3, help="VMC equilibration time step")
+    ap.add_argument("--energy-eq-dmc", type=int, default=100, help="DMC equilibration generations")
     ap.add_argument("--pgrad-walkers", type=int, default=8192,
                     help="walkers of the adjoint parameter-gradient side measurement (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=20,

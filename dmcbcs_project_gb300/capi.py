@@ -30,7 +30,7 @@ EXPORTS = [
     "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure", "dmc_dfmath_eval",
     "dmc_batch_create", "dmc_batch_destroy", "dmc_batch_last_error", "dmc_batch_set_grids", "dmc_batch_get_grids",
     "dmc_batch_plan", "dmc_batch_tune", "dmc_batch_generations", "dmc_param_count", "dmc_param_grad",
-    "dmc_generation_host",
+    "dmc_generation_host", "dmc_get_status", "dmc_walker_status",
 ]
 
 PREC_FP64 = 0
@@ -122,6 +122,8 @@ def load(path=LIB_PATH):
     L.dmc_branch_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(abi.DevStack),
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
     L.dmc_generation_host.argtypes = [vp, C.POINTER(Walkers), C.POINTER(Walkers), C.c_int]
+    L.dmc_get_status.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
+    L.dmc_walker_status.argtypes = [vp, C.c_int, _ip]
     L.dmc_param_count.argtypes = [vp, C.POINTER(C.c_int)]
     L.dmc_param_grad.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.dmc_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
@@ -541,6 +543,18 @@ class Context:
         w = self.walker_struct(dict(arrs, n=arrs["cap"]))
         self._check(load().dmc_get_walkers(self._h, C.byref(w)))
         return w.n
+
+    def status(self, clear=False):
+        """DMC_STATUS_* flags met since the last clear (dmc_get_status)."""
+        f = C.c_int()
+        self._check(load().dmc_get_status(self._h, C.byref(f), int(bool(clear))))
+        return f.value
+
+    def walker_status(self, nw):
+        """Per-walker DMC_STATUS_* flags of the last batched evaluation."""
+        out = np.zeros(nw, np.int32)
+        self._check(load().dmc_walker_status(self._h, int(nw), out))
+        return out
 
     def last_step_ms(self):
         ms = C.c_double()

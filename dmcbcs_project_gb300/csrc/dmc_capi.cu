@@ -159,6 +159,9 @@ struct dmc_ctx {
     int gprec = -1;
     DevBuf<double> est;
     DevBuf<int> counts, offs, status;
+    DevBuf<int> wstat;      // per-walker flags of the last batched evaluation
+    int wstat_n = 0;        // its walker count
+    int hstatus = 0;        // DMC_STATUS_* flags met on the host (stack overflow)
     DevBuf<unsigned long long> irn1, wtisto;
     // estimator block sums valblk, valblk2, wtblk: one buffer of
     // 3 DMC_NEST_MAX doubles (vb2 and wb point into it), read with one copy
@@ -211,7 +214,10 @@ int sync_n(dmc_ctx* c)
     c->n_stale = false;
     if (h[2]) {
         cudaMemsetAsync(c->pop.p + 2, 0, sizeof(int), c->stream);
-        if (h[2] & 2) return fail(c, DMC_ERR_OVERFLOW, "stack overflow in branch");
+        if (h[2] & 2) {
+            c->hstatus |= DMC_STATUS_OVERFLOW;
+            return fail(c, DMC_ERR_OVERFLOW, "stack overflow in branch");
+        }
         return fail(c, DMC_ERR_EMPTY, "population died out");
     }
     return DMC_OK;
@@ -404,6 +410,9 @@ int run_eval(dmc_ctx* c, int mode, int nw, const double* dx, double* psil, int* 
     a.xin = dx;
     a.o_psil = psil; a.o_is = is; a.o_dpsi = dpsi; a.o_d2psi = d2psi; a.o_v = v; a.o_vext = vext;
     a.o_psigl = psigl; a.o_dpsig = dpsig; a.o_d2psig = d2psig; a.o_sinv = sinv;
+    CK(c->wstat.alloc(nw));
+    a.wstatus = c->wstat.p;
+    c->wstat_n = nw;
     CK(launch_walker(c->P, a, c->L, grid_for(c, nw), st, c->precision == DMC_PREC_MIXED));
     return DMC_OK;
 }
@@ -580,7 +589,7 @@ int dmc_destroy(dmc_ctx* c)
     c->kv.release(); c->tud.release(); c->tss.release(); c->kv_mp.release(); c->tud_mp.release();
     c->tss_mp.release(); c->jumpA.release(); c->jumpC.release(); c->jq.release();
     c->gscratch.release(); c->st[0].release(); c->st[1].release(); c->est.release(); c->counts.release();
-    c->offs.release(); c->status.release(); c->irn1.release(); c->wtisto.release(); c->vb.release();
+    c->offs.release(); c->status.release(); c->wstat.release(); c->irn1.release(); c->wtisto.release(); c->vb.release();
     c->bx.release(); c->bpsil.release(); c->bdpsi.release();
     c->bd2psi.release(); c->bv.release(); c->bvext.release(); c->bpsigl.release(); c->bdpsig.release();
     c->bd2psig.release(); c->bsinv.release(); c->bis.release(); c->flush.release();
@@ -843,6 +852,31 @@ int dmc_restore_walkers(dmc_ctx* c, const char* path, double* tau)
     return DMC_OK;
 }
 
+int dmc_get_status(dmc_ctx* c, int* flags, int clear)
+{
+    if (!c || !flags) return DMC_ERR_INVALID;
+    int d = 0;
+    CK(cudaMemcpyAsync(&d, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *flags = d | c->hstatus;
+    if (clear) {
+        CK(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->hstatus = 0;
+    }
+    return DMC_OK;
+}
+
+int dmc_walker_status(dmc_ctx* c, int nw, int* status)
+{
+    if (!c || nw < 0 || (nw > 0 && !status)) return DMC_ERR_INVALID;
+    if (nw > c->wstat_n) return fail(c, DMC_ERR_INVALID, "more walkers than the last batched evaluation");
+    if (nw == 0) return DMC_OK;
+    CK(cudaMemcpyAsync(status, c->wstat.p, nw * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DMC_OK;
+}
+
 int dmc_num_walkers(dmc_ctx* c, int* n)
 {
     if (!c || !n) return DMC_ERR_INVALID;
@@ -854,31 +888,41 @@ int dmc_num_walkers(dmc_ctx* c, int* n)
     return DMC_OK;
 }
 
-// The device-side address of a caller's host array: pinned memory (mapped
-// into the device's address space), managed or device memory.  nullptr
-// for pageable memory, which then goes through cudaMemcpy.
-static void* device_view(const void* p)
+// The address under which the context's device reads a caller's array:
+// pinned memory (mapped into the device's address space), managed memory,
+// or device memory of this same device.  nullptr otherwise -- pageable
+// memory, and device memory of another GPU (which the walker kernel cannot
+// read without peer access) -- so the caller's arrays then go through
+// copies.
+static void* device_view(const void* p, int device)
 {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
-    if (a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeDevice) return const_cast<void*>(p);
+    if (a.type == cudaMemoryTypeHost) {
+        // the mapped address is the one of the current device (the
+        // context's device is current during every call)
+        int cur = -1;
+        if (cudaGetDevice(&cur) != cudaSuccess || cur != device) return nullptr;
+        return a.devicePointer;
+    }
+    if (a.type == cudaMemoryTypeManaged) return const_cast<void*>(p);
+    if (a.type == cudaMemoryTypeDevice && a.device == device) return const_cast<void*>(p);
     return nullptr;
 }
 
 // Device views of every non-null field of w; false when one of them is not
 // addressable from the device.  Looked up on every call: memory freed and
 // allocated again at the same address may be of another kind.
-static bool host_views(dmc_ctx*, const dmc_walkers* w, HostWalkers* h)
+static bool host_views(dmc_ctx* c, const dmc_walkers* w, HostWalkers* h)
 {
     void* key[15] = {w->x, w->dpsi, w->dpsig, w->psil, w->psigl, w->d2psi, w->d2psig, w->v, w->vext, w->weight,
                      w->psil0, w->psigl0, w->wt0, w->is, w->irn};
     void* view[15];
     for (int k = 0; k < 15; ++k) {
-        view[k] = key[k] ? device_view(key[k]) : nullptr;
+        view[k] = key[k] ? device_view(key[k], c->device) : nullptr;
         if (key[k] && !view[k]) return false;
     }
     double** d[13] = {&h->x, &h->dpsi, &h->dpsig, &h->psil, &h->psigl, &h->d2psi, &h->d2psig, &h->v, &h->vext,
@@ -1081,6 +1125,7 @@ int dmc_branch(dmc_ctx* c, double factor)
     if (total > c->cap) {
         c->n = c->cap;
         c->n_stale = false;
+        c->hstatus |= DMC_STATUS_OVERFLOW;
         return fail(c, DMC_ERR_OVERFLOW, "stack overflow in branch");
     }
     c->n = total;

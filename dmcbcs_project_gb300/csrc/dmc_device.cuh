@@ -133,7 +133,8 @@ struct KernelArgs {
     const unsigned long long* jumpC;   // LCG jump-ahead increments, [nrand+1]
     double* gscratch;            // per-CTA global scratch when the pair data do not fit on chip
     const double* jq;            // long-range Jastrow q records, [nql][8]
-    int* status;                 // per-walker status flags (bit 0: singular matrix)
+    int* status;                 // the context's status word, DMC_STATUS_* flags OR-ed over walkers
+    int* wstatus;                // batched evaluations: DMC_STATUS_* flags of walker w (nullptr: none)
     const double* in_wt0d;       // MODE_STEP: the old wt0 in double precision (input stack in the
                                  // caller's host arrays), else nullptr: in.wt0
 };

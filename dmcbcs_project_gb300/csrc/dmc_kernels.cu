@@ -9,6 +9,7 @@
 
 #include "dmc_device.cuh"
 #include "dmc_kernels.h"
+#include "dmc_attr.h"
 #include "dmc_walker.cuh"
 
 namespace dmc {
@@ -49,6 +50,21 @@ __device__ inline void step_decision(const DevParams& p, int opcomp, const StepS
     const double nfac = p.nfac;
     double wnew = o_weight;
     float wt0new = o_wt0;
+    // A DMC walker whose local energies are not finite (NaN or infinite
+    // inputs, flagged DMC_STATUS_NONFINITE by the walker kernel) gets weight 0
+    // and adds nothing to the estimators, so branching drops it; the
+    // reference has no such case (its int(w + u) of a NaN weight is
+    // undefined).  Finite walkers are untouched.
+    if (p.idmc >= 1 || p.idmc == -2) {
+        const bool fin = p.idmc == 2 ? (isfinite(eo) && (!take_new || isfinite(en)))
+                                     : (isfinite(eo) && isfinite(en) && isfinite(-hb * ol.d2psig + ol.v) &&
+                                        isfinite(-hb * nn.d2psig + nn.v));
+        if (!fin) {
+            wnew_out = 0.0;
+            wt0_out = o_wt0;
+            return;
+        }
+    }
     if (p.idmc == -1 || p.idmc == 0) {
         if (take_new) {
             const double ejf = -0.5 * hb * (nn.d2psi - ejfd) + nn.v;
@@ -261,7 +277,25 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         HRes h = walker::hpsi_eval<R>(c, a.mode == MODE_STEP ? MODE_STEP : hmode);
         double* dpsi = sm + L.acc;
         const double* dpsig = (p.a2 == 0.0) ? dpsi : sm + L.dg;
-        if (h.singular && threadIdx.x == 0 && a.status) atomicOr(a.status, 1);
+        // failure flags of this walker (DMC_STATUS_*): a singular pair matrix
+        // (matrixlapack.f90:19-25, psislaterbcs.f90:210) and results that are
+        // not finite (NaN or infinite positions, overflowing terms)
+        {
+            int bad = 0;
+            for (int e = threadIdx.x; e < n3; e += kThreads) {
+                const double val = a.mode == MODE_GETPHI ? sm[L.acc + 4 * P + e] : dpsi[e];
+                if (!isfinite(val)) bad = 1;
+            }
+            bad = __syncthreads_or(bad);
+            const double lap = a.mode == MODE_GETPHI ? h.d2u : (a.mode == MODE_BCS ? h.d2phi : h.d2psi);
+            const double lg = a.mode == MODE_GETPHI ? h.u : h.psil;
+            if (!isfinite(lap) || !isfinite(lg) || !isfinite(h.v)) bad = 1;
+            const int flags = (h.singular ? DMC_STATUS_SINGULAR : 0) | (bad ? DMC_STATUS_NONFINITE : 0);
+            if (threadIdx.x == 0) {
+                if (flags && a.status) atomicOr(a.status, flags);
+                if (a.wstatus && a.mode != MODE_STEP) a.wstatus[w] = flags;
+            }
+        }
         if (a.mode != MODE_STEP) {
             // ---- batched wavefunction outputs ----
             if (threadIdx.x == 0) {
@@ -320,7 +354,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
             block_sum<2>(acc1, sm + L.red);
             if (threadIdx.x == 0) {
                 double prob = (p.idmc == 2 ? 2.0 * (h.psigl - o_psigl) : 2.0 * (h.psil - o_psil)) + acc1[0];
-                prob = exp(fmin(0.0, prob));
+                prob = prob == prob ? exp(fmin(0.0, prob)) : 0.0;   // a NaN proposal is rejected
                 const double rn = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, nr + 1));
                 s_take_new = rn < prob;
             }
@@ -472,7 +506,7 @@ struct BranchDev {
 };
 
 __global__ void branch_count_kernel(DevStack in, int n, double factor, int* counts,
-                                    unsigned long long* irn1, unsigned long long* wtisto, BranchDev bd)
+                                    unsigned long long* irn1, unsigned long long* wtisto, BranchDev bd, int cap)
 {
     if (bd.pn) {
         n = *bd.pn;
@@ -488,7 +522,12 @@ __global__ void branch_count_kernel(DevStack in, int n, double factor, int* coun
     const unsigned long long s = in.irn[j] & kMask48;
     const unsigned long long s1 = (44485709377909ull * s + 96309754297ull) & kMask48;
     const double rn = lcg_uniform(s1);
-    const int iwt = (int)(wt + rn);
+    // int(w + u) as the reference truncates it, for weights in range; a
+    // non-finite or huge weight gives at most cap + 1 copies (the pass then
+    // reports an overflow) so the prefix sums stay bounded, NaN gives none
+    const double xw = wt + rn;
+    const double lim = (double)cap + 1.0;
+    const int iwt = xw != xw ? 0 : (xw >= lim ? (int)lim : (xw <= -lim ? -(int)lim : (int)xw));
     counts[m] = iwt > 0 ? iwt : 0;
     irn1[m] = s1;
     if (iwt >= 0 && iwt < DMC_WTISTO) atomicAdd(&wtisto[iwt], 1ull);
@@ -498,7 +537,7 @@ __global__ void branch_count_kernel(DevStack in, int n, double factor, int* coun
 // single-CTA exclusive scan of counts[0..n) -> offs, total in offs[n]
 __global__ void scan_kernel(const int* counts, int n, int* offs, int cap, BranchDev bd)
 {
-    __shared__ int part[1024];
+    __shared__ long long part[1024];
     if (bd.pn) {
         n = *bd.pn;
         if (bd.need && !*bd.need) {
@@ -509,27 +548,31 @@ __global__ void scan_kernel(const int* counts, int n, int* offs, int cap, Branch
     const int t = threadIdx.x, T = blockDim.x;
     const int chunk = (n + T - 1) / T;
     const int b = t * chunk, e = min(n, b + chunk);
-    int s = 0;
+    // sums in 64 bits, offsets stored saturated at cap + 1: copies at or
+    // beyond cap are dropped by the scatter, so no offset past cap is used
+    const long long sat = (long long)cap + 1;
+    long long s = 0;
     for (int i = b; i < e; ++i) s += counts[i];
     part[t] = s;
     __syncthreads();
     // Hillis-Steele on the partials
     for (int o = 1; o < T; o <<= 1) {
-        const int v = t >= o ? part[t - o] : 0;
+        const long long v = t >= o ? part[t - o] : 0;
         __syncthreads();
         part[t] += v;
         __syncthreads();
     }
-    int run = part[t] - s;
+    long long run = part[t] - s;
     for (int i = b; i < e; ++i) {
-        offs[i] = run;
+        offs[i] = (int)(run < sat ? run : sat);
         run += counts[i];
     }
     if (t == T - 1) {
-        offs[n] = part[T - 1];
+        const long long tot = part[T - 1];
+        offs[n] = (int)(tot < sat ? tot : sat);
         if (bd.pn_out) {
-            *bd.pn_out = min(part[T - 1], cap);
-            if (part[T - 1] > cap) atomicOr(bd.flags, 2);
+            *bd.pn_out = (int)(tot < cap ? tot : cap);
+            if (tot > cap) atomicOr(bd.flags, 2);
         }
     }
 }
@@ -643,52 +686,51 @@ int walker_static_smem_bytes()
     return (int)(a64.sharedSizeBytes > amx.sharedSizeBytes ? a64.sharedSizeBytes : amx.sharedSizeBytes);
 }
 
-static int g_smem_set_mixed = -1, g_smem_set_fp64 = -1;
+// attribute kinds of the per-device record
+enum : int { kAttrCarveout = 0, kAttrSmemMixed = 1, kAttrSmemFp64 = 2 };
+static AttrCache g_attr;
 
-cudaError_t prepare_walker(const SmemLayout& L)
+static cudaError_t walker_attrs(int smem, bool both, bool mixed)
 {
-    const int smem = L.total * 8;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
     // every launch asks for the largest shared-memory carveout, so CTAs of
     // launches with different layouts (systems of a batch) can share an SM
-    static bool carveout = false;
-    if (!carveout) {
-        cudaError_t e = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    int rc = g_attr.ensure(dev, kAttrCarveout, 1, [](int) {
+        cudaError_t r = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                              (int)cudaSharedmemCarveoutMaxShared);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        if (r == cudaSuccess)
+            r = cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxShared);
-        if (e != cudaSuccess) return e;
-        carveout = true;
+        return (int)r;
+    });
+    if (rc) return (cudaError_t)rc;
+    if (both || mixed) {
+        rc = g_attr.ensure(dev, kAttrSmemMixed, smem, [](int v) {
+            return (int)cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        });
+        if (rc) return (cudaError_t)rc;
     }
-    if (g_smem_set_mixed < smem) {
-        const cudaError_t e = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        g_smem_set_mixed = smem;
-    }
-    if (g_smem_set_fp64 < smem) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        g_smem_set_fp64 = smem;
+    if (both || !mixed) {
+        rc = g_attr.ensure(dev, kAttrSmemFp64, smem, [](int v) {
+            return (int)cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        });
+        if (rc) return (cudaError_t)rc;
     }
     return cudaSuccess;
 }
+
+cudaError_t prepare_walker(const SmemLayout& L) { return walker_attrs(L.total * 8, true, false); }
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed)
 {
     const size_t smem = (size_t)L.total * 8;
-    // the shared-memory opt-in is set once per size (prepare_walker sets it
-    // before any graph capture)
-    int& have = mixed ? g_smem_set_mixed : g_smem_set_fp64;
-    if (have < (int)smem) {
-        const cudaError_t e = mixed ? cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                           (int)smem)
-                                    : cudaFuncSetAttribute(walker_kernel<double>,
-                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        have = (int)smem;
-    }
+    // the shared-memory opt-in is recorded per device and size (prepare_walker
+    // sets it before any graph capture; this finds it set)
+    const cudaError_t e = walker_attrs((int)smem, false, mixed);
+    if (e != cudaSuccess) return e;
     if (mixed)
         walker_kernel<df><<<grid, kThreads, smem, st>>>(p, a, L);
     else
@@ -709,7 +751,7 @@ cudaError_t launch_branch(const DevStack& in, const DevStack& out, int n, int n3
 {
     if (n <= 0) return cudaSuccess;
     const BranchDev none{nullptr, nullptr, nullptr, nullptr, nullptr};
-    branch_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, factor, counts, irn1, wtisto, none);
+    branch_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, factor, counts, irn1, wtisto, none, cap);
     scan_kernel<<<1, 1024, 0, st>>>(counts, n, offs, cap, none);
     const int warps = n;
     branch_scatter_kernel<<<(warps * 32 + 255) / 256, 256, 0, st>>>(in, out, n, n3, cap, counts, offs, irn1, none);
@@ -721,7 +763,7 @@ cudaError_t launch_branch_dev(const DevStack& in, const DevStack& out, const int
                               unsigned long long* irn1, unsigned long long* wtisto, cudaStream_t st)
 {
     const BranchDev bd{pn, pn_out, need, dfactor, flags};
-    branch_count_kernel<<<nsm * 4, 256, 0, st>>>(in, 0, 1.0, counts, irn1, wtisto, bd);
+    branch_count_kernel<<<nsm * 4, 256, 0, st>>>(in, 0, 1.0, counts, irn1, wtisto, bd, cap);
     scan_kernel<<<1, 1024, 0, st>>>(counts, 0, offs, cap, bd);
     branch_scatter_kernel<<<nsm * 16, 256, 0, st>>>(in, out, 0, n3, cap, counts, offs, irn1, bd);
     if (need) stack_copy_kernel<<<nsm * 16, 256, 0, st>>>(out, in, pn_out, need, n3);

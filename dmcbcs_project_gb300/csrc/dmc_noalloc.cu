@@ -3,6 +3,7 @@
 // fixed file-scope device array instead of buffers obtained from cudaMalloc.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/dmcbcs_gpu.h"
@@ -55,15 +56,45 @@ dmc::DevStack view(const dmc_dev_stack& s)
     return d;
 }
 
+// byte ranges of the fields of a stack of `count` walkers
+int ranges(const dmc_dev_stack& s, int count, int npart, uintptr_t (*r)[2])
+{
+    const size_t n3 = (size_t)count * 3 * npart * sizeof(double), n1 = (size_t)count * sizeof(double);
+    const void* p[15] = {s.x, s.dpsi, s.dpsig, s.psil, s.psigl, s.d2psi, s.d2psig, s.v,
+                         s.vext, s.weight, s.psil0, s.psigl0, s.wt0, s.is, s.irn};
+    const size_t b[15] = {n3, n3, n3, n1, n1, n1, n1, n1, n1, n1, n1, n1, (size_t)count * sizeof(float),
+                          (size_t)count * sizeof(int), (size_t)count * sizeof(uint64_t)};
+    for (int k = 0; k < 15; ++k) {
+        r[k][0] = reinterpret_cast<uintptr_t>(p[k]);
+        r[k][1] = r[k][0] + b[k];
+    }
+    return 15;
+}
+
+// true when a field of the input stack (n walkers) overlaps a field of the
+// output stack (cap walkers): the scatter would read walkers it overwrites
+bool stacks_overlap(const dmc_dev_stack& in, int n, const dmc_dev_stack& out, int cap, int npart)
+{
+    uintptr_t a[15][2], b[15][2];
+    ranges(in, n, npart, a);
+    ranges(out, cap, npart, b);
+    for (int i = 0; i < 15; ++i)
+        for (int j = 0; j < 15; ++j)
+            if (a[i][0] < b[j][1] && b[j][0] < a[i][1]) return true;
+    return false;
+}
+
 }  // namespace
 
 extern "C" int dmc_branch_noalloc(int n, int npart, int cap, double factor, const dmc_dev_stack* in,
                                   const dmc_dev_stack* out, uint64_t* wtisto, int* nout, void* stream)
 {
     if (!in || !out || !nout || n < 0 || cap < 0 || npart < 1 || npart > DMC_MAX_PART) return DMC_ERR_INVALID;
+    if (!(factor >= 0.0) || !(factor <= 1.0e6)) return DMC_ERR_INVALID;   // also rejects NaN
     if (n > kMax || cap > kMax) return DMC_ERR_NOALLOC_LIMIT;
     *nout = 0;
     if (n == 0) return DMC_OK;
+    if (stacks_overlap(*in, n, *out, cap, npart)) return DMC_ERR_INVALID;
     unsigned char* base = nullptr;
     if (scratch_address(&base) != cudaSuccess) return DMC_ERR_CUDA;
     int* counts = reinterpret_cast<int*>(base + kCountsOff);

@@ -54,6 +54,15 @@ extern "C" {
 #define DMC_ERR_NOMEM 7        /* device or host allocation failed */
 #define DMC_ERR_NOALLOC_LIMIT 8 /* size above the fixed scratch of dmc_branch_noalloc */
 
+/* Failure flags (dmc_get_status, dmc_walker_status).  Neither is an error
+ * of the call that met it: the reference carries on past a singular matrix
+ * with its sentinel (matrixlapack.f90:19-25, psislaterbcs.f90:210) and
+ * stops on a full stack (stack.f90:88-91), which here is the call's
+ * DMC_ERR_OVERFLOW plus the flag. */
+#define DMC_STATUS_SINGULAR 1   /* a pair matrix was singular: log|det| = DMC_MINUSHUGE, zero drift */
+#define DMC_STATUS_NONFINITE 2  /* a walker's log|Psi|, Laplacian, potential or drift was NaN or infinite */
+#define DMC_STATUS_OVERFLOW 4   /* branching made more copies than the stack holds; the excess was dropped */
+
 /* Largest population dmc_branch_noalloc accepts (input walkers and output
  * capacity): its scratch is a fixed device array sized for this many. */
 #define DMC_NOALLOC_MAX_WALKERS 65536
@@ -192,6 +201,18 @@ int dmc_hpsi_batch(dmc_ctx* ctx, int nw, const double* x, double* psil, int* is,
 int dmc_hpsi_device(dmc_ctx* ctx, int nw, const double* x, double* psil, int* is,
                     double* dpsi, double* d2psi, double* v, double* vext,
                     double* psigl, double* dpsig, double* d2psig, void* stream);
+
+/* Failure flags of the context (DMC_STATUS_* OR-ed over every walker of
+ * every evaluation, step and generation since the last clear); clear != 0
+ * resets them.  Reading them waits for the context's stream.  No
+ * counterpart in the reference, which stops or carries a sentinel. */
+int dmc_get_status(dmc_ctx* ctx, int* flags, int clear);
+
+/* Per-walker DMC_STATUS_* flags of the last batched evaluation on this
+ * context (dmc_hpsi_batch/_device, dmc_bcs_batch, dmc_getphi_batch) for its
+ * first nw walkers (DMC_ERR_INVALID if nw exceeds that evaluation's batch).
+ * No counterpart in the reference. */
+int dmc_walker_status(dmc_ctx* ctx, int nw, int* status);
 
 /* Replaces bcs (psislaterbcs.f90:155-225): log|det|, sign, drift dphi[nw][npart][3],
  * Laplacian d2phi and (if smati != NULL) the inverse smati[nw][nd*nd]
@@ -462,9 +483,16 @@ typedef struct dmc_dev_stack {
  *    DMC_ERR_OVERFLOW with *nout = cap.
  *  - wtisto: optional device array of DMC_WTISTO counters, incremented like
  *    the reference's multiplicity histogram; NULL to skip it.
- *  - The first call on a device looks up that device's scratch address; make
- *    that first call before any stream capture.  The call waits on `stream`
- *    (a cudaStream_t, NULL for the default stream) to read the new count.
+ *  - The call waits on `stream` (a cudaStream_t, NULL for the default
+ *    stream): it copies the new count to the host and synchronises the
+ *    stream, so it must not be called while that stream, or any stream in a
+ *    global-mode capture, is being captured.
+ *  - The first call on a device looks up that device's scratch address and
+ *    keeps it for the life of the process: cudaDeviceReset on that device
+ *    (which unloads the library's device code) is not supported afterwards.
+ *  - DMC_ERR_INVALID when a field of `in` overlaps a field of `out` (the
+ *    scatter would read walkers it overwrites) or when factor is negative,
+ *    above 1e6 or not finite.
  *  - All calls share the scratch and every value in it is written before it
  *    is read within a call, so nothing needs clearing; calls that overlap on
  *    the GPU (other streams, other host threads) race on it. */

@@ -129,13 +129,36 @@ def test_deck_reader():
     assert e["operators"] == [0, 0, 0, 0]
 
 
+DECKS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks.json")
+
+
+@pytest.mark.parametrize("name", ["dmcbcs.dat", "input.dat"])
+def test_reference_decks_fixture(name):
+    """The committed parse of the reference's two decks builds valid
+    descriptors: 10 shells each, 33/33 DMC and polarised 9/8 VMC."""
+    import json
+
+    d = json.load(open(DECKS))[name]
+    s, r = abi.make_system(d["system"]), abi.make_run(d["run"])
+    assert s.norb == 10 and r.dt == 5e-5
+    if name == "dmcbcs.dat":
+        assert (s.nbin[0], s.nbin[1], r.idmc, r.dcut) == (33, 33, 1, -1.0)
+    else:
+        assert (s.nbin[0], s.nbin[1], s.nexup, r.idmc, r.dcut) == (9, 8, 1, -1, 0.0)
+
+
 @pytest.mark.parametrize("name", ["dmcbcs.dat", "input.dat"])
 def test_reference_decks_parse(name):
-    path = os.path.join("/root/reference", name)
-    if not os.path.exists(path):
-        pytest.skip("reference decks not present")
-    s, r, e = deck.load_deck(open(path).read())
-    assert s.norb == 10
+    """Where the reference tree is available (DMCBCS_REFERENCE names its
+    directory), the deck reader still gives the committed values."""
+    import json
+
+    ref = os.environ.get("DMCBCS_REFERENCE")
+    if not ref or not os.path.exists(os.path.join(ref, name)):
+        pytest.skip("reference decks not present (set DMCBCS_REFERENCE)")
+    s, r, e = deck.parse_deck(open(os.path.join(ref, name)).read())
+    want = json.load(open(DECKS))[name]
+    assert json.loads(json.dumps({"system": s, "run": r, "extra": e}, sort_keys=True)) == want
 
 
 def _plan_units(grids, per_sm):

@@ -1,18 +1,20 @@
-"""Run every public entry point of the library once on small synthetic
-inputs: wavefunction batches (hpsi, bcs, getphi, matinv), single-particle
-ratios (bcsone, getphione), parameter derivatives (getderbcs, getjasder, the
-adjoint gradients), the stochastic-reconfiguration sums and step, the
-operators (g(r), density, S(q), n(k)), generations on device stacks and on
-pinned host arrays, and a batch of two systems.  Used to profile the
-library's secondary kernels in one process:
+"""Every public entry point of the library once, on small synthetic inputs:
+wavefunction batches (hpsi, bcs, getphi, matinv), single-particle ratios
+(bcsone, getphione), parameter derivatives (getderbcs, getjasder, the adjoint
+gradients), the stochastic-reconfiguration sums and step, the operators
+(g(r), density, S(q), n(k)), generations on device stacks and on pinned host
+arrays, and a batch of two systems.  The calls raise on any status other
+than DMC_OK; the values are checked by the other tests.  Also the one
+process in which the secondary kernels are profiled:
 
-    python -m dmcbcs_project_gb300.exercise
-
-It checks nothing beyond the calls' status codes (the tests check values).
+    python -m pytest tests/test_gpu_exercise.py -q
 """
 import numpy as np
+import pytest
 
-from . import capi, configs
+from dmcbcs_project_gb300 import capi, configs
+
+pytestmark = pytest.mark.gpu
 
 
 def _pinned(torch, ctx):
@@ -27,8 +29,8 @@ def _pinned(torch, ctx):
     return host
 
 
-def main(nwalk=256):
-    import torch
+def test_every_entry_point_once(nwalk=256):
+    torch = pytest.importorskip("torch")
 
     rng = np.random.default_rng(7)
     sysd, rund, _ = configs.workload("n66", nwalk=nwalk, idmc=-1, longrange=(3, 1.0, 0.3))
@@ -73,8 +75,3 @@ def main(nwalk=256):
         b.generations(2, opcomp_last=True)
     for c in ctxs:
         c.close()
-    print("exercise ok")
-
-
-if __name__ == "__main__":
-    main()

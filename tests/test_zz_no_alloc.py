@@ -117,3 +117,19 @@ def test_branch_noalloc_rejects_sizes_above_its_scratch():
     st = L.dmc_branch_noalloc(2, 2, big, 1.0, C.byref(as_struct(a)), C.byref(as_struct(a)), None,
                               C.byref(nout), None)
     assert st == abi.DMC_ERR_NOALLOC_LIMIT
+
+
+def test_branch_noalloc_rejects_aliased_stacks_and_bad_factors():
+    """The scatter must not read walkers it overwrites, and int(w * factor + u)
+    is undefined for a non-finite factor: both are argument errors."""
+    torch = pytest.importorskip("torch")
+    L = capi.load()
+    a = device_stack(torch, 8, 2)
+    b = device_stack(torch, 8, 2)
+    nout = C.c_int(-1)
+    st = L.dmc_branch_noalloc(4, 2, 8, 1.0, C.byref(as_struct(a)), C.byref(as_struct(a)), None, C.byref(nout), None)
+    assert st == abi.DMC_ERR_INVALID
+    for f in (float("nan"), float("inf"), -1.0):
+        st = L.dmc_branch_noalloc(4, 2, 8, f, C.byref(as_struct(a)), C.byref(as_struct(b)), None, C.byref(nout),
+                                  None)
+        assert st == abi.DMC_ERR_INVALID, f
