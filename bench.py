@@ -355,13 +355,16 @@ def uneven_batch(args, rank):
 
 def param_gradients(args, rank):
     """dmc_param_grad (adjoint d log Psi / d theta and d E_L / d theta for
-    theta = vorb(1..7), bfact) on 8192 walkers of the N = 66 system, through
-    the C ABI with host buffers; median of three calls after one warm-up."""
+    theta = vorb(1..7), bfact, b, d and the 16 knots of the up-down Jastrow
+    spline: 26 parameters) on 8192 walkers of the N = 66 system, through the
+    C ABI with host buffers; median of three calls after one warm-up."""
     from dmcbcs_project_gb300 import capi, configs
 
     s, r, _ = configs.workload(WORKLOAD, nwalk=args.pgrad_walkers, idmc=-1)
     r.seed = replica_seed(rank)
+    knots = np.random.default_rng(2024).uniform(-0.3, 0.3, 16) * np.exp(-0.15 * np.arange(16))
     with capi.Context(s, r) as c:
+        c.set_jastrow_spline(knots)
         c.init_walkers()
         x = c.walkers()["x"]
         c.param_grad(x[:64])
@@ -373,6 +376,7 @@ def param_gradients(args, rank):
         np_ = c.param_count()
     t = float(np.median(times))
     return {"workload": "param_grad_n66_33u33d", "walkers": int(x.shape[0]), "parameters": np_,
+            "theta": "vorb(1..7), bfact, b, d, 16 Jastrow spline knots",
             "seconds_per_call": t, "walkers_per_s": x.shape[0] / t,
             "includes": "host-to-device copy of x, FP64 wavefunction and determinant evaluation, adjoint kernel, "
                         "device-to-host copy of both gradients"}

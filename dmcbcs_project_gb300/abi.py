@@ -26,6 +26,8 @@ DMC_ERR_NOMEM = 7
 DMC_ERR_NOALLOC_LIMIT = 8
 DMC_NOALLOC_MAX_WALKERS = 65536
 
+DMC_JASTROW_KNOTS = 16
+
 # failure flags of dmc_get_status / dmc_walker_status
 DMC_STATUS_SINGULAR = 1
 DMC_STATUS_NONFINITE = 2

@@ -30,7 +30,8 @@ EXPORTS = [
     "dmc_write_operators", "dmc_getjasder_batch", "dmc_sr_configure", "dmc_dfmath_eval",
     "dmc_batch_create", "dmc_batch_destroy", "dmc_batch_last_error", "dmc_batch_set_grids", "dmc_batch_get_grids",
     "dmc_batch_plan", "dmc_batch_tune", "dmc_batch_generations", "dmc_param_count", "dmc_param_grad",
-    "dmc_generation_host", "dmc_get_status", "dmc_walker_status",
+    "dmc_generation_host", "dmc_get_status", "dmc_walker_status", "dmc_set_jastrow_spline",
+    "dmc_get_jastrow_spline", "dmc_set_beta", "dmc_sr_configure_adjoint",
 ]
 
 PREC_FP64 = 0
@@ -123,6 +124,10 @@ def load(path=LIB_PATH):
                                      C.POINTER(abi.DevStack), vp, C.POINTER(C.c_int), vp]
     L.dmc_generation_host.argtypes = [vp, C.POINTER(Walkers), C.POINTER(Walkers), C.c_int]
     L.dmc_get_status.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
+    L.dmc_set_jastrow_spline.argtypes = [vp, vp, C.c_int]
+    L.dmc_set_beta.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.dmc_sr_configure_adjoint.argtypes = [vp]
+    L.dmc_get_jastrow_spline.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
     L.dmc_walker_status.argtypes = [vp, C.c_int, _ip]
     L.dmc_param_count.argtypes = [vp, C.POINTER(C.c_int)]
     L.dmc_param_grad.argtypes = [vp, C.c_int, _dp, _dp, _dp]
@@ -249,6 +254,8 @@ class Context:
             n = self.norb
         elif which == 11:
             n = 2
+        elif which == 12:
+            n = 3
         out = np.zeros(n)
         self._check(load().dmc_get_table(self._h, which, out, n))
         return out
@@ -382,8 +389,9 @@ class Context:
         return n.value
 
     def param_grad(self, x):
-        """Adjoint gradients for theta = (vorb(1..norb)[, bfact]): returns
-        (d log|Psi|/d theta, d E_L/d theta), each (nw, np)."""
+        """Adjoint gradients for theta = (vorb(1..norb)[, bfact, b, d][, the
+        16 Jastrow knots]): returns (d log|Psi|/d theta, d E_L/d theta), each
+        (nw, np)."""
         x = self._x(x)
         nw, np_ = x.shape[0], self.param_count()
         dl = np.zeros((nw, np_))
@@ -543,6 +551,30 @@ class Context:
         w = self.walker_struct(dict(arrs, n=arrs["cap"]))
         self._check(load().dmc_get_walkers(self._h, C.byref(w)))
         return w.n
+
+    def set_jastrow_spline(self, knots):
+        """The opt-in up-down Jastrow spline (16 knots; None or [] = off)."""
+        k = np.ascontiguousarray(knots if knots is not None else [], dtype=np.float64)
+        self._check(load().dmc_set_jastrow_spline(self._h, _opt(k) if k.size else None, int(k.size)))
+
+    def set_beta(self, b, d, bfact):
+        """New b, d and bfact of the beta function (tables rebuilt)."""
+        self._check(load().dmc_set_beta(self._h, float(b), float(d), float(bfact)))
+
+    def sr_configure_adjoint(self):
+        """SR over every adjoint-gradient parameter."""
+        self._check(load().dmc_sr_configure_adjoint(self._h))
+        self._nparm = self.param_count()
+
+    def beta_params(self):
+        """(bfact, b, d) of the beta function."""
+        return self.table(12)
+
+    def jastrow_spline(self):
+        n = C.c_int()
+        buf = np.zeros(abi.DMC_JASTROW_KNOTS)
+        self._check(load().dmc_get_jastrow_spline(self._h, _opt(buf), buf.size, C.byref(n)))
+        return buf[:n.value].copy()
 
     def status(self, clear=False):
         """DMC_STATUS_* flags met since the last clear (dmc_get_status)."""

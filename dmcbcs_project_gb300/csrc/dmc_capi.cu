@@ -174,9 +174,11 @@ struct dmc_ctx {
     // single-particle moves and parameter derivatives
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum, srene;
     DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
+    DevBuf<PgTab> pg_btab;                                      // d beta / d b, d beta / d d tables
     DevBuf<int> sip;
     int64_t sr_count = 0;
     bool sr_jas = false, sr_det = true;   // iopt(1), iopt(2) of the optimizer deck
+    bool sr_adj = false;                  // SR over every parameter of dmc_param_grad
     // operators (g(r), density profile, S(q), n(k))
     struct Ops {
         bool on = false;
@@ -666,8 +668,36 @@ int dmc_get_table(const dmc_ctx* c, int which, double* out, int n)
         out[0] = S.jbeta;
         out[1] = S.jgamma;
         return DMC_OK;
+    case 12:
+        if (n < 3) return DMC_ERR_INVALID;
+        out[0] = S.bfact;
+        out[1] = S.bbeta;
+        out[2] = S.dbeta;
+        return DMC_OK;
     }
     return DMC_ERR_INVALID;
+}
+
+int dmc_set_jastrow_spline(dmc_ctx* c, const double* knots, int nknots)
+{
+    if (!c) return DMC_ERR_INVALID;
+    int rc = c->S.set_jastrow_spline(knots, nknots, c->err);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    // the spline reaches L/2: the mixed path keeps the whole up-down Jastrow
+    // in double-float (no zero tail beyond the healing distance)
+    c->P.ntab0 = nknots > 0 ? c->S.ntab : c->S.ntab0;
+    return upload_tables(c);
+}
+
+int dmc_get_jastrow_spline(const dmc_ctx* c, double* knots, int cap, int* nknots)
+{
+    if (!c || !nknots) return DMC_ERR_INVALID;
+    const int n = (int)c->S.jknots.size();
+    *nknots = n;
+    if (n > 0 && (!knots || cap < n)) return DMC_ERR_INVALID;
+    for (int k = 0; k < n; ++k) knots[k] = c->S.jknots[k];
+    return DMC_OK;
 }
 
 int dmc_set_vorb(dmc_ctx* c, const double* vorb, int norb)
@@ -1450,7 +1480,25 @@ int dmc_getjasder_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)
     return DMC_OK;
 }
 
-static int pgrad_np(const dmc_ctx* c) { return c->S.norb + (c->P.nobeta ? 0 : 1); }
+static int pgrad_nbeta(const dmc_ctx* c) { return c->P.nobeta ? 0 : 3; }
+static int pgrad_nknot(const dmc_ctx* c) { return (int)c->S.jknots.size(); }
+static int pgrad_np(const dmc_ctx* c) { return c->S.norb + pgrad_nbeta(c) + pgrad_nknot(c); }
+
+// the b and d derivative tables of beta on the device (built once: b and d
+// do not change during a context's life)
+static int pgrad_btab(dmc_ctx* c)
+{
+    if (c->P.nobeta || c->pg_btab.p) return DMC_OK;
+    std::vector<double> t[2][3];
+    c->S.beta_param_tables(t);
+    const size_t nt = (size_t)c->S.ntabb + 1;
+    std::vector<PgTab> h(2 * nt);
+    for (int w = 0; w < 2; ++w)
+        for (size_t i = 0; i < nt; ++i) h[w * nt + i] = PgTab{t[w][0][i], t[w][1][i], t[w][2][i], 0.0};
+    CK(c->pg_btab.alloc(2 * nt));
+    CK(cudaMemcpy(c->pg_btab.p, h.data(), 2 * nt * sizeof(PgTab), cudaMemcpyHostToDevice));
+    return DMC_OK;
+}
 
 int dmc_param_count(const dmc_ctx* c, int* np)
 {
@@ -1459,31 +1507,28 @@ int dmc_param_count(const dmc_ctx* c, int* np)
     return DMC_OK;
 }
 
-int dmc_param_grad(dmc_ctx* c, int nw, const double* x, double* dlogpsi, double* deloc)
+// the adjoint gradients of nw walkers at device positions dx into device
+// arrays dlog[nw][np], del[nw][np] (stream-ordered)
+static int pgrad_device(dmc_ctx* c, int nw, const double* dx, double* dlog, double* del)
 {
-    if (!c) return DMC_ERR_INVALID;
-    if (nw < 0 || (nw > 0 && (!x || !dlogpsi || !deloc))) return fail(c, DMC_ERR_INVALID, "bad param_grad arguments");
-    if (nw == 0) return DMC_OK;
     const size_t n3 = (size_t)c->n3, nd2 = (size_t)c->S.nd * c->S.nd;
     const int np = pgrad_np(c);
-    CK(c->sx.alloc(nw * n3));
     CK(c->pg_dpsi.alloc(nw * n3));
     CK(c->pg_dphi.alloc(nw * n3));
     CK(c->ssinv.alloc(nw * nd2));
-    CK(c->pg_dlog.alloc((size_t)nw * np));
-    CK(c->pg_del.alloc((size_t)nw * np));
-    CK(cudaMemcpyAsync(c->sx.p, x, nw * n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     // the total drift and the determinant's drift and inverse, in FP64
     const int prec = c->precision;
     c->precision = DMC_PREC_FP64;
-    int rc = run_eval(c, MODE_HPSI, nw, c->sx.p, nullptr, nullptr, c->pg_dpsi.p, nullptr, nullptr, nullptr, nullptr,
+    int rc = run_eval(c, MODE_HPSI, nw, dx, nullptr, nullptr, c->pg_dpsi.p, nullptr, nullptr, nullptr, nullptr,
                       nullptr, nullptr, nullptr, c->stream);
     if (rc == DMC_OK)
-        rc = run_eval(c, MODE_BCS, nw, c->sx.p, nullptr, nullptr, c->pg_dphi.p, nullptr, nullptr, nullptr, nullptr,
+        rc = run_eval(c, MODE_BCS, nw, dx, nullptr, nullptr, c->pg_dphi.p, nullptr, nullptr, nullptr, nullptr,
                       nullptr, nullptr, c->ssinv.p, c->stream);
     c->precision = prec;
     if (rc) return rc;
     c->launches += 2;
+    rc = pgrad_btab(c);
+    if (rc) return rc;
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     const size_t need = pgrad_doubles(c->P);
@@ -1493,13 +1538,43 @@ int dmc_param_grad(dmc_ctx* c, int nw, const double* x, double* dlogpsi, double*
         CK(c->pg_scr.alloc((size_t)grid * need));
         scr = c->pg_scr.p;
     }
-    CK(launch_pgrad(c->P, c->kv.p, c->tud.p, c->sx.p, c->ssinv.p, c->pg_dpsi.p, c->pg_dphi.p, c->pg_dlog.p,
-                    c->pg_del.p, nw, np, c->sd.bfact, grid, scr, optin, c->stream));
+    CK(launch_pgrad(c->P, c->kv.p, c->tud.p, dx, c->ssinv.p, c->pg_dpsi.p, c->pg_dphi.p, dlog, del, nw, np,
+                    c->S.bfact, c->pg_btab.p, pgrad_nbeta(c), pgrad_nknot(c), grid, scr, optin, c->stream));
     ++c->launches;
+    return DMC_OK;
+}
+
+int dmc_param_grad(dmc_ctx* c, int nw, const double* x, double* dlogpsi, double* deloc)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (nw < 0 || (nw > 0 && (!x || !dlogpsi || !deloc))) return fail(c, DMC_ERR_INVALID, "bad param_grad arguments");
+    if (nw == 0) return DMC_OK;
+    const size_t n3 = (size_t)c->n3;
+    const int np = pgrad_np(c);
+    CK(c->sx.alloc(nw * n3));
+    CK(c->pg_dlog.alloc((size_t)nw * np));
+    CK(c->pg_del.alloc((size_t)nw * np));
+    CK(cudaMemcpyAsync(c->sx.p, x, nw * n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = pgrad_device(c, nw, c->sx.p, c->pg_dlog.p, c->pg_del.p);
+    if (rc) return rc;
     CK(cudaMemcpyAsync(dlogpsi, c->pg_dlog.p, (size_t)nw * np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(deloc, c->pg_del.p, (size_t)nw * np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return DMC_OK;
+}
+
+int dmc_set_beta(dmc_ctx* c, double b, double d, double bfact)
+{
+    if (!c) return DMC_ERR_INVALID;
+    if (c->P.nobeta || !(bfact > 0.0) || !(b > 0.0) || !(d > 0.0) || !std::isfinite(b * d * bfact))
+        return fail(c, DMC_ERR_INVALID, "dmc_set_beta needs the beta function on and b, d, bfact > 0");
+    CK(cudaStreamSynchronize(c->stream));
+    c->S.set_beta(b, d, bfact);
+    c->sd.bbeta = b;
+    c->sd.dbeta = d;
+    c->sd.bfact = bfact;
+    c->pg_btab.release();   // the b and d derivative tables follow on the next gradient
+    return upload_tables(c);
 }
 
 int dmc_getderbcs_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)
@@ -1849,8 +1924,13 @@ int dmc_write_operators(dmc_ctx* c, const char* dir, double tau)
 // ---- stochastic reconfiguration ---------------------------------------------
 
 // SR parameters: (beta, gamma) of the long-range Jastrow when iopt(1), then
-// vorb when iopt(2) (calder, optimizer.f90:100-104)
-static int sr_nparm(const dmc_ctx* c) { return (c->sr_jas ? 2 : 0) + (c->sr_det ? c->S.norb : 0); }
+// vorb when iopt(2) (calder, optimizer.f90:100-104); or, in the adjoint
+// mode, every parameter of dmc_param_grad
+static int sr_nparm(const dmc_ctx* c)
+{
+    if (c->sr_adj) return pgrad_np(c);
+    return (c->sr_jas ? 2 : 0) + (c->sr_det ? c->S.norb : 0);
+}
 
 static int sr_buffers(dmc_ctx* c)
 {
@@ -1870,6 +1950,16 @@ int dmc_sr_configure(dmc_ctx* c, int opt_jastrow, int opt_det)
     if (opt_jastrow && c->S.nql == 0) return fail(c, DMC_ERR_INVALID, "the long-range Jastrow is off (numq = 0)");
     c->sr_jas = opt_jastrow != 0;
     c->sr_det = opt_det != 0;
+    c->sr_adj = false;
+    c->srsum.release();
+    c->sr_count = 0;
+    return sr_buffers(c);
+}
+
+int dmc_sr_configure_adjoint(dmc_ctx* c)
+{
+    if (!c) return DMC_ERR_INVALID;
+    c->sr_adj = true;
     c->srsum.release();
     c->sr_count = 0;
     return sr_buffers(c);
@@ -1888,11 +1978,17 @@ int dmc_sr_accumulate(dmc_ctx* c, int64_t* nsamples)
     if (n > 0) {
         StackBufs& s = c->st[c->istin];
         CK(c->sder.alloc((size_t)n * np));
-        if (c->sr_jas) {
-            CK(launch_jasder(c->P, c->jq.p, s.x.p, c->sder.p, n, c->grid, c->stream, np));
-            ++c->launches;
+        if (c->sr_adj) {
+            // O_k = d log Psi / d theta_k of every adjoint parameter
+            CK(c->pg_del.alloc((size_t)n * np));
+            if ((rc = pgrad_device(c, n, s.x.p, c->sder.p, c->pg_del.p))) return rc;
+        } else {
+            if (c->sr_jas) {
+                CK(launch_jasder(c->P, c->jq.p, s.x.p, c->sder.p, n, c->grid, c->stream, np));
+                ++c->launches;
+            }
+            if (c->sr_det && (rc = derbcs_device(c, n, s.x.p, c->sder.p, np, c->sr_jas ? 2 : 0))) return rc;
         }
-        if (c->sr_det && (rc = derbcs_device(c, n, s.x.p, c->sder.p, np, c->sr_jas ? 2 : 0))) return rc;
         CK(c->srene.alloc((size_t)n));   // the walkers' local energies
         CK(launch_sr_sums(c->sder.p, s.d2psi.p, s.v.p, n, np, c->S.hbar, c->S.eunit, c->S.npart, c->srsum.p,
                           c->srene.p, c->stream));
@@ -1999,14 +2095,31 @@ int dmc_sr_update(dmc_ctx* c, double delta0, double eps, double* newpars, double
         dpar[i] = delta0 * sm;
     }
     // params = params + newpars; setjasparam / setdetparam (optimizer.f90:163, 72-88)
-    if (c->sr_jas) {
+    if (c->sr_adj) {
+        // vorb, then bfact, b, d, then the Jastrow knots (dmc_param_grad's order)
+        std::vector<double> vorb(c->S.vorb);
+        for (int i = 0; i < c->S.norb; ++i) vorb[i] += dpar[i];
+        if ((rc = dmc_set_vorb(c, vorb.data(), c->S.norb))) return rc;
+        int off = c->S.norb;
+        if (pgrad_nbeta(c)) {
+            if ((rc = dmc_set_beta(c, c->S.bbeta + dpar[off + 1], c->S.dbeta + dpar[off + 2],
+                                   c->S.bfact + dpar[off])))
+                return rc;
+            off += 3;
+        }
+        if (pgrad_nknot(c)) {
+            std::vector<double> kn(c->S.jknots);
+            for (size_t k = 0; k < kn.size(); ++k) kn[k] += dpar[off + k];
+            if ((rc = dmc_set_jastrow_spline(c, kn.data(), (int)kn.size()))) return rc;
+        }
+    } else if (c->sr_jas) {
         c->S.set_jaslong(c->S.jbeta + dpar[0], c->S.jgamma + dpar[1]);
         c->P.jbeta = c->S.jbeta;
         c->P.jgamma = c->S.jgamma;
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaMemcpy(c->jq.p, c->S.jq.data(), c->S.jq.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
-    if (c->sr_det) {
+    if (c->sr_det && !c->sr_adj) {
         const int off = c->sr_jas ? 2 : 0;
         std::vector<double> vorb(c->S.vorb);
         for (int i = 0; i < c->S.norb; ++i) vorb[i] += dpar[off + i];

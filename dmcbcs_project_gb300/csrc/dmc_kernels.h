@@ -56,12 +56,20 @@ cudaError_t launch_walkers_put(const HostWalkers& h, const DevStack& d, int n, i
 cudaError_t launch_walkers_get(const DevStack& d, const HostWalkers& h, int n, int n3, int grid, cudaStream_t st,
                                const int* pn = nullptr, int cap = 0);
 size_t derbcs_smem_bytes(const DevParams& p);
+// most parameters of the adjoint gradients: vorb (DMC_MAX_SHELLS), bfact,
+// b, d and the 16 Jastrow knots
+constexpr int kPgradMax = DMC_MAX_SHELLS + 3 + 16;
+// {f, f', lap f} records of the b and d derivative tables of beta
+struct PgTab {
+    double f, df, d2f, pad;
+};
 // adjoint parameter gradients (dmc_single.cu): doubles of one CTA's working
 // set; on chip when it fits in smem_limit bytes, else in gscr (grid x that)
 size_t pgrad_doubles(const DevParams& p);
 cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x, const double* sinv,
                          const double* dpsi, const double* dphi, double* dlog, double* deloc, int nw, int np,
-                         double bfact, int grid, double* gscr, int smem_limit, cudaStream_t st);
+                         double bfact, const PgTab* btd, int nbeta, int nknot, int grid, double* gscr, int smem_limit,
+                         cudaStream_t st);
 // dpsi[w*stride + off + shell]; stride < 0 means norb
 cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x, const double* smati, double* dpsi,
                           int nw, int grid, cudaStream_t st, int stride = -1, int off = 0);

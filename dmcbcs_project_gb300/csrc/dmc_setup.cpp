@@ -8,7 +8,10 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <complex>
 #include <cstring>
+
+#include "dmc_spline.h"
 
 namespace dmc {
 namespace {
@@ -82,20 +85,32 @@ int k_shells(double el, int nsh0, std::vector<KVec>& out, std::vector<int>& nums
 namespace {
 
 // ---- beta function (betafun.f90) ----------------------------------------
+//
+// The construction is templated on its scalar type: double builds the
+// tables, std::complex<double> with b or d given a tiny imaginary part
+// builds their exact derivatives with respect to b or d (complex-step
+// differentiation: Im f(p + i h) / h = f'(p) to rounding, with no
+// cancellation).  Branches and the image count follow the real parts, so the
+// derivative is that of the same piecewise construction.
 
+inline double re(double v) { return v; }
+inline double re(const std::complex<double>& v) { return v.real(); }
+
+template <class T>
 struct Beta {
-    double b, c, d, small, c0, c1, c2, c3, c4, el;
+    T b, c, d, small, c0, c1, c2, c3, c4;
+    double el;
 
     // beta0, betafun.f90:127-149
-    void beta0(double r, double& b1, double& b1p, double& b1pp) const
+    void beta0(double r, T& b1, T& b1p, T& b1pp) const
     {
-        const double x = b * r;
-        if (r < small) {
+        const T x = b * r;
+        if (r < re(small)) {
             b1 = c0 + x * (c1 + x * (c2 + x * (c3 + x * c4)));
             b1p = c1 + x * (2.0 * c2 + x * (3.0 * c3 + 4.0 * c4 * x));
             b1pp = 2.0 * c2 + x * (6.0 * c3 + 12.0 * c4 * x);
         } else {
-            const double ex = std::exp(-x), ex10 = std::exp(-d * x);
+            const T ex = std::exp(-x), ex10 = std::exp(-d * x);
             b1 = (1.0 + c * x) * (1.0 - ex10) * ex / x;
             b1p = ex * (-1.0 - x * (1.0 + c * x) + ex10 * (1.0 + x * (1.0 + d) * (1.0 + c * x))) / (x * x);
             b1pp = ex * (2.0 + x * (2.0 + x * (1.0 + c * x))
@@ -109,35 +124,37 @@ struct Beta {
     }
 
     // beta, betafun.f90:151-171: symmetric about L/2, zero at L/2
-    void beta(double r, double& b1, double& b1p, double& b1pp) const
+    void beta(double r, T& b1, T& b1p, T& b1pp) const
     {
         if (r > el * 0.5) {
-            b1 = b1p = b1pp = 0.0;
+            b1 = b1p = b1pp = T(0.0);
             return;
         }
-        double bet0, t1, t2, bet1, bet1p, bet1pp, bet2, bet2p, bet2pp;
+        T bet0, t1, t2, bet1, bet1p, bet1pp, bet2, bet2p, bet2pp;
         beta0(el * 0.5, bet0, t1, t2);
         beta0(r, bet1, bet1p, bet1pp);
         beta0(el - r, bet2, bet2p, bet2pp);
         b1 = bet1 + bet2 - 2.0 * bet0;
-        b1p = (r < 1.0e-14) ? 0.0 : bet1p - bet2p;
+        b1p = (r < 1.0e-14) ? T(0.0) : bet1p - bet2p;
         b1pp = bet1pp + bet2pp;
     }
 };
 
-// initbeta, betafun.f90:74-125, then the bfact scaling of setbeta (:62-64)
-void beta_tables(Setup& s, double bb, double dd, double bfact)
+// initbeta, betafun.f90:74-125, then the bfact scaling of setbeta (:62-64),
+// on n + 1 points of [0, L/2]
+template <class T>
+void beta_tables_t(double el, int n, T bb, T dd, double bfact, std::vector<T>& bt, std::vector<T>& dbt,
+                   std::vector<T>& d2bt)
 {
-    Beta B;
-    const double el = s.el;
+    Beta<T> B;
     B.el = el;
     B.b = bb;
     B.d = dd;
-    const double e1 = std::exp(bb * el * (1.0 + dd)), e2 = std::exp(dd * bb * el);
+    const T e1 = std::exp(bb * el * (1.0 + dd)), e2 = std::exp(dd * bb * el);
     B.c = 0.5 * (2.0 + 2.0 * dd * bb * el + (dd * bb * el) * (dd * bb * el) * e1 + 2.0 * dd * bb * bb * el * el * e1
                  + 2.0 * bb * el - 2.0 * e2 * bb * el - 2.0 * e2)
           / (el * el * (e2 - 1.0 - dd + dd * e1) * (bb * bb));
-    const double c = B.c, d = dd;
+    const T c = B.c, d = dd;
     B.c0 = d;
     B.small = 1.0e-3 / bb;
     B.c1 = -d + c * d - d * d / 2.0;
@@ -145,48 +162,52 @@ void beta_tables(Setup& s, double bb, double dd, double bfact)
     B.c3 = -d / 6.0 - d * d / 4.0 - d * d * d / 6.0 - d * d * d * d / 24.0 + c * (d / 2.0 + d * d / 2.0 + d * d * d / 6.0);
     B.c4 = d / 24.0 + d * d / 12.0 + d * d * d / 12.0 + d * d * d * d / 24.0 + d * d * d * d * d / 120.0
            - c * (d / 6.0 + d * d / 4.0 + d * d * d / 6.0 + d * d * d * d / 24.0);
-    const int n = s.ntabb;
     const double dr = 0.5 * el / n;
     // number of periodic images whose beta is still above 1e-10
     int nj = 0;
-    double betan = 10.0, t1, t2;
-    while (std::fabs(betan) > 1.0e-10) {
+    T betan = 10.0, t1, t2;
+    while (std::fabs(re(betan)) > 1.0e-10) {
         ++nj;
         B.beta(el * nj, betan, t1, t2);
     }
-    s.btab.assign(n + 1, 0.0);
-    s.dbtab.assign(n + 1, 0.0);
-    s.d2btab.assign(n + 1, 0.0);
+    bt.assign(n + 1, T(0.0));
+    dbt.assign(n + 1, T(0.0));
+    d2bt.assign(n + 1, T(0.0));
     for (int i = 0; i <= n; ++i) {
         const double r = i * dr;
-        double f, fp, fpp;
+        T f, fp, fpp;
         B.beta(r, f, fp, fpp);
         for (int j = 1; j <= nj; ++j) {
-            double b2, b2p, b2pp, b3, b3p, b3pp;
+            T b2, b2p, b2pp, b3, b3p, b3pp;
             B.beta(j * el - r, b2, b2p, b2pp);
             B.beta(j * el + r, b3, b3p, b3pp);
             f = f + b2 + b3;
             fp = fp - b2p + b3p;
             fpp = fpp + b2pp + b3pp;
         }
-        s.btab[i] = f;
-        s.dbtab[i] = fp;
-        s.d2btab[i] = fpp;
+        bt[i] = f;
+        dbt[i] = fp;
+        d2bt[i] = fpp;
     }
-    const double shift = s.btab[n];
+    const T shift = bt[n];
     for (int i = 0; i <= n; ++i) {
-        s.btab[i] -= shift;
+        bt[i] -= shift;
         if (i != 0)
-            s.d2btab[i] = s.d2btab[i] + 2.0 * s.dbtab[i] / (i * dr);   // + (ndim-1) f'/r
+            d2bt[i] = d2bt[i] + 2.0 * dbt[i] / (i * dr);   // + (ndim-1) f'/r
         else
-            s.d2btab[i] = 3.0 * s.d2btab[i];                         // quadratic at the origin
+            d2bt[i] = 3.0 * d2bt[i];                       // quadratic at the origin
     }
     const double af = std::fabs(bfact);
     for (int i = 0; i <= n; ++i) {
-        s.btab[i] *= af;
-        s.dbtab[i] *= af;
-        s.d2btab[i] *= af;
+        bt[i] *= af;
+        dbt[i] *= af;
+        d2bt[i] *= af;
     }
+}
+
+void beta_tables(Setup& s, double bb, double dd, double bfact)
+{
+    beta_tables_t<double>(s.el, s.ntabb, bb, dd, bfact, s.btab, s.dbtab, s.d2btab);
 }
 
 // ---- Jastrow from the two-body zero-energy equation (rungekutta.f90) ----
@@ -432,6 +453,14 @@ int Setup::build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string&
     }
     iop = true;   // the potential table switches opposite-spin pairs on (coshpot.f90:88)
     ieq = cjas[1] != 0.0;
+    // the reference's up-down Jastrow, kept for the opt-in spline on top of it
+    uref = utab[0];
+    duref = dutab[0];
+    d2uref = d2utab[0];
+    jknots.clear();
+    bbeta = sd.bbeta;
+    dbeta = sd.dbeta;
+    bfact = sd.bfact;
     // units, dmcbcs.f90:146-170
     if (rd.units) {
         kunit = std::pow(3.0 * (kPi * kPi) * (npart / (el * el * el)), 1.0 / 3.0);
@@ -460,6 +489,69 @@ void Setup::set_jaslong(double beta, double gamma)
         double* rec = &jq[8 * (size_t)q];
         const double qmod = std::sqrt(rec[3]);
         rec[4] = gamma * std::exp(-beta * qmod) / qmod;
+    }
+}
+
+int Setup::set_jastrow_spline(const double* knots, int n, std::string& err)
+{
+    if (n != 0 && n != kJastrowKnots) {
+        err = "the Jastrow spline has 16 knots (0 switches it off)";
+        return DMC_ERR_INVALID;
+    }
+    if (n > 0 && !knots) {
+        err = "no knot values";
+        return DMC_ERR_INVALID;
+    }
+    for (int k = 0; k < n; ++k)
+        if (!std::isfinite(knots[k])) {
+            err = "knot values must be finite";
+            return DMC_ERR_INVALID;
+        }
+    jknots.assign(knots, knots + n);
+    utab[0] = uref;
+    dutab[0] = duref;
+    d2utab[0] = d2uref;
+    if (n == 0) return DMC_OK;
+    const double h = el / kJastrowCells, dr = range / ntab;
+    for (int i = 0; i <= ntab; ++i) {
+        const double r = i * dr;
+        double u = 0.0, du = 0.0, d2u = 0.0;
+        for (int k = 0; k < n; ++k) {
+            double f, fp, fpp;
+            jastrow_knot_basis(k, r, h, f, fp, fpp);
+            u += jknots[k] * f;
+            du += jknots[k] * fp;
+            d2u += jknots[k] * fpp;
+        }
+        utab[0][i] += u;
+        dutab[0][i] += du;
+        d2utab[0][i] += d2u;
+    }
+    return DMC_OK;
+}
+
+void Setup::set_beta(double b, double d, double bf)
+{
+    bbeta = b;
+    dbeta = d;
+    bfact = bf;
+    beta_tables(*this, b, d, bf);
+}
+
+void Setup::beta_param_tables(std::vector<double> (&out)[2][3]) const
+{
+    using C = std::complex<double>;
+    const double h = 1.0e-20;
+    for (int which = 0; which < 2; ++which) {
+        std::vector<C> t[3];
+        const C bb(bbeta, which == 0 ? h * std::max(1.0, std::fabs(bbeta)) : 0.0);
+        const C dd(dbeta, which == 1 ? h * std::max(1.0, std::fabs(dbeta)) : 0.0);
+        const double step = which == 0 ? bb.imag() : dd.imag();
+        beta_tables_t<C>(el, ntabb, bb, dd, bfact, t[0], t[1], t[2]);
+        for (int m = 0; m < 3; ++m) {
+            out[which][m].resize(t[m].size());
+            for (size_t i = 0; i < t[m].size(); ++i) out[which][m][i] = t[m][i].imag() / step;
+        }
     }
 }
 

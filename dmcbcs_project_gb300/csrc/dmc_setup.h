@@ -67,7 +67,22 @@ struct Setup {
     bool cutdrift = false;
 
     // Returns DMC_OK or an error code with a message in err.
+    // beta parameters as read (setbeta, betafun.f90:19-21)
+    double bbeta = 0, dbeta = 0, bfact = 0;
+    // the reference's up-down Jastrow tables and the opt-in spline on top
+    // (dmc_spline.h): jknots empty = off
+    std::vector<double> uref, duref, d2uref;
+    std::vector<double> jknots;
+
     int build(const dmc_system_desc& sd, const dmc_run_desc& rd, std::string& err);
+    // the up-down Jastrow = reference + sum_k knots[k] phi_k (n = 16), or the
+    // reference alone (n = 0); rebuilds utab/dutab/d2utab[0]
+    int set_jastrow_spline(const double* knots, int n, std::string& err);
+    // d/db and d/dd of the beta tables (btab, dbtab, d2btab, bfact-scaled):
+    // out[0][*] for b, out[1][*] for d, each ntabb + 1 values
+    void beta_param_tables(std::vector<double> (&out)[2][3]) const;
+    // new b, d and bfact of the beta function (on): rebuilds its tables
+    void set_beta(double b, double d, double bf);
     int set_vorb(const double* v, int n, std::string& err);
     // setjasparam (jastrowlongrange.f90:57-61): new beta, gamma; recomputes
     // the q-vector weights

@@ -9,8 +9,9 @@
 //  - the sums that calder (optimizer.f90:90-116) accumulates over a walker
 //    population for the stochastic-reconfiguration step;
 //  - the adjoint parameter gradients d log Psi / d theta and d E_L / d theta
-//    for theta = (vorb(1..norb), bfact), the amplitudes the pair function
-//    phi (psislaterbcs.f90:249-293) is linear in.
+//    for theta = (vorb(1..norb), bfact, b, d) of the pair function
+//    (psislaterbcs.f90:249-293, betafun.f90:12-125) and the 16 knots of the
+//    opt-in Jastrow spline.
 // One warp per walker for the ratios (a few hundred flops each); one CTA per
 // walker for the derivatives, which contract the whole inverse.
 #include <cuda_runtime.h>
@@ -20,6 +21,7 @@
 #include "dmc_kernels.h"
 #include "dmc_walker.cuh"
 #include "dmc_single.cuh"
+#include "dmc_spline.h"
 
 namespace dmc {
 
@@ -156,6 +158,45 @@ __device__ __forceinline__ void beta_all(const DevParams& p, const TabUD* tud, d
     d2f = W.c1 * T[0].d2b + W.c2 * T[1].d2b + W.c3 * T[2].d2b + W.c4 * T[3].d2b;
 }
 
+// a {f, f', lap f} record table on the beta grid (the b and d derivative
+// tables of the adjoint gradients)
+__device__ __forceinline__ void btab_all(const DevParams& p, const PgTab* T0, double r, double& f, double& df,
+                                         double& d2f)
+{
+    f = df = d2f = 0.0;
+    if (p.nobeta || r > p.rangeb) return;
+    const walker::Lagrange<double> W = walker::lagrange(r, p.scaleb, p.ntab);
+    const PgTab* T = T0 + (W.idx - 1);
+    f = W.c1 * T[0].f + W.c2 * T[1].f + W.c3 * T[2].f + W.c4 * T[3].f;
+    df = W.c1 * T[0].df + W.c2 * T[1].df + W.c3 * T[2].df + W.c4 * T[3].df;
+    d2f = W.c1 * T[0].d2f + W.c2 * T[1].d2f + W.c3 * T[2].d2f + W.c4 * T[3].d2f;
+}
+
+// N sums over the CTA in a fixed order (warp trees, then the warps in
+// order); red holds at least kWarps * N doubles; sum k goes to outa[k] for
+// k < N/2 and to outb[k - N/2] otherwise
+template <int N>
+__device__ void block_sum_n(double (&v)[N], double* red, double* outa, double* outb)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        double a = v[k];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) red[warp * N + k] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double t = 0.0;
+        for (int q = 0; q < kWarps; ++q) t += red[q * N + threadIdx.x];
+        if (threadIdx.x < N / 2)
+            outa[threadIdx.x] = t;
+        else
+            outb[threadIdx.x - N / 2] = t;
+    }
+    __syncthreads();
+}
+
 __device__ double block_sum1(double v, double* red)
 {
     red[threadIdx.x] = v;
@@ -182,11 +223,24 @@ __device__ double block_sum1(double v, double* red)
 //   d log Psi / d theta = tr(S^-1 S')
 //   d Q / d theta       = tr(S^-1 M') - tr(T S'),   T = S^-1 M S^-1
 // and d E_L / d theta = -hbar dQ/dtheta: one extra pair of nd^3 products per
-// walker gives every parameter.  Only the up-down block depends on theta:
-// phi = vorb(1) + sum_k 2 vorb(shell k) cos(k.r) + beta(r) with beta linear
-// in bfact.  Inputs per walker: x, the inverse (column-major as smati), the
-// total and determinant drifts (grad / sqrt m) whose difference is grad J.
-// Outputs dlog[w*np + t], deloc[w*np + t] for t = vorb(1..norb), then bfact.
+// walker gives every parameter.  Only the up-down block depends on the pair
+// function's parameters: phi = vorb(1) + sum_k 2 vorb(shell k) cos(k.r) +
+// beta(r), beta linear in bfact and given with its b and d derivatives as
+// tables on the beta grid (the derivatives of the image-summed, shifted,
+// bfact-scaled table that Psi uses).
+//
+// The 16 knots t_k of the opt-in up-down Jastrow spline are Jastrow
+// parameters: J = ... + sum_pairs sum_k t_k phi_k(r), so
+//   d log Psi / d t_k = sum_pairs phi_k(r)
+//   d E_L / d t_k     = -hbar sum_pairs [ (1/m_i + 1/m_j)(phi_k'' + 2 phi_k'/r)
+//                        + 2 phi_k'/r d.(g_i - g_j) ],  g_p = grad_p log Psi / m_p,
+// with phi_k, phi_k', phi_k'' interpolated from their grid values exactly as
+// the pair loop interpolates the Jastrow table they are added to.
+// Inputs per walker: x, the inverse (column-major as smati), the total and
+// determinant drifts (grad / sqrt m) whose difference is grad J.  Outputs
+// dlog[w*np + t], deloc[w*np + t] for t = vorb(1..norb), then bfact, b, d
+// (nbeta = 3 with the beta function on), then the knots (nknot = 16 with the
+// spline on).
 __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__ DevParams p,
                                                          const KVecDev* __restrict__ kv,
                                                          const TabUD* __restrict__ tud, const double* __restrict__ x,
@@ -194,6 +248,7 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                                                          const double* __restrict__ dpsi,
                                                          const double* __restrict__ dphi, double* __restrict__ dlog,
                                                          double* __restrict__ deloc, int nw, int np, double bfact,
+                                                         const PgTab* __restrict__ btd, int nbeta, int nknot,
                                                          double* gscr, size_t per_cta)
 {
     extern __shared__ __align__(16) double smp[];
@@ -206,9 +261,11 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
     double* xs = B + nd2;              // [P][3]
     double* w = xs + 3 * P;            // [P][3]: grad J / m
     double* cs = w + 3 * P;            // [nq][P][2]: cos, sin of k_q . x_p
-    double* red = cs + 2 * (size_t)P * (nq > 0 ? nq : 1);
-    double* res = red + kThreads;      // [2][norb + 1]
-    int* sh0 = reinterpret_cast<int*>(res + 2 * (norb + 1));   // first k of each shell, [norb + 1]
+    double* gt = cs + 2 * (size_t)P * (nq > 0 ? nq : 1);    // [P][3]: grad log Psi / m
+    double* red = gt + 3 * P;
+    double* res = red + kThreads;      // [2][kPgradMax]: d log Psi, then d Q
+    int* sh0 = reinterpret_cast<int*>(res + 2 * kPgradMax);   // first k of each shell, [norb + 1]
+    const int npb = norb + nbeta;      // parameters of the pair function
     const double imu = p.imass[0], imd = p.imass[1], ims = imu + imd;
     if (threadIdx.x == 0) {
         // k vectors are sorted by shell; shell 1 is k = 0
@@ -226,6 +283,7 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
             xs[t] = x[g];
             const int sp = (t / 3) < nup ? 0 : 1;
             w[t] = (dpsi[g] - dphi[g]) * p.isqm[sp];
+            gt[t] = dpsi[g] * p.isqm[sp];
         }
         __syncthreads();
         for (int t = threadIdx.x; t < nq * P; t += kThreads) {
@@ -312,7 +370,7 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
         // per parameter: sums over the up-down pairs of S^-1_ji S'_ij and
         // S^-1_ji M'_ij - T_ji S'_ij
         const int npairs = nup * ndn;
-        for (int th = 0; th < np; ++th) {
+        for (int th = 0; th < npb; ++th) {
             double sl = 0.0, sq = 0.0;
             for (int t = threadIdx.x; t < npairs; t += kThreads) {
                 const int i = t / ndn, j = t % ndn, pj = nup + j;
@@ -339,13 +397,17 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                                                         g2 * (w[3 * i + 2] - w[3 * pj + 2]));
                     sl += a * ds;
                     sq += a * dm - tt * ds;
-                } else {   // bfact: beta / bfact
+                } else {   // bfact: beta / bfact; b, d: their derivative tables
                     double d[3];
                     for (int cc = 0; cc < 3; ++cc) d[cc] = walker::min_image(xs[3 * i + cc] - xs[3 * pj + cc], p);
                     const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
                     double f, df, d2f;
-                    beta_all(p, tud, r, f, df, d2f);
-                    const double ib = 1.0 / bfact;
+                    const int bq = th - norb;
+                    if (bq == 0)
+                        beta_all(p, tud, r, f, df, d2f);
+                    else
+                        btab_all(p, btd + (size_t)(bq - 1) * (p.ntab + 1), r, f, df, d2f);
+                    const double ib = bq == 0 ? 1.0 / bfact : 1.0;
                     const double dr = r > 0.0 ? df / r : 0.0;
                     const double dm = d2f * ims + 2.0 * dr * (d[0] * (w[3 * i] - w[3 * pj]) + d[1] * (w[3 * i + 1] - w[3 * pj + 1]) +
                                                               d[2] * (w[3 * i + 2] - w[3 * pj + 2]));
@@ -357,13 +419,52 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
             sq = block_sum1(sq, red);
             if (threadIdx.x == 0) {
                 res[th] = sl;
-                res[norb + 1 + th] = sq;
+                res[kPgradMax + th] = sq;
             }
+        }
+        if (nknot > 0) {
+            // the Jastrow knots, all in one pass over the up-down pairs
+            double acc[2 * kJastrowKnots];
+#pragma unroll
+            for (int k = 0; k < 2 * kJastrowKnots; ++k) acc[k] = 0.0;
+            const double h = p.el / kJastrowCells;
+            for (int t = threadIdx.x; t < npairs; t += kThreads) {
+                const int i = t / ndn, j = t % ndn, pj = nup + j;
+                double d[3];
+                for (int cc = 0; cc < 3; ++cc) d[cc] = walker::min_image(xs[3 * i + cc] - xs[3 * pj + cc], p);
+                const double r = fmax(sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), 1.0e-14);
+                if (!(r < p.range)) continue;
+                const walker::Lagrange<double> W = walker::lagrange(r, p.scale, p.ntab);
+                const double cw[4] = {W.c1, W.c2, W.c3, W.c4};
+                const double ri = 1.0 / r;
+                const double gd = d[0] * (gt[3 * i] - gt[3 * pj]) + d[1] * (gt[3 * i + 1] - gt[3 * pj + 1]) +
+                                  d[2] * (gt[3 * i + 2] - gt[3 * pj + 2]);
+                // knots whose support [k - 2, k + 2] h (and the mirror image of
+                // k = 1 below h) reaches the four grid points
+                const double t0 = (W.idx - 1) / (p.scale * h);
+                const int klo = max(0, (int)floor(t0) - 2);
+                const int khi = min(kJastrowKnots - 1, (int)ceil(t0 + 3.0 / (p.scale * h)) + 2);
+#pragma unroll 1
+                for (int k = klo; k <= khi; ++k) {
+                    double f = 0.0, fp = 0.0, fpp = 0.0;
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        double a, b, c;
+                        jastrow_knot_basis(k, (W.idx - 1 + m) / p.scale, h, a, b, c);
+                        f += cw[m] * a;
+                        fp += cw[m] * b;
+                        fpp += cw[m] * c;
+                    }
+                    acc[k] += f;
+                    acc[kJastrowKnots + k] += ims * (fpp + 2.0 * fp * ri) + 2.0 * fp * ri * gd;
+                }
+            }
+            block_sum_n<2 * kJastrowKnots>(acc, red, res + npb, res + kPgradMax + npb);
         }
         __syncthreads();
         for (int th = threadIdx.x; th < np; th += kThreads) {
             dlog[(size_t)wk * np + th] = res[th];
-            deloc[(size_t)wk * np + th] = -p.hbar * res[norb + 1 + th];
+            deloc[(size_t)wk * np + th] = -p.hbar * res[kPgradMax + th];
         }
         __syncthreads();
     }
@@ -497,14 +598,17 @@ cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x
 size_t pgrad_doubles(const DevParams& p)
 {
     const size_t nd2 = (size_t)p.nd * p.nd;
-    return 3 * nd2 + 6 * (size_t)p.npart + 2 * (size_t)p.npart * (p.nk > 1 ? p.nk - 1 : 1) + kThreads +
-           2 * (size_t)(p.norb + 1) + (size_t)(p.norb + 2);
+    return 3 * nd2 + 9 * (size_t)p.npart + 2 * (size_t)p.npart * (p.nk > 1 ? p.nk - 1 : 1) + kThreads +
+           2 * (size_t)kPgradMax + (size_t)(p.norb + 2);
 }
 
 cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x, const double* sinv,
                          const double* dpsi, const double* dphi, double* dlog, double* deloc, int nw, int np,
-                         double bfact, int grid, double* gscr, int smem_limit, cudaStream_t st)
+                         double bfact, const PgTab* btd, int nbeta, int nknot, int grid, double* gscr, int smem_limit,
+                         cudaStream_t st)
 {
+    if (np > kPgradMax || nknot > kJastrowKnots || np != p.norb + nbeta + nknot || (nbeta > 1 && !btd))
+        return cudaErrorInvalidValue;
     if (nw <= 0) return cudaSuccess;
     const size_t need = pgrad_doubles(p);
     const bool on_chip = need * 8 <= (size_t)smem_limit;
@@ -516,7 +620,8 @@ cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud
         return cudaErrorInvalidValue;
     }
     pgrad_kernel<<<grid < nw ? grid : nw, kThreads, smem, st>>>(p, kv, tud, x, sinv, dpsi, dphi, dlog, deloc, nw, np,
-                                                                bfact, on_chip ? nullptr : gscr, need);
+                                                                bfact, btd, nbeta, nknot, on_chip ? nullptr : gscr,
+                                                                need);
     return cudaGetLastError();
 }
 

@@ -157,7 +157,8 @@ int dmc_get_info(const dmc_ctx* ctx, dmc_info* out);
  * 3 vtab (each 2*(ntab+1) values, layout [ic][0..ntab] i.e. Fortran
  * (2,0:ntab) transposed), 4 swbtab, 5 swdbtab, 6 swd2btab (ntab+1 each),
  * 7 ak (3*nk), 8 ak2 (nk), 9 numsh (norb, as doubles), 10 vorb (norb),
- * 11 (beta, gamma) of the long-range Jastrow. */
+ * 11 (beta, gamma) of the long-range Jastrow, 12 (bfact, b, d) of the beta
+ * function. */
 int dmc_get_table(const dmc_ctx* ctx, int which, double* out, int n);
 
 /* Arithmetic of the walker kernel.  DMC_PREC_FP64 (the default) computes
@@ -247,17 +248,38 @@ int dmc_getphione_batch(dmc_ctx* ctx, int nw, const double* x, const int* ipart,
  * optbeta=.false.: d log|det| / d vorb(k), dpsi[nw][norb]. */
 int dmc_getderbcs_batch(dmc_ctx* ctx, int nw, const double* x, double* dpsi);
 
+/* Opt-in up-down Jastrow spline, no counterpart in the reference (whose
+ * Jastrow is the zero-energy two-body solution, coshpot.f90:14-143): the
+ * up-down pair Jastrow becomes the reference's plus
+ *   u_s(r) = sum_{k=0}^{15} knots[k] phi_k(r),  h = L/34,
+ *   phi_0(r) = B(r/h),  phi_k(r) = B(r/h - k) + B(r/h + k),
+ * B the centred cubic B-spline on [-2, 2]: even in r and zero with its
+ * first two derivatives at L/2.  nknots = DMC_JASTROW_KNOTS sets it,
+ * nknots = 0 switches it off (the reference's wavefunction, the default).
+ * The knots join the adjoint gradients' parameters. */
+#define DMC_JASTROW_KNOTS 16
+int dmc_set_jastrow_spline(dmc_ctx* ctx, const double* knots, int nknots);
+int dmc_get_jastrow_spline(const dmc_ctx* ctx, double* knots, int cap, int* nknots);
+
 /* No counterpart in the reference (its optimizer uses d log Psi only):
- * per-walker gradients with respect to the amplitudes the pair function is
- * linear in, theta = (vorb(1), ..., vorb(norb), bfact) -- bfact only when
- * the beta function is on (bfact != 0); dmc_param_count gives their number
- * np.  dlogpsi[nw][np] = d log|Psi| / d theta (the vorb part equals
- * getderbcs, psislaterbcs.f90:449-524) and deloc[nw][np] = d E_L / d theta
- * with E_L = -hbar d2psi + v in the units of v (step.f90:62,76), by the
- * adjoint of the determinant's kinetic terms: one extra pair of nd^3
- * products per walker for all parameters.  FP64 whatever the context's
- * precision. */
+ * per-walker gradients with respect to theta = (vorb(1), ..., vorb(norb),
+ * then bfact, b, d of the beta function when it is on (bfact != 0), then
+ * the DMC_JASTROW_KNOTS knots when the Jastrow spline is on);
+ * dmc_param_count gives their number np (7 + 3 + 16 = 26 at seven shells).
+ * dlogpsi[nw][np] = d log|Psi| / d theta (the vorb part equals getderbcs,
+ * psislaterbcs.f90:449-524) and deloc[nw][np] = d E_L / d theta with
+ * E_L = -hbar d2psi + v in the units of v (step.f90:62,76), by the adjoint
+ * of the determinant's kinetic terms: one extra pair of nd^3 products per
+ * walker for all pair-function parameters.  The b and d derivatives are
+ * those of the image-summed, shifted, bfact-scaled table that Psi uses
+ * (betafun.f90:62-64,100-122), not of the single-image beta that the
+ * reference's derbeta (betafun.f90:196-327) differentiates.  FP64 whatever
+ * the context's precision. */
 int dmc_param_count(const dmc_ctx* ctx, int* np);
+/* New b, d and bfact of the up-down beta function (setbeta/initbeta,
+ * betafun.f90:12-125): its tables are rebuilt.  The beta function must be
+ * on (bfact != 0 at creation) and all three positive. */
+int dmc_set_beta(dmc_ctx* ctx, double b, double d, double bfact);
 int dmc_param_grad(dmc_ctx* ctx, int nw, const double* x, double* dlogpsi, double* deloc);
 
 /* Replaces getjasder (jastrowlongrange.f90:63-78): dpsi[nw][2] = d U / d beta
@@ -272,6 +294,14 @@ int dmc_getjasder_batch(dmc_ctx* ctx, int nw, const double* x, double* dpsi);
  * nparm = 2 opt_jastrow + norb opt_det; the default is (0, 1).  Clears the
  * sums. */
 int dmc_sr_configure(dmc_ctx* ctx, int opt_jastrow, int opt_det);
+
+/* No counterpart in the reference: the SR step over every parameter of
+ * dmc_param_grad (vorb, then bfact, b, d, then the Jastrow knots when the
+ * spline is on), with O_k = d log Psi / d theta_k from the adjoint kernel;
+ * dmc_sr_update then moves all of them (dmc_set_vorb, dmc_set_beta,
+ * dmc_set_jastrow_spline).  Set the spline first: nparm follows
+ * dmc_param_count.  dmc_sr_configure switches back.  Clears the sums. */
+int dmc_sr_configure_adjoint(dmc_ctx* ctx);
 
 /* Replaces the calder loop of dmcbcs.f90:492-503 (optimizer.f90:90-116)
  * over the current population, in pop order: per walker the parameter

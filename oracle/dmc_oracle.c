@@ -140,6 +140,12 @@ typedef struct orc_state {
     double hbarp, v0, amu, range, scale, eli, cjas[2], djas, v0op, v0eq;
     int iop, ieq;
     double *utab, *dutab, *d2utab, *vtab;     /* (2,0:ntab): [ic + 2*i] */
+    /* opt-in up-down Jastrow spline on top of the reference's table (no
+       counterpart in the reference): the reference's ic = 0 columns and
+       the knot values, njk = 0 or 16 */
+    double *uref0, *duref0, *d2uref0;
+    double jknots[16];
+    int njk;
     /* step, step.f90:5-9 */
     int idmc, cutdrift, fn;
     double dt, etrial, nfac, wtcut, eunit;
@@ -512,6 +518,75 @@ static int setphi(orc_state* s, double hbin)
     }
     if (s->cjas[0] != 0.0) s->iop = 1;
     if (s->cjas[1] != 0.0) s->ieq = 1;
+    s->uref0 = (double*)calloc((size_t)ntab + 1, sizeof(double));
+    s->duref0 = (double*)calloc((size_t)ntab + 1, sizeof(double));
+    s->d2uref0 = (double*)calloc((size_t)ntab + 1, sizeof(double));
+    for (int i = 0; i <= ntab; i++) {
+        s->uref0[i] = s->utab[2 * i];
+        s->duref0[i] = s->dutab[2 * i];
+        s->d2uref0[i] = s->d2utab[2 * i];
+    }
+    s->njk = 0;
+    return 0;
+}
+
+/* The opt-in up-down Jastrow spline (the library's own addition, restated
+ * here from its definition): u_s(r) = sum_k t_k phi_k(r) with knot spacing
+ * h = L/34, phi_0(r) = B(r/h), phi_k(r) = B(r/h - k) + B(r/h + k), B the
+ * centred cubic B-spline on [-2, 2].  Returns phi_k and its first two
+ * r-derivatives. */
+static void cubic_bspline(double t, double* f, double* fp, double* fpp)
+{
+    double a = fabs(t), sg = t < 0.0 ? -1.0 : 1.0;
+    if (a >= 2.0) { *f = 0.0; *fp = 0.0; *fpp = 0.0; return; }
+    if (a < 1.0) {
+        *f = 2.0 / 3.0 - a * a + 0.5 * a * a * a;
+        *fp = sg * (-2.0 * a + 1.5 * a * a);
+        *fpp = -2.0 + 3.0 * a;
+    } else {
+        double q = 2.0 - a;
+        *f = q * q * q / 6.0;
+        *fp = -sg * 0.5 * q * q;
+        *fpp = q;
+    }
+}
+
+void orc_knot_basis(int k, double r, double h, double* out3)
+{
+    double f, fp, fpp;
+    cubic_bspline(r / h - k, &f, &fp, &fpp);
+    if (k > 0) {
+        double f2, p2, q2;
+        cubic_bspline(r / h + k, &f2, &p2, &q2);
+        f += f2; fp += p2; fpp += q2;
+    }
+    out3[0] = f;
+    out3[1] = fp / h;
+    out3[2] = fpp / (h * h);
+}
+
+/* Sets the spline (n = 16 knots) or removes it (n = 0): the up-down
+ * Jastrow table becomes the reference's plus u_s at every grid point. */
+int orc_set_jastrow_spline(orc_state* s, const double* knots, int n)
+{
+    if (n != 0 && n != 16) return -1;
+    s->njk = n;
+    for (int k = 0; k < n; k++) s->jknots[k] = knots[k];
+    double h = s->el / 34.0, dr = s->range / s->ntab;
+    for (int i = 0; i <= s->ntab; i++) {
+        double u = s->uref0[i], du = s->duref0[i], d2u = s->d2uref0[i];
+        for (int k = 0; k < n; k++) {
+            double b[3];
+            orc_knot_basis(k, i * dr, h, b);
+            u += s->jknots[k] * b[0];
+            du += s->jknots[k] * b[1];
+            d2u += s->jknots[k] * b[2];
+        }
+        s->utab[2 * i] = u;
+        s->dutab[2 * i] = du;
+        s->d2utab[2 * i] = d2u;
+    }
+    if (n > 0) s->iop = 1;
     return 0;
 }
 
@@ -554,6 +629,7 @@ void orc_destroy(orc_state* s)
     free(s->ak); free(s->ak2); free(s->akq); free(s->ak2q);
     free(s->swbtab); free(s->swdbtab); free(s->swd2btab);
     free(s->utab); free(s->dutab); free(s->d2utab); free(s->vtab);
+    free(s->uref0); free(s->duref0); free(s->d2uref0);
     free_stack(&s->st[0]);
     free_stack(&s->st[1]);
     free_ops(s->ops);

@@ -45,6 +45,8 @@ def lib():
         L.orc_info.argtypes = [C.c_void_p, C.POINTER(Info)]
         L.orc_get_table.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int]
         L.orc_set_vorb.argtypes = [C.c_void_p, _dp, C.c_int]
+        L.orc_set_jastrow_spline.argtypes = [C.c_void_p, _dp, C.c_int]
+        L.orc_knot_basis.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
         L.orc_ran1.restype = C.c_double
         L.orc_ran1.argtypes = [C.POINTER(C.c_int64)]
         L.orc_ran2.restype = C.c_double
@@ -155,6 +157,12 @@ class Oracle:
         v = np.ascontiguousarray(vorb, dtype=np.float64)
         if lib().orc_set_vorb(self._h, v, len(v)) != 0:
             raise ValueError("norb mismatch")
+
+    def set_jastrow_spline(self, knots):
+        """The opt-in up-down Jastrow spline (16 knots; None or [] = off)."""
+        k = np.ascontiguousarray(knots if knots is not None else np.zeros(0), dtype=np.float64)
+        if lib().orc_set_jastrow_spline(self._h, k if k.size else np.zeros(1), int(k.size)) != 0:
+            raise ValueError("the spline has 16 knots")
 
     def radialfun(self, r):
         o = np.zeros(3)
