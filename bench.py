@@ -382,6 +382,37 @@ def param_gradients(args, rank):
                         "device-to-host copy of both gradients"}
 
 
+def sm_sweeps(args, rank):
+    """Particle-by-particle VMC sweeps (dmc_sm_sweeps: FP32 ratios and
+    Sherman-Morrison inverse updates, FP64 recompute of the inverse every 16
+    sweeps, then the walkers re-evaluated by the mixed walker kernel) on the
+    N = 66 workload's 4096 walkers, through the C ABI: one call of 16
+    sweeps, median of three after one warm-up call."""
+    from dmcbcs_project_gb300 import capi, configs
+
+    s, r, _ = configs.workload(WORKLOAD, nwalk=args.walkers or configs.WORKLOADS[WORKLOAD][3], idmc=0)
+    r.seed = replica_seed(rank)
+    nsw = args.sweeps
+    with capi.Context(s, r, precision="mixed") as c:
+        c.init_walkers()
+        c.initial_eval()
+        c.sm_sweeps(2, 16)
+        times, accs = [], []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            a, m = c.sm_sweeps(nsw, 16)
+            times.append(time.perf_counter() - t0)
+            accs.append(a / m)
+        nw = c.num_walkers()
+    t = float(np.median(times))
+    return {"workload": "sm_sweeps_n66_33u33d", "walkers": nw, "sweeps_per_call": nsw, "recompute_every": 16,
+            "move_scheme": "particle-by-particle Metropolis, Gaussian proposal of width sigma (no drift)",
+            "unit": "walker-sweeps/s", "value": nw * nsw / t, "moves_per_s": nw * nsw * s.nbin[0] * 2 / t,
+            "ms_per_call": 1e3 * t, "acceptance": float(np.mean(accs)),
+            "includes": "FP64 inverse recompute every 16 sweeps, FP32 sweeps, final mixed re-evaluation of every "
+                        "walker"}
+
+
 def deck_system(name, nwalk, idmc=None, dt=None):
     """System and run descriptors of one of the reference's production decks
     (the committed parse in tests/golden/decks.json)."""
@@ -569,6 +600,7 @@ def run_gpu(args):
 
     batch = uneven_batch(args, rank) if args.batch_steps > 0 else None
     pgrad = param_gradients(args, rank) if args.pgrad_walkers > 0 else None
+    sweeps = sm_sweeps(args, rank) if args.sweeps > 0 else None
 
     if rank == 0:
         cpu = None
@@ -609,6 +641,8 @@ def run_gpu(args):
             line["uneven_batch"] = batch
         if pgrad:
             line["param_grad"] = pgrad
+        if sweeps:
+            line["sm_sweeps"] = sweeps
         print(json.dumps(line), flush=True)
     for c in ctxs.values():
         c.close()
@@ -638,12 +672,14 @@ def main():
                     help="blocks of the mixed-vs-FP64 DMC energy comparison on the dmcbcs.dat deck (0: skip)")
     ap.add_argument("--energy-steps", type=int, default=20, help="generations per energy block")
     ap.add_argument("--energy-walkers", type=int, default=1024, help="walkers per energy replica")
-    ap.add_argument("--energy-replicas", type=int, default=8, help="independent replicas per precision")
+    ap.add_argument("--energy-replicas", type=int, default=16, help="independent replicas per precision")
     ap.add_argument("--energy-eq", type=int, default=200, help="VMC equilibration generations")
     ap.add_argument("--energy-dt-eq", type=float, default=5e-3, help="VMC equilibration time step")
     ap.add_argument("--energy-eq-dmc", type=int, default=100, help="DMC equilibration generations")
     ap.add_argument("--pgrad-walkers", type=int, default=8192,
                     help="walkers of the adjoint parameter-gradient side measurement (0: skip)")
+    ap.add_argument("--sweeps", type=int, default=16,
+                    help="particle-by-particle sweeps per call of the Sherman-Morrison side measurement (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=20,
                     help="generations of the six-system uneven batch side measurement (0: skip)")
     args = ap.parse_args()

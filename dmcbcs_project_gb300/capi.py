@@ -31,7 +31,7 @@ EXPORTS = [
     "dmc_batch_create", "dmc_batch_destroy", "dmc_batch_last_error", "dmc_batch_set_grids", "dmc_batch_get_grids",
     "dmc_batch_plan", "dmc_batch_tune", "dmc_batch_generations", "dmc_param_count", "dmc_param_grad",
     "dmc_generation_host", "dmc_get_status", "dmc_walker_status", "dmc_set_jastrow_spline",
-    "dmc_get_jastrow_spline", "dmc_set_beta", "dmc_sr_configure_adjoint",
+    "dmc_get_jastrow_spline", "dmc_set_beta", "dmc_sr_configure_adjoint", "dmc_sm_sweeps", "dmc_sm_inverse",
 ]
 
 PREC_FP64 = 0
@@ -126,6 +126,8 @@ def load(path=LIB_PATH):
     L.dmc_get_status.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
     L.dmc_set_jastrow_spline.argtypes = [vp, vp, C.c_int]
     L.dmc_set_beta.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.dmc_sm_sweeps.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.dmc_sm_inverse.argtypes = [vp, C.c_int, _dp]
     L.dmc_sr_configure_adjoint.argtypes = [vp]
     L.dmc_get_jastrow_spline.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
     L.dmc_walker_status.argtypes = [vp, C.c_int, _ip]
@@ -575,6 +577,20 @@ class Context:
         buf = np.zeros(abi.DMC_JASTROW_KNOTS)
         self._check(load().dmc_get_jastrow_spline(self._h, _opt(buf), buf.size, C.byref(n)))
         return buf[:n.value].copy()
+
+    def sm_sweeps(self, nsweeps, recompute_every=16):
+        """Particle-by-particle sweeps with FP32 Sherman-Morrison updates;
+        returns (accepted, moves)."""
+        a, m = C.c_int64(), C.c_int64()
+        self._check(load().dmc_sm_sweeps(self._h, int(nsweeps), int(recompute_every), C.byref(a), C.byref(m)))
+        return a.value, m.value
+
+    def sm_inverse(self, nw):
+        """The FP32 inverses carried by the last sweeps, (nw, nd, nd) with
+        [w, r, c] = (S^-1)_{rc}."""
+        out = np.zeros(nw * self.nd * self.nd)
+        self._check(load().dmc_sm_inverse(self._h, int(nw), out))
+        return out.reshape(nw, self.nd, self.nd).transpose(0, 2, 1)
 
     def status(self, clear=False):
         """DMC_STATUS_* flags met since the last clear (dmc_get_status)."""

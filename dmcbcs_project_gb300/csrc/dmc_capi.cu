@@ -175,6 +175,12 @@ struct dmc_ctx {
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum, srene;
     DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
     DevBuf<PgTab> pg_btab;                                      // d beta / d b, d beta / d d tables
+    // particle-by-particle sweeps: FP32 inverses carried between calls, the
+    // cos/sin tables, accepted moves per walker
+    DevBuf<float> sm_inv;
+    DevBuf<float2> sm_tab;
+    DevBuf<unsigned long long> sm_acc, sm_jA, sm_jC;   // accepted moves; ran1 jumps of 0..5 npart steps
+    int sm_n = 0;                 // walkers whose FP32 inverse sm_inv holds (0: none)
     DevBuf<int> sip;
     int64_t sr_count = 0;
     bool sr_jas = false, sr_det = true;   // iopt(1), iopt(2) of the optimizer deck
@@ -1575,6 +1581,89 @@ int dmc_set_beta(dmc_ctx* c, double b, double d, double bfact)
     c->sd.bfact = bfact;
     c->pg_btab.release();   // the b and d derivative tables follow on the next gradient
     return upload_tables(c);
+}
+
+int dmc_sm_sweeps(dmc_ctx* c, int nsweeps, int recompute_every, int64_t* accepted, int64_t* moves)
+{
+    if (!c || nsweeps < 0 || recompute_every < 0) return DMC_ERR_INVALID;
+    if (c->P.onebody || c->P.nql > 0 || c->S.a2 != 0.0)
+        return fail(c, DMC_ERR_UNSUPPORTED,
+                    "particle-by-particle sweeps need no one-body or long-range Jastrow and a2 = 0");
+    int rc = sync_n(c);
+    if (rc) return rc;
+    const int n = c->n;
+    if (n == 0) return fail(c, DMC_ERR_EMPTY, "no walkers");
+    const size_t nd2 = (size_t)c->S.nd * c->S.nd, n3 = (size_t)c->n3;
+    const int nq = std::max(1, c->S.nk - 1);
+    CK(c->sm_inv.alloc((size_t)n * nd2));
+    CK(c->sm_tab.alloc((size_t)n * nq * c->S.npart));
+    CK(c->sm_acc.alloc((size_t)n));
+    CK(cudaMemsetAsync(c->sm_acc.p, 0, (size_t)n * sizeof(unsigned long long), c->stream));
+    if (!c->sm_jA.p) {
+        const int nj = 5 * c->S.npart + 1;
+        std::vector<unsigned long long> A(nj), Cc(nj);
+        A[0] = 1;
+        Cc[0] = 0;
+        for (int t = 1; t < nj; ++t) {
+            A[t] = (A[t - 1] * kMult1) & kMask48;
+            Cc[t] = (Cc[t - 1] * kMult1 + kAdd1) & kMask48;
+        }
+        CK(c->sm_jA.alloc(nj));
+        CK(c->sm_jC.alloc(nj));
+        CK(cudaMemcpy(c->sm_jA.p, A.data(), nj * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(c->sm_jC.p, Cc.data(), nj * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    }
+    StackBufs& s = c->st[c->istin];
+    const DevStack view = s.view();
+    // chunks of recompute_every sweeps, each starting from a fresh FP64
+    // inverse of the pair matrix (the walker kernel, FP64, MODE_BCS); with
+    // recompute_every = 0 only the first chunk starts from one
+    const int chunk = recompute_every > 0 ? recompute_every : std::max(nsweeps, 1);
+    for (int done = 0; done < nsweeps; done += chunk) {
+        const int ns = std::min(chunk, nsweeps - done);
+        const bool fresh = done == 0 || recompute_every > 0;
+        if (fresh) {
+            CK(c->ssinv.alloc((size_t)n * nd2));
+            CK(c->pg_dphi.alloc((size_t)n * n3));
+            const int prec = c->precision;
+            c->precision = DMC_PREC_FP64;
+            rc = run_eval(c, MODE_BCS, n, s.x.p, nullptr, nullptr, c->pg_dphi.p, nullptr, nullptr, nullptr, nullptr,
+                          nullptr, nullptr, c->ssinv.p, c->stream);
+            c->precision = prec;
+            if (rc) return rc;
+            ++c->launches;
+        }
+        CK(launch_sweeps(c->P, view, n, ns, fresh ? c->ssinv.p : nullptr, c->sm_inv.p, c->sm_tab.p, c->kv_mp.p,
+                         c->tud_mp.p, c->tss_mp.p, c->sm_jA.p, c->sm_jC.p, c->sm_acc.p, c->stream));
+        ++c->launches;
+    }
+    c->sm_n = n;
+    // the walkers' stored evaluation at their new positions (hpsi in the
+    // context's precision), so step1 and the estimators continue from them
+    rc = run_eval(c, MODE_HPSI, n, s.x.p, s.psil.p, s.is.p, s.dpsi.p, s.d2psi.p, s.v.p, s.vext.p, s.psigl.p,
+                  s.dpsig.p, s.d2psig.p, nullptr, c->stream);
+    if (rc) return rc;
+    ++c->launches;
+    std::vector<unsigned long long> acc(n);
+    CK(cudaMemcpyAsync(acc.data(), c->sm_acc.p, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int64_t a = 0;
+    for (unsigned long long v : acc) a += (int64_t)v;
+    if (accepted) *accepted = a;
+    if (moves) *moves = (int64_t)n * nsweeps * c->S.npart;
+    return DMC_OK;
+}
+
+int dmc_sm_inverse(dmc_ctx* c, int nw, double* sinv)
+{
+    if (!c || nw < 0 || (nw > 0 && !sinv)) return DMC_ERR_INVALID;
+    if (nw > c->sm_n) return fail(c, DMC_ERR_INVALID, "more walkers than the last sweeps carried");
+    const size_t nd2 = (size_t)c->S.nd * c->S.nd;
+    std::vector<float> h((size_t)nw * nd2);
+    CK(cudaMemcpyAsync(h.data(), c->sm_inv.p, h.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (size_t e = 0; e < h.size(); ++e) sinv[e] = h[e];
+    return DMC_OK;
 }
 
 int dmc_getderbcs_batch(dmc_ctx* c, int nw, const double* x, double* dpsi)

@@ -441,6 +441,29 @@ int dmc_branch(dmc_ctx* ctx, double factor);
  * drastic population control; returns the population in *nt. */
 int dmc_generation(dmc_ctx* ctx, int opcomp, int* nt);
 
+/* Particle-by-particle VMC sweeps, no counterpart in the reference's walker
+ * loop (its moves are all-particle, step.f90:43-285; it uses the
+ * single-particle ratios of bcsone/getphione, psislaterbcs.f90:296-376 and
+ * coshpot.f90:207-264, only for n(k)).  Every walker of the current stack
+ * moves each particle in turn (nsweeps sweeps): proposal x_i + sigma_i g
+ * (three deviates of gaussian, ran.f90:74-104, from the walker's stream,
+ * then one uniform), Metropolis acceptance with |R|^2 exp(2 dU), R the
+ * determinant ratio from the inverse pair matrix and the new row or column,
+ * dU the Jastrow change.  Ratios, Jastrow and the Sherman-Morrison rank-one
+ * updates of the inverse run in FP32; the inverse is recomputed from the
+ * pair matrix in FP64 every recompute_every sweeps (0: only at the start of
+ * the call).  Positions and random states are updated in place; the
+ * walkers' stored wavefunction values are then re-evaluated at the new
+ * positions in the context's precision.  accepted and moves (may be NULL)
+ * receive the counts.  DMC_ERR_UNSUPPORTED with the one-body or long-range
+ * Jastrow on or a2 != 0. */
+int dmc_sm_sweeps(dmc_ctx* ctx, int nsweeps, int recompute_every, int64_t* accepted, int64_t* moves);
+
+/* The FP32 inverses the last dmc_sm_sweeps left, for the first nw walkers
+ * of the stack: sinv[nw][nd*nd], column-major as smati.  No counterpart in
+ * the reference. */
+int dmc_sm_inverse(dmc_ctx* ctx, int nw, double* sinv);
+
 /* Replaces zerest (estimator.f90:37-55). */
 int dmc_zero_estimators(dmc_ctx* ctx);
 

@@ -2038,6 +2038,66 @@ int orc_sr_update(int nparm, const double* ovec_s, const double* ovecw_s, const 
 }
 
 /* ------------------------------------------------------------------------ */
+/* particle-by-particle sweeps (the library's own addition, restated in FP64) */
+/* ------------------------------------------------------------------------ */
+
+/* nsweep sweeps of every walker of the current stack, particles in order:
+ * positions wrapped into the box first (as step.f90:59 wraps them), then per
+ * move five ran1 draws of the walker's stream -- gaussian(3) from four
+ * uniforms (ran.f90:74-104) and one acceptance uniform -- the proposal
+ * x_i + sigma_i g wrapped into the box, and Metropolis acceptance with
+ * exp(2 (log|Psi'| - log|Psi|)) from two full FP64 evaluations (hpsi): the
+ * exact ratio the GPU's FP32 Sherman-Morrison path approximates.  The
+ * walkers' stored values are then re-evaluated at the new positions.
+ * Returns the accepted moves. */
+int64_t orc_sm_sweeps(orc_state* s, int nsweep)
+{
+    wstack* st = &s->st[s->istin];
+    int n = st->n, P = s->npart, n3 = 3 * P;
+    int64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total) num_threads(s->nthreads)
+    for (int w = 0; w < n; w++) {
+        walker wk;
+        wget(s, st, w, &wk);
+        double x[3 * MAXP], xn[3 * MAXP], dp[3 * MAXP], dg[3 * MAXP];
+        for (int e = 0; e < n3; e++) x[e] = wk.x[e] - s->el * fnint(wk.x[e] / s->el);
+        hres h;
+        hpsi(s, x, &h, dp, dg);
+        double psil = h.psil;
+        int64_t irn = wk.irn, acc = 0;
+        for (int sw = 0; sw < nsweep; sw++) {
+            for (int i = 0; i < P; i++) {
+                double g[3];
+                gaussian(&irn, 3, g);
+                double rn = orc_ran1(&irn);
+                double sig = s->sigma[i];
+                memcpy(xn, x, sizeof(double) * n3);
+                for (int c = 0; c < 3; c++) {
+                    double v = x[3 * i + c] + sig * g[c];
+                    xn[3 * i + c] = v - s->el * fnint(v / s->el);
+                }
+                hres hn;
+                hpsi(s, xn, &hn, dp, dg);
+                double prob = exp(2.0 * (hn.psil - psil));
+                if (rn < prob) {
+                    memcpy(x, xn, sizeof(double) * n3);
+                    psil = hn.psil;
+                    acc++;
+                }
+            }
+        }
+        memcpy(wk.x, x, sizeof(double) * n3);
+        hpsi(s, x, &h, wk.dpsi, wk.dpsig);
+        wk.psil = h.psil; wk.is = h.is; wk.d2psi = h.d2psi; wk.v = h.v; wk.vext = h.vext;
+        wk.psigl = h.psigl; wk.d2psig = h.d2psig;
+        wk.irn = irn;
+        wput(s, st, w, &wk);
+        total += acc;
+    }
+    return total;
+}
+
+/* ------------------------------------------------------------------------ */
 /* operators: operators.f90:7-141 with gofr.f90 (g(r) and the density       */
 /* profile), sofq.f90 (S(q)) and momentum3d.f90 (n(k))                      */
 /* ------------------------------------------------------------------------ */

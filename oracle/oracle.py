@@ -47,6 +47,8 @@ def lib():
         L.orc_set_vorb.argtypes = [C.c_void_p, _dp, C.c_int]
         L.orc_set_jastrow_spline.argtypes = [C.c_void_p, _dp, C.c_int]
         L.orc_knot_basis.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
+        L.orc_sm_sweeps.restype = C.c_int64
+        L.orc_sm_sweeps.argtypes = [C.c_void_p, C.c_int]
         L.orc_ran1.restype = C.c_double
         L.orc_ran1.argtypes = [C.POINTER(C.c_int64)]
         L.orc_ran2.restype = C.c_double
@@ -163,6 +165,11 @@ class Oracle:
         k = np.ascontiguousarray(knots if knots is not None else np.zeros(0), dtype=np.float64)
         if lib().orc_set_jastrow_spline(self._h, k if k.size else np.zeros(1), int(k.size)) != 0:
             raise ValueError("the spline has 16 knots")
+
+    def sm_sweeps(self, nsweeps):
+        """Particle-by-particle Metropolis sweeps with exact FP64 ratios;
+        returns the accepted moves."""
+        return int(lib().orc_sm_sweeps(self._h, int(nsweeps)))
 
     def radialfun(self, r):
         o = np.zeros(3)
