@@ -550,6 +550,17 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
             }
         }
     }
+    if (per_sm == 1) {
+        // one CTA per SM: twice the threads (16 warps) on the same walker in
+        // the mixed kernel, with the larger reduction buffer they need, when
+        // that still fits (N = 132: 578k -> 719k walker-steps/s; the FP64
+        // kernel keeps 256 threads, the buffer is simply larger than it needs)
+        SmemLayout L512;
+        walker_smem_bytes(c->P, limit, &L512, 2 * kThreads);
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+        if (L512.total * 8 <= limit && L512.total * 8 + static_smem + 1024 <= smem_sm) c->L = L512;
+    }
     c->grid = c->nsm * per_sm;
     if (!c->L.pb_in_smem) {
         e = c->gscratch.alloc((size_t)c->grid * c->L.pb_size);

@@ -141,6 +141,7 @@ struct KernelArgs {
 
 // On-chip layout of one walker CTA, offsets in doubles.
 struct SmemLayout {
+    int nt;               // threads of the walker CTA (256, or 512 at one CTA per SM)
     int x, xr, xo, dx, drift, dg, kq, S, pb, R, U, D, E, acc, colk, red, total;
     int ksoa;             // k-vector fields as arrays: kx, ky, kz, k^2, v [5][nk],
                           // then the integer components n [3][nk]
@@ -153,9 +154,10 @@ struct SmemLayout {
 
 __host__ __device__ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
-__host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_limit_bytes)
+__host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_limit_bytes, int nt = kThreads)
 {
     SmemLayout L;
+    L.nt = nt;
     const int n3 = p.npart * 3;
     int off = 0;
     auto take = [&](int nd) { int o = off; off += round_up(nd, 2); return o; };
@@ -170,7 +172,7 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
     L.S = take(p.nd * p.ldS);     // pair matrix -> inverse
     L.colk = take(2 * p.nd + 2);  // pivot column of the unblocked Gauss-Jordan
     L.acc = take(p.npart * 8);    // per particle: drift(3), lap, du(3), spare
-    L.red = take(kThreads * 8);   // reductions and per-thread partial sums
+    L.red = take(nt * 8);        // reductions and per-thread partial sums
     // union region: Jastrow pair vectors, then orbitals U|D|E, then beta terms
     const int nE = p.npart * 3 * (p.nmax + 1) * 2;
     const int nUDE = p.nup * p.ldU + p.ndn * p.ldU + nE;

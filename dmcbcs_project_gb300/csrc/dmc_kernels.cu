@@ -169,19 +169,19 @@ __device__ inline void step_decision(const DevParams& p, int opcomp, const StepS
 // ---------------------------------------------------------------------------
 // The walker kernel: persistent CTAs, one walker per CTA per iteration.
 // ---------------------------------------------------------------------------
-template <class R>
-__global__ void __launch_bounds__(kThreads, 2)
+template <class R, int NT>
+__global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1)
 walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ KernelArgs a, SmemLayout L)
 {
     extern __shared__ __align__(16) double sm[];
     const int P = p.npart, n3 = 3 * P;
     const double* kvsrc = reinterpret_cast<const double*>(walker::Prec<R>::kv(a));
-    for (int i = threadIdx.x; i < p.nk * 8; i += kThreads) sm[L.kq + i] = kvsrc[i];
+    for (int i = threadIdx.x; i < p.nk * 8; i += NT) sm[L.kq + i] = kvsrc[i];
     {
         using KV = typename walker::Prec<R>::KV;
         const KV* kg = walker::Prec<R>::kv(a);
         R* ks = walker::at<R>(sm, L.ksoa);
-        for (int q = threadIdx.x; q < p.nk; q += kThreads) {
+        for (int q = threadIdx.x; q < p.nk; q += NT) {
             ks[q] = kg[q].k[0];
             ks[p.nk + q] = kg[q].k[1];
             ks[2 * p.nk + q] = kg[q].k[2];
@@ -192,7 +192,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         }
     }
     double* pb = L.pb_in_smem ? sm + L.pb : a.gscratch + (size_t)blockIdx.x * L.pb_size;
-    Ctx<R> c{p, a, L, sm, pb};
+    Ctx<R, NT> c{p, a, L, sm, pb};
     __shared__ double s_old[9];
     __syncthreads();
     const int nw = a.pn ? *a.pn : a.nw;   // the population is counted on the device in a generation
@@ -206,9 +206,9 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         if (a.mode == MODE_STEP) {
             // step.f90:59-74: wrap, gaussians, drift, proposal
             s0 = a.in.irn[src] & kMask48;
-            if (threadIdx.x >= kThreads - 32 && threadIdx.x < kThreads - 32 + 9) {
+            if (threadIdx.x >= NT - 32 && threadIdx.x < NT - 32 + 9) {
                 // the popped walker's scalars for the step decision (latency hidden behind the proposal)
-                const int k = threadIdx.x - (kThreads - 32);
+                const int k = threadIdx.x - (NT - 32);
                 double v;
                 switch (k) {
                     case 0: v = a.in.psil[src]; break;
@@ -225,11 +225,11 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
             }
             const double* x1 = a.in.x + (size_t)src * n3;
             const double* g1 = a.in.dpsig + (size_t)src * n3;
-            for (int e = threadIdx.x; e < n3; e += kThreads) xo[e] = min_image(x1[e], p);
+            for (int e = threadIdx.x; e < n3; e += NT) xo[e] = min_image(x1[e], p);
             // Box-Muller pairs (ran.f90:74-104): draws t = 1..nrand from the
             // walker's stream, pair i uses draws 2i-1, 2i
             const int npairs = (n3 + 1) / 2;
-            for (int q = threadIdx.x; q < npairs; q += kThreads) {
+            for (int q = threadIdx.x; q < npairs; q += NT) {
                 double gs, gc;   // r sin(2 pi u1), r cos(2 pi u1), r = sqrt(-2 log u2)
                 if constexpr (walker::is_df<R>::value) {
                     // the same deviates in double-float on the FP32 pipe:
@@ -259,7 +259,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                 }
             }
             __syncthreads();
-            for (int e = threadIdx.x; e < n3; e += kThreads) {
+            for (int e = threadIdx.x; e < n3; e += NT) {
                 const int sp = (e / 3) < p.nup ? 0 : 1;
                 const double sig = p.sigma[sp];
                 double d = g1[e] * (sig * sig) * p.sqm[sp];
@@ -270,7 +270,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                 x[e] = min_image(xo[e] + dxe, p);
             }
         } else {
-            for (int e = threadIdx.x; e < n3; e += kThreads) x[e] = a.xin[(size_t)w * n3 + e];
+            for (int e = threadIdx.x; e < n3; e += NT) x[e] = a.xin[(size_t)w * n3 + e];
         }
         __syncthreads();
         const int hmode = a.mode == MODE_STEP ? MODE_HPSI : a.mode;
@@ -282,7 +282,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         // not finite (NaN or infinite positions, overflowing terms)
         {
             int bad = 0;
-            for (int e = threadIdx.x; e < n3; e += kThreads) {
+            for (int e = threadIdx.x; e < n3; e += NT) {
                 const double val = a.mode == MODE_GETPHI ? sm[L.acc + 4 * P + e] : dpsi[e];
                 if (!isfinite(val)) bad = 1;
             }
@@ -308,17 +308,17 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                 if (a.o_d2psig) a.o_d2psig[w] = h.d2psig;
             }
             if (a.o_dpsi)
-                for (int e = threadIdx.x; e < n3; e += kThreads) {
+                for (int e = threadIdx.x; e < n3; e += NT) {
                     double val = dpsi[e];
                     if (a.mode == MODE_GETPHI) val = sm[L.acc + 4 * P + e];
                     a.o_dpsi[(size_t)w * n3 + e] = val;
                 }
             if (a.o_dpsig)
-                for (int e = threadIdx.x; e < n3; e += kThreads) a.o_dpsig[(size_t)w * n3 + e] = dpsig[e];
+                for (int e = threadIdx.x; e < n3; e += NT) a.o_dpsig[(size_t)w * n3 + e] = dpsig[e];
             if (a.o_sinv) {
                 const int nd = p.nd;
                 // column-major nd x nd as the reference's smati(nd,nd)
-                for (int t = threadIdx.x; t < nd * nd; t += kThreads) {
+                for (int t = threadIdx.x; t < nd * nd; t += NT) {
                     const int r = t % nd, cc = t / nd;
                     a.o_sinv[(size_t)w * nd * nd + t] =
                         h.singular ? 0.0 : to_double(walker::at<R>(sm, L.S)[r * p.ldS + cc]);
@@ -342,7 +342,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         if (metro) {
             // Metropolis with the drift Green's function ratio (step.f90:80-91)
             double acc1[2] = {0.0, 0.0};
-            for (int e = threadIdx.x; e < n3; e += kThreads) {
+            for (int e = threadIdx.x; e < n3; e += NT) {
                 const int sp = (e / 3) < p.nup ? 0 : 1;
                 const double sig = p.sigma[sp];
                 double dn = dpsig[e] * (sig * sig) * p.sqm[sp];
@@ -351,7 +351,7 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                 const double d2 = drift[e] - dn - 2.0 * dxs[e];
                 acc1[0] += d1 * d2 / (2.0 * (sig * sig));
             }
-            block_sum<2>(acc1, sm + L.red);
+            block_sum<2, NT>(acc1, sm + L.red);
             if (threadIdx.x == 0) {
                 double prob = (p.idmc == 2 ? 2.0 * (h.psigl - o_psigl) : 2.0 * (h.psil - o_psil)) + acc1[0];
                 prob = prob == prob ? exp(fmin(0.0, prob)) : 0.0;   // a NaN proposal is rejected
@@ -366,11 +366,11 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
         double ejfd[1] = {0.0};
         if (p.idmc == -1 || p.idmc == 0) {
             const double* dsrc = take_new ? dpsi : a.in.dpsi + (size_t)src * n3;
-            for (int e = threadIdx.x; e < n3; e += kThreads) {
+            for (int e = threadIdx.x; e < n3; e += NT) {
                 const int sp = (e / 3) < p.nup ? 0 : 1;
                 ejfd[0] += dsrc[e] * dsrc[e] * p.imass[sp];
             }
-            block_sum<1>(ejfd, sm + L.red);
+            block_sum<1, NT>(ejfd, sm + L.red);
         }
         // scalars of the pushed walker
         const int k = w;   // push order = pop order
@@ -410,13 +410,13 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
             o.psigl0[k] = a.in.psigl0[src];
         }
         if (take_new) {
-            for (int e = threadIdx.x; e < n3; e += kThreads) {
+            for (int e = threadIdx.x; e < n3; e += NT) {
                 a.out.x[(size_t)k * n3 + e] = x[e];
                 a.out.dpsi[(size_t)k * n3 + e] = dpsi[e];
                 a.out.dpsig[(size_t)k * n3 + e] = dpsig[e];
             }
         } else {
-            for (int e = threadIdx.x; e < n3; e += kThreads) {
+            for (int e = threadIdx.x; e < n3; e += NT) {
                 a.out.x[(size_t)k * n3 + e] = xo[e];
                 a.out.dpsi[(size_t)k * n3 + e] = a.in.dpsi[(size_t)src * n3 + e];
                 a.out.dpsig[(size_t)k * n3 + e] = a.in.dpsig[(size_t)src * n3 + e];
@@ -671,26 +671,36 @@ __global__ void popctl_kernel(const int* pn, double nwalk, double popup, double 
 // host launchers
 // ---------------------------------------------------------------------------
 
-int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout)
+int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int nt)
 {
-    SmemLayout L = make_layout(p, limit_bytes);
+    SmemLayout L = make_layout(p, limit_bytes, nt);
     if (Lout) *Lout = L;
     return L.total * 8;
 }
 
 int walker_static_smem_bytes()
 {
-    cudaFuncAttributes a64{}, amx{};
-    if (cudaFuncGetAttributes(&a64, walker_kernel<double>) != cudaSuccess) return -1;
-    if (cudaFuncGetAttributes(&amx, walker_kernel<df>) != cudaSuccess) return -1;
-    return (int)(a64.sharedSizeBytes > amx.sharedSizeBytes ? a64.sharedSizeBytes : amx.sharedSizeBytes);
+    cudaFuncAttributes a[3]{};
+    if (cudaFuncGetAttributes(&a[0], walker_kernel<double, kThreads>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&a[1], walker_kernel<df, kThreads>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&a[2], walker_kernel<df, 2 * kThreads>) != cudaSuccess) return -1;
+    size_t m = 0;
+    for (const auto& x : a) m = x.sharedSizeBytes > m ? x.sharedSizeBytes : m;
+    return (int)m;
 }
 
-// attribute kinds of the per-device record
-enum : int { kAttrCarveout = 0, kAttrSmemMixed = 1, kAttrSmemFp64 = 2 };
+// attribute kinds of the per-device record: the carveout, then the dynamic
+// shared-memory opt-in of walker_kernel<df / double, 256 / 512 threads>
+enum : int { kAttrCarveout = 0, kAttrSmemBase = 1 };
 static AttrCache g_attr;
 
-static cudaError_t walker_attrs(int smem, bool both, bool mixed)
+template <class R, int NT>
+static int set_smem_attr(int v)
+{
+    return (int)cudaFuncSetAttribute(walker_kernel<R, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+}
+
+static cudaError_t walker_attrs(int smem, int nt, bool both, bool mixed)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -698,30 +708,32 @@ static cudaError_t walker_attrs(int smem, bool both, bool mixed)
     // every launch asks for the largest shared-memory carveout, so CTAs of
     // launches with different layouts (systems of a batch) can share an SM
     int rc = g_attr.ensure(dev, kAttrCarveout, 1, [](int) {
-        cudaError_t r = cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                             (int)cudaSharedmemCarveoutMaxShared);
+        const int c = (int)cudaSharedmemCarveoutMaxShared;
+        cudaError_t r = cudaFuncSetAttribute(walker_kernel<df, kThreads>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
         if (r == cudaSuccess)
-            r = cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     (int)cudaSharedmemCarveoutMaxShared);
+            r = cudaFuncSetAttribute(walker_kernel<double, kThreads>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+        if (r == cudaSuccess)
+            r = cudaFuncSetAttribute(walker_kernel<df, 2 * kThreads>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     c);
         return (int)r;
     });
     if (rc) return (cudaError_t)rc;
+    // the mixed kernel runs with the layout's thread count, the FP64 kernel
+    // always with 256 (it is FP64-pipe bound: 16 warps did not speed it up)
+    const bool wide = nt != kThreads;
     if (both || mixed) {
-        rc = g_attr.ensure(dev, kAttrSmemMixed, smem, [](int v) {
-            return (int)cudaFuncSetAttribute(walker_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-        });
+        rc = g_attr.ensure(dev, kAttrSmemBase + (wide ? 2 : 0), smem,
+                           wide ? set_smem_attr<df, 2 * kThreads> : set_smem_attr<df, kThreads>);
         if (rc) return (cudaError_t)rc;
     }
     if (both || !mixed) {
-        rc = g_attr.ensure(dev, kAttrSmemFp64, smem, [](int v) {
-            return (int)cudaFuncSetAttribute(walker_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-        });
+        rc = g_attr.ensure(dev, kAttrSmemBase + 1, smem, set_smem_attr<double, kThreads>);
         if (rc) return (cudaError_t)rc;
     }
     return cudaSuccess;
 }
 
-cudaError_t prepare_walker(const SmemLayout& L) { return walker_attrs(L.total * 8, true, false); }
+cudaError_t prepare_walker(const SmemLayout& L) { return walker_attrs(L.total * 8, L.nt, true, false); }
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed)
@@ -729,12 +741,14 @@ cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLay
     const size_t smem = (size_t)L.total * 8;
     // the shared-memory opt-in is recorded per device and size (prepare_walker
     // sets it before any graph capture; this finds it set)
-    const cudaError_t e = walker_attrs((int)smem, false, mixed);
+    const cudaError_t e = walker_attrs((int)smem, L.nt, false, mixed);
     if (e != cudaSuccess) return e;
-    if (mixed)
-        walker_kernel<df><<<grid, kThreads, smem, st>>>(p, a, L);
+    if (!mixed)
+        walker_kernel<double, kThreads><<<grid, kThreads, smem, st>>>(p, a, L);
+    else if (L.nt == 2 * kThreads)
+        walker_kernel<df, 2 * kThreads><<<grid, 2 * kThreads, smem, st>>>(p, a, L);
     else
-        walker_kernel<double><<<grid, kThreads, smem, st>>>(p, a, L);
+        walker_kernel<df, kThreads><<<grid, kThreads, smem, st>>>(p, a, L);
     return cudaGetLastError();
 }
 

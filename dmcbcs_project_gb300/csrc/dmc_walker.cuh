@@ -42,7 +42,7 @@ __device__ __forceinline__ double warp_sum(double v)
 
 // Deterministic block sum of NV values (fixed tree); the result is returned
 // in v on every thread.
-template <int NV>
+template <int NV, int NT = kThreads>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* red)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -55,12 +55,12 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* red)
     __syncthreads();
     if (threadIdx.x < NV) {
         double s = 0.0;
-        for (int k = 0; k < kWarps; ++k) s += red[k * NV + threadIdx.x];
-        red[kWarps * NV + threadIdx.x] = s;
+        for (int k = 0; k < (NT / 32); ++k) s += red[k * NV + threadIdx.x];
+        red[(NT / 32) * NV + threadIdx.x] = s;
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < NV; ++q) v[q] = red[kWarps * NV + q];
+    for (int q = 0; q < NV; ++q) v[q] = red[(NT / 32) * NV + q];
     __syncthreads();
 }
 
@@ -70,8 +70,8 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* red)
 // on every thread.
 __device__ __forceinline__ double wsum(double v) { return warp_sum(v); }
 __device__ __forceinline__ df wsum(df v) { return dfm::warp_sum(v); }
-template <int NV, class T>
-__device__ __forceinline__ void block_sum_t(T (&v)[NV], T* red, int nw = kWarps)
+template <int NV, int NT, class T>
+__device__ __forceinline__ void block_sum_t(T (&v)[NV], T* red, int nw = NT / 32)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     __syncthreads();
@@ -86,11 +86,11 @@ __device__ __forceinline__ void block_sum_t(T (&v)[NV], T* red, int nw = kWarps)
     if (threadIdx.x < NV) {
         T s = red[threadIdx.x];
         for (int k = 1; k < nw; ++k) s = s + red[k * NV + threadIdx.x];
-        red[kWarps * NV + threadIdx.x] = s;
+        red[(NT / 32) * NV + threadIdx.x] = s;
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < NV; ++q) v[q] = red[kWarps * NV + q];
+    for (int q = 0; q < NV; ++q) v[q] = red[(NT / 32) * NV + q];
     __syncthreads();
 }
 
@@ -260,8 +260,9 @@ __device__ __forceinline__ Lagrange<float> lagrange_f(float t, int idx)
     return L;
 }
 
-template <class R>
+template <class R, int NT = kThreads>
 struct Ctx {
+    static constexpr int nt = NT;   // threads of the walker CTA
     const DevParams& p;
     const KernelArgs& a;
     const SmemLayout& L;
@@ -297,8 +298,8 @@ __device__ __forceinline__ T* at(double* sm, int off) { return reinterpret_cast<
 // Laplacian part: jt[] for the up-down pairs in the Jastrow type, ss[] for
 // the same-spin pairs (FP64 on both paths).
 // ---------------------------------------------------------------------------
-template <class R>
-__device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double (&ss)[3])
+template <class R, int NT>
+__device__ void pair_stage(const Ctx<R, NT>& c, typename Prec<R>::J (&jt)[3], double (&ss)[3])
 {
     using J = typename Prec<R>::J;
     const DevParams& p = c.p;
@@ -313,7 +314,7 @@ __device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double
     const double imu_ud = 1.0 / (p.mass[0] * p.mass[1] / (p.mass[0] + p.mass[1]));
     const R imu_df = from_dbl<R>(imu_ud);
     (void)imu_df;
-    for (int i = threadIdx.x; i < 3 * p.npart; i += kThreads) du[i] = 0.0;
+    for (int i = threadIdx.x; i < 3 * p.npart; i += NT) du[i] = 0.0;
     // per-thread partial sums in the Jastrow type
     J tu = rzero<J>(), tv = rzero<J>(), td = rzero<J>();
     __syncthreads();
@@ -321,7 +322,7 @@ __device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double
         const int r1 = min(nup, r0 + c.L.rows_jas);
         const int npc = (r1 - r0) * ndn;
         const UDiv dv(ndn);
-        for (int q = threadIdx.x; q < npc; q += kThreads) {
+        for (int q = threadIdx.x; q < npc; q += NT) {
             const int qi = dv.quo(q);
             const int i = r0 + qi, j = q - qi * ndn;
             const R* xi = x + 3 * i;
@@ -417,7 +418,7 @@ __device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double
         // row sums -> up particles (+), column sums -> down particles (-);
         // one thread per (particle, component)
         const int nr = r1 - r0;
-        for (int tc = threadIdx.x; tc < 3 * (nr + ndn); tc += kThreads) {
+        for (int tc = threadIdx.x; tc < 3 * (nr + ndn); tc += NT) {
             const int t = tc / 3, cmp = tc % 3;
             typename AccOf<J>::type sacc;
             acc_init(sacc);
@@ -454,7 +455,7 @@ __device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double
         for (int r0 = 0; r0 < n; r0 += rows) {
             const int r1 = min(n, r0 + rows);
             const int npc = (r1 - r0) * n;
-            for (int q = threadIdx.x; q < npc; q += kThreads) {
+            for (int q = threadIdx.x; q < npc; q += NT) {
                 const int i = r0 + q / n, j = q % n;
                 double g0 = 0.0, g1 = 0.0, g2 = 0.0;
                 if (j > i) {
@@ -488,7 +489,7 @@ __device__ void pair_stage(const Ctx<R>& c, typename Prec<R>::J (&jt)[3], double
             }
             __syncthreads();
             const int nr = r1 - r0;
-            for (int t = threadIdx.x; t < nr + n; t += kThreads) {
+            for (int t = threadIdx.x; t < nr + n; t += NT) {
                 double s0 = 0.0, s1 = 0.0, s2 = 0.0;
                 if (t < nr) {
                     const double* row = pvd + 3 * (t * n);
@@ -566,8 +567,8 @@ __device__ __forceinline__ void cmul(df ar, df ai, df br, df bi, df& cr, df& ci)
 // D[j][0] = 1,       D[j][2q-1] = cos(k_q.x_j),     D[j][2q] = sin(k_q.x_j)
 // Then the unpaired plane-wave rows and columns of S (:171-206).
 // ---------------------------------------------------------------------------
-template <class R>
-__device__ void orbital_stage(const Ctx<R>& c)
+template <class R, int NT>
+__device__ void orbital_stage(const Ctx<R, NT>& c)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -578,7 +579,7 @@ __device__ void orbital_stage(const Ctx<R>& c)
     R* S = at<R>(sm, c.L.S);
     const int np1 = p.nmax + 1;
     // powers e^{i m theta_c}, m = 0..nmax, E[(p*3+c)*np1 + m] = (re, im)
-    for (int t = threadIdx.x; t < 3 * p.npart; t += kThreads) {
+    for (int t = threadIdx.x; t < 3 * p.npart; t += NT) {
         R s1, c1;
         if constexpr (is_df<R>::value) {
             // base angle 2 pi x / L in double-float, off the FP64 pipe
@@ -614,9 +615,9 @@ __device__ void orbital_stage(const Ctx<R>& c)
     // product of the three component powers is taken branch-free: a zero
     // component multiplies by e^0 = (1, 0), which is exact.
     const int nq1 = nq + 1, items = p.npart * nq1;
-    const int dpart = kThreads / nq1, dq = kThreads % nq1;
+    const int dpart = NT / nq1, dq = NT % nq1;
     int part = (int)threadIdx.x / nq1, q = (int)threadIdx.x % nq1;
-    for (int t = threadIdx.x; t < items; t += kThreads) {
+    for (int t = threadIdx.x; t < items; t += NT) {
         const bool up = part < p.nup;
         R* row = up ? U + part * p.ldU : D + (part - p.nup) * p.ldU;
         if (q == 0) {
@@ -655,7 +656,7 @@ __device__ void orbital_stage(const Ctx<R>& c)
     }
     // unpaired plane waves: up columns ndn.., down rows nup.., zero corner
     const int ldS = p.ldS;
-    for (int t = threadIdx.x; t < p.nup * p.nexup; t += kThreads) {
+    for (int t = threadIdx.x; t < p.nup * p.nexup; t += NT) {
         const int i = t / p.nexup, jj = t % p.nexup;
         const double* xi = x + 3 * i;
         const double arg = p.akup[jj][0] * xi[0] + p.akup[jj][1] * xi[1] + p.akup[jj][2] * xi[2];
@@ -663,7 +664,7 @@ __device__ void orbital_stage(const Ctx<R>& c)
         sincos(arg, &s, &co);
         S[i * ldS + p.ndn + jj] = from_dbl<R>(p.sinup[jj] ? s : co);
     }
-    for (int t = threadIdx.x; t < p.ndn * p.nexdn; t += kThreads) {
+    for (int t = threadIdx.x; t < p.ndn * p.nexdn; t += NT) {
         const int j = t / p.nexdn, jj = t % p.nexdn;
         const double* xj = x + 3 * (p.nup + j);
         const double arg = p.akdn[jj][0] * xj[0] + p.akdn[jj][1] * xj[1] + p.akdn[jj][2] * xj[2];
@@ -671,7 +672,7 @@ __device__ void orbital_stage(const Ctx<R>& c)
         sincos(arg, &s, &co);
         S[(p.nup + jj) * ldS + j] = from_dbl<R>(p.sindn[jj] ? s : co);
     }
-    for (int t = threadIdx.x; t < p.nexdn * p.nexup; t += kThreads) {
+    for (int t = threadIdx.x; t < p.nexdn * p.nexup; t += NT) {
         const int r = t / p.nexup, cc = t % p.nexup;
         S[(p.nup + r) * ldS + p.ndn + cc] = rzero<R>();
     }
@@ -685,8 +686,8 @@ __device__ void orbital_stage(const Ctx<R>& c)
 // of 256 threads at N = 66.  16-byte pair loads over the padded rows (the
 // padding is zero).
 constexpr int kGJ = 5;
-template <class R>
-__device__ void gemm_stage(const Ctx<R>& c)
+template <class R, int NT>
+__device__ void gemm_stage(const Ctx<R, NT>& c)
 {
     using Acc = typename AccOf<R>::type;
     const DevParams& p = c.p;
@@ -708,7 +709,7 @@ __device__ void gemm_stage(const Ctx<R>& c)
         sig = pow2_ceil(4.0f * 1.001f * sv);
     }
     const UDiv dg(ng);
-    for (int t = threadIdx.x; t < p.nup * ng; t += kThreads) {
+    for (int t = threadIdx.x; t < p.nup * ng; t += NT) {
         const int i = dg.quo(t), g = t - i * ng;
         const R* u = U + i * ldU;
         const R* d[kGJ];
@@ -804,8 +805,10 @@ __device__ __forceinline__ df shfl_r(df v, int src)
 
 // Named barrier 1 over the whole CTA: the panel warp waits, the others only
 // arrive.
-__device__ __forceinline__ void bar1_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreads) : "memory"); }
-__device__ __forceinline__ void bar1_arrive() { asm volatile("bar.arrive 1, %0;" ::"n"(kThreads) : "memory"); }
+template <int NT>
+__device__ __forceinline__ void bar1_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory"); }
+template <int NT>
+__device__ __forceinline__ void bar1_arrive() { asm volatile("bar.arrive 1, %0;" ::"n"(NT) : "memory"); }
 
 constexpr int kPanelWarps = 1;
 
@@ -932,8 +935,8 @@ __device__ __forceinline__ R gj_apply(const R* cur, int ld, int i, int j, int k0
     return acc_value(a);
 }
 
-template <class R, int RPL, int B>
-__device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
+template <class R, int RPL, int B, int NT>
+__device__ bool inverse_blocked(const Ctx<R, NT>& c, double& logdet, int& sgn)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -946,7 +949,7 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
     __shared__ double s_logdet;
     const int n = p.nd, ld = p.ldS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < n; i += kThreads) rowpos[i] = n;
+    for (int i = threadIdx.x; i < n; i += NT) rowpos[i] = n;
     if (threadIdx.x == 0) s_sing = 0;
     __syncthreads();
     // Pass 0 applies no block (it copies S into the second buffer) while the
@@ -971,20 +974,20 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
         if (bw1 > 0) {
             // columns of the next panel first, by everyone
             const UDiv db(bw1);
-            for (int e = threadIdx.x; e < n * bw1; e += kThreads) {
+            for (int e = threadIdx.x; e < n * bw1; e += NT) {
                 const int i = db.quo(e), j = k1 + e - i * bw1;
                 nxt[i * ld + j] = gj_apply<R, B>(cur, ld, i, j, k0, bw, prow, rowpos);
             }
             if (warp < kPanelWarps) {
-                bar1_sync();
+                bar1_sync<NT>();
                 if (!gj_panel<R, RPL, B>(nxt, ld, n, k1, bw1, piv, pvals, rowpos) && threadIdx.x == 0) s_sing = 1;
             } else {
-                bar1_arrive();
+                bar1_arrive<NT>();
             }
         }
         if (bw1 == 0 || warp >= kPanelWarps) {
             // every other column: the non-panel warps (all warps in the last block)
-            const int nt = bw1 > 0 ? kThreads - 32 * kPanelWarps : kThreads;
+            const int nt = bw1 > 0 ? NT - 32 * kPanelWarps : NT;
             const int t0 = bw1 > 0 ? (int)threadIdx.x - 32 * kPanelWarps : (int)threadIdx.x;
             const int nc = n - bw1;
             const UDiv dc(nc);
@@ -1013,12 +1016,12 @@ __device__ bool inverse_blocked(const Ctx<R>& c, double& logdet, int& sgn)
     if (!sing) {
         const bool copy = (cur == A1);
         const UDiv dn(n);
-        for (int e = threadIdx.x; e < n * n; e += kThreads) {
+        for (int e = threadIdx.x; e < n * n; e += NT) {
             const int a = dn.quo(e), b = e - a * n;
             if (copy) A0[a * ld + b] = A1[piv[a] * ld + rowpos[b]];
             if (a < b && piv[a] > piv[b]) odd ^= 1;
         }
-        for (int q = threadIdx.x; q < n; q += kThreads)
+        for (int q = threadIdx.x; q < n; q += NT)
             if (is_neg(pvals[q])) odd ^= 1;
         if (warp == 0) {
             if constexpr (is_df<R>::value) {
@@ -1081,8 +1084,8 @@ __device__ __forceinline__ int warp_pivot(const R* A, int ld, int n, int k, R& p
     return bi;
 }
 
-template <class R>
-__device__ bool inverse_unblocked(const Ctx<R>& c, double& logdet, int& sgn)
+template <class R, int NT>
+__device__ bool inverse_unblocked(const Ctx<R, NT>& c, double& logdet, int& sgn)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1109,7 +1112,7 @@ __device__ bool inverse_unblocked(const Ctx<R>& c, double& logdet, int& sgn)
         }
     }
     __syncthreads();
-    const int ew = kThreads - 32;
+    const int ew = NT - 32;
     const int e0 = (int)threadIdx.x - 32;
     const int di = ew / n, dc = ew % n;
     for (int k = 0; k < n; ++k) {
@@ -1117,7 +1120,7 @@ __device__ bool inverse_unblocked(const Ctx<R>& c, double& logdet, int& sgn)
         const int pr = s_piv;
         const R pinv = s_pinv;
         // save column k (rows in swapped order), swap rows k/pr, scale row k
-        for (int t = threadIdx.x; t < n; t += kThreads) {
+        for (int t = threadIdx.x; t < n; t += NT) {
             const int src = (t == k) ? pr : ((t == pr) ? k : t);
             const R ck = A[src * ld + k];
             const R a = A[k * ld + t];
@@ -1173,7 +1176,7 @@ __device__ bool inverse_unblocked(const Ctx<R>& c, double& logdet, int& sgn)
     if (!sing) {
         // undo the row interchanges on the columns, last first (dgetri);
         // each thread owns whole rows, so no barrier between swaps
-        for (int r = threadIdx.x; r < n; r += kThreads)
+        for (int r = threadIdx.x; r < n; r += NT)
             for (int q = n - 1; q >= 0; --q) {
                 const int pq = piv[q];
                 if (pq != q) {
@@ -1209,8 +1212,8 @@ __device__ bool inverse_unblocked(const Ctx<R>& c, double& logdet, int& sgn)
     return !sing;
 }
 
-template <class R>
-__device__ bool inverse_stage(const Ctx<R>& c, double& logdet, int& sgn)
+template <class R, int NT>
+__device__ bool inverse_stage(const Ctx<R, NT>& c, double& logdet, int& sgn)
 {
     const int n = c.p.nd;
     if (c.L.S2 >= 0) {
@@ -1247,13 +1250,14 @@ struct DriftSplit {
 // rest.  A chunk must not span more than two particles (chunk <= ng, the
 // tasks per particle); when a split cannot guarantee that, half 0 takes
 // every particle on all threads.
+template <int NT>
 __device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int ng)
 {
     DriftSplit s;
     const int P = nup + ndn;
-    int wu = P > 0 ? (kWarps * nup + P / 2) / P : 0;
+    int wu = P > 0 ? ((NT / 32) * nup + P / 2) / P : 0;
     if (nup > 0 && wu < 1) wu = 1;
-    if (ndn > 0 && wu > kWarps - 1) wu = kWarps - 1;
+    if (ndn > 0 && wu > (NT / 32) - 1) wu = (NT / 32) - 1;
     s.pbeg[0] = 0;
     s.np[0] = nup;
     s.tbeg[0] = 0;
@@ -1261,7 +1265,7 @@ __device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int ng)
     s.pbeg[1] = nup;
     s.np[1] = ndn;
     s.tbeg[1] = 32 * wu;
-    s.nth[1] = kThreads - 32 * wu;
+    s.nth[1] = NT - 32 * wu;
     bool ok = nup > 0 && ndn > 0;
     for (int h = 0; h < 2; ++h) {
         s.chunk[h] = s.nth[h] > 0 ? (s.np[h] * ng + s.nth[h] - 1) / s.nth[h] : 0;
@@ -1269,10 +1273,10 @@ __device__ __forceinline__ DriftSplit drift_split(int nup, int ndn, int ng)
     }
     if (!ok) {
         s.np[0] = P;
-        s.nth[0] = kThreads;
-        s.chunk[0] = (P * ng + kThreads - 1) / kThreads;
+        s.nth[0] = NT;
+        s.chunk[0] = (P * ng + NT - 1) / NT;
         s.np[1] = 0;
-        s.tbeg[1] = kThreads;
+        s.tbeg[1] = NT;
         s.nth[1] = 0;
         s.chunk[1] = 1;
     }
@@ -1323,8 +1327,8 @@ __device__ __forceinline__ float abs_hi(double v) { return (float)fabs(v); }
 // partial contraction of one (particle, k vector) item over the terms
 // k0, k0 + kstep, ...: G (up particle) or H (down particle) for the cos and
 // sin parts of k vector q (1-based)
-template <class R>
-__device__ __forceinline__ void drift_dots(const Ctx<R>& c, const float* bound, int pt, int q, int k0, int kstep,
+template <class R, int NT>
+__device__ __forceinline__ void drift_dots(const Ctx<R, NT>& c, const float* bound, int pt, int q, int k0, int kstep,
                                            R& vc, R& vs)
 {
     const DevParams& p = c.p;
@@ -1371,8 +1375,8 @@ __device__ __forceinline__ void drift_dots(const Ctx<R>& c, const float* bound, 
 
 // the 4 terms (3 drift components, Laplacian) of k vector q (1-based) for
 // particle pt from its contractions vc, vs
-template <class R>
-__device__ __forceinline__ void drift_terms(const Ctx<R>& c, int pt, int q, R vc, R vs, R (&out)[4])
+template <class R, int NT>
+__device__ __forceinline__ void drift_terms(const Ctx<R, NT>& c, int pt, int q, R vc, R vs, R (&out)[4])
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1402,8 +1406,8 @@ __device__ __forceinline__ void drift_terms(const Ctx<R>& c, int pt, int q, R vc
 // Sinv rows with U, and in both cases
 //   t = O_c V_s - O_s V_c,  l = O_c V_c + O_s V_s
 // with O the particle's own orbital row and V the contraction.
-template <class R>
-__device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, bool down, int blk, int qch, int nqc,
+template <class R, int NT>
+__device__ __forceinline__ void drift_tile(const Ctx<R, NT>& c, const float* bound, bool down, int blk, int qch, int nqc,
                                            R* pbuf)
 {
     const DevParams& p = c.p;
@@ -1548,8 +1552,8 @@ __device__ __forceinline__ void drift_tile(const Ctx<R>& c, const float* bound, 
             for (int z = 0; z < 4; ++z) pbuf[((pbase + pi[k]) * nqc + qch) * 4 + z] = ts[k][z];
 }
 
-template <class R>
-__device__ bool drift_tiled(const Ctx<R>& c, const float* bound)
+template <class R, int NT>
+__device__ bool drift_tiled(const Ctx<R, NT>& c, const float* bound)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1557,21 +1561,21 @@ __device__ bool drift_tiled(const Ctx<R>& c, const float* bound)
     const int nqc = (nq + kTB * kTS - 1) / (kTB * kTS);   // k-vector chunks of 40
     const int tu = p.nup % (kTA * kTR), td = p.ndn % (kTA * kTR);
     const int ntail = (tu + td) * nq;
-    if (p.nup == 0 || p.ndn == 0 || (P * nqc + ntail) * 4 > kThreads * 8) return false;
+    if (p.nup == 0 || p.ndn == 0 || (P * nqc + ntail) * 4 > NT * 8) return false;
     double* acc = sm + c.L.acc;
     R* pbuf = at<R>(sm, c.L.red);              // [P][nqc][4], then tail items [ntail][4]
     R* tbuf = pbuf + P * nqc * 4;
     const int warp = threadIdx.x >> 5;
-    const int half = warp >= kWarps / 2 ? 1 : 0, hw = warp & (kWarps / 2 - 1);
+    const int half = warp >= (NT / 32) / 2 ? 1 : 0, hw = warp & ((NT / 32) / 2 - 1);
     const int n = half ? p.ndn : p.nup;        // particles of this spin
     const int nb = n / (kTA * kTR);            // full blocks of 8
-    for (int tau = hw; tau < nb * nqc; tau += kWarps / 2)
+    for (int tau = hw; tau < nb * nqc; tau += (NT / 32) / 2)
         drift_tile<R>(c, bound, half != 0, tau / nqc, tau % nqc, nqc, pbuf);
     // particles beyond the full blocks: (particle, k vector) items, 10 per
     // warp, each contraction split over 3 lanes and added in lane order
     {
         const int lane = threadIdx.x & 31, grp = lane / 3, sub = lane % 3;
-        for (int r0 = 0; r0 < ntail; r0 += kWarps * 10) {
+        for (int r0 = 0; r0 < ntail; r0 += (NT / 32) * 10) {
             const int it = r0 + warp * 10 + grp;
             const bool act = grp < 10 && it < ntail;
             const int pl = act ? it / nq : 0, q = act ? it % nq + 1 : 1;
@@ -1589,7 +1593,7 @@ __device__ bool drift_tiled(const Ctx<R>& c, const float* bound)
         }
     }
     __syncthreads();
-    for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+    for (int pt = threadIdx.x; pt < P; pt += NT) {
         const bool dn = pt >= p.nup;
         const int pl = dn ? pt - p.nup : pt, nn = dn ? p.ndn : p.nup, tt = dn ? td : tu;
         R r[4];
@@ -1611,8 +1615,8 @@ __device__ bool drift_tiled(const Ctx<R>& c, const float* bound)
     return true;
 }
 
-template <class R>
-__device__ void drift_stage(const Ctx<R>& c)
+template <class R, int NT>
+__device__ void drift_stage(const Ctx<R, NT>& c)
 {
     using KV = typename Prec<R>::KV;
     const DevParams& p = c.p;
@@ -1625,12 +1629,12 @@ __device__ void drift_stage(const Ctx<R>& c)
     R* part = at<R>(sm, c.L.red);           // per thread: 2 segments x 4 sums
     const int nq = p.nk - 1, nk = p.nk, P = p.npart, ld = p.ldS, ldU = p.ldU;
     const int ng = (nq + kQT - 1) / kQT;    // tasks per particle
-    const DriftSplit sp = drift_split(p.nup, p.ndn, ng);
+    const DriftSplit sp = drift_split<NT>(p.nup, p.ndn, ng);
     // double-float path: abs column sums (bound[i], for G) and row sums
     // (bound[nd + j], for H) of the inverse bound the dot products
     float* bound = reinterpret_cast<float*>(sm + c.L.colk);
     if constexpr (is_df<R>::value) {
-        for (int t = threadIdx.x; t < 2 * p.nd; t += kThreads) {
+        for (int t = threadIdx.x; t < 2 * p.nd; t += NT) {
             float sacc = 0.0f;
             if (t < p.nd)
                 for (int j = 0; j < p.nd; ++j) sacc += fabsf(Si[j * ld + t].hi);
@@ -1749,7 +1753,7 @@ __device__ void drift_stage(const Ctx<R>& c)
     __syncthreads();
     // particle pl of a half is covered by that half's local threads
     // floor(pl*ng/chunk) .. floor((pl*ng+ng-1)/chunk)
-    for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+    for (int pt = threadIdx.x; pt < P; pt += NT) {
         const int hh = (sp.nth[1] > 0 && pt >= sp.pbeg[1]) ? 1 : 0;
         const int pl = pt - sp.pbeg[hh], ch = sp.chunk[hh], ni = sp.np[hh] * ng;
         R r[4];
@@ -1776,8 +1780,8 @@ __device__ void drift_stage(const Ctx<R>& c)
 // through :213-222): per up-down pair h = Sinv[j][i] f'/r dx, l = Sinv[j][i]
 // lap f; row sums go to the up particle, column sums (negated drift) to the
 // down particle.  Then the unpaired plane waves.
-template <class R>
-__device__ void beta_drift_stage(const Ctx<R>& c)
+template <class R, int NT>
+__device__ void beta_drift_stage(const Ctx<R, NT>& c)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1793,7 +1797,7 @@ __device__ void beta_drift_stage(const Ctx<R>& c)
             const int r1 = min(nup, r0 + c.L.rows_beta);
             const int npc = (r1 - r0) * ndn;
             const UDiv dv(ndn);
-            for (int q = threadIdx.x; q < npc; q += kThreads) {
+            for (int q = threadIdx.x; q < npc; q += NT) {
                 const int qi = dv.quo(q);
                 const int i = r0 + qi, j = q - qi * ndn;
                 const R* xi = xr + 3 * i;
@@ -1808,7 +1812,7 @@ __device__ void beta_drift_stage(const Ctx<R>& c)
             }
             __syncthreads();
             const int nr = r1 - r0;
-            for (int tc = threadIdx.x; tc < 4 * (nr + ndn); tc += kThreads) {
+            for (int tc = threadIdx.x; tc < 4 * (nr + ndn); tc += NT) {
                 const int t = tc / 4, cmp = tc % 4;
                 typename AccOf<R>::type sacc;
                 acc_init(sacc);
@@ -1831,7 +1835,7 @@ __device__ void beta_drift_stage(const Ctx<R>& c)
     }
     // unpaired plane waves (psislaterbcs.f90:171-206 with :211-223)
     if (p.nexup > 0 || p.nexdn > 0) {
-        for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+        for (int pt = threadIdx.x; pt < P; pt += NT) {
             const double* xp = x + 3 * pt;
             double g0 = 0, g1 = 0, g2 = 0, lp = 0;
             if (pt < nup) {
@@ -1882,6 +1886,7 @@ __device__ void beta_drift_stage(const Ctx<R>& c)
 // O(N n_q) instead of O(N^2 n_q).  Leaves dU in sm[L.dg] (free until the
 // guide-function gradient is written) and uses the union region for rho_q.
 // ---------------------------------------------------------------------------
+template <int NT>
 __device__ inline void jaslong_stage(const DevParams& p, const KernelArgs& a, const SmemLayout& L, double* sm, double& ul,
                               double& d2l)
 {
@@ -1889,7 +1894,7 @@ __device__ inline void jaslong_stage(const DevParams& p, const KernelArgs& a, co
     double* rho = sm + L.R;
     double* dl = sm + L.dg;
     const int P = p.npart;
-    for (int q = threadIdx.x; q < p.nql; q += kThreads) {
+    for (int q = threadIdx.x; q < p.nql; q += NT) {
         const double* Q = a.jq + 8 * q;
         double re = 0.0, im = 0.0;
         for (int i = 0; i < P; ++i) {
@@ -1902,7 +1907,7 @@ __device__ inline void jaslong_stage(const DevParams& p, const KernelArgs& a, co
         rho[2 * q + 1] = im;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < P; i += kThreads) {
+    for (int i = threadIdx.x; i < P; i += NT) {
         double g0 = 0.0, g1 = 0.0, g2 = 0.0;
         for (int q = 0; q < p.nql; ++q) {
             const double* Q = a.jq + 8 * q;
@@ -1941,8 +1946,8 @@ struct HRes {
 // dpsi in acc[0..3N) and dpsig in sm[L.dg] when a2 != 0.
 // mode MODE_GETPHI stops after the Jastrow; MODE_BCS skips the Jastrow.
 // ---------------------------------------------------------------------------
-template <class R>
-__device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
+template <class R, int NT>
+__device__ HRes hpsi_eval(const Ctx<R, NT>& c, int mode)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1952,7 +1957,7 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     const double* x = sm + c.L.x;
     {
         R* xr = at<R>(sm, c.L.xr);
-        for (int i = threadIdx.x; i < n3; i += kThreads) xr[i] = from_dbl<R>(x[i]);
+        for (int i = threadIdx.x; i < n3; i += NT) xr[i] = from_dbl<R>(x[i]);
         __syncthreads();
     }
     HRes h;
@@ -1962,19 +1967,19 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     pair_stage<R>(c, jt, ss);   // also fills the beta part of S (needed by MODE_BCS too)
     double su = 0.0, sv = 0.0, sd2 = 0.0;
     if (mode == MODE_BCS) {
-        for (int i = threadIdx.x; i < n3; i += kThreads) du[i] = 0.0;
+        for (int i = threadIdx.x; i < n3; i += NT) du[i] = 0.0;
         __syncthreads();
     } else {
         // Jastrow, potential and pair-Laplacian sums in the Jastrow type
         // (double-float on the mixed path: no FP64 shuffle tree)
-        block_sum_t<3>(jt, at<J>(sm, c.L.red));
+        block_sum_t<3, NT>(jt, at<J>(sm, c.L.red));
         if (threadIdx.x < 32) {   // only warp 0 assembles the scalar results
             su = to_double(jt[0]);
             sv = to_double(jt[1]);
             sd2 = to_double(jt[2]);
         }
         if (p.ieq) {
-            block_sum_t<3>(ss, sm + c.L.red);
+            block_sum_t<3, NT>(ss, sm + c.L.red);
             su += ss[0];
             sv += ss[1];
             sd2 += ss[2];
@@ -1984,7 +1989,7 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     // not of getphi or bcs
     const bool jl = p.nql > 0 && (mode == MODE_HPSI || mode == MODE_STEP);
     double ulong = 0.0, d2long = 0.0;
-    if (jl) jaslong_stage(c.p, c.a, c.L, sm, ulong, d2long);
+    if (jl) jaslong_stage<NT>(c.p, c.a, c.L, sm, ulong, d2long);
     double logdet = 0.0;
     int sgn = 1;
     bool ok = true;
@@ -1996,11 +2001,11 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
             drift_stage<R>(c);
             beta_drift_stage<R>(c);
         } else {
-            for (int i = threadIdx.x; i < 4 * P; i += kThreads) acc[i] = 0.0;
+            for (int i = threadIdx.x; i < 4 * P; i += NT) acc[i] = 0.0;
             __syncthreads();
         }
     } else {
-        for (int i = threadIdx.x; i < 4 * P; i += kThreads) acc[i] = 0.0;
+        for (int i = threadIdx.x; i < 4 * P; i += NT) acc[i] = 0.0;
         __syncthreads();
     }
     // one-body term (psislaterbcs.f90:378-395) and per-particle combination
@@ -2010,7 +2015,7 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     double g1 = 0.0, d2g = 0.0, dudg = 0.0;
     double ll = 0.0, dudl = 0.0, dgdl = 0.0;   // |dUlong|^2, du.dUlong, dg.dUlong
     const double* dl = sm + c.L.dg;
-    for (int pt = threadIdx.x; pt < P; pt += kThreads) {
+    for (int pt = threadIdx.x; pt < P; pt += NT) {
         const int sp = pt < p.nup ? 0 : 1;
         const double isq = p.isqm[sp], im = p.imass[sp];
         double dph[3], dj[3];
@@ -2048,10 +2053,10 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     sums[6] = g1;
     // per-particle sums live on the first ceil(P/32) warps; the one-body
     // and long-range terms are reduced only when present
-    const int pw = min(kWarps, (P + 31) / 32);
+    const int pw = min((NT / 32), (P + 31) / 32);
     {
         double ps[3] = {sums[3], sums[4], sums[5]};
-        block_sum_t<3>(ps, sm + c.L.red, pw);
+        block_sum_t<3, NT>(ps, sm + c.L.red, pw);
         sums[3] = ps[0];
         sums[4] = ps[1];
         sums[5] = ps[2];
@@ -2059,7 +2064,7 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
     double more[5] = {d2g, dudg, ll, dudl, dgdl};
     if (ob || jl) {
         double ex[7] = {sums[6], sums[7], more[0], more[1], more[2], more[3], more[4]};
-        block_sum_t<7>(ex, sm + c.L.red, pw);
+        block_sum_t<7, NT>(ex, sm + c.L.red, pw);
         sums[6] = ex[0];
         sums[7] = ex[1];
         for (int q = 0; q < 5; ++q) more[q] = ex[2 + q];
@@ -2093,13 +2098,13 @@ __device__ HRes hpsi_eval(const Ctx<R>& c, int mode)
         h.d2psig = h.d2psi;
     } else {
         double sd[1] = {0.0};
-        for (int i = threadIdx.x; i < n3; i += kThreads) sd[0] += acc[i] * acc[i];
-        block_sum<1>(sd, sm + c.L.red);
+        for (int i = threadIdx.x; i < n3; i += NT) sd[0] += acc[i] * acc[i];
+        block_sum<1, NT>(sd, sm + c.L.red);
         const double psi = exp(h.psil);
         const double psig2 = psi * psi + p.a2;
         const double f = psi * psi / psig2;
         double* dg = sm + c.L.dg;
-        for (int i = threadIdx.x; i < n3; i += kThreads) dg[i] = f * acc[i];
+        for (int i = threadIdx.x; i < n3; i += NT) dg[i] = f * acc[i];
         h.d2psig = (sd[0] + h.d2psi) * f - psi * psi * psi * psi * sd[0] / (psig2 * psig2);
         h.psigl = 0.5 * log(psig2);
         __syncthreads();
