@@ -671,7 +671,7 @@ def main():
     ap.add_argument("--energy-blocks", type=int, default=10,
                     help="blocks of the mixed-vs-FP64 DMC energy comparison on the dmcbcs.dat deck (0: skip)")
     ap.add_argument("--energy-steps", type=int, default=20, help="generations per energy block")
-    ap.add_argument("--energy-walkers", type=int, default=1024, help="walkers per energy replica")
+    ap.add_argument("--energy-walkers", type=int, default=2048, help="walkers per energy replica")
     ap.add_argument("--energy-replicas", type=int, default=16, help="independent replicas per precision")
     ap.add_argument("--energy-eq", type=int, default=200, help="VMC equilibration generations")
     ap.add_argument("--energy-dt-eq", type=float, default=5e-3, help="VMC equilibration time step")

@@ -158,20 +158,6 @@ __device__ __forceinline__ void beta_all(const DevParams& p, const TabUD* tud, d
     d2f = W.c1 * T[0].d2b + W.c2 * T[1].d2b + W.c3 * T[2].d2b + W.c4 * T[3].d2b;
 }
 
-// a {f, f', lap f} record table on the beta grid (the b and d derivative
-// tables of the adjoint gradients)
-__device__ __forceinline__ void btab_all(const DevParams& p, const PgTab* T0, double r, double& f, double& df,
-                                         double& d2f)
-{
-    f = df = d2f = 0.0;
-    if (p.nobeta || r > p.rangeb) return;
-    const walker::Lagrange<double> W = walker::lagrange(r, p.scaleb, p.ntab);
-    const PgTab* T = T0 + (W.idx - 1);
-    f = W.c1 * T[0].f + W.c2 * T[1].f + W.c3 * T[2].f + W.c4 * T[3].f;
-    df = W.c1 * T[0].df + W.c2 * T[1].df + W.c3 * T[2].df + W.c4 * T[3].df;
-    d2f = W.c1 * T[0].d2f + W.c2 * T[1].d2f + W.c3 * T[2].d2f + W.c4 * T[3].d2f;
-}
-
 // N sums over the CTA in a fixed order (warp trees, then the warps in
 // order); red holds at least kWarps * N doubles; sum k goes to outa[k] for
 // k < N/2 and to outb[k - N/2] otherwise
@@ -370,7 +356,7 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
         // per parameter: sums over the up-down pairs of S^-1_ji S'_ij and
         // S^-1_ji M'_ij - T_ji S'_ij
         const int npairs = nup * ndn;
-        for (int th = 0; th < npb; ++th) {
+        for (int th = 0; th < norb; ++th) {
             double sl = 0.0, sq = 0.0;
             for (int t = threadIdx.x; t < npairs; t += kThreads) {
                 const int i = t / ndn, j = t % ndn, pj = nup + j;
@@ -397,22 +383,6 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                                                         g2 * (w[3 * i + 2] - w[3 * pj + 2]));
                     sl += a * ds;
                     sq += a * dm - tt * ds;
-                } else {   // bfact: beta / bfact; b, d: their derivative tables
-                    double d[3];
-                    for (int cc = 0; cc < 3; ++cc) d[cc] = walker::min_image(xs[3 * i + cc] - xs[3 * pj + cc], p);
-                    const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-                    double f, df, d2f;
-                    const int bq = th - norb;
-                    if (bq == 0)
-                        beta_all(p, tud, r, f, df, d2f);
-                    else
-                        btab_all(p, btd + (size_t)(bq - 1) * (p.ntab + 1), r, f, df, d2f);
-                    const double ib = bq == 0 ? 1.0 / bfact : 1.0;
-                    const double dr = r > 0.0 ? df / r : 0.0;
-                    const double dm = d2f * ims + 2.0 * dr * (d[0] * (w[3 * i] - w[3 * pj]) + d[1] * (w[3 * i + 1] - w[3 * pj + 1]) +
-                                                              d[2] * (w[3 * i + 2] - w[3 * pj + 2]));
-                    sl += a * f * ib;
-                    sq += (a * dm - tt * f) * ib;
                 }
             }
             sl = block_sum1(sl, red);
@@ -422,12 +392,54 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                 res[kPgradMax + th] = sq;
             }
         }
+        if (nbeta > 0) {
+            // bfact (beta / bfact), b and d (their derivative tables) in one
+            // pass: one distance and one set of Lagrange weights per pair
+            double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            const double ib = 1.0 / bfact;
+            const PgTab* Tb = btd;
+            const PgTab* Td = btd + (size_t)(p.ntab + 1);
+            for (int t = threadIdx.x; t < npairs; t += kThreads) {
+                const int i = t / ndn, j = t % ndn, pj = nup + j;
+                double d[3];
+                for (int cc = 0; cc < 3; ++cc) d[cc] = walker::min_image(xs[3 * i + cc] - xs[3 * pj + cc], p);
+                const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                if (p.nobeta || r > p.rangeb) continue;
+                const double a = Si[j + (size_t)i * nd], tt = M[j + (size_t)i * nd];
+                const walker::Lagrange<double> W = walker::lagrange(r, p.scaleb, p.ntab);
+                const double ri = r > 0.0 ? 1.0 / r : 0.0;
+                const double gw = d[0] * (w[3 * i] - w[3 * pj]) + d[1] * (w[3 * i + 1] - w[3 * pj + 1]) +
+                                  d[2] * (w[3 * i + 2] - w[3 * pj + 2]);
+                const int o = W.idx - 1;
+                double f[3], df[3], d2f[3];
+                {
+                    const TabUD* T = tud + o;
+                    f[0] = (W.c1 * T[0].b + W.c2 * T[1].b + W.c3 * T[2].b + W.c4 * T[3].b) * ib;
+                    df[0] = (W.c1 * T[0].db + W.c2 * T[1].db + W.c3 * T[2].db + W.c4 * T[3].db) * ib;
+                    d2f[0] = (W.c1 * T[0].d2b + W.c2 * T[1].d2b + W.c3 * T[2].d2b + W.c4 * T[3].d2b) * ib;
+                }
+                for (int q = 1; q < 3; ++q) {
+                    const PgTab* T = (q == 1 ? Tb : Td) + o;
+                    f[q] = W.c1 * T[0].f + W.c2 * T[1].f + W.c3 * T[2].f + W.c4 * T[3].f;
+                    df[q] = W.c1 * T[0].df + W.c2 * T[1].df + W.c3 * T[2].df + W.c4 * T[3].df;
+                    d2f[q] = W.c1 * T[0].d2f + W.c2 * T[1].d2f + W.c3 * T[2].d2f + W.c4 * T[3].d2f;
+                }
+                for (int q = 0; q < 3; ++q) {
+                    const double dm = d2f[q] * ims + 2.0 * df[q] * ri * gw;
+                    acc[q] += a * f[q];
+                    acc[3 + q] += a * dm - tt * f[q];
+                }
+            }
+            block_sum_n<6>(acc, red, res + norb, res + kPgradMax + norb);
+        }
         if (nknot > 0) {
             // the Jastrow knots, all in one pass over the up-down pairs
             double acc[2 * kJastrowKnots];
 #pragma unroll
             for (int k = 0; k < 2 * kJastrowKnots; ++k) acc[k] = 0.0;
-            const double h = p.el / kJastrowCells;
+            // grid points in units of the knot spacing: t = r / h with
+            // r = (idx - 1 + m) / scale; no divisions in the pair loop
+            const double h = p.el / kJastrowCells, ih = 1.0 / h, ih2 = ih * ih, tstep = ih / p.scale;
             for (int t = threadIdx.x; t < npairs; t += kThreads) {
                 const int i = t / ndn, j = t % ndn, pj = nup + j;
                 double d[3];
@@ -439,22 +451,32 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                 const double ri = 1.0 / r;
                 const double gd = d[0] * (gt[3 * i] - gt[3 * pj]) + d[1] * (gt[3 * i + 1] - gt[3 * pj + 1]) +
                                   d[2] * (gt[3 * i + 2] - gt[3 * pj + 2]);
-                // knots whose support [k - 2, k + 2] h (and the mirror image of
-                // k = 1 below h) reaches the four grid points
-                const double t0 = (W.idx - 1) / (p.scale * h);
-                const int klo = max(0, (int)floor(t0) - 2);
-                const int khi = min(kJastrowKnots - 1, (int)ceil(t0 + 3.0 / (p.scale * h)) + 2);
+                const double t0 = (W.idx - 1) * tstep;
+                // knots whose support [k - 2, k + 2] (and the mirror image of
+                // k = 1 below one spacing) reaches the four grid points
+                const int klo = max(0, (int)t0 - 2);
+                const int khi = min(kJastrowKnots - 1, (int)(t0 + 3.0 * tstep) + 3);
 #pragma unroll 1
                 for (int k = klo; k <= khi; ++k) {
                     double f = 0.0, fp = 0.0, fpp = 0.0;
 #pragma unroll
                     for (int m = 0; m < 4; ++m) {
+                        const double tm = t0 + m * tstep;
                         double a, b, c;
-                        jastrow_knot_basis(k, (W.idx - 1 + m) / p.scale, h, a, b, c);
+                        bspline3(tm - k, a, b, c);
+                        if (k > 0) {
+                            double a2, b2, c2;
+                            bspline3(tm + k, a2, b2, c2);
+                            a += a2;
+                            b += b2;
+                            c += c2;
+                        }
                         f += cw[m] * a;
                         fp += cw[m] * b;
                         fpp += cw[m] * c;
                     }
+                    fp *= ih;
+                    fpp *= ih2;
                     acc[k] += f;
                     acc[kJastrowKnots + k] += ims * (fpp + 2.0 * fp * ri) + 2.0 * fp * ri * gd;
                 }

@@ -9,10 +9,11 @@
 // One warp per walker.  Per move of particle i (in order 0..npart-1, every
 // sweep):
 //   - five draws of the walker's ran1 stream (ran.f90:8-27): three Gaussian
-//     deviates (gaussian(3), ran.f90:74-104) and one uniform, made for the
-//     whole sweep ahead of its moves, one move per lane;
-//   - proposal x_i' = x_i + sigma_i g (sigma of setstep, step.f90:29-30),
-//     wrapped into the box;
+//     deviates (gaussian(3), ran.f90:74-104) and one uniform, and the
+//     proposal x_i' = x_i + sigma_i g (sigma of setstep, step.f90:29-30)
+//     wrapped into the box, all in FP64 for the whole sweep ahead of its
+//     moves, one move per lane (particle i has not moved before its own move
+//     of the sweep);
 //   - distances in FP32;
 //   - the new row (up particle) or column (down particle) s' of the pair
 //     matrix: phi(r_i' - r_j) = v_0 + sum_q 2 vorb(shell q) cos(k_q.(r_i'-r_j))
@@ -155,7 +156,10 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
         // the sweep's draws, one move per lane: move i takes ran1 draws
         // 5i+1 .. 5i+5 of the stream -- gaussian(3) from four uniforms, then
         // the acceptance uniform -- reached by jump-ahead (one FP64
-        // Box-Muller per lane instead of one per move on a single lane)
+        // Box-Muller per lane instead of one per move on a single lane).
+        // Particle i moves only at its own move, so its proposal
+        // x_i + sigma g is fixed by the sweep's start and is made here too:
+        // the moves themselves do no FP64 arithmetic
         for (int i = lane; i < P; i += 32) {
             unsigned long long t = (jA[5 * i] * s + jC[5 * i]) & walker::kMask48;
             const double u1 = ran1_step(t), u2 = ran1_step(t), u3 = ran1_step(t), u4 = ran1_step(t);
@@ -163,19 +167,16 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
             double sn, cs;
             sincospi(2.0 * u1, &sn, &cs);
             const double r12 = sqrt(-2.0 * log(u2));
-            drw[4 * i] = sn * r12;
-            drw[4 * i + 1] = cs * r12;
-            drw[4 * i + 2] = cospi(2.0 * u3) * sqrt(-2.0 * log(u4));
+            const double g[3] = {sn * r12, cs * r12, cospi(2.0 * u3) * sqrt(-2.0 * log(u4))};
+            const double sig = p.sigma[i < nup ? 0 : 1];
+            for (int c = 0; c < 3; ++c) drw[4 * i + c] = walker::min_image(xs[3 * i + c] + sig * g[c], p);
             drw[4 * i + 3] = rn;
         }
         s = (jA[5 * P] * s + jC[5 * P]) & walker::kMask48;
         __syncwarp();
         for (int i = 0; i < P; ++i) {
             const bool up = i < nup;
-            const int sp = up ? 0 : 1;
-            const double sig = p.sigma[sp];
-            double xn[3];
-            for (int c = 0; c < 3; ++c) xn[c] = walker::min_image(xs[3 * i + c] + sig * drw[4 * i + c], p);
+            const double* xn = drw + 4 * i;   // the proposal, FP64
             const float xf[3] = {(float)xn[0], (float)xn[1], (float)xn[2]};
             // the moved particle's plane waves
             for (int q = lane; q < nq; q += 32) {
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
                     const int u = e - nloop;
                     const double* a = up ? p.akup[u] : p.akdn[u];
                     const int sn = up ? p.sinup[u] : p.sindn[u];
-                    const float arg = (float)(a[0] * xn[0] + a[1] * xn[1] + a[2] * xn[2]);
+                    const float arg = (float)a[0] * xf[0] + (float)a[1] * xf[1] + (float)a[2] * xf[2];
                     ph = sn ? sinf(arg) : cosf(arg);
                 }
                 snew[e] = ph;
@@ -259,8 +260,8 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
             du = warp_sum_f(du);
             __syncwarp();
             const float R = vw[cix];
-            const double prob = (double)R * (double)R * exp(2.0 * (double)du);
-            const bool acc = drw[4 * i + 3] < prob;   // R = 0 or NaN: rejected
+            const float prob = R * R * expf(2.0f * du);
+            const bool acc = drw[4 * i + 3] < (double)prob;   // R = 0 or NaN: rejected
             if (acc) {
                 const float iR = 1.0f / R;
                 // Sherman-Morrison (rank one): every column (row) but cix first

@@ -121,3 +121,60 @@ def test_sweeps_unsupported_terms():
         with pytest.raises(capi.DMCError) as ei:
             ctx.sm_sweeps(1)
         assert ei.value.status == 3
+
+
+def unpaired_system(nup, ndn, ikup, ikdn, nwalk, seed=99):
+    from dmcbcs_project_gb300.abi import make_run, make_system
+
+    sp = configs.system_params(max(nup, ndn), max(nup, ndn), 5, seed=seed)
+    sp.update(nbin=[nup, ndn], nexup=len(ikup), ikup=[list(k) for k in ikup], nexdn=len(ikdn),
+              ikdn=[list(k) for k in ikdn])
+    return make_system(sp), make_run(configs.run_params(nwalk, 0.002, idmc=0))
+
+
+@pytest.mark.parametrize("nup,ndn,ikup,ikdn", [(7, 8, [], [(0, 0, 0)]),
+                                               (9, 10, [(0, 0, 0)], [(1, 0, 0), (-1, 0, 0)])])
+def test_sweeps_unpaired_down_states(nup, ndn, ikup, ikdn):
+    """Unpaired down plane waves are extra rows of the pair matrix that a down
+    move replaces in its new column (psislaterbcs.f90:189-206); with unpaired
+    states of both spins the up moves also fill unpaired columns."""
+    sysd, rund = unpaired_system(nup, ndn, ikup, ikdn, 32)
+    ctx = capi.Context(sysd, rund)
+    orc = oracle.Oracle(sysd, rund)
+    try:
+        for c in (ctx, orc):
+            c.init_walkers()
+            c.initial_eval()
+        acc, moves = ctx.sm_sweeps(2, recompute_every=16)
+        acc_o = orc.sm_sweeps(2)
+        wg, wo = ctx.walkers(), orc.walkers()
+    finally:
+        ctx.close()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    same = np.array([np.max(np.abs(wg["x"][w] - wo["x"][w])) < 1e-10 for w in range(32)])
+    print(f"{nup}/{ndn}: accepted {acc}/{moves} (oracle {acc_o}); on the oracle's path {same.sum()}/32")
+    assert same.sum() >= 31
+    assert np.max(np.abs(wg["psil"][same] - wo["psil"][same])) < 1e-10
+
+
+def test_sweeps_with_the_jastrow_spline():
+    """The spline is part of the pair tables, so the sweeps' Jastrow ratios
+    include it; the oracle adds the same spline."""
+    knots = np.random.default_rng(4).uniform(-0.3, 0.3, 16) * np.exp(-0.15 * np.arange(16))
+    sysd, rund, _ = configs.workload("n14", nwalk=32, idmc=0)
+    ctx = capi.Context(sysd, rund)
+    orc = oracle.Oracle(sysd, rund)
+    try:
+        ctx.set_jastrow_spline(knots)
+        orc.set_jastrow_spline(knots)
+        for c in (ctx, orc):
+            c.init_walkers()
+            c.initial_eval()
+        ctx.sm_sweeps(2, recompute_every=16)
+        orc.sm_sweeps(2)
+        wg, wo = ctx.walkers(), orc.walkers()
+    finally:
+        ctx.close()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    same = np.array([np.max(np.abs(wg["x"][w] - wo["x"][w])) < 1e-10 for w in range(32)])
+    assert same.sum() >= 31
