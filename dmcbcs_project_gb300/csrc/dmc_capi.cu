@@ -1604,8 +1604,12 @@ int dmc_sm_sweeps(dmc_ctx* c, int nsweeps, int recompute_every, int64_t* accepte
     if (rc) return rc;
     const int n = c->n;
     if (n == 0) return fail(c, DMC_ERR_EMPTY, "no walkers");
+    if (accepted) *accepted = 0;
+    if (moves) *moves = 0;
+    if (nsweeps == 0) return DMC_OK;   // nothing moves; the walkers keep their values
     const size_t nd2 = (size_t)c->S.nd * c->S.nd, n3 = (size_t)c->n3;
     const int nq = std::max(1, c->S.nk - 1);
+    c->sm_n = 0;                       // no carried inverse until these sweeps end
     CK(c->sm_inv.alloc((size_t)n * nd2));
     CK(c->sm_tab.alloc((size_t)n * nq * c->S.npart));
     CK(c->sm_acc.alloc((size_t)n));

@@ -75,7 +75,7 @@ cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud
 // updated in place); the inverse comes from inv64 (FP64, fresh) or, when
 // inv64 is null, from inv32, and leaves in inv32; tab is cos/sin scratch
 // [n][nk-1][npart]; accepted[w] counts the walker's accepted moves
-size_t sweep_smem_bytes(const DevParams& p);
+size_t sweep_smem_bytes(const DevParams& p, int walkers_per_cta);
 // jA/jC: ran1 jump-ahead tables for 0 .. 5 npart steps
 cudaError_t launch_sweeps(const DevParams& p, const DevStack& st, int n, int nsweep, const double* inv64,
                           float* inv32, float2* tab, const KVecMP* kv, const TabUDmp* tud, const TabSSmp* tss,

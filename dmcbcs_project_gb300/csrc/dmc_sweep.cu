@@ -37,7 +37,7 @@
 namespace dmc {
 namespace {
 
-constexpr int kSweepWarps = 4;   // walkers per CTA, one warp each
+constexpr int kSweepWarps = 4;   // most walkers per CTA, one warp each
 
 // floats of one warp's shared memory: positions (3 npart FP64, then 3 npart
 // FP32 for distances), the sweep's draws (npart x 4 FP64: three deviates and
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
                                                                  const TabSSmp* __restrict__ tss,
                                                                  const unsigned long long* __restrict__ jA,
                                                                  const unsigned long long* __restrict__ jC,
-                                                                 unsigned long long* __restrict__ accepted)
+                                                                 unsigned long long* __restrict__ accepted, int wpc)
 {
     extern __shared__ __align__(16) double smw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
     float2* oraw = onew + (nq > 0 ? nq : 1);                                                 // plain
     const float v0 = kv[0].v.hi;
     const float elf = (float)p.el, elif = (float)p.eli;
-    const int w = blockIdx.x * kSweepWarps + wib;
+    const int w = blockIdx.x * wpc + wib;
     if (w >= n) return;   // whole warps only: the warp is the unit below
     // ---- load the walker: positions (wrapped), inverse, cos/sin table ----
     for (int e = lane; e < 3 * P; e += 32) {
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
 
 }  // namespace
 
-size_t sweep_smem_bytes(const DevParams& p) { return (size_t)kSweepWarps * (sweep_warp_floats(p) / 2 + 1) * 8; }
+size_t sweep_smem_bytes(const DevParams& p, int wpc) { return (size_t)wpc * (sweep_warp_floats(p) / 2 + 1) * 8; }
 
 cudaError_t launch_sweeps(const DevParams& p, const DevStack& st, int n, int nsweep, const double* inv64,
                           float* inv32, float2* tab, const KVecMP* kv, const TabUDmp* tud, const TabSSmp* tss,
@@ -314,14 +314,23 @@ cudaError_t launch_sweeps(const DevParams& p, const DevStack& st, int n, int nsw
                           cudaStream_t stream)
 {
     if (n <= 0 || nsweep <= 0) return cudaSuccess;
-    const size_t smem = sweep_smem_bytes(p);
+    // walkers per CTA: four, or fewer where a walker's shared memory (its
+    // inverse is nd^2 floats) would not fit four times
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    int wpc = kSweepWarps;
+    while (wpc > 1 && sweep_smem_bytes(p, wpc) > (size_t)optin) wpc /= 2;
+    const size_t smem = sweep_smem_bytes(p, wpc);
+    if (smem > (size_t)optin) return cudaErrorInvalidValue;
     if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    const int grid = (n + kSweepWarps - 1) / kSweepWarps;
-    sweep_kernel<<<grid, 32 * kSweepWarps, smem, stream>>>(p, st, n, nsweep, inv64, inv32, tab, kv, tud, tss, jA,
-                                                           jC, accepted);
+    const int grid = (n + wpc - 1) / wpc;
+    sweep_kernel<<<grid, 32 * wpc, smem, stream>>>(p, st, n, nsweep, inv64, inv32, tab, kv, tud, tss, jA, jC,
+                                                   accepted, wpc);
     return cudaGetLastError();
 }
 

@@ -455,8 +455,9 @@ int dmc_generation(dmc_ctx* ctx, int opcomp, int* nt);
  * the call).  Positions and random states are updated in place; the
  * walkers' stored wavefunction values are then re-evaluated at the new
  * positions in the context's precision.  accepted and moves (may be NULL)
- * receive the counts.  DMC_ERR_UNSUPPORTED with the one-body or long-range
- * Jastrow on or a2 != 0. */
+ * receive the counts; nsweeps = 0 moves nothing and changes nothing.
+ * DMC_ERR_UNSUPPORTED with the one-body or long-range Jastrow on or
+ * a2 != 0. */
 int dmc_sm_sweeps(dmc_ctx* ctx, int nsweeps, int recompute_every, int64_t* accepted, int64_t* moves);
 
 /* The FP32 inverses the last dmc_sm_sweeps left, for the first nw walkers

@@ -37,7 +37,7 @@ def pair(name, nw, prec="fp64", seed=1234):
     return sysd, ctx, orc
 
 
-@pytest.mark.parametrize("name,nw,nsw", [("n14", 64, 2), ("p33_30", 16, 1), ("n66", 16, 1)])
+@pytest.mark.parametrize("name,nw,nsw", [("n14", 64, 2), ("p33_30", 16, 1), ("n66", 16, 1), ("n132", 8, 1)])
 def test_sweeps_follow_the_oracle(name, nw, nsw):
     sysd, ctx, orc = pair(name, nw)
     try:
@@ -109,6 +109,20 @@ def test_sweeps_then_generation_continue():
             assert np.array_equal(w[k], h[k]), k
         ctx.step(True)
         assert ctx.num_walkers() == 32
+    finally:
+        ctx.close()
+
+
+def test_zero_sweeps_change_nothing():
+    sysd, ctx, orc = pair("n14", 16)
+    try:
+        w0 = ctx.walkers()
+        assert ctx.sm_sweeps(0) == (0, 0)
+        w1 = ctx.walkers()
+        for k in ("x", "irn", "psil", "d2psi"):
+            assert np.array_equal(w0[k], w1[k]), k
+        with pytest.raises(capi.DMCError):
+            ctx.sm_inverse(1)            # no sweeps carried an inverse yet
     finally:
         ctx.close()
 
