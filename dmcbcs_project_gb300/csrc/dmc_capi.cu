@@ -246,7 +246,7 @@ int nest_for(int idmc)
 {
     switch (idmc) {
     case -1: case 0: return 6;
-    case -2: case 1: return 14;
+    case -2: case 1: case 10: return 14;
     case 2: return 13;
     }
     return -1;
@@ -500,9 +500,8 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     c->sd = *sd;
     c->rd = *rd;
     if (nest_for(rd->idmc) < 0) {
-        int r = rd->idmc == 10 ? DMC_ERR_UNSUPPORTED : DMC_ERR_INVALID;
         delete c;
-        return r;
+        return DMC_ERR_INVALID;
     }
     if (rd->nwalk < 1 || !(rd->dt > 0.0)) {
         delete c;
@@ -528,7 +527,7 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     }
     // on-chip layout; two walker CTAs per SM when they fit (dynamic + static
     // shared memory + the 1 KB the runtime reserves per block)
-    const int static_smem = std::max(0, walker_static_smem_bytes());
+    const int static_smem = std::max(0, walker_static_smem_bytes(c->rd.idmc == 10));
     const int limit = std::min(optin, 227 * 1024) - 64 - static_smem;
     walker_smem_bytes(c->P, limit, &c->L);
     int per_sm = 1;
@@ -592,6 +591,7 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     cudaMemset(c->pop.p, 0, 4 * sizeof(int));
     cudaMemset(c->psteps.p, 0, sizeof(unsigned long long));
     e = prepare_walker(c->L);
+    if (e == cudaSuccess && c->rd.idmc == 10) e = prepare_walker(c->L, true);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         dmc_destroy(c);

@@ -1,8 +1,9 @@
-// Kernels of the GB300 DMCBS walker path (sm_103a): the walker kernel (one
-// DMC move plus the full wavefunction and local energy of a walker per CTA),
-// in plain FP64 and in the mixed double-float / FP32 form, and the
-// population kernels (estimator sums, branching, stack reversal, batched
-// inverse).  The walker stages are in dmc_walker.cuh.
+// Kernels of the GB300 DMCBS walker path (sm_103a): the walker kernel
+// instances of every idmc but 10 (one DMC move plus the full wavefunction and
+// local energy of a walker per CTA, in plain FP64 and in the mixed
+// double-float / FP32 form; the kernel is in dmc_walker_kernel.cuh, its
+// stages in dmc_walker.cuh), and the population kernels (estimator sums,
+// branching, stack reversal, batched inverse).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -10,421 +11,11 @@
 #include "dmc_device.cuh"
 #include "dmc_kernels.h"
 #include "dmc_attr.h"
-#include "dmc_walker.cuh"
+#include "dmc_walker_kernel.cuh"
 
 namespace dmc {
 
-using walker::block_sum;
-using walker::Ctx;
-using walker::HRes;
-using walker::lcg_jump;
-using walker::lcg_uniform;
-using walker::min_image;
-using walker::warp_sum;
-
 constexpr unsigned long long kMask48 = walker::kMask48;
-
-// Scalar part of one DMC/VMC move (step.f90:76-226): the estimator record
-// est[nest][2] of the pushed walker, its new weight and sign weight.  nn and
-// ol are the proposed and the old walker; take_new is the Metropolis
-// decision (always true for idmc = 1, -2); ejfd = sum |dpsi|^2/m of the
-// pushed walker (idmc = -1, 0).
-struct StepScalars {
-    double psil, psigl, d2psi, d2psig, v, vext;
-    int is;
-};
-__device__ inline void step_decision(const DevParams& p, int opcomp, const StepScalars& nn, const StepScalars& ol,
-                                     double o_weight, float o_wt0, bool take_new, double ejfd, double* est,
-                                     double& wnew_out, float& wt0_out)
-{
-    const double hb = p.hbar;
-    // psi/psi_G: exactly 1 when the guide function is psi itself (a2 = 0)
-    auto gratio = [](double l, double lg) { return l == lg ? 1.0 : exp(l - lg); };
-    const double eo = -hb * ol.d2psi + ol.v;     // old and new local energies
-    const double en = -hb * nn.d2psi + nn.v;
-    for (int q = 0; q < 2 * p.nest; ++q) est[q] = 0.0;
-    auto add = [&](int i1, double val, double wt) {
-        est[2 * (i1 - 1)] = val;
-        est[2 * (i1 - 1) + 1] = wt;
-    };
-    const double nfac = p.nfac;
-    double wnew = o_weight;
-    float wt0new = o_wt0;
-    // A DMC walker whose local energies are not finite (NaN or infinite
-    // inputs, flagged DMC_STATUS_NONFINITE by the walker kernel) gets weight 0
-    // and adds nothing to the estimators, so branching drops it; the
-    // reference has no such case (its int(w + u) of a NaN weight is
-    // undefined).  Finite walkers are untouched.
-    if (p.idmc >= 1 || p.idmc == -2) {
-        const bool fin = p.idmc == 2 ? (isfinite(eo) && (!take_new || isfinite(en)))
-                                     : (isfinite(eo) && isfinite(en) && isfinite(-hb * ol.d2psig + ol.v) &&
-                                        isfinite(-hb * nn.d2psig + nn.v));
-        if (!fin) {
-            wnew_out = 0.0;
-            wt0_out = o_wt0;
-            return;
-        }
-    }
-    if (p.idmc == -1 || p.idmc == 0) {
-        if (take_new) {
-            const double ejf = -0.5 * hb * (nn.d2psi - ejfd) + nn.v;
-            add(1, en * nfac, o_weight);
-            add(2, (en - nn.v) * nfac, o_weight);
-            add(3, nn.v * nfac, o_weight);
-            add(4, nn.vext * nfac, o_weight);
-            add(5, ejf * nfac, o_weight);
-            add(6, 1.0, 1.0);
-            wt0new = (float)nn.is;
-        } else {
-            const double ejf = -0.5 * hb * (ol.d2psi - ejfd) + ol.v;
-            add(1, eo * nfac, o_weight);
-            add(2, (eo - ol.v) * nfac, o_weight);
-            add(3, ol.v * nfac, o_weight);
-            add(4, ol.vext * nfac, o_weight);
-            add(5, ejf * nfac, o_weight);
-            add(6, 0.0, 1.0);
-        }
-    } else if (p.idmc == 1 || p.idmc == -2) {
-        const double ego = -hb * ol.d2psig + ol.v;
-        const double egn = -hb * nn.d2psig + nn.v;
-        double wt = exp(-(0.5 * (ego + egn) - p.etrial) * p.dt);
-        wnew = fmin(p.wtcut, wt);
-        if (nn.is != ol.is) {
-            if (p.fn) {
-                wnew = 0.0;
-                wt = 0.0;
-            }
-            add(5, 1.0, 1.0);
-        } else {
-            add(5, 0.0, 1.0);
-        }
-        const double wtg = wt * gratio(nn.psil, nn.psigl) * nn.is * (double)o_wt0;
-        if (opcomp) {
-            add(1, en * nfac, wtg);
-            add(2, (en - nn.v) * nfac, wtg);
-            add(3, nn.v * nfac, wtg);
-            add(4, nn.vext * nfac, wtg);
-            add(6, 0.5 * (ego + egn) * nfac, 1.0);
-            add(7, gratio(nn.psil, nn.psigl), 1.0);
-            add(8, nn.is * exp(nn.psil), 1.0);
-            add(9, exp(nn.psigl), 1.0);
-            add(10, 1.0 * nn.is, 1.0);
-            add(11, wt, 1.0);
-            add(12, wtg, 1.0);
-            add(13, copysign(1.0, wtg), 1.0);
-            add(14, copysign(1.0, wtg), wtg);
-        }
-    } else {   // idmc == 2
-        if (take_new) {
-            double wt = exp(-(0.5 * (eo + en) - p.etrial) * p.dt);
-            wnew = fmin(p.wtcut, wt);
-            if (nn.is != ol.is) {
-                if (p.fn) {
-                    wnew = 0.0;
-                    wt = 0.0;
-                }
-                add(4, 1.0, 1.0);
-            } else {
-                add(4, 0.0, 1.0);
-            }
-            const double wtg = wt * gratio(nn.psil, nn.psigl) * nn.is * (double)o_wt0;
-            if (opcomp) {
-                add(1, en * nfac, wtg);
-                add(2, (en - nn.v) * nfac, wtg);
-                add(3, nn.v * nfac, wtg);
-                add(6, gratio(nn.psil, nn.psigl), 1.0);
-                add(7, nn.is * exp(nn.psil), 1.0);
-                add(8, exp(nn.psigl), 1.0);
-                add(9, 1.0 * nn.is, 1.0);
-                add(10, wt, 1.0);
-                add(11, wtg, 1.0);
-                add(12, copysign(1.0, wtg), 1.0);
-                add(13, copysign(1.0, wtg), wtg);
-            }
-            add(5, 1.0, 1.0);
-        } else {
-            const double wt = exp(-(eo - p.etrial) * p.dt);
-            const double wtg = wt * gratio(ol.psil, ol.psigl) * ol.is * (double)o_wt0;
-            wnew = fmin(p.wtcut, wt * o_weight);
-            if (opcomp) {
-                add(1, eo * nfac, wtg);
-                add(2, (eo - ol.v) * nfac, wtg);
-                add(3, ol.v * nfac, wtg);
-                add(6, gratio(ol.psil, ol.psigl), 1.0);
-                add(7, ol.is * exp(ol.psil), 1.0);
-                add(8, exp(ol.psigl), 1.0);
-                add(9, 1.0 * ol.is, 1.0);
-                add(10, wt, 1.0);
-                add(11, wtg, 1.0);
-                add(12, copysign(1.0, wtg), 1.0);
-                add(13, copysign(1.0, wtg), wtg);
-            }
-            add(5, 0.0, 1.0);
-        }
-    }
-    wnew_out = wnew;
-    wt0_out = wt0new;
-}
-
-// ---------------------------------------------------------------------------
-// The walker kernel: persistent CTAs, one walker per CTA per iteration.
-// ---------------------------------------------------------------------------
-template <class R, int NT>
-__global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1)
-walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ KernelArgs a, SmemLayout L)
-{
-    extern __shared__ __align__(16) double sm[];
-    const int P = p.npart, n3 = 3 * P;
-    const double* kvsrc = reinterpret_cast<const double*>(walker::Prec<R>::kv(a));
-    for (int i = threadIdx.x; i < p.nk * 8; i += NT) sm[L.kq + i] = kvsrc[i];
-    {
-        using KV = typename walker::Prec<R>::KV;
-        const KV* kg = walker::Prec<R>::kv(a);
-        R* ks = walker::at<R>(sm, L.ksoa);
-        for (int q = threadIdx.x; q < p.nk; q += NT) {
-            ks[q] = kg[q].k[0];
-            ks[p.nk + q] = kg[q].k[1];
-            ks[2 * p.nk + q] = kg[q].k[2];
-            ks[3 * p.nk + q] = kg[q].k2;
-            ks[4 * p.nk + q] = kg[q].v;
-            int* kn = reinterpret_cast<int*>(ks + 5 * p.nk);
-            for (int cc = 0; cc < 3; ++cc) kn[cc * p.nk + q] = kg[q].n[cc];
-        }
-    }
-    double* pb = L.pb_in_smem ? sm + L.pb : a.gscratch + (size_t)blockIdx.x * L.pb_size;
-    Ctx<R, NT> c{p, a, L, sm, pb};
-    __shared__ double s_old[9];
-    __syncthreads();
-    const int nw = a.pn ? *a.pn : a.nw;   // the population is counted on the device in a generation
-    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
-        double* x = sm + L.x;
-        double* xo = sm + L.xo;
-        double* dxs = sm + L.dx;
-        double* drift = sm + L.drift;
-        const int src = nw - 1 - w;   // MODE_STEP pops from the top
-        unsigned long long s0 = 0;
-        if (a.mode == MODE_STEP) {
-            // step.f90:59-74: wrap, gaussians, drift, proposal
-            s0 = a.in.irn[src] & kMask48;
-            if (threadIdx.x >= NT - 32 && threadIdx.x < NT - 32 + 9) {
-                // the popped walker's scalars for the step decision (latency hidden behind the proposal)
-                const int k = threadIdx.x - (NT - 32);
-                double v;
-                switch (k) {
-                    case 0: v = a.in.psil[src]; break;
-                    case 1: v = a.in.psigl[src]; break;
-                    case 2: v = a.in.d2psi[src]; break;
-                    case 3: v = a.in.d2psig[src]; break;
-                    case 4: v = a.in.v[src]; break;
-                    case 5: v = a.in.vext[src]; break;
-                    case 6: v = a.in.weight[src]; break;
-                    case 7: v = a.in_wt0d ? (double)(float)a.in_wt0d[src] : (double)a.in.wt0[src]; break;
-                    default: v = (double)a.in.is[src]; break;
-                }
-                s_old[k] = v;
-            }
-            const double* x1 = a.in.x + (size_t)src * n3;
-            const double* g1 = a.in.dpsig + (size_t)src * n3;
-            for (int e = threadIdx.x; e < n3; e += NT) xo[e] = min_image(x1[e], p);
-            // Box-Muller pairs (ran.f90:74-104): draws t = 1..nrand from the
-            // walker's stream, pair i uses draws 2i-1, 2i
-            const int npairs = (n3 + 1) / 2;
-            for (int q = threadIdx.x; q < npairs; q += NT) {
-                double gs, gc;   // r sin(2 pi u1), r cos(2 pi u1), r = sqrt(-2 log u2)
-                if constexpr (walker::is_df<R>::value) {
-                    // the same deviates in double-float on the FP32 pipe:
-                    // u = (state | 1) 2^-48 is exact there
-                    const unsigned long long m1 = lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 1) | 1ull;
-                    const unsigned long long m2 = lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 2) | 1ull;
-                    df sn, cs;
-                    dfm::sincos2pi_u48(m1, sn, cs);
-                    const df lg = dfm::log_df(dfm::u48(m2));
-                    const df r = dsqrt(df{-2.0f * lg.hi, -2.0f * lg.lo});
-                    gs = to_double(sn * r);
-                    gc = to_double(cs * r);
-                } else {
-                    const double u1 = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 1));
-                    const double u2 = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, 2 * q + 2));
-                    double sn, cs;
-                    sincospi(2.0 * u1, &sn, &cs);
-                    const double r = sqrt(-2.0 * log(u2));
-                    gs = sn * r;
-                    gc = cs * r;
-                }
-                if (2 * q + 1 < n3) {
-                    dxs[2 * q] = gs;
-                    dxs[2 * q + 1] = gc;
-                } else {
-                    dxs[2 * q] = gc;   // odd count: the last one uses cos (ran.f90:95-102)
-                }
-            }
-            __syncthreads();
-            for (int e = threadIdx.x; e < n3; e += NT) {
-                const int sp = (e / 3) < p.nup ? 0 : 1;
-                const double sig = p.sigma[sp];
-                double d = g1[e] * (sig * sig) * p.sqm[sp];
-                if (p.cutdrift) d = fmin(p.dcut[sp], fmax(-p.dcut[sp], d));
-                drift[e] = d;
-                const double dxe = d + sig * dxs[e];
-                dxs[e] = dxe;
-                x[e] = min_image(xo[e] + dxe, p);
-            }
-        } else {
-            for (int e = threadIdx.x; e < n3; e += NT) x[e] = a.xin[(size_t)w * n3 + e];
-        }
-        __syncthreads();
-        const int hmode = a.mode == MODE_STEP ? MODE_HPSI : a.mode;
-        HRes h = walker::hpsi_eval<R>(c, a.mode == MODE_STEP ? MODE_STEP : hmode);
-        double* dpsi = sm + L.acc;
-        const double* dpsig = (p.a2 == 0.0) ? dpsi : sm + L.dg;
-        // failure flags of this walker (DMC_STATUS_*): a singular pair matrix
-        // (matrixlapack.f90:19-25, psislaterbcs.f90:210) and results that are
-        // not finite (NaN or infinite positions, overflowing terms)
-        {
-            int bad = 0;
-            for (int e = threadIdx.x; e < n3; e += NT) {
-                const double val = a.mode == MODE_GETPHI ? sm[L.acc + 4 * P + e] : dpsi[e];
-                if (!isfinite(val)) bad = 1;
-            }
-            bad = __syncthreads_or(bad);
-            const double lap = a.mode == MODE_GETPHI ? h.d2u : (a.mode == MODE_BCS ? h.d2phi : h.d2psi);
-            const double lg = a.mode == MODE_GETPHI ? h.u : h.psil;
-            if (!isfinite(lap) || !isfinite(lg) || !isfinite(h.v)) bad = 1;
-            const int flags = (h.singular ? DMC_STATUS_SINGULAR : 0) | (bad ? DMC_STATUS_NONFINITE : 0);
-            if (threadIdx.x == 0) {
-                if (flags && a.status) atomicOr(a.status, flags);
-                if (a.wstatus && a.mode != MODE_STEP) a.wstatus[w] = flags;
-            }
-        }
-        if (a.mode != MODE_STEP) {
-            // ---- batched wavefunction outputs ----
-            if (threadIdx.x == 0) {
-                if (a.o_psil) a.o_psil[w] = h.psil;
-                if (a.o_is) a.o_is[w] = h.is;
-                if (a.o_d2psi) a.o_d2psi[w] = a.mode == MODE_GETPHI ? h.d2u : (a.mode == MODE_BCS ? h.d2phi : h.d2psi);
-                if (a.o_v) a.o_v[w] = h.v;
-                if (a.o_vext) a.o_vext[w] = h.vext;
-                if (a.o_psigl) a.o_psigl[w] = h.psigl;
-                if (a.o_d2psig) a.o_d2psig[w] = h.d2psig;
-            }
-            if (a.o_dpsi)
-                for (int e = threadIdx.x; e < n3; e += NT) {
-                    double val = dpsi[e];
-                    if (a.mode == MODE_GETPHI) val = sm[L.acc + 4 * P + e];
-                    a.o_dpsi[(size_t)w * n3 + e] = val;
-                }
-            if (a.o_dpsig)
-                for (int e = threadIdx.x; e < n3; e += NT) a.o_dpsig[(size_t)w * n3 + e] = dpsig[e];
-            if (a.o_sinv) {
-                const int nd = p.nd;
-                // column-major nd x nd as the reference's smati(nd,nd)
-                for (int t = threadIdx.x; t < nd * nd; t += NT) {
-                    const int r = t % nd, cc = t / nd;
-                    a.o_sinv[(size_t)w * nd * nd + t] =
-                        h.singular ? 0.0 : to_double(walker::at<R>(sm, L.S)[r * p.ldS + cc]);
-                }
-            }
-            __syncthreads();
-            continue;
-        }
-        // ---- step1 decision (step.f90:76-226) ----
-        __shared__ int s_take_new;
-        // the popped walker's scalars, fetched into shared memory before hpsi
-        const double o_psil = s_old[0], o_psigl = s_old[1], o_d2psi = s_old[2];
-        const double o_d2psig = s_old[3], o_v = s_old[4], o_vext = s_old[5];
-        const double o_weight = s_old[6];
-        const float o_wt0 = (float)s_old[7];
-        const int o_is = (int)s_old[8];
-        const int nr = p.nrand;
-        unsigned long long irn_out = lcg_jump(s0, a.jumpA, a.jumpC, nr);
-        double* est = a.est + (size_t)w * p.nest * 2;
-        const bool metro = (p.idmc == -1 || p.idmc == 0 || p.idmc == 2);
-        if (metro) {
-            // Metropolis with the drift Green's function ratio (step.f90:80-91)
-            double acc1[2] = {0.0, 0.0};
-            for (int e = threadIdx.x; e < n3; e += NT) {
-                const int sp = (e / 3) < p.nup ? 0 : 1;
-                const double sig = p.sigma[sp];
-                double dn = dpsig[e] * (sig * sig) * p.sqm[sp];
-                if (p.cutdrift) dn = fmin(p.dcut[sp], fmax(-p.dcut[sp], dn));
-                const double d1 = drift[e] + dn;
-                const double d2 = drift[e] - dn - 2.0 * dxs[e];
-                acc1[0] += d1 * d2 / (2.0 * (sig * sig));
-            }
-            block_sum<2, NT>(acc1, sm + L.red);
-            if (threadIdx.x == 0) {
-                double prob = (p.idmc == 2 ? 2.0 * (h.psigl - o_psigl) : 2.0 * (h.psil - o_psil)) + acc1[0];
-                prob = prob == prob ? exp(fmin(0.0, prob)) : 0.0;   // a NaN proposal is rejected
-                const double rn = lcg_uniform(lcg_jump(s0, a.jumpA, a.jumpC, nr + 1));
-                s_take_new = rn < prob;
-            }
-            irn_out = lcg_jump(s0, a.jumpA, a.jumpC, nr + 1);
-            __syncthreads();
-        }
-        const bool take_new = metro ? s_take_new != 0 : true;
-        // sum |dpsi|^2/m of the pushed walker for the Jackson-Feenberg energy
-        double ejfd[1] = {0.0};
-        if (p.idmc == -1 || p.idmc == 0) {
-            const double* dsrc = take_new ? dpsi : a.in.dpsi + (size_t)src * n3;
-            for (int e = threadIdx.x; e < n3; e += NT) {
-                const int sp = (e / 3) < p.nup ? 0 : 1;
-                ejfd[0] += dsrc[e] * dsrc[e] * p.imass[sp];
-            }
-            block_sum<1, NT>(ejfd, sm + L.red);
-        }
-        // scalars of the pushed walker
-        const int k = w;   // push order = pop order
-        if (threadIdx.x == 0) {
-            const StepScalars nn{h.psil, h.psigl, h.d2psi, h.d2psig, h.v, h.vext, h.is};
-            const StepScalars ol{o_psil, o_psigl, o_d2psi, o_d2psig, o_v, o_vext, o_is};
-            double wnew = o_weight;
-            float wt0new = o_wt0;
-            // idmc = 1, -2: weights and estimators in step_decide_kernel, one
-            // thread per walker after this kernel
-            if (!a.defer)
-                step_decision(p, a.opcomp, nn, ol, o_weight, o_wt0, take_new, ejfd[0], est, wnew, wt0new);
-            DevStack o = a.out;
-            if (take_new) {
-                o.psil[k] = h.psil;
-                o.psigl[k] = h.psigl;
-                o.d2psi[k] = h.d2psi;
-                o.d2psig[k] = h.d2psig;
-                o.v[k] = h.v;
-                o.vext[k] = h.vext;
-                o.is[k] = h.is;
-            } else {
-                o.psil[k] = o_psil;
-                o.psigl[k] = o_psigl;
-                o.d2psi[k] = o_d2psi;
-                o.d2psig[k] = o_d2psig;
-                o.v[k] = o_v;
-                o.vext[k] = o_vext;
-                o.is[k] = o_is;
-            }
-            if (!a.defer) {
-                o.weight[k] = wnew;
-                o.wt0[k] = wt0new;
-            }
-            o.irn[k] = irn_out;
-            o.psil0[k] = a.in.psil0[src];
-            o.psigl0[k] = a.in.psigl0[src];
-        }
-        if (take_new) {
-            for (int e = threadIdx.x; e < n3; e += NT) {
-                a.out.x[(size_t)k * n3 + e] = x[e];
-                a.out.dpsi[(size_t)k * n3 + e] = dpsi[e];
-                a.out.dpsig[(size_t)k * n3 + e] = dpsig[e];
-            }
-        } else {
-            for (int e = threadIdx.x; e < n3; e += NT) {
-                a.out.x[(size_t)k * n3 + e] = xo[e];
-                a.out.dpsi[(size_t)k * n3 + e] = a.in.dpsi[(size_t)src * n3 + e];
-                a.out.dpsig[(size_t)k * n3 + e] = a.in.dpsig[(size_t)src * n3 + e];
-            }
-        }
-        __syncthreads();
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Deferred step decision for idmc = 1, -2 (every proposal is kept): one
@@ -678,15 +269,18 @@ int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int
     return L.total * 8;
 }
 
-int walker_static_smem_bytes()
+int walker_static_smem_bytes(bool gf)
 {
     cudaFuncAttributes a[3]{};
-    if (cudaFuncGetAttributes(&a[0], walker_kernel<double, kThreads>) != cudaSuccess) return -1;
-    if (cudaFuncGetAttributes(&a[1], walker_kernel<df, kThreads>) != cudaSuccess) return -1;
-    if (cudaFuncGetAttributes(&a[2], walker_kernel<df, 2 * kThreads>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&a[0], walker_kernel<double, kThreads, false>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&a[1], walker_kernel<df, kThreads, false>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&a[2], walker_kernel<df, 2 * kThreads, false>) != cudaSuccess) return -1;
     size_t m = 0;
     for (const auto& x : a) m = x.sharedSizeBytes > m ? x.sharedSizeBytes : m;
-    return (int)m;
+    if (!gf) return (int)m;
+    const int g = walker_gf_static_smem_bytes();
+    if (g < 0) return -1;
+    return (int)m > g ? (int)m : g;
 }
 
 // attribute kinds of the per-device record: the carveout, then the dynamic
@@ -697,7 +291,7 @@ static AttrCache g_attr;
 template <class R, int NT>
 static int set_smem_attr(int v)
 {
-    return (int)cudaFuncSetAttribute(walker_kernel<R, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    return (int)cudaFuncSetAttribute(walker_kernel<R, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
 }
 
 static cudaError_t walker_attrs(int smem, int nt, bool both, bool mixed)
@@ -709,11 +303,11 @@ static cudaError_t walker_attrs(int smem, int nt, bool both, bool mixed)
     // launches with different layouts (systems of a batch) can share an SM
     int rc = g_attr.ensure(dev, kAttrCarveout, 1, [](int) {
         const int c = (int)cudaSharedmemCarveoutMaxShared;
-        cudaError_t r = cudaFuncSetAttribute(walker_kernel<df, kThreads>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+        cudaError_t r = cudaFuncSetAttribute(walker_kernel<df, kThreads, false>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
         if (r == cudaSuccess)
-            r = cudaFuncSetAttribute(walker_kernel<double, kThreads>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+            r = cudaFuncSetAttribute(walker_kernel<double, kThreads, false>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
         if (r == cudaSuccess)
-            r = cudaFuncSetAttribute(walker_kernel<df, 2 * kThreads>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            r = cudaFuncSetAttribute(walker_kernel<df, 2 * kThreads, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      c);
         return (int)r;
     });
@@ -733,22 +327,26 @@ static cudaError_t walker_attrs(int smem, int nt, bool both, bool mixed)
     return cudaSuccess;
 }
 
-cudaError_t prepare_walker(const SmemLayout& L) { return walker_attrs(L.total * 8, L.nt, true, false); }
+cudaError_t prepare_walker(const SmemLayout& L, bool gf)
+{
+    return gf ? walker_gf_attrs(L.total * 8, L.nt, true, false) : walker_attrs(L.total * 8, L.nt, true, false);
+}
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed)
 {
+    if (a.mode == MODE_STEP && p.idmc == 10) return launch_walker_gf(p, a, L, grid, st, mixed);
     const size_t smem = (size_t)L.total * 8;
     // the shared-memory opt-in is recorded per device and size (prepare_walker
     // sets it before any graph capture; this finds it set)
     const cudaError_t e = walker_attrs((int)smem, L.nt, false, mixed);
     if (e != cudaSuccess) return e;
     if (!mixed)
-        walker_kernel<double, kThreads><<<grid, kThreads, smem, st>>>(p, a, L);
+        walker_kernel<double, kThreads, false><<<grid, kThreads, smem, st>>>(p, a, L);
     else if (L.nt == 2 * kThreads)
-        walker_kernel<df, 2 * kThreads><<<grid, 2 * kThreads, smem, st>>>(p, a, L);
+        walker_kernel<df, 2 * kThreads, false><<<grid, 2 * kThreads, smem, st>>>(p, a, L);
     else
-        walker_kernel<df, kThreads><<<grid, kThreads, smem, st>>>(p, a, L);
+        walker_kernel<df, kThreads, false><<<grid, kThreads, smem, st>>>(p, a, L);
     return cudaGetLastError();
 }
 

@@ -11,10 +11,17 @@ namespace dmc {
 // the on-chip layout.  limit_bytes is the per-CTA budget.
 int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int nt = kThreads);
 // dynamic shared-memory opt-in of both walker kernels for layout L (once,
-// before any graph capture)
-cudaError_t prepare_walker(const SmemLayout& L);
-// static shared memory of the walker kernels (the larger of the two), -1 on error
-int walker_static_smem_bytes();
+// before any graph capture); gf: the idmc = 10 instances (their moves) too
+cudaError_t prepare_walker(const SmemLayout& L, bool gf = false);
+// static shared memory of the walker kernels (the largest instance; gf: the
+// idmc = 10 instances included), -1 on error
+int walker_static_smem_bytes(bool gf = false);
+// the idmc = 10 instances (dmc_walker_gf.cu): static shared memory, the
+// shared-memory opt-in, and the move launch that launch_walker forwards to
+int walker_gf_static_smem_bytes();
+cudaError_t walker_gf_attrs(int smem, int nt, bool both, bool mixed);
+cudaError_t launch_walker_gf(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
+                             bool mixed);
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed = false);

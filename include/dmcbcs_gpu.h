@@ -106,7 +106,8 @@ typedef struct dmc_system_desc {
 /* Run parameters: dmcbcs.f90:44-60 plus the stack size factor (:224-230). */
 typedef struct dmc_run_desc {
     int64_t seed;         /* random number seed for the initial walkers */
-    int idmc;             /* -2,-1,0 (VMC), 1 (DMC local weight), 2 (DMC Metropolis) */
+    int idmc;             /* -2,-1,0 (VMC), 1 (DMC local weight), 2 (DMC Metropolis),
+                             10 (DMC without drift, two-point Green's function) */
     int isite;            /* 1 = random initial walkers, 0 = walkers loaded */
     int nwalk;            /* target population */
     int neq, nav, nstep;  /* equilibration blocks, averaging blocks, steps/block */

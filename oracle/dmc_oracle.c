@@ -1577,6 +1577,79 @@ void orc_block_update(orc_state* s, double* valnow, double* errnow)
 /* step1, step.f90:43-285                                                   */
 /* ------------------------------------------------------------------------ */
 
+/* idmc = 10, step.f90:231-279: direct sampling of the Green's function with
+ * importance sampling.  The two proposals x + sigma g and x - sigma g (no
+ * drift, not wrapped), each weighted by exp(-v dt) Psi_G'/Psi_G; one more
+ * uniform picks the first with its share of the summed weight, or always
+ * when the second crossed a node; fixed node, weight 0.5 wt exp(etrial dt).
+ * Estimator 6 is 0.5 (ego + egn) with ego, egn the old and the chosen
+ * walker's guide local energies: the reference reads ego and egn there
+ * without setting them on this path (step.f90:265). */
+static const walker* step_gf(const orc_state* s, walker* w1, walker* w2, const double* g, int64_t* irn, int opcomp,
+                             ecan* e)
+{
+    static __thread walker wb;   /* the second proposal */
+    int npart = s->npart, n3 = 3 * npart;
+    double hbar = s->hbar, nfac = s->nfac;
+    double dx[3 * MAXP];
+    for (int i = 0; i < npart; i++)
+        for (int c = 0; c < 3; c++) dx[3 * i + c] = s->sigma[i] * g[3 * i + c];
+    hres h;
+    for (int k = 0; k < n3; k++) w2->x[k] = w1->x[k] + dx[k];
+    hpsi(s, w2->x, &h, w2->dpsi, w2->dpsig);
+    w2->psil = h.psil; w2->d2psi = h.d2psi; w2->v = h.v; w2->vext = h.vext;
+    w2->psigl = h.psigl; w2->d2psig = h.d2psig; w2->is = h.is;
+    double wt1 = exp(-w2->v * s->dt) * exp(w2->psigl - w1->psigl);
+    for (int k = 0; k < n3; k++) wb.x[k] = w1->x[k] - dx[k];
+    hpsi(s, wb.x, &h, wb.dpsi, wb.dpsig);
+    wb.psil = h.psil; wb.d2psi = h.d2psi; wb.v = h.v; wb.vext = h.vext;
+    wb.psigl = h.psigl; wb.d2psig = h.d2psig; wb.is = h.is;
+    double wt2 = exp(-wb.v * s->dt) * exp(wb.psigl - w1->psigl);
+    double wt = wt1 + wt2;
+    wt1 = wt1 / wt;
+    double rn = orc_ran1(irn);
+    walker* w = (rn < wt1 || wb.is != w1->is) ? w2 : &wb;
+    if (w->is != w1->is) {
+        if (s->fn) wt = 0.0;
+        addv(e, 5, 1.0, 1.0);
+    } else {
+        addv(e, 5, 0.0, 1.0);
+    }
+    wt = 0.5 * wt * exp(s->etrial * s->dt);
+    w->weight = wt;
+    double en = -hbar * w->d2psi + w->v;
+    double wtg = wt * exp(w->psil - w->psigl) * w->is * (double)w1->wt0;
+    double ego = -hbar * w1->d2psig + w1->v, egn = -hbar * w->d2psig + w->v;
+    if (opcomp) {
+        addv(e, 1, en * nfac, wtg);
+        addv(e, 2, (en - w->v) * nfac, wtg);
+        addv(e, 3, w->v * nfac, wtg);
+        addv(e, 4, w->vext * nfac, wtg);
+        addv(e, 6, 0.5 * (ego + egn) * nfac, 1.0);
+    }
+    addv(e, 7, exp(w->psil - w->psigl), 1.0);
+    addv(e, 8, w->is * exp(w->psil), 1.0);
+    addv(e, 9, exp(w->psigl), 1.0);
+    addv(e, 10, 1.0 * w->is, 1.0);
+    addv(e, 11, wt, 1.0);
+    addv(e, 12, wtg, 1.0);
+    addv(e, 13, fsign(1.0, wtg), 1.0);
+    addv(e, 14, fsign(1.0, wtg), wtg);
+    if (w == &wb) {
+        /* the second proposal goes out through w2 */
+        memcpy(w2->x, wb.x, sizeof(double) * n3);
+        memcpy(w2->dpsi, wb.dpsi, sizeof(double) * n3);
+        memcpy(w2->dpsig, wb.dpsig, sizeof(double) * n3);
+        w2->psil = wb.psil; w2->d2psi = wb.d2psi; w2->v = wb.v; w2->vext = wb.vext;
+        w2->psigl = wb.psigl; w2->d2psig = wb.d2psig; w2->is = wb.is; w2->weight = wb.weight;
+    }
+    w2->irn = *irn;
+    w2->wt0 = w1->wt0;
+    w2->psil0 = w1->psil0;
+    w2->psigl0 = w1->psigl0;
+    return w2;
+}
+
 /* One walker through step1's loop body.  w1 is the popped walker (modified
  * in place as the reference modifies it), w2 the proposal; returns the
  * walker that step1 pushes. */
@@ -1592,6 +1665,7 @@ static const walker* step_one(const orc_state* s, walker* w1, walker* w2, int op
     irn = w1->irn & MASK48;                                      /* setrn */
     double eo = -hbar * w1->d2psi + w1->v;
     gaussian(&irn, n3, gauss);
+    if (s->idmc == 10) return step_gf(s, w1, w2, gauss, &irn, opcomp, e);
     for (int i = 0; i < npart; i++) {
         mass_i = s->pmass[i];
         sig = s->sigma[i];
@@ -1773,7 +1847,7 @@ static const walker* step_one(const orc_state* s, walker* w1, walker* w2, int op
  * Returns 0, or -1 for idmc values not handled here. */
 int orc_step(orc_state* s, int opcomp)
 {
-    if (s->idmc != -2 && s->idmc != -1 && s->idmc != 0 && s->idmc != 1 && s->idmc != 2) return -1;
+    if (s->idmc != -2 && s->idmc != -1 && s->idmc != 0 && s->idmc != 1 && s->idmc != 2 && s->idmc != 10) return -1;
     wstack* in = &s->st[s->istin];
     wstack* out = &s->st[1 - s->istin];
     int n = in->n;

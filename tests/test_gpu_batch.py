@@ -40,7 +40,7 @@ def assert_same(a, b, label):
 
 
 @pytest.mark.parametrize("idmc,precision,split", [(1, "fp64", "plan"), (0, "fp64", "ones"), (1, "mixed", "tuned"),
-                                                  (2, "fp64", "plan")])
+                                                  (2, "fp64", "plan"), (10, "fp64", "plan")])
 def test_batch_matches_single(idmc, precision, split):
     gens = 5
     A, B = make(idmc, precision), make(idmc, precision)

@@ -67,7 +67,8 @@ def test_pinned_and_pageable_walker_io(name, nw, idmc):
         assert m == wa["n"] and np.array_equal(host["x"][:m], wa["x"])
 
 
-@pytest.mark.parametrize("name,nw,idmc", [("n14", 64, 1), ("n14", 40, 0), ("p33_30", 24, 2), ("n66", 32, -2)])
+@pytest.mark.parametrize("name,nw,idmc", [("n14", 64, 1), ("n14", 40, 0), ("p33_30", 24, 2), ("n66", 32, -2),
+                                         ("n14", 32, 10)])
 def test_generation_host_matches_device_stacks(name, nw, idmc):
     torch = pytest.importorskip("torch")
     sysd, rund, _ = configs.workload(name, nwalk=nw, idmc=idmc)

@@ -291,6 +291,55 @@ def test_generation_independent_of_threads():
     assert all(np.array_equal(a, b) for a, b in zip(e1, e2))
 
 
+def _fnint(a):
+    return np.sign(a) * np.floor(np.abs(a) + 0.5)
+
+
+def test_gf_step_restates_step_f90():
+    """idmc = 10 (step.f90:231-279) restated in numpy around the oracle's own
+    hpsi: the two proposals x +- sigma g (no drift, not wrapped) from the
+    walker's stream, the pick with one more uniform (the first with its
+    share of exp(-v dt) Psi_G'/Psi_G, or always when the second crossed a
+    node), weight 0.5 (wt1 + wt2) exp(etrial dt), 0 on a node crossing."""
+    sysd, rund, _ = configs.workload("n14", nwalk=24, idmc=10)
+    o = oracle.Oracle(sysd, rund, threads=1)
+    o.init_walkers()
+    o.initial_eval()
+    o.generation(False)      # a populated stack with non-unit weights
+    before = o.walkers()
+    o.step(True)
+    after = o.walkers()
+    n, npart = before["n"], o.npart
+    assert after["n"] == n
+    sig = np.array([o.info.sigma[0]] * o.info.nup + [o.info.sigma[1]] * o.info.ndn)
+    el, dt, et = o.info.el, rund.dt, o.info.etrial
+    picks = [0, 0]
+    for k in range(n):
+        src = n - 1 - k
+        x1 = before["x"][src] - el * _fnint(before["x"][src] / el)
+        g, s = oracle.gaussian(int(before["irn"][src]) & ((1 << 48) - 1), 3 * npart)
+        rn, s = oracle.ran1(s)
+        dx = sig[:, None] * g.reshape(npart, 3)
+        xa, xb = x1 + dx, x1 - dx
+        ha, hb = o.hpsi(xa[None]), o.hpsi(xb[None])
+        wt1 = np.exp(-ha["v"][0] * dt) * np.exp(ha["psigl"][0] - before["psigl"][src])
+        wt2 = np.exp(-hb["v"][0] * dt) * np.exp(hb["psigl"][0] - before["psigl"][src])
+        first = rn < wt1 / (wt1 + wt2) or hb["is_"][0] != before["is_"][src]
+        h, xc = (ha, xa) if first else (hb, xb)
+        picks[0 if first else 1] += 1
+        wt = 0.0 if h["is_"][0] != before["is_"][src] else wt1 + wt2
+        assert np.max(np.abs(after["x"][k] - xc)) < 1e-13
+        assert after["irn"][k] == s
+        assert after["is_"][k] == h["is_"][0]
+        assert abs(after["weight"][k] - 0.5 * wt * np.exp(et * dt)) <= 1e-13 * max(1.0, abs(after["weight"][k]))
+        assert abs(after["psil"][k] - h["psil"][0]) < 1e-12
+        assert after["wt0"][k] == before["wt0"][src]
+    assert picks[0] > 0 and picks[1] > 0
+    # estimators: node crossings (5), the walker count of 10 (sign), 11 (weight)
+    vb, _, wb = o.estimators()
+    assert wb[10] >= n and vb[10] > 0
+
+
 def test_branch_copies_are_contiguous_and_advance_ran2():
     sysd, rund, _ = configs.workload("n14", nwalk=20)
     o = oracle.Oracle(sysd, rund, threads=1)
