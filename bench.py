@@ -593,6 +593,29 @@ def run_gpu(args):
             cx.close()
         return out
 
+    # idmc = 10 (the driftless two-point move, two wavefunction evaluations
+    # per walker-step) on the headline system, both paths (reported beside
+    # the headline)
+    def gf_move():
+        s_, r_, _ = configs.workload(WORKLOAD, nwalk=nwalk, idmc=10)
+        r_.seed = replica_seed(rank)
+        sub_args = argparse.Namespace(**vars(args))
+        sub_args.steps = args.gf_steps
+        sub = {}
+        for prec in ("mixed", "fp64"):
+            cx = capi.Context(s_, r_, precision=prec)
+            cx.init_walkers()
+            cx.initial_eval()
+            t = time_path(cx, sub_args, world, local, barrier)
+            sub[prec] = {"value": t["value"], "ms_per_step": t["ms_per_step"], "avg_walkers": t["avg_n"],
+                         "kernel_ms_per_launch": t["kern_ms"], "gpu_launches": t["launches"], "clocks": t["clocks"]}
+            cx.close()
+        return {"workload": "dmc_n66_33u33d_idmc10", "idmc": 10, "walkers": nwalk, "steps": args.gf_steps,
+                "unit": UNIT, "wavefunction_evaluations_per_walker_step": 2, "mixed": sub["mixed"],
+                "fp64": sub["fp64"], "speedup_vs_fp64": sub["mixed"]["value"] / sub["fp64"]["value"]}
+
+    gf = gf_move() if len(ctxs) == 2 and args.gf_steps > 0 else None
+
     n132 = n66_8192 = None
     if len(ctxs) == 2 and args.n132_steps > 0:
         n132 = mixed_config("n132", "dmc_n132_66u66d")
@@ -643,6 +666,8 @@ def run_gpu(args):
             line["param_grad"] = pgrad
         if sweeps:
             line["sm_sweeps"] = sweeps
+        if gf:
+            line["idmc10"] = gf
         print(json.dumps(line), flush=True)
     for c in ctxs.values():
         c.close()
@@ -680,6 +705,8 @@ def main():
                     help="walkers of the adjoint parameter-gradient side measurement (0: skip)")
     ap.add_argument("--sweeps", type=int, default=16,
                     help="particle-by-particle sweeps per call of the Sherman-Morrison side measurement (0: skip)")
+    ap.add_argument("--gf-steps", type=int, default=10,
+                    help="generations of the idmc = 10 side measurement (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=20,
                     help="generations of the six-system uneven batch side measurement (0: skip)")
     args = ap.parse_args()
