@@ -145,3 +145,31 @@ def test_gf_timed_generations_equal_generations():
         for ea, eb in zip(a.estimators(), b.estimators()):
             assert np.array_equal(ea, eb)
 
+
+
+@pytest.mark.parametrize("fn", [0, 1])
+def test_gf_node_crossings_with_and_without_fixed_node(fn):
+    """A larger time step makes proposals cross nodes: with fn on the
+    crossing walker's weight is 0, with fn off it keeps 0.5 (wt1 + wt2)
+    exp(etrial dt); populations, estimator 5 (the crossing rate) and the
+    walkers follow the oracle either way."""
+    sysd, rund, _ = configs.workload("n14", nwalk=64, idmc=10)
+    rund.fn = fn
+    rund.dt = rund.dt * 5           # about 12 % of the moves cross a node
+    orc = oracle.Oracle(sysd, rund)
+    with capi.Context(sysd, rund) as ctx:
+        start(ctx, orc)
+        for g in range(4):
+            op = g == 3
+            assert ctx.generation(op) == orc.generation(op)
+        wg, wo = ctx.walkers(), orc.walkers()
+        vb_g, _, wb_g = ctx.estimators()
+        vb_o, _, wb_o = orc.estimators()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    assert np.array_equal(wg["is_"], wo["is_"])
+    assert rel(wg["x"], wo["x"]) < 1e-10
+    assert rel_each(wg["weight"], wo["weight"]) < TOL
+    assert rel_each(vb_g, vb_o) < 1e-9 and rel_each(wb_g, wb_o) < 1e-9
+    crossings = vb_o[4] / wb_o[4]
+    print(f"fn={fn}: node-crossing rate {crossings:.3f}")
+    assert crossings > 0

@@ -6,7 +6,8 @@ d2psig, wavefunction.f90:525-535), alone and together.  Every hpsi output
 against the oracle (FP64 to 1e-10 relative, the mixed path to the
 benchmark's 1e-6, as in the other parity tests), and generations
 with exact populations and random streams (idmc = 1 uses the guide's
-Laplacian in the weights, idmc = 2 its ratio in the Metropolis test)."""
+Laplacian in the weights, idmc = 2 its ratio in the Metropolis test,
+idmc = 10 its ratio in the two proposals' weights)."""
 import numpy as np
 import pytest
 
@@ -55,7 +56,7 @@ def test_hpsi_terms(term, precision, tol, nup):
         assert float(np.max(np.abs(hg[k] - ho[k]))) / scale < tol, k
 
 
-@pytest.mark.parametrize("term,idmc", [("onebody", 1), ("guide", 1), ("guide", 2), ("both", 2)])
+@pytest.mark.parametrize("term,idmc", [("onebody", 1), ("guide", 1), ("guide", 2), ("both", 2), ("both", 10)])
 def test_generations_with_terms(term, idmc):
     sysd, rund = system(term, nwalk=24, idmc=idmc)
     orc = oracle.Oracle(sysd, rund)
