@@ -139,7 +139,7 @@ def fp64_peak_tflops(torch):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def cpu_reference_rate(nwalk, budget_s, threads, gens_max=None):
+def cpu_reference_rate(nwalk, max_s, threads, gens_max=None):
     """The oracle (CPU restatement of the reference) on the host cores:
     walker-steps/s of full DMC generations of the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -158,7 +158,7 @@ def cpu_reference_rate(nwalk, budget_s, threads, gens_max=None):
         o.generation(False)
         gens += 1
         el = time.perf_counter() - t0
-        if el > budget_s or (gens_max and gens >= gens_max):
+        if el > max_s or (gens_max and gens >= gens_max):
             break
     return steps / el, steps, gens, el
 
@@ -311,7 +311,7 @@ BATCH_SYSTEMS = ["n14", "n38", "n66", "p33_30", "p38_33", "n132"]
 BATCH_WALKERS = 16384
 
 
-def uneven_batch(args, rank):
+def uneven_batch(args, rank, precision="fp64"):
     """Batched generations of the six systems with the tuned CTA split, then
     the same contexts one after another (dmc_timed_generations each), both
     with the L2 flushed before every generation."""
@@ -325,7 +325,7 @@ def uneven_batch(args, rank):
     for i, (name, nw) in enumerate(zip(BATCH_SYSTEMS, nws)):
         s, r, meta = configs.workload(name, nwalk=int(nw), seed=1234 + i)
         r.seed = replica_seed(rank) + 7919 * i
-        c = capi.Context(s, r, precision="fp64")
+        c = capi.Context(s, r, precision=precision)
         c.init_walkers()
         c.initial_eval()
         ctxs.append(c)
@@ -346,7 +346,7 @@ def uneven_batch(args, rank):
         c.close()
     value = steps / (ms * 1e-3)
     seq = seq_steps / (seq_ms * 1e-3)
-    return {"workload": "uneven_batch_6_systems", "systems": systems, "walkers": BATCH_WALKERS, "precision": "fp64",
+    return {"workload": "uneven_batch_6_systems", "systems": systems, "walkers": BATCH_WALKERS, "precision": precision,
             "steps": gens, "unit": UNIT, "value": value, "ms_per_step": ms / max(gens, 1), "gpu_launches": nl,
             "grids_tuned": [int(g) for g in grids], "grids_initial": initial, "tune_pass_ms": tune_ms,
             "sequential": {"value": seq, "ms_per_step": seq_ms / max(gens, 1)},
@@ -621,7 +621,13 @@ def run_gpu(args):
         n132 = mixed_config("n132", "dmc_n132_66u66d")
         n66_8192 = mixed_config("n66", "dmc_n66_33u33d_8192")
 
-    batch = uneven_batch(args, rank) if args.batch_steps > 0 else None
+    batch = None
+    if args.batch_steps > 0:
+        batch = uneven_batch(args, rank)
+        mixed_batch = uneven_batch(args, rank, "mixed")
+        batch["mixed"] = {k: mixed_batch[k] for k in ("value", "ms_per_step", "gpu_launches", "grids_tuned",
+                                                      "sequential", "speedup_vs_sequential")}
+        batch["mixed"]["speedup_vs_fp64_batch"] = mixed_batch["value"] / batch["value"]
     pgrad = param_gradients(args, rank) if args.pgrad_walkers > 0 else None
     sweeps = sm_sweeps(args, rank) if args.sweeps > 0 else None
 

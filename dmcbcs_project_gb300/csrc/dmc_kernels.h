@@ -8,7 +8,7 @@
 namespace dmc {
 
 // Bytes of dynamic shared memory of the walker kernel for these sizes; fills
-// the on-chip layout.  limit_bytes is the per-CTA budget.
+// the on-chip layout.  limit_bytes is the per-CTA limit.
 int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int nt = kThreads);
 // dynamic shared-memory opt-in of both walker kernels for layout L (once,
 // before any graph capture); gf: the idmc = 10 instances (their moves) too

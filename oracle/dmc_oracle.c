@@ -2,10 +2,10 @@
  * dmc_oracle.c -- CPU oracle for the DMCBS walker hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is a plain-C restatement of the
- * reference Fortran (CalebRHicks/DMCBS_Project) for the walker hot path.  It
- * is the checker for the CUDA product library: only the tests, the smoke
- * check and the CPU-baseline leg of the benchmark load it.  The product
- * never links, loads or calls it.
+ * reference Fortran (CalebRHicks/DMCBS_Project) for the walker hot path.
+ * The tests hold the CUDA product library against it: only the tests, the
+ * smoke check and the CPU-baseline leg of the benchmark load it.  The
+ * product never links, loads or calls it.
  *
  * Parity status.  The reference is Fortran + MPI + MKL and cannot be built
  * on these machines (no Fortran compiler, no MPI, no MKL/LAPACK), and it

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (``oracle/dmc_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY: the tests, the smoke check and the CPU-baseline
-leg of the benchmark use this module as the checker.  The product library
+leg of the benchmark use this module, as the reference to compare with.  The product library
 never imports it.  See the header of ``dmc_oracle.c`` for what the oracle
 restates and how far its parity with the reference is pinned.
 """
