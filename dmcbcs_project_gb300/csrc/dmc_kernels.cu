@@ -168,27 +168,51 @@ __global__ void scan_kernel(const int* counts, int n, int* offs, int cap, Branch
     }
 }
 
-// one warp per source walker; copy c (1-based) advanced by c ran2 steps
+// ran2 (ran.f90:29-48) applied k times: the affine map s -> a s + c mod 2^48
+// raised to the k-th power by squaring
+__device__ __forceinline__ unsigned long long ran2_jump(unsigned long long s, unsigned k)
+{
+    unsigned long long A = 1ull, C = 0ull, a = 34522712143931ull, c = 55789347517ull;
+    while (k) {
+        if (k & 1u) {
+            A = (a * A) & kMask48;
+            C = (a * C + c) & kMask48;
+        }
+        c = (a * c + c) & kMask48;
+        a = (a * a) & kMask48;
+        k >>= 1;
+    }
+    return (A * s + C) & kMask48;
+}
+
+// One warp per output slot d < min(total, cap), so that a walker with many
+// copies is spread over many warps: its source is the pop index m with
+// offs[m] <= d < offs[m + 1] (binary search over the non-decreasing offsets;
+// walkers without copies have offs[m] == offs[m + 1] and are never found),
+// and copy c = d - offs[m] carries the state c + 1 ran2 steps after irn1[m]
+// (the reference's loop advances the stream once per copy before the push).
 __global__ void branch_scatter_kernel(DevStack in, DevStack out, int n, int n3, int cap, const int* counts,
                                       const int* offs, const unsigned long long* irn1, BranchDev bd)
 {
+    (void)counts;
     const int lane = threadIdx.x & 31;
     if (bd.pn) {
         n = *bd.pn;
         if (bd.need && !*bd.need) return;   // no population control this generation
     }
+    if (n <= 0) return;
+    const int total = min(offs[n], cap);
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < n; m += nwarps) {
-    const int j = n - 1 - m;
-
-    const int cnt = counts[m];
-    const int o0 = offs[m];
-    unsigned long long s = irn1[m];
-    const double wsign = copysign(1.0, in.weight[j]);
-    for (int cp = 0; cp < cnt; ++cp) {
-        s = (34522712143931ull * s + 55789347517ull) & kMask48;   // ran2 (ran.f90:29-48)
-        const int d = o0 + cp;
-        if (d >= cap) break;
+    for (int d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; d < total; d += nwarps) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (offs[mid] <= d)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const int m = lo, j = n - 1 - m;
         for (int e = lane; e < n3; e += 32) {
             out.x[(size_t)d * n3 + e] = in.x[(size_t)j * n3 + e];
             out.dpsi[(size_t)d * n3 + e] = in.dpsi[(size_t)j * n3 + e];
@@ -201,14 +225,13 @@ __global__ void branch_scatter_kernel(DevStack in, DevStack out, int n, int n3, 
             out.d2psig[d] = in.d2psig[j];
             out.v[d] = in.v[j];
             out.vext[d] = in.vext[j];
-            out.weight[d] = wsign;
+            out.weight[d] = copysign(1.0, in.weight[j]);
             out.psil0[d] = in.psil0[j];
             out.psigl0[d] = in.psigl0[j];
             out.wt0[d] = in.wt0[j];
             out.is[d] = in.is[j];
-            out.irn[d] = s;
+            out.irn[d] = ran2_jump(irn1[m], (unsigned)(d - offs[m]) + 1u);
         }
-    }
     }
 }
 

@@ -50,3 +50,35 @@ def test_population_control_acts(ratio, idmc):
         assert rel_each(wg[k], wo[k]) < 1e-10, k
     for a, b in zip(eg, eo):
         assert rel_each(a, b) < 1e-9
+
+
+@pytest.mark.parametrize("weights", ["one_heavy", "spread"])
+def test_branch_many_copies_of_one_walker(weights):
+    """dmc_branch with walker weights far from one: one walker carrying
+    almost the whole population (hundreds of copies, spread over many warps
+    of the scatter) or weights spread over [0, 12); copies, their order and
+    each copy's ran2-advanced stream against the oracle's branch."""
+    sysd, rund, _ = configs.workload("n14", nwalk=40, idmc=1)
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    w0 = orc.walkers()
+    n0 = w0["n"]
+    rng = np.random.default_rng(21)
+    wt = np.full(n0, 0.3) if weights == "one_heavy" else rng.uniform(0.0, 12.0, n0)
+    if weights == "one_heavy":
+        wt[7] = 311.6
+    irn = (np.arange(n0, dtype=np.int64) * 2654435761 + 99991) & ((1 << 48) - 1)
+    with capi.Context(sysd, rund) as ctx:
+        ctx.load_walkers(w0["x"], irn, weight=wt)
+        orc.load_walkers(w0["x"], weight=wt, irn=irn)
+        ctx.branch(1.0)
+        orc.branch(1.0)
+        assert ctx.num_walkers() == orc.num_walkers()
+        wg, wo = ctx.walkers(), orc.walkers()
+        hg, ho = ctx.wtisto(), orc.wtisto()
+    print(f"{weights}: {wg['n']} walkers after branching")
+    assert wg["n"] > (300 if weights == "one_heavy" else n0)
+    assert np.array_equal(wg["irn"], wo["irn"])
+    assert np.array_equal(wg["x"], wo["x"])
+    assert np.array_equal(wg["weight"], wo["weight"])
+    assert np.array_equal(hg, ho)
