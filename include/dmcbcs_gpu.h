@@ -159,7 +159,8 @@ int dmc_get_info(const dmc_ctx* ctx, dmc_info* out);
  * (2,0:ntab) transposed), 4 swbtab, 5 swdbtab, 6 swd2btab (ntab+1 each),
  * 7 ak (3*nk), 8 ak2 (nk), 9 numsh (norb, as doubles), 10 vorb (norb),
  * 11 (beta, gamma) of the long-range Jastrow, 12 (bfact, b, d) of the beta
- * function. */
+ * function.  10 and 12 are the parameters getbcspar (psislaterbcs.f90:421-447,
+ * through getdetparam, wavefunction.f90:260-287) returns. */
 int dmc_get_table(const dmc_ctx* ctx, int which, double* out, int n);
 
 /* Arithmetic of the walker kernel.  DMC_PREC_FP64 (the default) computes
@@ -186,8 +187,9 @@ int dmc_probe_peak(int kind, double* tflops);
  * fn 2: in = double x[n] > 0, out[i] = log x. */
 int dmc_dfmath_eval(int fn, int n, const void* in, double* out);
 
-/* Replaces setbcspar (psislaterbcs.f90:401-419) with optbeta=.false.:
- * new s-wave amplitudes vorb(1:norb). */
+/* Replaces setbcspar (psislaterbcs.f90:401-419, through setdetparam,
+ * wavefunction.f90:231-258) with optbeta=.false.: new s-wave amplitudes
+ * vorb(1:norb); dmc_set_beta covers its optbeta branch. */
 int dmc_set_vorb(dmc_ctx* ctx, const double* vorb, int norb);
 
 /* ---- wavefunction and local energy, batched ----------------------------- */
@@ -216,9 +218,11 @@ int dmc_get_status(dmc_ctx* ctx, int* flags, int clear);
  * No counterpart in the reference. */
 int dmc_walker_status(dmc_ctx* ctx, int nw, int* status);
 
-/* Replaces bcs (psislaterbcs.f90:155-225): log|det|, sign, drift dphi[nw][npart][3],
- * Laplacian d2phi and (if smati != NULL) the inverse smati[nw][nd*nd]
- * column-major, which the reference keeps as smatisave. */
+/* Replaces bcs (psislaterbcs.f90:155-225), which getpsi
+ * (wavefunction.f90:98-131) calls for the BCS wavefunction: log|det|, sign,
+ * drift dphi[nw][npart][3], Laplacian d2phi and (if smati != NULL) the
+ * inverse smati[nw][nd*nd] column-major, which the reference keeps as
+ * smatisave. */
 int dmc_bcs_batch(dmc_ctx* ctx, int nw, const double* x, double* phil, int* is,
                   double* dphi, double* d2phi, double* smati);
 
@@ -245,8 +249,9 @@ int dmc_bcsone_batch(dmc_ctx* ctx, int nw, const double* x, const double* smati,
 int dmc_getphione_batch(dmc_ctx* ctx, int nw, const double* x, const int* ipart,
                         const double* drr, double* ratio);
 
-/* Replaces getderbcs (psislaterbcs.f90:449-524) with optsw=.true.,
- * optbeta=.false.: d log|det| / d vorb(k), dpsi[nw][norb]. */
+/* Replaces getderbcs (psislaterbcs.f90:449-524), which getderpsi
+ * (wavefunction.f90:203-229) calls for the BCS wavefunction, with
+ * optsw=.true., optbeta=.false.: d log|det| / d vorb(k), dpsi[nw][norb]. */
 int dmc_getderbcs_batch(dmc_ctx* ctx, int nw, const double* x, double* dpsi);
 
 /* Opt-in up-down Jastrow spline, no counterpart in the reference (whose
