@@ -561,6 +561,13 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
         if (L512.total * 8 <= limit && L512.total * 8 + static_smem + 1024 <= smem_sm) c->L = L512;
     }
     c->grid = c->nsm * per_sm;
+    // the layout without the beta pair data must fit one CTA's shared
+    // memory (the pair matrix, its second buffer and the orbitals stay on
+    // chip): about N = 144 at seven shells
+    if ((long long)c->L.total * 8 > (long long)limit) {
+        dmc_destroy(c);
+        return DMC_ERR_UNSUPPORTED;
+    }
     if (!c->L.pb_in_smem) {
         e = c->gscratch.alloc((size_t)c->grid * c->L.pb_size);
         if (e != cudaSuccess) {

@@ -242,3 +242,38 @@ def test_new_entry_points_reject_bad_arguments(lib):
     assert lib.dmc_param_count(None, ctypes.byref(n)) == abi.DMC_ERR_INVALID
     assert lib.dmc_param_grad(None, 1, None, None, None) == abi.DMC_ERR_INVALID
     assert lib.dmc_generation_host(None, None, None, 0) == abi.DMC_ERR_INVALID
+
+
+def test_create_rejects_bad_decks_before_any_device_call(lib):
+    """dmc_create checks the deck values on the host first: more particles
+    than DMC_MAX_PART, more shells than DMC_MAX_SHELLS, an idmc the
+    reference does not have, a non-positive time step or no walkers give
+    DMC_ERR_INVALID (no device is needed to see it)."""
+    from dmcbcs_project_gb300 import configs
+
+    lib.dmc_create.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    cases = []
+    sp = configs.system_params(150, 150, 7)
+    cases.append((sp, configs.run_params(4, 0.001)))
+    sp = configs.system_params(7, 7, 5)
+    sp["norb"] = abi.DMC_MAX_SHELLS + 1
+    cases.append((sp, configs.run_params(4, 0.001)))
+    for idmc in (3, 11, -3):
+        cases.append((configs.system_params(7, 7, 5), configs.run_params(4, 0.001, idmc=idmc)))
+    r = configs.run_params(4, 0.001)
+    r["dt"] = 0.0
+    cases.append((configs.system_params(7, 7, 5), r))
+    r = configs.run_params(4, 0.001)
+    r["nwalk"] = 0
+    cases.append((configs.system_params(7, 7, 5), r))
+    for sp, rp in cases:
+        s = abi.make_system(sp) if sp["norb"] <= abi.DMC_MAX_SHELLS else None
+        if s is None:
+            sp2 = dict(sp)
+            sp2["norb"] = 5
+            s = abi.make_system(sp2)
+            s.norb = abi.DMC_MAX_SHELLS + 1
+        out = ctypes.c_void_p()
+        st = lib.dmc_create(ctypes.byref(s), ctypes.byref(abi.make_run(rp)), ctypes.byref(out))
+        assert st == abi.DMC_ERR_INVALID, (sp["nbin"], sp["norb"], rp)
+        assert not out.value

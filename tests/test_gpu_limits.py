@@ -1,0 +1,86 @@
+"""Size limits of the walker path.
+
+The walker kernel keeps the pair matrix, its second inverse buffer and the
+orbitals of one walker in shared memory, so the largest system is set by
+what fits one CTA: about N = 144 at seven shells (K = 81).  The largest
+system well inside that bound (70 up / 70 down) must still match the oracle
+(FP64 to 1e-10, mixed to 1e-6, generations with identical streams);
+a system beyond it is refused with DMC_ERR_UNSUPPORTED at creation, before
+any launch; a single walker runs generations like any population.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from dmcbcs_project_gb300 import abi, capi, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_each(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0)))
+
+
+def system(nup, ndn, norb=7, nwalk=4, idmc=1):
+    return (abi.make_system(configs.system_params(nup, ndn, norb)),
+            abi.make_run(configs.run_params(nwalk, 0.001, idmc=idmc)))
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed", 1e-6)])
+def test_largest_layout_against_oracle(prec, tol):
+    sysd, rund = system(70, 70)
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    x = orc.walkers()["x"][:4] + np.random.default_rng(5).normal(scale=0.3, size=(4, 140, 3))
+    ref = orc.hpsi(x)
+    with capi.Context(sysd, rund, precision=prec) as ctx:
+        got = ctx.hpsi(x)
+    el_g = -sysd.hbar * got["d2psi"] + got["v"]
+    el_r = -sysd.hbar * ref["d2psi"] + ref["v"]
+    print(f"N = 140 {prec}: E_L rel err {rel_each(el_g, el_r):.2e}")
+    assert np.array_equal(got["is_"], ref["is_"])
+    assert rel_each(el_g, el_r) < tol
+    assert rel_each(got["psil"], ref["psil"]) < tol
+    for w in range(4):
+        scale = max(1.0, float(np.max(np.abs(ref["dpsi"][w]))))
+        assert float(np.max(np.abs(got["dpsi"][w] - ref["dpsi"][w]))) / scale < tol
+
+
+def test_largest_layout_generations():
+    sysd, rund = system(70, 70, nwalk=8)
+    orc = oracle.Oracle(sysd, rund)
+    with capi.Context(sysd, rund) as ctx:
+        ctx.init_walkers()
+        orc.init_walkers()
+        ctx.initial_eval()
+        orc.initial_eval()
+        for g in range(2):
+            assert ctx.generation(g == 1) == orc.generation(g == 1)
+        wg, wo = ctx.walkers(), orc.walkers()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    assert float(np.max(np.abs(wg["x"] - wo["x"]))) < 1e-9
+    assert rel_each(wg["weight"], wo["weight"]) < 1e-10
+
+
+@pytest.mark.parametrize("nup,norb", [(80, 7), (128, 7), (66, 12)])
+def test_layout_beyond_one_cta_is_unsupported(nup, norb):
+    sysd, rund = system(nup, nup, norb)
+    with pytest.raises(capi.DMCError) as err:
+        capi.Context(sysd, rund)
+    assert err.value.status == abi.DMC_ERR_UNSUPPORTED
+
+
+def test_single_walker_generations():
+    sysd, rund, _ = configs.workload("n14", nwalk=1)
+    orc = oracle.Oracle(sysd, rund)
+    with capi.Context(sysd, rund) as ctx:
+        ctx.init_walkers()
+        orc.init_walkers()
+        ctx.initial_eval()
+        orc.initial_eval()
+        for g in range(5):
+            assert ctx.generation(g == 4) == orc.generation(g == 4)
+        wg, wo = ctx.walkers(), orc.walkers()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    assert rel_each(wg["psil"], wo["psil"]) < 1e-10
