@@ -3,11 +3,13 @@ oracle's FP64 sweeps.
 
 The oracle restates the same moves (same draws of each walker's stream,
 same proposals, same particle order) with the exact FP64 ratio of two full
-wavefunction evaluations.  The GPU's acceptance decisions use FP32 ratios, so
-a decision can flip only when the uniform falls within ~1e-6 of the
+wavefunction evaluations.  The GPU's acceptance decisions use FP32 ratios
+from the carried FP32 inverse, so a decision can flip when the uniform falls
+within the ratio's FP32 error (about cond(S) x 1e-7 relative) of the
 acceptance probability: walkers must follow the oracle exactly except for
-such rare flips (at most 1 in 32 walkers here), and every random stream must
-end in the same state (each move draws five numbers whatever it decides).
+such rare flips (at most one walker per system here; measured about one
+flip per thousand moves at N = 132), and every random stream must end in
+the same state (each move draws five numbers whatever it decides).
 
 Bars: positions 1e-10 on the walkers that follow the oracle; the walkers'
 re-evaluated log|Psi| 1e-10 (FP64 context) and E_L 1e-6 relative (mixed
