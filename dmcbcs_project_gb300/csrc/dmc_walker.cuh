@@ -488,32 +488,35 @@ __device__ void pair_stage(const Ctx<R, NT>& c, typename Prec<R>::J (&jt)[3], do
                 pvd[3 * q + 2] = g2;
             }
             __syncthreads();
+            // row sums (+) then column sums (-): rows and columns are the
+            // same particles here, so the two passes are separated by a
+            // barrier (one thread per particle in each)
             const int nr = r1 - r0;
-            for (int t = threadIdx.x; t < nr + n; t += NT) {
+            for (int t = threadIdx.x; t < nr; t += NT) {
                 double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-                if (t < nr) {
-                    const double* row = pvd + 3 * (t * n);
-                    for (int j = 0; j < n; ++j) {
-                        s0 += row[3 * j];
-                        s1 += row[3 * j + 1];
-                        s2 += row[3 * j + 2];
-                    }
-                    const int i = base + r0 + t;
-                    du[3 * i + 0] += s0 * isq;
-                    du[3 * i + 1] += s1 * isq;
-                    du[3 * i + 2] += s2 * isq;
-                } else {
-                    const int j = t - nr;
-                    for (int r = 0; r < nr; ++r) {
-                        const double* e = pvd + 3 * (r * n + j);
-                        s0 += e[0];
-                        s1 += e[1];
-                        s2 += e[2];
-                    }
-                    du[3 * (base + j) + 0] -= s0 * isq;
-                    du[3 * (base + j) + 1] -= s1 * isq;
-                    du[3 * (base + j) + 2] -= s2 * isq;
+                const double* row = pvd + 3 * (t * n);
+                for (int j = 0; j < n; ++j) {
+                    s0 += row[3 * j];
+                    s1 += row[3 * j + 1];
+                    s2 += row[3 * j + 2];
                 }
+                const int i = base + r0 + t;
+                du[3 * i + 0] += s0 * isq;
+                du[3 * i + 1] += s1 * isq;
+                du[3 * i + 2] += s2 * isq;
+            }
+            __syncthreads();
+            for (int j = threadIdx.x; j < n; j += NT) {
+                double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+                for (int r = 0; r < nr; ++r) {
+                    const double* e = pvd + 3 * (r * n + j);
+                    s0 += e[0];
+                    s1 += e[1];
+                    s2 += e[2];
+                }
+                du[3 * (base + j) + 0] -= s0 * isq;
+                du[3 * (base + j) + 1] -= s1 * isq;
+                du[3 * (base + j) + 2] -= s2 * isq;
             }
             __syncthreads();
         }

@@ -1,8 +1,9 @@
 """The optional terms of hpsi (wavefunction.f90:161-201) that the benchmark
 workloads leave off: the one-body external potential and its Jastrow
 factor (v0ex, v0exjas, nqex: vext and the one-body cross terms of the
-Laplacian) and the guiding function psi_G = sqrt(psi^2 + a2) (psigl, dpsig,
-d2psig, wavefunction.f90:525-535), alone and together.  Every hpsi output
+Laplacian), the guiding function psi_G = sqrt(psi^2 + a2) (psigl, dpsig,
+d2psig, wavefunction.f90:525-535), alone and together, and non-trivial
+pair Jastrow tables (effective interactions v0op, v0eq != 0).  Every hpsi output
 against the oracle (FP64 to 1e-10 relative, the mixed path to the
 benchmark's 1e-6, as in the other parity tests), and generations
 with exact populations and random streams (idmc = 1 uses the guide's
@@ -21,6 +22,10 @@ TERMS = {
     "onebody": dict(v0ex=0.5, v0exjas=0.3, nqex=[1, 0, 0]),
     "guide": dict(a2=0.05),
     "both": dict(a2=0.05, v0ex=0.5, v0exjas=0.3, nqex=[0, 1, 1]),
+    # the Jastrow factors of an attractive effective up-down interaction and
+    # a repulsive same-spin one (coshpot.f90:90-133 with v0op, v0eq != 0):
+    # non-trivial RK tables, where the benchmark decks' v0op = 0 gives f = 1
+    "jastrow": dict(v0op=0.5, v0eq=-0.5, cjas=[1.0, 1.0]),
 }
 
 
@@ -56,7 +61,8 @@ def test_hpsi_terms(term, precision, tol, nup):
         assert float(np.max(np.abs(hg[k] - ho[k]))) / scale < tol, k
 
 
-@pytest.mark.parametrize("term,idmc", [("onebody", 1), ("guide", 1), ("guide", 2), ("both", 2), ("both", 10)])
+@pytest.mark.parametrize("term,idmc", [("onebody", 1), ("guide", 1), ("guide", 2), ("both", 2), ("both", 10),
+                                       ("jastrow", 1)])
 def test_generations_with_terms(term, idmc):
     sysd, rund = system(term, nwalk=24, idmc=idmc)
     orc = oracle.Oracle(sysd, rund)

@@ -118,6 +118,52 @@ def test_jastrow_and_potential_tables():
     assert np.allclose(d2u[0, i], fd, rtol=1e-4, atol=1e-6)
 
 
+@pytest.mark.parametrize("ic", [0, 1])
+def test_jastrow_table_solves_the_pair_equation(ic):
+    """The RK4 + bisection Jastrow (rungekutta.f90:8-100, coshpot.f90:90-133)
+    for non-zero effective interactions, against an independent solve of the
+    same radial equation f'' + 2 f'/r = (v(r) - E) f / hbar: E from the
+    tables' own residual, f integrated from the origin with scipy's adaptive
+    Runge-Kutta, u = cjas ln(f / f(d)) compared on the grid up to the healing
+    distance d, where f' vanishes."""
+    integrate = pytest.importorskip("scipy.integrate")
+    sp = configs.system_params(33, 33, 7)
+    sp.update(v0op=0.5, v0eq=-0.5, cjas=[1.0, 0.7])
+    sysd = abi.make_system(sp)
+    o = oracle.Oracle(sysd, abi.make_run(configs.run_params(4, 0.001)), threads=1)
+    nt = o.info.ntab + 1
+    u, du, d2u = (o.table(i).reshape(2, nt)[ic] for i in range(3))
+    cj = sysd.cjas[ic]
+    dr = 0.5 * o.info.el / o.info.ntab
+    n0 = int(o.info.ntab * sysd.djas / (0.5 * o.info.el))
+    v0 = (sysd.v0op, sysd.v0eq)[ic]
+    hb, mu = sysd.hbar, sysd.amu
+    vpot = lambda r: -2.0 * v0 * mu * mu * hb / np.cosh(mu * r) ** 2
+    i = np.arange(5, n0, 11)
+    r = i * dr
+    # the tables are cjas ln f, cjas f'/f, cjas (f''/f - (f'/f)^2)
+    a, b, c = u[i] / cj, du[i] / cj, d2u[i] / cj
+    e_res = -hb * (c + b * b + 2.0 * b / r - vpot(r) / hb)
+    assert np.ptp(e_res) < 1e-9 * max(1.0, abs(e_res.mean()))
+    ene = float(e_res.mean())
+    assert ene < 0.0 if v0 > 0 else ene > 0.0      # bound (attractive) or scattering (repulsive)
+
+    def rhs(rr, y):
+        return [y[1], (vpot(rr) - ene) * y[0] / hb - 2.0 * y[1] / rr]
+
+    r0 = 1e-6
+    f0 = 1.0 + (vpot(0.0) - ene) * r0 * r0 / (6.0 * hb)
+    sol = integrate.solve_ivp(rhs, (r0, n0 * dr), [f0, (vpot(0.0) - ene) * r0 / (3.0 * hb)],
+                              t_eval=np.append(r, n0 * dr), rtol=1e-12, atol=1e-14, method="DOP853")
+    f = sol.y[0]
+    lnf = np.log(f[:-1] / f[-1])
+    print(f"ic={ic}: E = {ene:.6g}, max |ln f - u| = {np.max(np.abs(lnf - a)):.2e}, "
+          f"max |f'/f - du| = {np.max(np.abs(sol.y[1][:-1] / f[:-1] - b)):.2e}")
+    assert np.max(np.abs(lnf - a)) < 1e-6 * max(1.0, np.max(np.abs(a)))
+    assert np.max(np.abs(sol.y[1][:-1] / f[:-1] - b)) < 1e-5 * max(1.0, np.max(np.abs(b)))
+    assert abs(du[n0]) < 1e-6 and np.max(np.abs(a)) > 0.1        # f'(d) = 0; a non-trivial Jastrow
+
+
 def test_beta_table():
     sysd, rund, _ = configs.workload("n14", nwalk=4)
     o = oracle.Oracle(sysd, rund, threads=1)
