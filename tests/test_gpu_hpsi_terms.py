@@ -2,8 +2,8 @@
 workloads leave off: the one-body external potential and its Jastrow
 factor (v0ex, v0exjas, nqex: vext and the one-body cross terms of the
 Laplacian), the guiding function psi_G = sqrt(psi^2 + a2) (psigl, dpsig,
-d2psig, wavefunction.f90:525-535), alone and together, and non-trivial
-pair Jastrow tables (effective interactions v0op, v0eq != 0).  Every hpsi output
+d2psig, wavefunction.f90:525-535), alone and together, and the same-spin
+pair Jastrow (cjas(2) != 0) with its own effective interaction.  Every hpsi output
 against the oracle (FP64 to 1e-10 relative, the mixed path to the
 benchmark's 1e-6, as in the other parity tests), and generations
 with exact populations and random streams (idmc = 1 uses the guide's
@@ -22,9 +22,9 @@ TERMS = {
     "onebody": dict(v0ex=0.5, v0exjas=0.3, nqex=[1, 0, 0]),
     "guide": dict(a2=0.05),
     "both": dict(a2=0.05, v0ex=0.5, v0exjas=0.3, nqex=[0, 1, 1]),
-    # the Jastrow factors of an attractive effective up-down interaction and
-    # a repulsive same-spin one (coshpot.f90:90-133 with v0op, v0eq != 0):
-    # non-trivial RK tables, where the benchmark decks' v0op = 0 gives f = 1
+    # a same-spin Jastrow from a repulsive effective interaction next to a
+    # weaker up-down one (coshpot.f90:40-43,90-133: v0op, v0eq = 0 would
+    # mean v0; the workloads switch the same-spin factor off, cjas(2) = 0)
     "jastrow": dict(v0op=0.5, v0eq=-0.5, cjas=[1.0, 1.0]),
 }
 

@@ -11,8 +11,13 @@ from dmcbcs_project_gb300 import capi, configs
 pytestmark = pytest.mark.gpu
 
 
-def run_both(name, nwalk, gens, tabs):
+def run_both(name, nwalk, gens, tabs, same_spin=False):
     sysd, rund, _ = configs.workload(name, nwalk=nwalk)
+    if same_spin:
+        # the same-spin Jastrow on: n(k)'s single-particle ratios then carry
+        # both Jastrow tables
+        sysd.v0op, sysd.v0eq = 0.5, -0.5
+        sysd.cjas[0], sysd.cjas[1] = 1.0, 1.0
     orc = oracle.Oracle(sysd, rund)
     ctx = capi.Context(sysd, rund)
     for m in (ctx, orc):
@@ -29,9 +34,11 @@ def close(a, b, rtol):
     return np.max(np.abs(a - b)) <= rtol * scale
 
 
-@pytest.mark.parametrize("name,nwalk,tabs", [("n14", 24, (25, 4, 12)), ("p33_30", 6, (20, 3, 6))])
-def test_operator_pass_matches_oracle(name, nwalk, tabs):
-    sysd, ctx, orc = run_both(name, nwalk, 2, tabs)
+@pytest.mark.parametrize("name,nwalk,tabs,same_spin", [("n14", 24, (25, 4, 12), False),
+                                                       ("p33_30", 6, (20, 3, 6), False),
+                                                       ("n66", 6, (20, 3, 6), True)])
+def test_operator_pass_matches_oracle(name, nwalk, tabs, same_spin):
+    sysd, ctx, orc = run_both(name, nwalk, 2, tabs, same_spin)
     try:
         wg0, wo0 = ctx.walkers(), orc.walkers()
         assert np.array_equal(wg0["irn"], wo0["irn"])

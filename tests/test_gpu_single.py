@@ -16,8 +16,13 @@ TOL = 1e-10
 NAMES = ["n14", "n66", "p33_30", "p38_33"]
 
 
-def setup(name, nw, seed):
+def setup(name, nw, seed, jastrow=False):
     sysd, rund, _ = configs.workload(name, nwalk=nw, seed=seed)
+    if jastrow:
+        # the same-spin Jastrow on (the workloads have cjas(2) = 0) with its
+        # own effective interaction, and a weaker up-down one
+        sysd.v0op, sysd.v0eq = 0.5, -0.5
+        sysd.cjas[0], sysd.cjas[1] = 1.0, 1.0
     orc = oracle.Oracle(sysd, rund)
     orc.init_walkers()
     x = orc.walkers()["x"][:nw] + np.random.default_rng(seed).normal(scale=0.3, size=(nw, orc.npart, 3))
@@ -53,9 +58,10 @@ def test_bcsone_against_oracle_and_full_evaluation(name):
     assert rel(got, full).max() < 1e-8
 
 
+@pytest.mark.parametrize("jastrow", [False, True])
 @pytest.mark.parametrize("name", NAMES)
-def test_getphione_against_oracle_and_full_evaluation(name):
-    sysd, rund, orc, x = setup(name, 24, 5)
+def test_getphione_against_oracle_and_full_evaluation(name, jastrow):
+    sysd, rund, orc, x = setup(name, 24, 5, jastrow)
     # small steps so that some pairs cross the healing distance
     ip, drr = moves(orc.npart, x.shape[0], 6, scale=0.2)
     with capi.Context(sysd, rund) as ctx:
@@ -64,13 +70,16 @@ def test_getphione_against_oracle_and_full_evaluation(name):
         xn[np.arange(len(ip)), ip - 1] -= drr
         u0, u1 = ctx.getphi(x)["u"], ctx.getphi(xn)["u"]
     ref = np.array([orc.getphione(x[w], drr[w], ip[w]) for w in range(len(ip))])
-    print(f"{name}: getphione rel err vs oracle {rel(got, ref).max():.2e}")
+    print(f"{name} (same-spin Jastrow {'on' if jastrow else 'off'}): getphione rel err vs oracle {rel(got, ref).max():.2e}, "
+          f"ratios in [{got.min():.3g}, {got.max():.3g}]")
     assert rel(got, ref).max() < TOL
     assert rel(got, np.exp(u1 - u0)).max() < 1e-9
+    if jastrow:
+        assert np.max(np.abs(got - 1.0)) > 1e-3     # the moves change the Jastrow
 
 
 def test_move1_is_the_product():
-    sysd, rund, orc, x = setup("p33_30", 16, 7)
+    sysd, rund, orc, x = setup("p33_30", 16, 7, jastrow=True)
     ip, dr = moves(orc.npart, x.shape[0], 8)
     xnew = x[np.arange(len(ip)), ip - 1] - dr
     with capi.Context(sysd, rund) as ctx:

@@ -194,3 +194,26 @@ def test_sweeps_with_the_jastrow_spline():
     assert np.array_equal(wg["irn"], wo["irn"])
     same = np.array([np.max(np.abs(wg["x"][w] - wo["x"][w])) < 1e-10 for w in range(32)])
     assert same.sum() >= 31
+
+
+def test_sweeps_with_the_same_spin_jastrow():
+    """The same-spin Jastrow on (cjas(2) = 1, effective interaction v0eq):
+    the sweeps' FP32 Jastrow ratios read both pair tables."""
+    sysd, rund, _ = configs.workload("n66", nwalk=16, idmc=0)
+    sysd.v0op, sysd.v0eq = 0.5, -0.5
+    sysd.cjas[0], sysd.cjas[1] = 1.0, 1.0
+    ctx = capi.Context(sysd, rund)
+    orc = oracle.Oracle(sysd, rund)
+    try:
+        for c in (ctx, orc):
+            c.init_walkers()
+            c.initial_eval()
+        acc, moves = ctx.sm_sweeps(1, recompute_every=16)
+        acc_o = orc.sm_sweeps(1)
+        wg, wo = ctx.walkers(), orc.walkers()
+    finally:
+        ctx.close()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    same = np.array([np.max(np.abs(wg["x"][w] - wo["x"][w])) < 1e-10 for w in range(16)])
+    print(f"same-spin Jastrow: accepted {acc}/{moves} (oracle {acc_o}), on the oracle's path {same.sum()}/16")
+    assert same.sum() >= 15
