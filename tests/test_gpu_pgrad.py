@@ -24,7 +24,8 @@ Checks:
     adjoint d log Psi over the population in pop order, and the update moves
     every parameter by the step it returns.
 Systems: 7/7, polarised 33/30 (unpaired columns enter M but not S'), 33/33,
-and 7/7 with the long-range Jastrow on (its gradient enters w)."""
+7/7 with the long-range Jastrow on (its gradient enters w), and 33/33 with
+the same-spin Jastrow on (its pair terms enter w)."""
 import numpy as np
 import pytest
 
@@ -44,8 +45,13 @@ def knots_for(seed):
     return rng.uniform(-0.3, 0.3, 16) * np.exp(-0.15 * np.arange(16))
 
 
-def walkers(name, nw, seed=11, longrange=None):
+def walkers(name, nw, seed=11, longrange=None, same_spin=False):
     sysd, rund, _ = configs.workload(name, nwalk=nw, seed=seed, longrange=longrange)
+    if same_spin:
+        # the same-spin Jastrow on: grad J, which the d E_L terms use, then
+        # has same-spin pair terms
+        sysd.v0op, sysd.v0eq = 0.5, -0.5
+        sysd.cjas[0], sysd.cjas[1] = 1.0, 1.0
     orc = oracle.Oracle(sysd, rund)
     orc.init_walkers()
     x = orc.walkers()["x"][:nw].copy()
@@ -118,12 +124,16 @@ def rel_err(a, ref):
     return float(np.max(np.abs(a - ref) / scale))
 
 
-@pytest.mark.parametrize("name,nw,longrange,spline", [("n14", 8, None, False), ("p33_30", 4, None, False),
-                                                      ("n66", 4, None, False), ("n14", 6, LR, False),
-                                                      ("n66", 4, None, True), ("n14", 8, None, True),
-                                                      ("p33_30", 4, None, True)])
-def test_param_grad_against_oracle_fd(name, nw, longrange, spline):
-    sysd, rund, x = walkers(name, nw, longrange=longrange)
+@pytest.mark.parametrize("name,nw,longrange,spline,same_spin", [("n14", 8, None, False, False),
+                                                                ("p33_30", 4, None, False, False),
+                                                                ("n66", 4, None, False, False),
+                                                                ("n14", 6, LR, False, False),
+                                                                ("n66", 4, None, True, False),
+                                                                ("n14", 8, None, True, False),
+                                                                ("p33_30", 4, None, True, False),
+                                                                ("n66", 4, None, True, True)])
+def test_param_grad_against_oracle_fd(name, nw, longrange, spline, same_spin):
+    sysd, rund, x = walkers(name, nw, longrange=longrange, same_spin=same_spin)
     knots = knots_for(5) if spline else None
     norb = int(sysd.norb)
     with capi.Context(sysd, rund) as ctx:
