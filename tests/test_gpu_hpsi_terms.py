@@ -3,7 +3,8 @@ workloads leave off: the one-body external potential and its Jastrow
 factor (v0ex, v0exjas, nqex: vext and the one-body cross terms of the
 Laplacian), the guiding function psi_G = sqrt(psi^2 + a2) (psigl, dpsig,
 d2psig, wavefunction.f90:525-535), alone and together, and the same-spin
-pair Jastrow (cjas(2) != 0) with its own effective interaction.  Every hpsi output
+pair Jastrow (cjas(2) != 0) with its own effective interaction, at N = 14,
+66 and 132 (the last on the mixed path's 16-warp CTA).  Every hpsi output
 against the oracle (FP64 to 1e-10 relative, the mixed path to the
 benchmark's 1e-6, as in the other parity tests), and generations
 with exact populations and random streams (idmc = 1 uses the guide's
@@ -42,7 +43,7 @@ def rel_each(a, b):
 
 @pytest.mark.parametrize("term", list(TERMS))
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-6)])
-@pytest.mark.parametrize("nup", [7, 33])
+@pytest.mark.parametrize("nup", [7, 33, 66])
 def test_hpsi_terms(term, precision, tol, nup):
     sysd, rund = system(term, nup=nup)
     orc = oracle.Oracle(sysd, rund)

@@ -1,5 +1,6 @@
 """Long-range Jastrow (jastrowlongrange.f90:22-46, switched on by numq > 0)
-on both GPU paths against the oracle: hpsi values and whole generations."""
+on both GPU paths against the oracle: hpsi values (N = 132 runs the mixed
+path on its 16-warp CTA) and whole generations."""
 import numpy as np
 import pytest
 
@@ -19,7 +20,7 @@ def _x(name, nw, seed):
     return sysd, rund, orc, x
 
 
-@pytest.mark.parametrize("name", ["n14", "n66", "p33_30"])
+@pytest.mark.parametrize("name", ["n14", "n66", "p33_30", "n132"])
 def test_hpsi_with_long_range_jastrow(name):
     sysd, rund, orc, x = _x(name, 16, 31)
     ref = orc.hpsi(x)

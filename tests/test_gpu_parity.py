@@ -68,9 +68,14 @@ def test_bcs_and_inverse(name, nw):
         assert rel(got["smati"][w], ref["smati"][w]) < 1e-9
 
 
-@pytest.mark.parametrize("name", ["n14", "n66"])
-def test_getphi(name):
+@pytest.mark.parametrize("name,same_spin", [("n14", False), ("n66", False), ("n66", True)])
+def test_getphi(name, same_spin):
     sysd, rund, orc, x = configs_for(name, 8, seed=3)
+    if same_spin:
+        # the same-spin Jastrow on (cjas(2) = 1, its own effective interaction)
+        sysd.v0op, sysd.v0eq = 0.5, -0.5
+        sysd.cjas[0], sysd.cjas[1] = 1.0, 1.0
+        orc = oracle.Oracle(sysd, rund)
     with capi.Context(sysd, rund) as ctx:
         got = ctx.getphi(x)
     for w in range(x.shape[0]):
