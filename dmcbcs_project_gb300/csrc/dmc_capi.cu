@@ -764,6 +764,9 @@ int dmc_matinv_batch(dmc_ctx* c, int n, int nb, double* a, double* detl, int* is
     if (!c || n < 1 || n > 2 * DMC_MAX_PART || nb < 0 || (nb > 0 && (!a || !detl || !is)))
         return fail(c, DMC_ERR_INVALID, "bad matinv arguments");
     if (nb == 0) return DMC_OK;
+    const int fits = matinv_fits(n);
+    if (fits < 0) return fail(c, DMC_ERR_CUDA, "matinv: device query");
+    if (!fits) return fail(c, DMC_ERR_UNSUPPORTED, "matinv: the matrix does not fit one CTA's shared memory");
     const size_t n2 = (size_t)n * n;
     DevBuf<double> da, dd;
     DevBuf<int> di;

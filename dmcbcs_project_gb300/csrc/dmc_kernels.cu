@@ -516,6 +516,25 @@ matinv_kernel(const double* a, double* inv, double* detl, int* is, int n, DevPar
     }
 }
 
+// doubles of one n x n matrix with the pivot column and reduction scratch of
+// the batched inverse (the second buffer of the blocked form comes on top)
+static int matinv_doubles(int n)
+{
+    const int ld = n | 1;
+    return round_up(n * ld, 2) + round_up(2 * n + 2, 2) + kThreads * 8;
+}
+
+int matinv_fits(int n, bool* two_buffers)
+{
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return -1;
+    const size_t one = (size_t)matinv_doubles(n) * 8 + 1024;
+    if (two_buffers) *two_buffers = one + (size_t)round_up(n * (n | 1), 2) * 8 <= (size_t)optin;
+    return one <= (size_t)optin ? 1 : 0;
+}
+
 cudaError_t launch_matinv(const double* a, double* inv, double* detl, int* is, int n, int nb, cudaStream_t st)
 {
     DevParams p;

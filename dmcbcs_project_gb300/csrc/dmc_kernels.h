@@ -26,6 +26,11 @@ cudaError_t launch_walker_gf(const DevParams& p, const KernelArgs& a, const Smem
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed = false);
 
+// whether the batched inverse of one n x n matrix fits one CTA's shared
+// memory (1), not (0), or the device query failed (-1); *two_buffers: the
+// blocked form's second buffer fits as well
+int matinv_fits(int n, bool* two_buffers = nullptr);
+
 cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, cudaStream_t st,
                               const int* pn = nullptr, unsigned long long* steps = nullptr);
 

@@ -236,7 +236,9 @@ int dmc_getphi_batch(dmc_ctx* ctx, int nw, const double* x, double* u,
 /* Replaces rmatinv (matrixlapack.f90:13-41), i.e. MKL dgetrf+dgetri, on nb
  * column-major n x n matrices a[nb][n*n] in place: inverse, log|det| and
  * sign.  A singular matrix gives detl = DMC_MINUSHUGE and is left
- * unspecified, as the reference leaves it. */
+ * unspecified, as the reference leaves it.  One matrix is held in one CTA's
+ * shared memory: the blocked Gauss-Jordan form up to n of about 114, a
+ * single-buffer form above it, DMC_ERR_UNSUPPORTED beyond about n = 160. */
 int dmc_matinv_batch(dmc_ctx* ctx, int n, int nb, double* a, double* detl, int* is);
 
 /* Replaces bcsone (psislaterbcs.f90:296-376): determinant ratio for moving

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle
-from dmcbcs_project_gb300 import capi, configs
+from dmcbcs_project_gb300 import abi, capi, configs
 
 TOL = 1e-10
 pytestmark = pytest.mark.gpu
@@ -86,8 +86,10 @@ def test_getphi(name, same_spin):
         assert rel(got["du"][w], r["du"]) < TOL
 
 
-@pytest.mark.parametrize("n", [1, 2, 7, 33, 66])
+@pytest.mark.parametrize("n", [1, 2, 7, 33, 66, 96, 110, 128, 150])
 def test_matinv(n):
+    """Blocked Gauss-Jordan with 2, 3 and 4 rows per lane (n <= 64, 96,
+    ~114 where the second buffer fits) and the single-buffer form above."""
     rng = np.random.default_rng(n)
     a = rng.normal(size=(5, n, n))
     sysd, rund, _ = configs.workload("n14", nwalk=4)
@@ -99,6 +101,14 @@ def test_matinv(n):
         assert s[b] == rs
         assert abs(d[b] - rd) < 1e-11 * max(1.0, abs(rd))
         assert rel(inv[b], ri) < 1e-10
+
+
+def test_matinv_too_large_is_unsupported():
+    sysd, rund, _ = configs.workload("n14", nwalk=4)
+    with capi.Context(sysd, rund) as ctx:
+        with pytest.raises(capi.DMCError) as err:
+            ctx.matinv(np.eye(200)[None])
+    assert err.value.status == abi.DMC_ERR_UNSUPPORTED
 
 
 def test_matinv_singular():
