@@ -131,7 +131,8 @@ def rel_err(a, ref):
                                                                 ("n66", 4, None, True, False),
                                                                 ("n14", 8, None, True, False),
                                                                 ("p33_30", 4, None, True, False),
-                                                                ("n66", 4, None, True, True)])
+                                                                ("n66", 4, None, True, True),
+                                                                ("n132", 2, None, True, False)])
 def test_param_grad_against_oracle_fd(name, nw, longrange, spline, same_spin):
     sysd, rund, x = walkers(name, nw, longrange=longrange, same_spin=same_spin)
     knots = knots_for(5) if spline else None

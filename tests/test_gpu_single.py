@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-10
 NAMES = ["n14", "n66", "p33_30", "p38_33"]
+NAMES_RATIO = NAMES + ["n132"]   # nd = 66: three passes of the warp over a row
 
 
 def setup(name, nw, seed, jastrow=False):
@@ -41,7 +42,7 @@ def rel(a, b):
     return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", NAMES_RATIO)
 def test_bcsone_against_oracle_and_full_evaluation(name):
     sysd, rund, orc, x = setup(name, 24, 3)
     ip, dr = moves(orc.npart, x.shape[0], 4)
@@ -59,7 +60,7 @@ def test_bcsone_against_oracle_and_full_evaluation(name):
 
 
 @pytest.mark.parametrize("jastrow", [False, True])
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", NAMES_RATIO)
 def test_getphione_against_oracle_and_full_evaluation(name, jastrow):
     sysd, rund, orc, x = setup(name, 24, 5, jastrow)
     # small steps so that some pairs cross the healing distance
