@@ -84,3 +84,35 @@ def test_single_walker_generations():
         wg, wo = ctx.walkers(), orc.walkers()
     assert np.array_equal(wg["irn"], wo["irn"])
     assert rel_each(wg["psil"], wo["psil"]) < 1e-10
+
+
+@pytest.mark.parametrize("nup,ndn,norb", [(1, 1, 2), (2, 1, 2), (3, 3, 3), (5, 2, 3)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed", 1e-6)])
+def test_smallest_systems_against_oracle(nup, ndn, norb, prec, tol):
+    """The smallest systems: a 1 x 1 pair matrix, unpaired states with one
+    or two pairs, fewer particles than a warp's tile rows in every stage."""
+    sysd = abi.make_system(configs.system_params(nup, ndn, norb))
+    rund = abi.make_run(configs.run_params(16, 0.002))
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    x = orc.walkers()["x"][:16] + np.random.default_rng(nup + 7 * ndn).normal(scale=0.3, size=(16, nup + ndn, 3))
+    ref = orc.hpsi(x)
+    with capi.Context(sysd, rund, precision=prec) as ctx:
+        got = ctx.hpsi(x)
+        if prec == "fp64":
+            ctx.init_walkers()
+            orc.init_walkers()
+            ctx.initial_eval()
+            orc.initial_eval()
+            for g in range(3):
+                assert ctx.generation(g == 2) == orc.generation(g == 2)
+            wg, wo = ctx.walkers(), orc.walkers()
+            assert np.array_equal(wg["irn"], wo["irn"])
+            assert float(np.max(np.abs(wg["x"] - wo["x"]))) < 1e-10
+    assert np.array_equal(got["is_"], ref["is_"])
+    el_g = -sysd.hbar * got["d2psi"] + got["v"]
+    el_r = -sysd.hbar * ref["d2psi"] + ref["v"]
+    assert rel_each(el_g, el_r) < tol
+    assert rel_each(got["psil"], ref["psil"]) < tol
+    scale = max(1.0, float(np.max(np.abs(ref["dpsi"]))))
+    assert float(np.max(np.abs(got["dpsi"] - ref["dpsi"]))) / scale < tol

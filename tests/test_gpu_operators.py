@@ -36,7 +36,8 @@ def close(a, b, rtol):
 
 @pytest.mark.parametrize("name,nwalk,tabs,same_spin", [("n14", 24, (25, 4, 12), False),
                                                        ("p33_30", 6, (20, 3, 6), False),
-                                                       ("n66", 6, (20, 3, 6), True)])
+                                                       ("n66", 6, (20, 3, 6), True),
+                                                       ("n132", 3, (20, 3, 4), False)])
 def test_operator_pass_matches_oracle(name, nwalk, tabs, same_spin):
     sysd, ctx, orc = run_both(name, nwalk, 2, tabs, same_spin)
     try:
