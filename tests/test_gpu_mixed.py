@@ -49,14 +49,15 @@ def test_mixed_hpsi_against_fp64_oracle(name, nw):
     assert psil_err.max() < 1e-6
 
 
-def test_mixed_generations_track_fp64():
-    """Short DMC runs from the same walkers: the mixed path follows the FP64
-    trajectories (same random streams, same branching; weights and
-    positions differ only by the mixed path's rounding).  The pair matrix is
-    accumulated against a bound of sum_q |v_q|, which leaves drift errors up
-    to ~1e-8 relative for walkers near a node; after four generations the
-    positions agree to 1e-7."""
-    sysd, rund, _ = configs.workload("n66", nwalk=64)
+@pytest.mark.parametrize("idmc", [1, 2, 0, -2])
+def test_mixed_generations_track_fp64(idmc):
+    """Short runs of every run type from the same walkers: the mixed path
+    follows the FP64 trajectories (same random streams, same Metropolis
+    decisions and branching; weights and positions differ only by the mixed
+    path's rounding).  The pair matrix is accumulated against a bound of
+    sum_q |v_q|, which leaves drift errors up to ~1e-8 relative for walkers
+    near a node; after four generations the positions agree to 1e-7."""
+    sysd, rund, _ = configs.workload("n66", nwalk=64, idmc=idmc)
     res = {}
     for prec in ("fp64", "mixed"):
         with capi.Context(sysd, rund, precision=prec) as ctx:
