@@ -17,7 +17,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["dmc_kernels.cu", "dmc_capi.cu", "dmc_setup.cpp", "dmc_noalloc.cu", "dmc_single.cu", "dmc_fort9.cpp", "dmc_ops.cu",
-           "dmc_sweep.cu", "dmc_walker_gf.cu"]
+           "dmc_sweep.cu", "dmc_walker_gf.cu", "dmc_walker_big.cu"]
 
 
 def _nvcc():

@@ -560,16 +560,27 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
         if (L512.total * 8 <= limit && L512.total * 8 + static_smem + 1024 <= smem_sm) c->L = L512;
     }
-    c->grid = c->nsm * per_sm;
-    // the layout without the beta pair data must fit one CTA's shared
-    // memory (the pair matrix, its second buffer and the orbitals stay on
-    // chip): about N = 144 at seven shells
     if ((long long)c->L.total * 8 > (long long)limit) {
-        dmc_destroy(c);
-        return DMC_ERR_UNSUPPORTED;
+        // the orbitals, their powers and the second inverse buffer do not fit
+        // on chip (above about N = 144 at seven shells, N = 120 at ten): the
+        // union region goes to an L2-resident global slice per CTA and only
+        // the pair matrix, positions and accumulators stay in shared memory
+        const int static_big = std::max(0, walker_big_static_smem_bytes());
+        const int limit_big = std::min(optin, 227 * 1024) - 64 - static_big;
+        SmemLayout LB;
+        walker_smem_bytes(c->P, limit_big, &LB, kThreads, true);
+        if ((long long)LB.total * 8 > (long long)limit_big) {
+            dmc_destroy(c);
+            return DMC_ERR_UNSUPPORTED;
+        }
+        c->L = LB;
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+        per_sm = std::max(1, std::min(2, smem_sm / (LB.total * 8 + static_big + 1024)));
     }
-    if (!c->L.pb_in_smem) {
-        e = c->gscratch.alloc((size_t)c->grid * c->L.pb_size);
+    c->grid = c->nsm * per_sm;
+    if (c->L.gstride > 0) {
+        e = c->gscratch.alloc((size_t)c->grid * c->L.gstride);
         if (e != cudaSuccess) {
             dmc_destroy(c);
             return DMC_ERR_NOMEM;

@@ -150,11 +150,19 @@ struct SmemLayout {
     int pb_size;          // doubles of pair data per walker
     int rows_jas, rows_beta;   // rows of the up-down block per reduction chunk
     int rsize;            // doubles in the union region
+    int un_in_smem;       // 0: the union region (U, D, E, S2, pair vectors) lives in
+                          // the CTA's global scratch slice, at offset 0 of it
+    int gstride;          // doubles of global scratch per CTA: the union region
+                          // (when not on chip), then the beta pair data (idem)
 };
 
 __host__ __device__ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
-__host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_limit_bytes, int nt = kThreads)
+// union_global: the union region goes to the CTA's global scratch slice
+// (systems whose orbitals and second inverse buffer do not fit on chip); its
+// offsets keep their values, above every on-chip offset.
+__host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_limit_bytes, int nt = kThreads,
+                                                  bool union_global = false)
 {
     SmemLayout L;
     L.nt = nt;
@@ -189,7 +197,8 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
     const int minrows = 1;
     // at least one row of pair data must fit
     if (rsize < row_pairs * 4) rsize = row_pairs * 4;
-    off += round_up(rsize, 2);
+    L.un_in_smem = union_global ? 0 : 1;
+    if (!union_global) off += round_up(rsize, 2);
     L.rsize = rsize;
     L.rows_jas = rsize / (row_pairs * 3);
     L.rows_beta = rsize / (row_pairs * 4);
@@ -198,7 +207,7 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
     // beta pair data (f'/r, lap f) per up-down pair
     L.pb_size = p.nup * p.ndn * 2;
     const int with_pb = off + round_up(L.pb_size, 2);
-    if (with_pb * 8 <= smem_limit_bytes) {
+    if (!union_global && with_pb * 8 <= smem_limit_bytes) {
         L.pb = off;
         off = with_pb;
         L.pb_in_smem = 1;
@@ -206,6 +215,7 @@ __host__ __device__ inline SmemLayout make_layout(const DevParams& p, int smem_l
         L.pb = -1;
         L.pb_in_smem = 0;
     }
+    L.gstride = (union_global ? round_up(rsize, 2) : 0) + (L.pb_in_smem ? 0 : round_up(L.pb_size, 2));
     L.total = off;
     return L;
 }

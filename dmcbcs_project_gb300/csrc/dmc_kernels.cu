@@ -285,9 +285,9 @@ __global__ void popctl_kernel(const int* pn, double nwalk, double popup, double 
 // host launchers
 // ---------------------------------------------------------------------------
 
-int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int nt)
+int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int nt, bool union_global)
 {
-    SmemLayout L = make_layout(p, limit_bytes, nt);
+    SmemLayout L = make_layout(p, limit_bytes, nt, union_global);
     if (Lout) *Lout = L;
     return L.total * 8;
 }
@@ -352,12 +352,14 @@ static cudaError_t walker_attrs(int smem, int nt, bool both, bool mixed)
 
 cudaError_t prepare_walker(const SmemLayout& L, bool gf)
 {
+    if (!L.un_in_smem) return walker_big_attrs(L.total * 8);
     return gf ? walker_gf_attrs(L.total * 8, L.nt, true, false) : walker_attrs(L.total * 8, L.nt, true, false);
 }
 
 cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                           bool mixed)
 {
+    if (!L.un_in_smem) return launch_walker_big(p, a, L, grid, st, mixed, a.mode == MODE_STEP && p.idmc == 10);
     if (a.mode == MODE_STEP && p.idmc == 10) return launch_walker_gf(p, a, L, grid, st, mixed);
     const size_t smem = (size_t)L.total * 8;
     // the shared-memory opt-in is recorded per device and size (prepare_walker

@@ -9,7 +9,8 @@ namespace dmc {
 
 // Bytes of dynamic shared memory of the walker kernel for these sizes; fills
 // the on-chip layout.  limit_bytes is the per-CTA limit.
-int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int nt = kThreads);
+int walker_smem_bytes(const DevParams& p, int limit_bytes, SmemLayout* Lout, int nt = kThreads,
+                      bool union_global = false);
 // dynamic shared-memory opt-in of both walker kernels for layout L (once,
 // before any graph capture); gf: the idmc = 10 instances (their moves) too
 cudaError_t prepare_walker(const SmemLayout& L, bool gf = false);
@@ -19,6 +20,12 @@ int walker_static_smem_bytes(bool gf = false);
 // the idmc = 10 instances (dmc_walker_gf.cu): static shared memory, the
 // shared-memory opt-in, and the move launch that launch_walker forwards to
 int walker_gf_static_smem_bytes();
+// the instances with the union region in global scratch (dmc_walker_big.cu),
+// launch_walker forwards every launch with L.un_in_smem == 0 to them
+int walker_big_static_smem_bytes();
+cudaError_t walker_big_attrs(int smem);
+cudaError_t launch_walker_big(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
+                              bool mixed, bool gf);
 cudaError_t walker_gf_attrs(int smem, int nt, bool both, bool mixed);
 cudaError_t launch_walker_gf(const DevParams& p, const KernelArgs& a, const SmemLayout& L, int grid, cudaStream_t st,
                              bool mixed);

@@ -260,7 +260,7 @@ __device__ __forceinline__ Lagrange<float> lagrange_f(float t, int idx)
     return L;
 }
 
-template <class R, int NT = kThreads>
+template <class R, int NT = kThreads, bool BIG = false>
 struct Ctx {
     static constexpr int nt = NT;   // threads of the walker CTA
     const DevParams& p;
@@ -268,6 +268,17 @@ struct Ctx {
     const SmemLayout& L;
     double* sm;
     double* pb;
+    double* un;   // BIG: the union region in the CTA's global scratch slice
+    // a region of the union (pair vectors, U, D, E, S2): on chip, or (BIG)
+    // in the global slice at its offset from the union's start
+    template <class T>
+    __device__ __forceinline__ T* uat(int off) const
+    {
+        if constexpr (BIG)
+            return reinterpret_cast<T*>(un + (off - L.R));
+        else
+            return reinterpret_cast<T*>(sm + off);
+    }
 };
 
 // two consecutive values (16-byte aligned) with one shared-memory load
@@ -298,15 +309,15 @@ __device__ __forceinline__ T* at(double* sm, int off) { return reinterpret_cast<
 // Laplacian part: jt[] for the up-down pairs in the Jastrow type, ss[] for
 // the same-spin pairs (FP64 on both paths).
 // ---------------------------------------------------------------------------
-template <class R, int NT>
-__device__ void pair_stage(const Ctx<R, NT>& c, typename Prec<R>::J (&jt)[3], double (&ss)[3])
+template <class R, int NT, bool BIG>
+__device__ void pair_stage(const Ctx<R, NT, BIG>& c, typename Prec<R>::J (&jt)[3], double (&ss)[3])
 {
     using J = typename Prec<R>::J;
     const DevParams& p = c.p;
     double* sm = c.sm;
     const R* x = at<R>(sm, c.L.xr);
     R* S = at<R>(sm, c.L.S);
-    J* pv = at<J>(sm, c.L.R);
+    J* pv = c.template uat<J>(c.L.R);
     R* pb = reinterpret_cast<R*>(c.pb);
     double* du = sm + c.L.acc + 4 * p.npart;
     const int nup = p.nup, ndn = p.ndn, ldS = p.ldS;
@@ -450,7 +461,7 @@ __device__ void pair_stage(const Ctx<R, NT>& c, typename Prec<R>::J (&jt)[3], do
         const double imu = 1.0 / (p.mass[blk] * 0.5);
         const double isq = p.isqm[blk];
         if (n < 2) continue;
-        double* pvd = sm + c.L.R;
+        double* pvd = c.template uat<double>(c.L.R);
         const int rows = max(1, c.L.rsize / (3 * n));
         for (int r0 = 0; r0 < n; r0 += rows) {
             const int r1 = min(n, r0 + rows);
@@ -570,15 +581,15 @@ __device__ __forceinline__ void cmul(df ar, df ai, df br, df bi, df& cr, df& ci)
 // D[j][0] = 1,       D[j][2q-1] = cos(k_q.x_j),     D[j][2q] = sin(k_q.x_j)
 // Then the unpaired plane-wave rows and columns of S (:171-206).
 // ---------------------------------------------------------------------------
-template <class R, int NT>
-__device__ void orbital_stage(const Ctx<R, NT>& c)
+template <class R, int NT, bool BIG>
+__device__ void orbital_stage(const Ctx<R, NT, BIG>& c)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
     const double* x = sm + c.L.x;
-    R* U = at<R>(sm, c.L.U);
-    R* D = at<R>(sm, c.L.D);
-    R* E = at<R>(sm, c.L.E);
+    R* U = c.template uat<R>(c.L.U);
+    R* D = c.template uat<R>(c.L.D);
+    R* E = c.template uat<R>(c.L.E);
     R* S = at<R>(sm, c.L.S);
     const int np1 = p.nmax + 1;
     // powers e^{i m theta_c}, m = 0..nmax, E[(p*3+c)*np1 + m] = (re, im)
@@ -689,14 +700,14 @@ __device__ void orbital_stage(const Ctx<R, NT>& c)
 // of 256 threads at N = 66.  16-byte pair loads over the padded rows (the
 // padding is zero).
 constexpr int kGJ = 5;
-template <class R, int NT>
-__device__ void gemm_stage(const Ctx<R, NT>& c)
+template <class R, int NT, bool BIG>
+__device__ void gemm_stage(const Ctx<R, NT, BIG>& c)
 {
     using Acc = typename AccOf<R>::type;
     const DevParams& p = c.p;
     double* sm = c.sm;
-    const R* U = at<R>(sm, c.L.U);
-    const R* D = at<R>(sm, c.L.D);
+    const R* U = c.template uat<R>(c.L.U);
+    const R* D = c.template uat<R>(c.L.D);
     R* S = at<R>(sm, c.L.S);
     const int ldU = p.ldU;
     const int ng = (p.ndn + kGJ - 1) / kGJ;
@@ -938,13 +949,13 @@ __device__ __forceinline__ R gj_apply(const R* cur, int ld, int i, int j, int k0
     return acc_value(a);
 }
 
-template <class R, int RPL, int B, int NT>
-__device__ bool inverse_blocked(const Ctx<R, NT>& c, double& logdet, int& sgn)
+template <class R, int RPL, int B, int NT, bool BIG>
+__device__ bool inverse_blocked(const Ctx<R, NT, BIG>& c, double& logdet, int& sgn)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
     R* const A0 = at<R>(sm, c.L.S);
-    R* const A1 = at<R>(sm, c.L.S2);
+    R* const A1 = c.template uat<R>(c.L.S2);
     int* piv = reinterpret_cast<int*>(sm + c.L.red + 512);                           // nd ints
     R* pvals = reinterpret_cast<R*>(sm + c.L.red + 512 + 2 * DMC_MAX_PART);          // nd pivots
     int* rowpos = reinterpret_cast<int*>(sm + c.L.red + 512 + 4 * DMC_MAX_PART);     // nd ints
@@ -1087,8 +1098,8 @@ __device__ __forceinline__ int warp_pivot(const R* A, int ld, int n, int k, R& p
     return bi;
 }
 
-template <class R, int NT>
-__device__ bool inverse_unblocked(const Ctx<R, NT>& c, double& logdet, int& sgn)
+template <class R, int NT, bool BIG>
+__device__ bool inverse_unblocked(const Ctx<R, NT, BIG>& c, double& logdet, int& sgn)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1215,8 +1226,8 @@ __device__ bool inverse_unblocked(const Ctx<R, NT>& c, double& logdet, int& sgn)
     return !sing;
 }
 
-template <class R, int NT>
-__device__ bool inverse_stage(const Ctx<R, NT>& c, double& logdet, int& sgn)
+template <class R, int NT, bool BIG>
+__device__ bool inverse_stage(const Ctx<R, NT, BIG>& c, double& logdet, int& sgn)
 {
     const int n = c.p.nd;
     if (c.L.S2 >= 0) {
@@ -1330,14 +1341,14 @@ __device__ __forceinline__ float abs_hi(double v) { return (float)fabs(v); }
 // partial contraction of one (particle, k vector) item over the terms
 // k0, k0 + kstep, ...: G (up particle) or H (down particle) for the cos and
 // sin parts of k vector q (1-based)
-template <class R, int NT>
-__device__ __forceinline__ void drift_dots(const Ctx<R, NT>& c, const float* bound, int pt, int q, int k0, int kstep,
+template <class R, int NT, bool BIG>
+__device__ __forceinline__ void drift_dots(const Ctx<R, NT, BIG>& c, const float* bound, int pt, int q, int k0, int kstep,
                                            R& vc, R& vs)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
-    const R* U = at<R>(sm, c.L.U);
-    const R* D = at<R>(sm, c.L.D);
+    const R* U = c.template uat<R>(c.L.U);
+    const R* D = c.template uat<R>(c.L.D);
     const R* Si = at<R>(sm, c.L.S);
     const R* ks = at<R>(sm, c.L.ksoa);
     const int nk = p.nk, ld = p.ldS, ldU = p.ldU, qc = 2 * q - 2;
@@ -1378,8 +1389,8 @@ __device__ __forceinline__ void drift_dots(const Ctx<R, NT>& c, const float* bou
 
 // the 4 terms (3 drift components, Laplacian) of k vector q (1-based) for
 // particle pt from its contractions vc, vs
-template <class R, int NT>
-__device__ __forceinline__ void drift_terms(const Ctx<R, NT>& c, int pt, int q, R vc, R vs, R (&out)[4])
+template <class R, int NT, bool BIG>
+__device__ __forceinline__ void drift_terms(const Ctx<R, NT, BIG>& c, int pt, int q, R vc, R vs, R (&out)[4])
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1388,12 +1399,12 @@ __device__ __forceinline__ void drift_terms(const Ctx<R, NT>& c, int pt, int q, 
     R t, l;
     if (pt < p.nup) {
         R uc, us;
-        ld2(at<R>(sm, c.L.U) + pt * ldU + qc, uc, us);
+        ld2(c.template uat<R>(c.L.U) + pt * ldU + qc, uc, us);
         t = uc * vs - us * vc;
         l = uc * vc + us * vs;
     } else {
         R dc, ds;
-        ld2(at<R>(sm, c.L.D) + (pt - p.nup) * ldU + qc, dc, ds);
+        ld2(c.template uat<R>(c.L.D) + (pt - p.nup) * ldU + qc, dc, ds);
         t = vs * dc - vc * ds;
         l = vc * dc + vs * ds;
     }
@@ -1409,16 +1420,16 @@ __device__ __forceinline__ void drift_terms(const Ctx<R, NT>& c, int pt, int q, 
 // Sinv rows with U, and in both cases
 //   t = O_c V_s - O_s V_c,  l = O_c V_c + O_s V_s
 // with O the particle's own orbital row and V the contraction.
-template <class R, int NT>
-__device__ __forceinline__ void drift_tile(const Ctx<R, NT>& c, const float* bound, bool down, int blk, int qch, int nqc,
+template <class R, int NT, bool BIG>
+__device__ __forceinline__ void drift_tile(const Ctx<R, NT, BIG>& c, const float* bound, bool down, int blk, int qch, int nqc,
                                            R* pbuf)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
     const R* Si = at<R>(sm, c.L.S);
     const R* ks = at<R>(sm, c.L.ksoa);
-    const R* B = at<R>(sm, down ? c.L.U : c.L.D);     // contraction operand
-    const R* O = at<R>(sm, down ? c.L.D : c.L.U);     // the particles' own orbital rows
+    const R* B = c.template uat<R>(down ? c.L.U : c.L.D);     // contraction operand
+    const R* O = c.template uat<R>(down ? c.L.D : c.L.U);     // the particles' own orbital rows
     const int nq = p.nk - 1, nk = p.nk, ld = p.ldS, ldU = p.ldU;
     const int lane = threadIdx.x & 31, ai = lane & (kTA - 1), bi = lane / kTA;
     const int nK = down ? p.nup : p.ndn;
@@ -1555,8 +1566,8 @@ __device__ __forceinline__ void drift_tile(const Ctx<R, NT>& c, const float* bou
             for (int z = 0; z < 4; ++z) pbuf[((pbase + pi[k]) * nqc + qch) * 4 + z] = ts[k][z];
 }
 
-template <class R, int NT>
-__device__ bool drift_tiled(const Ctx<R, NT>& c, const float* bound)
+template <class R, int NT, bool BIG>
+__device__ bool drift_tiled(const Ctx<R, NT, BIG>& c, const float* bound)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1618,14 +1629,14 @@ __device__ bool drift_tiled(const Ctx<R, NT>& c, const float* bound)
     return true;
 }
 
-template <class R, int NT>
-__device__ void drift_stage(const Ctx<R, NT>& c)
+template <class R, int NT, bool BIG>
+__device__ void drift_stage(const Ctx<R, NT, BIG>& c)
 {
     using KV = typename Prec<R>::KV;
     const DevParams& p = c.p;
     double* sm = c.sm;
-    const R* U = at<R>(sm, c.L.U);
-    const R* D = at<R>(sm, c.L.D);
+    const R* U = c.template uat<R>(c.L.U);
+    const R* D = c.template uat<R>(c.L.D);
     const R* Si = at<R>(sm, c.L.S);
     const R* ks = at<R>(sm, c.L.ksoa);      // kx, ky, kz, k^2, v by k vector
     double* acc = sm + c.L.acc;             // drift [3N], lap [N]
@@ -1783,15 +1794,15 @@ __device__ void drift_stage(const Ctx<R, NT>& c)
 // through :213-222): per up-down pair h = Sinv[j][i] f'/r dx, l = Sinv[j][i]
 // lap f; row sums go to the up particle, column sums (negated drift) to the
 // down particle.  Then the unpaired plane waves.
-template <class R, int NT>
-__device__ void beta_drift_stage(const Ctx<R, NT>& c)
+template <class R, int NT, bool BIG>
+__device__ void beta_drift_stage(const Ctx<R, NT, BIG>& c)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
     const R* xr = at<R>(sm, c.L.xr);
     const double* x = sm + c.L.x;
     const R* Si = at<R>(sm, c.L.S);
-    R* pv = at<R>(sm, c.L.R);
+    R* pv = c.template uat<R>(c.L.R);
     const R* pb = reinterpret_cast<const R*>(c.pb);
     double* acc = sm + c.L.acc;
     const int nup = p.nup, ndn = p.ndn, ld = p.ldS, P = p.npart;
@@ -1890,11 +1901,10 @@ __device__ void beta_drift_stage(const Ctx<R, NT>& c)
 // guide-function gradient is written) and uses the union region for rho_q.
 // ---------------------------------------------------------------------------
 template <int NT>
-__device__ inline void jaslong_stage(const DevParams& p, const KernelArgs& a, const SmemLayout& L, double* sm, double& ul,
-                              double& d2l)
+__device__ inline void jaslong_stage(const DevParams& p, const KernelArgs& a, const SmemLayout& L, double* sm,
+                                     double* rho, double& ul, double& d2l)
 {
     const double* x = sm + L.x;
-    double* rho = sm + L.R;
     double* dl = sm + L.dg;
     const int P = p.npart;
     for (int q = threadIdx.x; q < p.nql; q += NT) {
@@ -1949,8 +1959,8 @@ struct HRes {
 // dpsi in acc[0..3N) and dpsig in sm[L.dg] when a2 != 0.
 // mode MODE_GETPHI stops after the Jastrow; MODE_BCS skips the Jastrow.
 // ---------------------------------------------------------------------------
-template <class R, int NT>
-__device__ HRes hpsi_eval(const Ctx<R, NT>& c, int mode)
+template <class R, int NT, bool BIG>
+__device__ HRes hpsi_eval(const Ctx<R, NT, BIG>& c, int mode)
 {
     const DevParams& p = c.p;
     double* sm = c.sm;
@@ -1992,7 +2002,7 @@ __device__ HRes hpsi_eval(const Ctx<R, NT>& c, int mode)
     // not of getphi or bcs
     const bool jl = p.nql > 0 && (mode == MODE_HPSI || mode == MODE_STEP);
     double ulong = 0.0, d2long = 0.0;
-    if (jl) jaslong_stage<NT>(c.p, c.a, c.L, sm, ulong, d2long);
+    if (jl) jaslong_stage<NT>(c.p, c.a, c.L, sm, c.template uat<double>(c.L.R), ulong, d2long);
     double logdet = 0.0;
     int sgn = 1;
     bool ok = true;

@@ -1,9 +1,11 @@
 // The walker kernel of the GB300 DMCBS path (sm_103a): one DMC/VMC move plus
 // the full wavefunction and local energy of a walker per CTA, persistent
 // CTAs, and the scalar step decision (step.f90:59-279).  Included by
-// dmc_kernels.cu (the kernels of every idmc but 10) and dmc_walker_gf.cu
-// (GF = true: idmc = 10, two wavefunction evaluations per move), so that the
-// second evaluation costs the other kernels no registers.
+// dmc_kernels.cu (the kernels of every idmc but 10), dmc_walker_gf.cu
+// (GF = true: idmc = 10, two wavefunction evaluations per move, so that the
+// second evaluation costs the other kernels no registers) and
+// dmc_walker_big.cu (BIG = true: the union region of the layout in the CTA's
+// global scratch slice, for systems whose orbitals do not fit on chip).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -199,7 +201,7 @@ __device__ inline void step_decision(const DevParams& p, int opcomp, const StepS
 // ---------------------------------------------------------------------------
 // The walker kernel: persistent CTAs, one walker per CTA per iteration.
 // ---------------------------------------------------------------------------
-template <class R, int NT, bool GF>
+template <class R, int NT, bool GF, bool BIG = false>
 __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1)
 walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ KernelArgs a, SmemLayout L)
 {
@@ -221,8 +223,11 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
             for (int cc = 0; cc < 3; ++cc) kn[cc * p.nk + q] = kg[q].n[cc];
         }
     }
-    double* pb = L.pb_in_smem ? sm + L.pb : a.gscratch + (size_t)blockIdx.x * L.pb_size;
-    Ctx<R, NT> c{p, a, L, sm, pb};
+    // the CTA's global scratch slice: the union region when it is not on
+    // chip (BIG), then the beta pair data when they are not on chip
+    double* gs = a.gscratch ? a.gscratch + (size_t)blockIdx.x * L.gstride : nullptr;
+    double* pb = L.pb_in_smem ? sm + L.pb : gs + (L.un_in_smem ? 0 : round_up(L.rsize, 2));
+    Ctx<R, NT, BIG> c{p, a, L, sm, pb, BIG ? gs : nullptr};
     __shared__ double s_old[9];
     __syncthreads();
     const int nw = a.pn ? *a.pn : a.nw;   // the population is counted on the device in a generation

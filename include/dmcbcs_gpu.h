@@ -38,9 +38,10 @@ extern "C" {
 
 #define DMC_MAX_SHELLS 32     /* s-wave pairing shells (norb) */
 #define DMC_MAX_UNPAIRED 16   /* unpaired plane-wave states per spin */
-#define DMC_MAX_PART 256      /* particles per system (the walker kernel's on-chip layout bounds it
-                                 further: dmc_create returns DMC_ERR_UNSUPPORTED above about
-                                 N = 144 at seven shells) */
+#define DMC_MAX_PART 256      /* particles per system; above about N = 144 at seven shells
+                                 the walker's orbitals live in global scratch, and
+                                 dmc_create returns DMC_ERR_UNSUPPORTED only when the
+                                 pair matrix and k records do not fit one CTA */
 #define DMC_NEST_MAX 16       /* estimators (14 for DMC, 13 for idmc=2, 6 for VMC) */
 #define DMC_WTISTO 500        /* multiplicity histogram bins (step.f90:9) */
 #define DMC_MINUSHUGE (-1.0e30) /* log|det| of a singular matrix (matrixlapack.f90:19) */

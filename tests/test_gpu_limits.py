@@ -1,12 +1,14 @@
 """Size limits of the walker path.
 
 The walker kernel keeps the pair matrix, its second inverse buffer and the
-orbitals of one walker in shared memory, so the largest system is set by
-what fits one CTA: about N = 144 at seven shells (K = 81).  The largest
-system well inside that bound (70 up / 70 down) must still match the oracle
-(FP64 to 1e-10, mixed to 1e-6, generations with identical streams);
-a system beyond it is refused with DMC_ERR_UNSUPPORTED at creation, before
-any launch; a single walker runs generations like any population.
+orbitals of one walker in shared memory up to about N = 144 at seven shells
+(K = 81); above that the orbitals, their powers and the second buffer move
+to an L2-resident global slice per CTA.  Both sides of the bound (70/70 on
+chip, 80/80 at seven shells and 66/66 and 128/128 at ten with the slice)
+must match the oracle (FP64 to 1e-10, mixed to 1e-6, generations with
+identical streams); a system whose pair matrix and records do not fit even
+then is refused with DMC_ERR_UNSUPPORTED at creation, before any launch;
+the smallest systems and a single walker run like any other.
 """
 import numpy as np
 import pytest
@@ -63,9 +65,56 @@ def test_largest_layout_generations():
     assert rel_each(wg["weight"], wo["weight"]) < 1e-10
 
 
-@pytest.mark.parametrize("nup,norb", [(80, 7), (128, 7), (66, 12)])
-def test_layout_beyond_one_cta_is_unsupported(nup, norb):
-    sysd, rund = system(nup, nup, norb)
+@pytest.mark.parametrize("nup,norb,prec,tol", [(80, 7, "fp64", 1e-10), (80, 7, "mixed", 1e-6),
+                                               (66, 10, "fp64", 1e-10), (66, 10, "mixed", 1e-6),
+                                               (128, 10, "fp64", 1e-10), (128, 10, "mixed", 1e-6)])
+def test_union_in_global_scratch_against_oracle(nup, norb, prec, tol):
+    """Systems whose orbitals and second inverse buffer do not fit one CTA
+    (N = 160 at seven shells, N = 132 and 256 at the production decks' ten
+    shells) run with that region in an L2-resident global slice per CTA.
+    (128 pairs need more than the 81 pair-function columns of seven shells:
+    there the pair matrix is nearly singular and no two implementations
+    agree to 1e-10.)"""
+    sysd, rund = system(nup, nup, norb, nwalk=4)
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    x = orc.walkers()["x"][:4] + np.random.default_rng(nup + norb).normal(scale=0.3, size=(4, 2 * nup, 3))
+    ref = orc.hpsi(x)
+    with capi.Context(sysd, rund, precision=prec) as ctx:
+        got = ctx.hpsi(x)
+        held = ctx.info.device_bytes
+    el_g = -sysd.hbar * got["d2psi"] + got["v"]
+    el_r = -sysd.hbar * ref["d2psi"] + ref["v"]
+    print(f"N = {2 * nup}, {norb} shells {prec}: E_L rel err {rel_each(el_g, el_r):.2e}, "
+          f"device memory {held / 2**20:.0f} MiB")
+    assert np.array_equal(got["is_"], ref["is_"])
+    assert rel_each(el_g, el_r) < tol
+    assert rel_each(got["psil"], ref["psil"]) < tol
+    for w in range(4):
+        scale = max(1.0, float(np.max(np.abs(ref["dpsi"][w]))))
+        assert float(np.max(np.abs(got["dpsi"][w] - ref["dpsi"][w]))) / scale < tol
+
+
+def test_union_in_global_scratch_generations():
+    sysd, rund = system(80, 80, 7, nwalk=8)
+    orc = oracle.Oracle(sysd, rund)
+    with capi.Context(sysd, rund) as ctx:
+        ctx.init_walkers()
+        orc.init_walkers()
+        ctx.initial_eval()
+        orc.initial_eval()
+        for g in range(2):
+            assert ctx.generation(g == 1) == orc.generation(g == 1)
+        wg, wo = ctx.walkers(), orc.walkers()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    assert float(np.max(np.abs(wg["x"] - wo["x"]))) < 1e-9
+    assert rel_each(wg["weight"], wo["weight"]) < 1e-10
+
+
+def test_layout_beyond_one_cta_is_unsupported():
+    """Even with the union region off chip, the pair matrix, positions and
+    k-vector records must fit: 128/128 at 32 shells does not."""
+    sysd, rund = system(128, 128, 32)
     with pytest.raises(capi.DMCError) as err:
         capi.Context(sysd, rund)
     assert err.value.status == abi.DMC_ERR_UNSUPPORTED
