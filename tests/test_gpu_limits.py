@@ -165,3 +165,79 @@ def test_smallest_systems_against_oracle(nup, ndn, norb, prec, tol):
     assert rel_each(got["psil"], ref["psil"]) < tol
     scale = max(1.0, float(np.max(np.abs(ref["dpsi"]))))
     assert float(np.max(np.abs(got["dpsi"] - ref["dpsi"]))) / scale < tol
+
+
+def _fd_relative(sysd, rund, x, eps):
+    """Central differences of log|Psi| and E_L with a step relative to each
+    parameter (vorb(1..norb), bfact, b, d): the high-shell amplitudes are
+    small, and an absolute step of 1e-5 moves them by ~1 % at N = 160."""
+    norb = int(sysd.norb)
+    theta = list(sysd.vorb[:norb]) + [sysd.bfact, sysd.bbeta, sysd.dbeta]
+    dl = np.zeros((x.shape[0], len(theta)))
+    de = np.zeros_like(dl)
+    base = oracle.Oracle(sysd, rund)
+    for k, t in enumerate(theta):
+        h = eps * max(abs(t), 1e-3)
+        vals = []
+        for sgn in (1.0, -1.0):
+            if k < norb:
+                v = np.array(theta[:norb])
+                v[k] += sgn * h
+                base.set_vorb(v)
+                vals.append(base.hpsi(x))
+                base.set_vorb(np.array(theta[:norb]))
+            else:
+                s2 = type(sysd).from_buffer_copy(sysd)
+                field = ("bfact", "bbeta", "dbeta")[k - norb]
+                setattr(s2, field, getattr(sysd, field) + sgn * h)
+                vals.append(oracle.Oracle(s2, rund).hpsi(x))
+        dl[:, k] = (vals[0]["psil"] - vals[1]["psil"]) / (2 * h)
+        e0 = -sysd.hbar * vals[0]["d2psi"] + vals[0]["v"]
+        e1 = -sysd.hbar * vals[1]["d2psi"] + vals[1]["v"]
+        de[:, k] = (e0 - e1) / (2 * h)
+    return dl, de
+
+
+def test_union_in_global_scratch_gradients_and_sweeps():
+    """The entry points with layouts of their own at N = 160: the adjoint
+    gradients (their scratch then spills from shared memory to global
+    memory) against the oracle's analytic d log|det| / d vorb (getderbcs)
+    and extrapolated central differences with relative steps, and the
+    particle-by-particle sweeps against the oracle's exact ratios."""
+    from test_gpu_pgrad import rel_err
+
+    sysd, rund = system(80, 80, 10, nwalk=8, idmc=0)
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    x = orc.walkers()["x"][:2] + np.random.default_rng(12).normal(scale=0.3, size=(2, 160, 3))
+    with capi.Context(sysd, rund) as ctx:
+        dl, de = ctx.param_grad(x)
+    norb = int(sysd.norb)
+    od = np.array([orc.getderbcs(x[w]) for w in range(2)])
+    assert np.max(np.abs(dl[:, :norb] - od)) < 1e-9 * np.max(np.abs(od))
+    l1, e1 = _fd_relative(sysd, rund, x, 1e-4)
+    l2, e2 = _fd_relative(sysd, rund, x, 5e-5)
+    fl, fe = (4 * l2 - l1) / 3, (4 * e2 - e1) / 3
+    print(f"N = 160 ({dl.shape[1]} parameters): d log Psi rel err {rel_err(dl, fl):.2e}, "
+          f"d E_L rel err {rel_err(de, fe):.2e}")
+    assert rel_err(dl, fl) < 1e-6 and rel_err(de, fe) < 1e-6
+    ctx = capi.Context(sysd, rund)
+    orc = oracle.Oracle(sysd, rund)
+    try:
+        for c in (ctx, orc):
+            c.init_walkers()
+            c.initial_eval()
+        acc, moves = ctx.sm_sweeps(1, recompute_every=16)
+        acc_o = orc.sm_sweeps(1)
+        wg, wo = ctx.walkers(), orc.walkers()
+    finally:
+        ctx.close()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    same = [float(np.max(np.abs(wg["x"][w] - wo["x"][w]))) < 1e-10 for w in range(8)]
+    print(f"N = 160 sweeps: accepted {acc}/{moves} (oracle {acc_o}), on the oracle's path {sum(same)}/8")
+    # the pair matrices here have |S^-1| ~ 3e3, so the FP32 ratios flip more
+    # Metropolis decisions against the oracle's FP64 ratios than at N = 66;
+    # every walker's state must still be that of its own positions
+    assert sum(same) >= 4 and abs(acc - acc_o) < 0.02 * moves
+    ref = orc.hpsi(wg["x"])
+    assert rel_each(wg["psil"], ref["psil"]) < 1e-9
