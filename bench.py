@@ -584,6 +584,12 @@ def run_gpu(args):
             t = time_path(cx, sub_args, world, local, barrier)
             sub[prec] = {"value": t["value"], "ms_per_step": t["ms_per_step"], "avg_walkers": t["avg_n"],
                          "clocks": t["clocks"]}
+            # the layout tuner on the same context (dmc_tune_layout), then the
+            # same generations again with the layout it keeps
+            kind, _ = cx.tune_layout(3)
+            tt = time_path(cx, sub_args, world, local, barrier)
+            sub[prec]["tuned_layout"] = {"kind": ["heuristic", "on-chip 256 threads", "union in global scratch"][kind],
+                                         "value": tt["value"], "ms_per_step": tt["ms_per_step"]}
             cs[prec] = cx
         out = {"workload": workload, "walkers": 8192, "steps": args.n132_steps, "unit": UNIT,
                "mixed": sub["mixed"], "fp64": sub["fp64"], "speedup_vs_fp64": sub["mixed"]["value"] / sub["fp64"]["value"],

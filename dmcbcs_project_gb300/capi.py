@@ -21,6 +21,7 @@ EXPORTS = [
     "dmc_abi_version", "dmc_status_string", "dmc_last_error", "dmc_create", "dmc_destroy", "dmc_get_info",
     "dmc_get_table", "dmc_set_vorb", "dmc_hpsi_batch", "dmc_hpsi_device", "dmc_bcs_batch", "dmc_getphi_batch",
     "dmc_matinv_batch", "dmc_bcsone_batch", "dmc_getphione_batch", "dmc_getderbcs_batch", "dmc_init_walkers",
+    "dmc_tune_layout",
     "dmc_load_walkers", "dmc_get_walkers", "dmc_initial_eval", "dmc_num_walkers", "dmc_step", "dmc_branch",
     "dmc_generation", "dmc_zero_estimators", "dmc_get_estimators", "dmc_block_update", "dmc_get_wtisto",
     "dmc_last_step_ms", "dmc_timed_generations", "dmc_put_walkers", "dmc_branch_noalloc",
@@ -91,6 +92,7 @@ def load(path=LIB_PATH):
     L.dmc_step.argtypes = [vp, C.c_int]
     L.dmc_branch.argtypes = [vp, C.c_double]
     L.dmc_generation.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    L.dmc_tune_layout.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     L.dmc_zero_estimators.argtypes = [vp]
     L.dmc_get_estimators.argtypes = [vp, _dp, _dp, _dp]
     L.dmc_block_update.argtypes = [vp, _dp, _dp]
@@ -518,6 +520,13 @@ class Context:
         h = np.zeros(DMC_WTISTO, np.int64)
         self._check(load().dmc_get_wtisto(self._h, h))
         return h
+
+    def tune_layout(self, passes=3):
+        """dmc_tune_layout: time the candidate walker layouts on the current
+        walkers and keep the fastest; returns (kind, ms per evaluation)."""
+        k, ms = C.c_int(), C.c_double()
+        self._check(load().dmc_tune_layout(self._h, int(passes), C.byref(k), C.byref(ms)))
+        return k.value, ms.value
 
     def timed_generations(self, ngen, opcomp_last=True, flush_l2=True):
         """Run ngen generations; returns (walker_steps, device_ms, kernel_launches)."""

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -157,6 +158,8 @@ struct dmc_ctx {
     DevParams gP;
     KernelArgs gA;
     int gprec = -1;
+    int layout_gen = 0;     // bumped by every change of the walker layout
+    int glayout = -1;       // the layout_gen the captured generations saw
     DevBuf<double> est;
     DevBuf<int> counts, offs, status;
     DevBuf<int> wstat;      // per-walker flags of the last batched evaluation
@@ -489,6 +492,86 @@ const char* dmc_status_string(int s)
     return "unknown status";
 }
 
+// Walker layouts a context can run (threads per CTA, CTAs per SM, what stays
+// on chip).  LAYOUT_HEURISTIC: on chip, two CTAs per SM when they fit (with
+// the beta pair data moved to global scratch if that makes them fit), else
+// one CTA with 16 warps for the mixed kernel; the union region off chip only
+// when nothing else fits.  The others are the alternatives the layout tuner
+// times: on chip with 256 threads throughout, and the union region in global
+// scratch at the CTAs per SM its smaller on-chip part allows.
+enum { LAYOUT_HEURISTIC = 0, LAYOUT_ONCHIP_256 = 1, LAYOUT_UNION_GLOBAL = 2, LAYOUT_KINDS = 3 };
+
+static int plan_layout(dmc_ctx* c, int optin, int kind, SmemLayout* Lout, int* per_sm_out)
+{
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+    const int regs_ok = 2;   // launch bounds give <= 128 registers at 256 threads
+    if (kind != LAYOUT_UNION_GLOBAL) {
+        // dynamic + static shared memory + the 1 KB the runtime reserves per block
+        const int static_smem = std::max(0, walker_static_smem_bytes(c->rd.idmc == 10));
+        const int limit = std::min(optin, 227 * 1024) - 64 - static_smem;
+        SmemLayout L;
+        walker_smem_bytes(c->P, limit, &L);
+        const int need = L.total * 8 + static_smem + 1024;
+        int per_sm = std::max(1, std::min(regs_ok, smem_sm / need));
+        if (per_sm < regs_ok) {
+            // two CTAs per SM when the beta pair data move to global scratch
+            // (L2-resident, written by the pair stage and read once by the
+            // beta drift terms) and the rest of the layout fits twice
+            SmemLayout L2;
+            walker_smem_bytes(c->P, smem_sm / regs_ok - static_smem - 1024, &L2);
+            if (L2.total * 8 + static_smem + 1024 <= smem_sm / regs_ok) {
+                L = L2;
+                per_sm = regs_ok;
+            }
+        }
+        if (per_sm == 1 && kind == LAYOUT_HEURISTIC) {
+            // one CTA per SM: twice the threads (16 warps) on the same walker
+            // in the mixed kernel, with the larger reduction buffer they need,
+            // when that still fits (N = 132: 578k -> 719k walker-steps/s; the
+            // FP64 kernel keeps 256 threads, the buffer is simply larger than
+            // it needs)
+            SmemLayout L512;
+            walker_smem_bytes(c->P, limit, &L512, 2 * kThreads);
+            if (L512.total * 8 <= limit && L512.total * 8 + static_smem + 1024 <= smem_sm) L = L512;
+        }
+        if ((long long)L.total * 8 <= (long long)limit) {
+            *Lout = L;
+            *per_sm_out = per_sm;
+            return DMC_OK;
+        }
+        if (kind != LAYOUT_HEURISTIC) return DMC_ERR_UNSUPPORTED;
+        // the orbitals, their powers and the second inverse buffer do not fit
+        // on chip (above about N = 144 at seven shells, N = 120 at ten)
+    }
+    // the union region in an L2-resident global slice per CTA; the pair
+    // matrix, positions and accumulators stay in shared memory
+    const int static_big = std::max(0, walker_big_static_smem_bytes());
+    const int limit_big = std::min(optin, 227 * 1024) - 64 - static_big;
+    SmemLayout LB;
+    walker_smem_bytes(c->P, limit_big, &LB, kThreads, true);
+    if ((long long)LB.total * 8 > (long long)limit_big) return DMC_ERR_UNSUPPORTED;
+    *Lout = LB;
+    *per_sm_out = std::max(1, std::min(regs_ok, smem_sm / (LB.total * 8 + static_big + 1024)));
+    return DMC_OK;
+}
+
+// Make L the context's layout: grid, global scratch, kernel attributes; the
+// captured generations of the old layout are dropped at their next use.
+static int apply_layout(dmc_ctx* c, const SmemLayout& L, int per_sm)
+{
+    const int grid = c->nsm * per_sm;
+    if (L.gstride > 0 && c->gscratch.alloc((size_t)grid * L.gstride) != cudaSuccess)
+        return fail(c, DMC_ERR_NOMEM, "walker scratch");
+    cudaError_t e = prepare_walker(L);
+    if (e == cudaSuccess && c->rd.idmc == 10) e = prepare_walker(L, true);
+    if (e != cudaSuccess) return fail(c, DMC_ERR_CUDA, std::string("walker layout: ") + cudaGetErrorString(e));
+    c->L = L;
+    c->grid = grid;
+    ++c->layout_gen;
+    return DMC_OK;
+}
+
 const char* dmc_last_error(const dmc_ctx* c) { return c ? c->err.c_str() : "no context"; }
 
 int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
@@ -525,65 +608,14 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
         dmc_destroy(c);
         return DMC_ERR_CUDA;
     }
-    // on-chip layout; two walker CTAs per SM when they fit (dynamic + static
-    // shared memory + the 1 KB the runtime reserves per block)
-    const int static_smem = std::max(0, walker_static_smem_bytes(c->rd.idmc == 10));
-    const int limit = std::min(optin, 227 * 1024) - 64 - static_smem;
-    walker_smem_bytes(c->P, limit, &c->L);
-    int per_sm = 1;
     {
-        int regs_ok = 2;   // launch bounds give <= 128 registers at 256 threads
-        int smem_sm = 0;
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
-        const int need = c->L.total * 8 + static_smem + 1024;
-        per_sm = std::max(1, std::min(regs_ok, smem_sm / need));
-        if (per_sm < regs_ok) {
-            // two CTAs per SM when the beta pair data move to global scratch
-            // (L2-resident, written by the pair stage and read once by the
-            // beta drift terms) and the rest of the layout fits twice
-            SmemLayout L2;
-            walker_smem_bytes(c->P, smem_sm / regs_ok - static_smem - 1024, &L2);
-            if (L2.total * 8 + static_smem + 1024 <= smem_sm / regs_ok) {
-                c->L = L2;
-                per_sm = regs_ok;
-            }
-        }
-    }
-    if (per_sm == 1) {
-        // one CTA per SM: twice the threads (16 warps) on the same walker in
-        // the mixed kernel, with the larger reduction buffer they need, when
-        // that still fits (N = 132: 578k -> 719k walker-steps/s; the FP64
-        // kernel keeps 256 threads, the buffer is simply larger than it needs)
-        SmemLayout L512;
-        walker_smem_bytes(c->P, limit, &L512, 2 * kThreads);
-        int smem_sm = 0;
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
-        if (L512.total * 8 <= limit && L512.total * 8 + static_smem + 1024 <= smem_sm) c->L = L512;
-    }
-    if ((long long)c->L.total * 8 > (long long)limit) {
-        // the orbitals, their powers and the second inverse buffer do not fit
-        // on chip (above about N = 144 at seven shells, N = 120 at ten): the
-        // union region goes to an L2-resident global slice per CTA and only
-        // the pair matrix, positions and accumulators stay in shared memory
-        const int static_big = std::max(0, walker_big_static_smem_bytes());
-        const int limit_big = std::min(optin, 227 * 1024) - 64 - static_big;
-        SmemLayout LB;
-        walker_smem_bytes(c->P, limit_big, &LB, kThreads, true);
-        if ((long long)LB.total * 8 > (long long)limit_big) {
+        SmemLayout L;
+        int per_sm = 1;
+        int rc2 = plan_layout(c, optin, LAYOUT_HEURISTIC, &L, &per_sm);
+        if (rc2 == DMC_OK) rc2 = apply_layout(c, L, per_sm);
+        if (rc2 != DMC_OK) {
             dmc_destroy(c);
-            return DMC_ERR_UNSUPPORTED;
-        }
-        c->L = LB;
-        int smem_sm = 0;
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
-        per_sm = std::max(1, std::min(2, smem_sm / (LB.total * 8 + static_big + 1024)));
-    }
-    c->grid = c->nsm * per_sm;
-    if (c->L.gstride > 0) {
-        e = c->gscratch.alloc((size_t)c->grid * c->L.gstride);
-        if (e != cudaSuccess) {
-            dmc_destroy(c);
-            return DMC_ERR_NOMEM;
+            return rc2;
         }
     }
     const double stmax = rd->stmax > 0.0 ? rd->stmax : 10.0;
@@ -608,9 +640,7 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     cudaMemset(c->status.p, 0, sizeof(int));
     cudaMemset(c->pop.p, 0, 4 * sizeof(int));
     cudaMemset(c->psteps.p, 0, sizeof(unsigned long long));
-    e = prepare_walker(c->L);
-    if (e == cudaSuccess && c->rd.idmc == 10) e = prepare_walker(c->L, true);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         dmc_destroy(c);
         return DMC_ERR_CUDA;
@@ -1280,7 +1310,7 @@ static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch, const DevStack* in_ho
 static void check_graphs(dmc_ctx* c)
 {
     const KernelArgs A = base_args(c);
-    if (c->gprec == c->precision && std::memcmp(&c->gP, &c->P, sizeof c->P) == 0 &&
+    if (c->gprec == c->precision && c->glayout == c->layout_gen && std::memcmp(&c->gP, &c->P, sizeof c->P) == 0 &&
         std::memcmp(&c->gA, &A, sizeof A) == 0)
         return;
     for (auto& a : c->gexec)
@@ -1293,6 +1323,7 @@ static void check_graphs(dmc_ctx* c)
     std::memcpy(&c->gP, &c->P, sizeof c->P);
     std::memcpy(&c->gA, &A, sizeof A);
     c->gprec = c->precision;
+    c->glayout = c->layout_gen;
 }
 
 // One generation as a captured graph, one per (opcomp, stack parity,
@@ -1331,6 +1362,59 @@ static int gen_graph(dmc_ctx* c, int opcomp, int* nlaunch)
     advance_parities(c);
     c->launches += c->gnl[op][pi][pc];
     if (nlaunch) *nlaunch = c->gnl[op][pi][pc];
+    return DMC_OK;
+}
+
+int dmc_tune_layout(dmc_ctx* c, int passes, int* kind_out, double* ms_out)
+{
+    if (!c || passes < 1) return DMC_ERR_INVALID;
+    int rc = sync_n(c);
+    if (rc) return rc;
+    if (c->n == 0) return fail(c, DMC_ERR_EMPTY, "no walkers to time the layouts on");
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    double best = 0.0;
+    int best_kind = -1, best_psm = 1;
+    SmemLayout bestL{};
+    std::vector<std::array<int, 4>> seen;   // (threads, CTAs per SM, union on chip, beta data on chip)
+    for (int kind = 0; kind < LAYOUT_KINDS; ++kind) {
+        SmemLayout L;
+        int psm = 1;
+        if (plan_layout(c, optin, kind, &L, &psm) != DMC_OK) continue;
+        const std::array<int, 4> key{L.nt, psm, L.un_in_smem, L.pb_in_smem};
+        if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+        seen.push_back(key);
+        rc = apply_layout(c, L, psm);
+        if (rc) return rc;
+        // one wavefunction evaluation of the current walkers per pass (the
+        // walker state does not change), after one untimed pass
+        KernelArgs a = base_args(c);
+        a.mode = MODE_HPSI;
+        a.nw = c->n;
+        a.xin = c->st[c->istin].x.p;
+        a.status = nullptr;
+        const bool mixed = c->precision == DMC_PREC_MIXED;
+        CK(launch_walker(c->P, a, c->L, c->grid, c->stream, mixed));
+        CK(cudaEventRecord(c->ev0, c->stream));
+        for (int i = 0; i < passes; ++i) CK(launch_walker(c->P, a, c->L, c->grid, c->stream, mixed));
+        CK(cudaEventRecord(c->ev1, c->stream));
+        CK(cudaEventSynchronize(c->ev1));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        const double per = ms / passes;
+        if (best_kind < 0 || per < best) {
+            best = per;
+            best_kind = kind;
+            bestL = L;
+            best_psm = psm;
+        }
+    }
+    if (best_kind < 0) return fail(c, DMC_ERR_UNSUPPORTED, "no walker layout fits");
+    rc = apply_layout(c, bestL, best_psm);
+    if (rc) return rc;
+    if (kind_out) *kind_out = best_kind;
+    if (ms_out) *ms_out = best;
     return DMC_OK;
 }
 
@@ -2422,7 +2506,7 @@ struct dmc_batch {
     std::map<uint64_t, Graph> graphs;
     std::vector<DevParams> gP;
     std::vector<KernelArgs> gA;
-    std::vector<int> gprec, ggrid;
+    std::vector<int> gprec, ggrid, glayout;
     DevBuf<unsigned char> flush;
     std::string err;
 };
@@ -2695,6 +2779,7 @@ int dmc_batch_tune(dmc_batch* b, int rounds, int* grids, double* ms)
         CKB(cudaStreamSynchronize(c->stream));
     }
     std::vector<int> nw(ns), psm(ns), mg(ns), full(ns);
+    for (int s = 0; s < ns; ++s) b->grid[s] = std::max(1, std::min(b->grid[s], b->sys[s]->grid));
     for (int s = 0; s < ns; ++s) {
         const dmc_ctx* c = b->sys[s];
         nw[s] = c->n;
@@ -2773,26 +2858,31 @@ int dmc_batch_generations(dmc_batch* b, int ngen, int opcomp_last, int flush_l2,
         const size_t fb = std::max<size_t>((size_t)2 * l2, 64u << 20);
         CKB(b->flush.alloc(fb));
     }
+    // a system's own layout may have changed (dmc_tune_layout): never more
+    // CTAs than its grid, whose global scratch slices exist
+    for (int s = 0; s < ns; ++s) b->grid[s] = std::max(1, std::min(b->grid[s], b->sys[s]->grid));
     // drop the captured generations when anything they baked in changed
     {
         bool same = (int)b->gP.size() == ns && b->ggrid == b->grid;
         for (int s = 0; s < ns && same; ++s) {
             dmc_ctx* c = b->sys[s];
             const KernelArgs A = base_args(c);
-            same = b->gprec[s] == c->precision && std::memcmp(&b->gP[s], &c->P, sizeof c->P) == 0 &&
-                   std::memcmp(&b->gA[s], &A, sizeof A) == 0;
+            same = b->gprec[s] == c->precision && b->glayout[s] == c->layout_gen &&
+                   std::memcmp(&b->gP[s], &c->P, sizeof c->P) == 0 && std::memcmp(&b->gA[s], &A, sizeof A) == 0;
         }
         if (!same) {
             drop_graphs(b);
             b->gP.resize(ns);
             b->gA.resize(ns);
             b->gprec.resize(ns);
+            b->glayout.resize(ns);
             for (int s = 0; s < ns; ++s) {
                 dmc_ctx* c = b->sys[s];
                 const KernelArgs A = base_args(c);
                 std::memcpy(&b->gP[s], &c->P, sizeof c->P);
                 std::memcpy(&b->gA[s], &A, sizeof A);
                 b->gprec[s] = c->precision;
+                b->glayout[s] = c->layout_gen;
             }
             b->ggrid = b->grid;
         }

@@ -448,6 +448,20 @@ int dmc_step(dmc_ctx* ctx, int opcomp);
  * weight*factor. */
 int dmc_branch(dmc_ctx* ctx, double factor);
 
+/* No counterpart in the reference: chooses the context's walker layout by
+ * timing.  The candidates are the layout dmc_create picks (shared memory
+ * for everything that fits, two CTAs per SM when they fit, else one CTA
+ * with 16 warps for the mixed kernel), the same on chip with 256 threads
+ * throughout, and the union region (orbitals, their powers, the second
+ * inverse buffer, pair vectors) in an L2-resident global slice per CTA;
+ * each is timed over `passes` wavefunction evaluations of the current
+ * walkers (which do not change) and the fastest is kept.  kind_out: 0, 1 or
+ * 2 in that order; ms_out: milliseconds per evaluation.  Captured
+ * generations of the old layout are dropped (also those of a batch holding
+ * the context, at its next call).  Results change only by the rounding of
+ * the thread count's reduction order. */
+int dmc_tune_layout(dmc_ctx* ctx, int passes, int* kind_out, double* ms_out);
+
 /* Replaces one generation of dmcbcs.f90:436-448: step1, branch (DMC),
  * drastic population control; returns the population in *nt. */
 int dmc_generation(dmc_ctx* ctx, int opcomp, int* nt);
