@@ -98,3 +98,27 @@ def test_mixed_pair_within_fp32_ulp_of_half_box(rel):
     err = np.abs(el_g - el_r) / np.maximum(np.abs(el_r), 1.0)
     print(f"rel {rel:+.1e}: max rel err E_L {err.max():.2e}")
     assert err.max() < EL_TOL
+
+
+@pytest.mark.parametrize("name", ["n14", "n66", "p33_30"])
+def test_mixed_bcs_and_getphi_against_oracle(name):
+    """The determinant alone (dmc_bcs_batch, bcs) and the Jastrow with the
+    potential alone (dmc_getphi_batch, getphi) from a mixed context: the
+    same bars as hpsi (1e-6), the inverse within 1e-6 of its largest entry."""
+    sysd, rund, orc, x = walkers(name, 16, 41)
+    rb = orc.bcs(x, want_inverse=True)
+    with capi.Context(sysd, rund, precision="mixed") as ctx:
+        gb = ctx.bcs(x, want_inverse=True)
+        gj = ctx.getphi(x)
+    assert np.array_equal(gb["is_"], rb["is_"])
+    assert np.max(np.abs(gb["phil"] - rb["phil"])) < 1e-6
+    lap = np.abs(gb["d2phi"] - rb["d2phi"]) / np.maximum(np.abs(rb["d2phi"]), 1.0)
+    assert lap.max() < EL_TOL
+    for w in range(16):
+        assert np.max(np.abs(gb["dphi"][w] - rb["dphi"][w])) < EL_TOL * max(1.0, np.max(np.abs(rb["dphi"][w])))
+        assert np.max(np.abs(gb["smati"][w] - rb["smati"][w])) < 1e-6 * np.max(np.abs(rb["smati"][w]))
+        r = orc.getphi(x[w])
+        assert abs(gj["u"][w] - r["u"]) < EL_TOL * max(1.0, abs(r["u"]))
+        assert abs(gj["d2u"][w] - r["d2u"]) < EL_TOL * max(1.0, abs(r["d2u"]))
+        assert abs(gj["v"][w] - r["v"]) < EL_TOL * max(1.0, abs(r["v"]))
+        assert np.max(np.abs(gj["du"][w] - r["du"])) < EL_TOL * max(1.0, np.max(np.abs(r["du"])))
