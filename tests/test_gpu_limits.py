@@ -241,3 +241,26 @@ def test_union_in_global_scratch_gradients_and_sweeps():
     assert sum(same) >= 4 and abs(acc - acc_o) < 0.02 * moves
     ref = orc.hpsi(wg["x"])
     assert rel_each(wg["psil"], ref["psil"]) < 1e-9
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_union_in_global_scratch_two_point_moves(prec):
+    """idmc = 10 (two wavefunction evaluations per move) with the union
+    region in global scratch: the GF and BIG kernel instance together."""
+    sysd, rund = system(80, 80, 10, nwalk=8, idmc=10)
+    orc = oracle.Oracle(sysd, rund)
+    with capi.Context(sysd, rund, precision=prec) as ctx:
+        ctx.init_walkers()
+        orc.init_walkers()
+        ctx.initial_eval()
+        orc.initial_eval()
+        for g in range(2):
+            assert ctx.generation(g == 1) == orc.generation(g == 1)
+        wg, wo = ctx.walkers(), orc.walkers()
+        eg, _, wbg = ctx.estimators()
+        eo, _, wbo = orc.estimators()
+    assert np.array_equal(wg["irn"], wo["irn"])
+    assert float(np.max(np.abs(wg["x"] - wo["x"]))) < (1e-10 if prec == "fp64" else 1e-7)
+    tol = 1e-10 if prec == "fp64" else 1e-6
+    assert rel_each(wg["weight"], wo["weight"]) < tol
+    assert rel_each(eg, eo) < (1e-9 if prec == "fp64" else 1e-6)
