@@ -264,3 +264,36 @@ def test_union_in_global_scratch_two_point_moves(prec):
     tol = 1e-10 if prec == "fp64" else 1e-6
     assert rel_each(wg["weight"], wo["weight"]) < tol
     assert rel_each(eg, eo) < (1e-9 if prec == "fp64" else 1e-6)
+
+
+def test_batch_with_a_global_union_system():
+    """A batch holding a system in the global-union layout next to an
+    on-chip one: every system's walkers bit for bit those of its context
+    run alone (FP64)."""
+    specs = [(7, 7, 5, 48), (80, 80, 10, 24)]
+
+    def make():
+        out = []
+        for i, (nup, ndn, norb, nw) in enumerate(specs):
+            sysd = abi.make_system(configs.system_params(nup, ndn, norb, seed=500 + i))
+            rund = abi.make_run(configs.run_params(nw, 0.001))
+            c = capi.Context(sysd, rund)
+            c.init_walkers()
+            c.initial_eval()
+            out.append(c)
+        return out
+
+    A, B = make(), make()
+    try:
+        with capi.Batch(A) as b:
+            b.generations(3, opcomp_last=True)
+        for g in range(3):
+            for c in B:
+                c.generation(g == 2)
+        for a, c in zip(A, B):
+            wa, wc = a.walkers(), c.walkers()
+            for k in ("x", "irn", "weight", "psil", "d2psi"):
+                assert np.array_equal(wa[k], wc[k]), k
+    finally:
+        for c in A + B:
+            c.close()
