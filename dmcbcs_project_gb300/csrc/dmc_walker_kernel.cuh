@@ -223,11 +223,19 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
             for (int cc = 0; cc < 3; ++cc) kn[cc * p.nk + q] = kg[q].n[cc];
         }
     }
-    // the CTA's global scratch slice: the union region when it is not on
-    // chip (BIG), then the beta pair data when they are not on chip
-    double* gs = a.gscratch ? a.gscratch + (size_t)blockIdx.x * L.gstride : nullptr;
-    double* pb = L.pb_in_smem ? sm + L.pb : gs + (L.un_in_smem ? 0 : round_up(L.rsize, 2));
-    Ctx<R, NT, BIG> c{p, a, L, sm, pb, BIG ? gs : nullptr};
+    // the CTA's global scratch slice: the union region (BIG), then the beta
+    // pair data when they are not on chip.  The on-chip instances compute
+    // their pointer in the original form: the general one cost the mixed
+    // kernel 1 % (measured), from code generation alone.
+    double* gs = nullptr;
+    double* pb;
+    if constexpr (BIG) {
+        gs = a.gscratch + (size_t)blockIdx.x * L.gstride;
+        pb = gs + round_up(L.rsize, 2);
+    } else {
+        pb = L.pb_in_smem ? sm + L.pb : a.gscratch + (size_t)blockIdx.x * L.pb_size;
+    }
+    Ctx<R, NT, BIG> c{p, a, L, sm, pb, gs};
     __shared__ double s_old[9];
     __syncthreads();
     const int nw = a.pn ? *a.pn : a.nw;   // the population is counted on the device in a generation
