@@ -2,8 +2,8 @@
 wavefunction batches (hpsi, bcs, getphi, matinv), single-particle ratios
 (bcsone, getphione), parameter derivatives (getderbcs, getjasder, the adjoint
 gradients), the stochastic-reconfiguration sums and step, the operators
-(g(r), density, S(q), n(k)), generations on device stacks and on pinned host
-arrays, and a batch of two systems.  The calls raise on any status other
+(g(r), density, S(q), n(k)), the layout tuner, generations on device
+stacks and on pinned host arrays, and a batch of two systems.  The calls raise on any status other
 than DMC_OK; the values are checked by the other tests.  Also the one
 process in which the secondary kernels are profiled:
 
@@ -56,6 +56,7 @@ def test_every_entry_point_once(nwalk=256):
         ctx.generation(False)
         ctx.add_operators()
         ctx.update_operators()
+        ctx.tune_layout(1)
         host = _pinned(torch, ctx)
         n = ctx.get_walkers_into(host)
         ctx.put_walkers(dict(host, n=n))
