@@ -149,7 +149,12 @@ typedef struct dmc_ctx dmc_ctx;
  * setbeta/initbeta (betafun.f90:12-125), setphi (coshpot.f90:14-143),
  * setstep (step.f90:11-41) and create (stack.f90:51-80).  Builds the k
  * shells, the beta, Jastrow and potential tables on the host and uploads
- * them to the current CUDA device. */
+ * them to the current CUDA device, and picks the walker layout (threads per
+ * CTA, CTAs per SM, what stays in shared memory; dmc_tune_layout may change
+ * it later).  DMC_ERR_INVALID for deck values out of range (checked on the
+ * host first), DMC_ERR_UNSUPPORTED for a beta table read from unit 80
+ * (bfact < 0) or a system whose pair matrix and k records do not fit one
+ * CTA's shared memory. */
 int dmc_create(const dmc_system_desc* sys, const dmc_run_desc* run, dmc_ctx** out);
 int dmc_destroy(dmc_ctx* ctx);
 const char* dmc_last_error(const dmc_ctx* ctx);
