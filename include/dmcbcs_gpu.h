@@ -152,9 +152,9 @@ typedef struct dmc_ctx dmc_ctx;
  * them to the current CUDA device, and picks the walker layout (threads per
  * CTA, CTAs per SM, what stays in shared memory; dmc_tune_layout may change
  * it later).  DMC_ERR_INVALID for deck values out of range (checked on the
- * host first), DMC_ERR_UNSUPPORTED for a beta table read from unit 80
- * (bfact < 0) or a system whose pair matrix and k records do not fit one
- * CTA's shared memory. */
+ * host first), DMC_ERR_UNSUPPORTED for ndim other than 3, a beta table read
+ * from unit 80 (bfact < 0) or a system whose pair matrix and k records do
+ * not fit one CTA's shared memory. */
 int dmc_create(const dmc_system_desc* sys, const dmc_run_desc* run, dmc_ctx** out);
 int dmc_destroy(dmc_ctx* ctx);
 const char* dmc_last_error(const dmc_ctx* ctx);
