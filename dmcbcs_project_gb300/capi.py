@@ -16,6 +16,10 @@ from .abi import DMC_NEST_MAX, DMC_WTISTO, Info, RunDesc, SystemDesc, Walkers
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libdmcbcs_gb300.so")
 
+# the array fields of dmc_walkers: thirteen double arrays, then is and irn
+_WALKER_FIELDS = ("x", "dpsi", "dpsig", "psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0",
+                  "psigl0", "wt0", "is_", "irn")
+
 # every entry point declared in include/dmcbcs_gpu.h
 EXPORTS = [
     "dmc_abi_version", "dmc_status_string", "dmc_last_error", "dmc_create", "dmc_destroy", "dmc_get_info",
@@ -202,6 +206,16 @@ def probe_peak(kind):
     if st != abi.DMC_OK:
         raise DMCError(st, "dmc_probe_peak")
     return v.value
+
+
+def _walker_view(arrs):
+    w = Walkers()
+    w.n = int(arrs["n"])
+    for k in _WALKER_FIELDS[:13]:
+        setattr(w, k, arrs[k].ctypes.data_as(C.POINTER(C.c_double)))
+    w.is_ = arrs["is_"].ctypes.data_as(C.POINTER(C.c_int))
+    w.irn = arrs["irn"].ctypes.data_as(C.POINTER(C.c_int64))
+    return w
 
 
 class Context:
@@ -535,16 +549,26 @@ class Context:
                                                  C.byref(st), C.byref(ms), C.byref(nl)))
         return st.value, ms.value, nl.value
 
-    def walker_struct(self, arrs):
-        """dmc_walkers view of a dict of arrays (as returned by walkers())."""
-        w = Walkers()
-        w.n = int(arrs["n"])
-        for k in ("x", "dpsi", "dpsig", "psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0",
-                  "psigl0", "wt0"):
-            setattr(w, k, arrs[k].ctypes.data_as(C.POINTER(C.c_double)))
-        w.is_ = arrs["is_"].ctypes.data_as(C.POINTER(C.c_int))
-        w.irn = arrs["irn"].ctypes.data_as(C.POINTER(C.c_int64))
-        return w
+    def walker_struct(self, arrs, slot=None):
+        """dmc_walkers view of a dict of arrays (as returned by walkers()).
+
+        With a slot name the view is kept for the next call with the same
+        array objects in that slot (only n is set again): a host that hands
+        the same population arrays over every generation pays the fifteen
+        pointer conversions once.  The cache holds references to the arrays,
+        so their ids (and data pointers) stay theirs while cached."""
+        if slot is not None:
+            key = (slot,) + tuple(id(arrs[k]) for k in _WALKER_FIELDS)
+            cache = self.__dict__.setdefault("_wcache", {})
+            hit = cache.get(key)
+            if hit is None:
+                if len(cache) >= 8:
+                    cache.pop(next(iter(cache)))
+                hit = (_walker_view(arrs), [arrs[k] for k in _WALKER_FIELDS])
+                cache[key] = hit
+            hit[0].n = int(arrs["n"])
+            return hit[0]
+        return _walker_view(arrs)
 
     def put_walkers(self, arrs):
         self._check(load().dmc_put_walkers(self._h, C.byref(self.walker_struct(arrs))))
@@ -552,8 +576,8 @@ class Context:
     def generation_host(self, arrs_in, arrs_out, opcomp):
         """One generation on a population held in host arrays (dicts as for
         put_walkers; arrs_out['cap'] is its capacity); returns the new count."""
-        wi = self.walker_struct(arrs_in)
-        wo = self.walker_struct(dict(arrs_out, n=arrs_out["cap"]))
+        wi = self.walker_struct(arrs_in, "in")
+        wo = self.walker_struct(dict(arrs_out, n=arrs_out["cap"]), "out")
         self._check(load().dmc_generation_host(self._h, C.byref(wi), C.byref(wo), int(bool(opcomp))))
         return wo.n
 

@@ -277,3 +277,42 @@ def test_create_rejects_bad_decks_before_any_device_call(lib):
         st = lib.dmc_create(ctypes.byref(s), ctypes.byref(abi.make_run(rp)), ctypes.byref(out))
         assert st == abi.DMC_ERR_INVALID, (sp["nbin"], sp["norb"], rp)
         assert not out.value
+
+
+def test_walker_views_are_cached_per_slot_and_array_set():
+    """The dmc_walkers view of a population is built once per slot and set
+    of arrays (the host generation hands the same arrays over every time):
+    its pointers are the arrays' data, n follows every call, the in and out
+    slots never share a view, and the cache stays bounded."""
+    import numpy as np
+
+    def population(cap, npart):
+        h = {k: np.zeros((cap, npart, 3)) for k in ("x", "dpsi", "dpsig")}
+        for k in ("psil", "psigl", "d2psi", "d2psig", "v", "vext", "weight", "psil0", "psigl0", "wt0"):
+            h[k] = np.zeros(cap)
+        h["is_"] = np.zeros(cap, np.int32)
+        h["irn"] = np.zeros(cap, np.int64)
+        return h
+
+    class Holder:
+        pass
+
+    ctx = Holder()
+    view = capi.Context.walker_struct
+    host = population(16, 2)
+    a = view(ctx, dict(host, n=5), "in")
+    b = view(ctx, dict(host, n=16), "out")
+    assert a is not b and a.n == 5 and b.n == 16
+    for k in capi._WALKER_FIELDS:
+        ptr = ctypes.cast(getattr(a, k), ctypes.c_void_p).value
+        assert ptr == host[k].ctypes.data == ctypes.cast(getattr(b, k), ctypes.c_void_p).value
+    assert view(ctx, dict(host, n=7), "in") is a and a.n == 7
+    other = population(16, 2)
+    c = view(ctx, dict(other, n=3), "in")
+    assert c is not a and ctypes.cast(c.x, ctypes.c_void_p).value == other["x"].ctypes.data
+    keep = [population(4, 1) for _ in range(12)]
+    for h in keep:
+        view(ctx, dict(h, n=1), "in")
+    assert len(ctx._wcache) <= 8
+    # without a slot a fresh view every call
+    assert view(ctx, dict(host, n=2)) is not view(ctx, dict(host, n=2))
