@@ -178,6 +178,8 @@ struct dmc_ctx {
     DevBuf<double> sx, sdr, sratio, sder, ssinv, srsum, srene;
     DevBuf<double> pg_dpsi, pg_dphi, pg_dlog, pg_del, pg_scr;   // adjoint parameter gradients
     DevBuf<PgTab> pg_btab;                                      // d beta / d b, d beta / d d tables
+    DevBuf<PgTab> pg_ktab;                                      // Jastrow knot basis on the table grid
+    DevBuf<double> pg_slice;                                    // per-CTA slices of the adjoint kernel
     // particle-by-particle sweeps: FP32 inverses carried between calls, the
     // cos/sin tables, accepted moves per walker
     DevBuf<float> sm_inv;
@@ -1622,6 +1624,20 @@ static int pgrad_btab(dmc_ctx* c)
     return DMC_OK;
 }
 
+// the Jastrow knot basis on the up-down table grid (built once: the grid
+// and the knot spacing do not change during a context's life)
+static int pgrad_ktab(dmc_ctx* c)
+{
+    if (c->S.jknots.empty() || c->pg_ktab.p) return DMC_OK;
+    std::vector<double> t[3];
+    c->S.knot_basis_tables(t);
+    std::vector<PgTab> h(t[0].size());
+    for (size_t i = 0; i < h.size(); ++i) h[i] = PgTab{t[0][i], t[1][i], t[2][i], 0.0};
+    CK(c->pg_ktab.alloc(h.size()));
+    CK(cudaMemcpy(c->pg_ktab.p, h.data(), h.size() * sizeof(PgTab), cudaMemcpyHostToDevice));
+    return DMC_OK;
+}
+
 int dmc_param_count(const dmc_ctx* c, int* np)
 {
     if (!c || !np) return DMC_ERR_INVALID;
@@ -1650,18 +1666,22 @@ static int pgrad_device(dmc_ctx* c, int nw, const double* dx, double* dlog, doub
     if (rc) return rc;
     c->launches += 2;
     rc = pgrad_btab(c);
+    if (rc == DMC_OK) rc = pgrad_ktab(c);
     if (rc) return rc;
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     const size_t need = pgrad_doubles(c->P);
-    const int grid = std::max(1, std::min(nw, 2 * c->nsm));
+    const int grid = pgrad_grid(c->P, nw, c->nsm, optin);
+    if (grid < 1) return fail(c, DMC_ERR_CUDA, "adjoint kernel occupancy");
     double* scr = nullptr;
     if (need * 8 > (size_t)optin) {
         CK(c->pg_scr.alloc((size_t)grid * need));
         scr = c->pg_scr.p;
     }
+    CK(c->pg_slice.alloc((size_t)grid * pgrad_slice_doubles(c->P)));
     CK(launch_pgrad(c->P, c->kv.p, c->tud.p, dx, c->ssinv.p, c->pg_dpsi.p, c->pg_dphi.p, dlog, del, nw, np,
-                    c->S.bfact, c->pg_btab.p, pgrad_nbeta(c), pgrad_nknot(c), grid, scr, optin, c->stream));
+                    c->S.bfact, c->pg_btab.p, c->pg_ktab.p, pgrad_nbeta(c), pgrad_nknot(c), grid, scr,
+                    c->pg_slice.p, optin, c->stream));
     ++c->launches;
     return DMC_OK;
 }

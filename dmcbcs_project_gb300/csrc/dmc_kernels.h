@@ -82,13 +82,18 @@ constexpr int kPgradMax = DMC_MAX_SHELLS + 3 + 16;
 struct PgTab {
     double f, df, d2f, pad;
 };
-// adjoint parameter gradients (dmc_single.cu): doubles of one CTA's working
-// set; on chip when it fits in smem_limit bytes, else in gscr (grid x that)
+// adjoint parameter gradients (dmc_single.cu): doubles of one CTA's core
+// (on chip when it fits in smem_limit bytes, else in gscr: grid x that) and
+// of its global slice (slices: grid x that, always); the grid that keeps
+// every SM's resident CTAs busy (0 on a CUDA error); ktd the Jastrow knot
+// basis on the table grid ([16][ntab+1], needed with nknot > 0)
 size_t pgrad_doubles(const DevParams& p);
+size_t pgrad_slice_doubles(const DevParams& p);
+int pgrad_grid(const DevParams& p, int nw, int nsm, int smem_limit);
 cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x, const double* sinv,
                          const double* dpsi, const double* dphi, double* dlog, double* deloc, int nw, int np,
-                         double bfact, const PgTab* btd, int nbeta, int nknot, int grid, double* gscr, int smem_limit,
-                         cudaStream_t st);
+                         double bfact, const PgTab* btd, const PgTab* ktd, int nbeta, int nknot, int grid,
+                         double* gscr, double* slices, int smem_limit, cudaStream_t st);
 // particle-by-particle sweeps with Sherman-Morrison updates (dmc_sweep.cu):
 // nsweep sweeps of the n walkers of stack st (positions and random states
 // updated in place); the inverse comes from inv64 (FP64, fresh) or, when

@@ -538,6 +538,21 @@ void Setup::set_beta(double b, double d, double bf)
     beta_tables(*this, b, d, bf);
 }
 
+void Setup::knot_basis_tables(std::vector<double> (&out)[3]) const
+{
+    const double h = el / kJastrowCells, dr = range / ntab;
+    const size_t nt = (size_t)ntab + 1;
+    for (auto& o : out) o.assign((size_t)kJastrowKnots * nt, 0.0);
+    for (int k = 0; k < kJastrowKnots; ++k)
+        for (int i = 0; i <= ntab; ++i) {
+            double f, fp, fpp;
+            jastrow_knot_basis(k, i * dr, h, f, fp, fpp);
+            out[0][k * nt + i] = f;
+            out[1][k * nt + i] = fp;
+            out[2][k * nt + i] = fpp;
+        }
+}
+
 void Setup::beta_param_tables(std::vector<double> (&out)[2][3]) const
 {
     using C = std::complex<double>;

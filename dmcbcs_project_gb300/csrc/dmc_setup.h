@@ -78,6 +78,10 @@ struct Setup {
     // the up-down Jastrow = reference + sum_k knots[k] phi_k (n = 16), or the
     // reference alone (n = 0); rebuilds utab/dutab/d2utab[0]
     int set_jastrow_spline(const double* knots, int n, std::string& err);
+    // phi_k, phi_k', phi_k'' of every knot k < 16 at every point of the
+    // up-down table grid (the values set_jastrow_spline adds to the table):
+    // out[m][k * (ntab + 1) + i]
+    void knot_basis_tables(std::vector<double> (&out)[3]) const;
     // d/db and d/dd of the beta tables (btab, dbtab, d2btab, bfact-scaled):
     // out[0][*] for b, out[1][*] for d, each ntabb + 1 values
     void beta_param_tables(std::vector<double> (&out)[2][3]) const;

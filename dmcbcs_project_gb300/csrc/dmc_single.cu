@@ -215,18 +215,34 @@ __device__ double block_sum1(double v, double* red)
 // tables on the beta grid (the derivatives of the image-summed, shifted,
 // bfact-scaled table that Psi uses).
 //
+// Per up-down pair (i, j) and shell s >= 2 (all k of a shell have the same
+// k^2 and amplitude v_s = 2 vorb(s)), with C_s = sum_{k in s} cos(k.r_ij) and
+// H_s = sum_{k in s} k sin(k.r_ij):
+//   S_ij  = ... + v_s C_s                      S'_s,ij = 2 C_s
+//   M_ij  = ... - v_s (k_s^2 C_s (1/m_i + 1/m_j) + 2 H_s . (w_i - w_j))
+//   M'_s,ij = -2 k_s^2 C_s (1/m_i + 1/m_j) - 4 H_s . (w_i - w_j)
+// The pass that forms M keeps (S'_s, M'_s) of every pair and shell, so the
+// shell parameters' sums after T cost three multiply-adds per pair and shell
+// instead of a second pass over the k vectors.
+//
 // The 16 knots t_k of the opt-in up-down Jastrow spline are Jastrow
 // parameters: J = ... + sum_pairs sum_k t_k phi_k(r), so
 //   d log Psi / d t_k = sum_pairs phi_k(r)
 //   d E_L / d t_k     = -hbar sum_pairs [ (1/m_i + 1/m_j)(phi_k'' + 2 phi_k'/r)
 //                        + 2 phi_k'/r d.(g_i - g_j) ],  g_p = grad_p log Psi / m_p,
-// with phi_k, phi_k', phi_k'' interpolated from their grid values exactly as
-// the pair loop interpolates the Jastrow table they are added to.
+// with phi_k, phi_k', phi_k'' interpolated from their values on the Jastrow
+// table's grid (ktd[k][g]: the values the table itself was built from) with
+// the pair's Lagrange weights, exactly as the pair loop interpolates the
+// Jastrow table they are added to.
 // Inputs per walker: x, the inverse (column-major as smati), the total and
 // determinant drifts (grad / sqrt m) whose difference is grad J.  Outputs
 // dlog[w*np + t], deloc[w*np + t] for t = vorb(1..norb), then bfact, b, d
 // (nbeta = 3 with the beta function on), then the knots (nknot = 16 with the
 // spline on).
+// Memory: the CTA's core (inverse, M, product buffer, per-particle vectors,
+// reductions) in shared memory (in core_g when it does not fit); the axis
+// powers e^{i 2 pi m x_a / L}, the plane waves of every k at every particle
+// and the per-pair shell derivatives in the CTA's slice of slice_g (L2).
 __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__ DevParams p,
                                                          const KVecDev* __restrict__ kv,
                                                          const TabUD* __restrict__ tud, const double* __restrict__ x,
@@ -234,11 +250,12 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                                                          const double* __restrict__ dpsi,
                                                          const double* __restrict__ dphi, double* __restrict__ dlog,
                                                          double* __restrict__ deloc, int nw, int np, double bfact,
-                                                         const PgTab* __restrict__ btd, int nbeta, int nknot,
-                                                         double* gscr, size_t per_cta)
+                                                         const PgTab* __restrict__ btd, const PgTab* __restrict__ ktd,
+                                                         int nbeta, int nknot, double* core_g, size_t core_per,
+                                                         double* slice_g, size_t slice_per)
 {
     extern __shared__ __align__(16) double smp[];
-    double* base = gscr ? gscr + (size_t)blockIdx.x * per_cta : smp;
+    double* base = core_g ? core_g + (size_t)blockIdx.x * core_per : smp;
     const int nd = p.nd, nup = p.nup, ndn = p.ndn, P = p.npart, nq = p.nk - 1, norb = p.norb;
     const size_t nd2 = (size_t)nd * nd;
     double* Si = base;                 // (S^-1)_{rc} = Si[r + c nd]
@@ -246,11 +263,14 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
     double* B = M + nd2;               // M S^-1
     double* xs = B + nd2;              // [P][3]
     double* w = xs + 3 * P;            // [P][3]: grad J / m
-    double* cs = w + 3 * P;            // [nq][P][2]: cos, sin of k_q . x_p
-    double* gt = cs + 2 * (size_t)P * (nq > 0 ? nq : 1);    // [P][3]: grad log Psi / m
+    double* gt = w + 3 * P;            // [P][3]: grad log Psi / m
     double* red = gt + 3 * P;
     double* res = red + kThreads;      // [2][kPgradMax]: d log Psi, then d Q
-    int* sh0 = reinterpret_cast<int*>(res + 2 * kPgradMax);   // first k of each shell, [norb + 1]
+    int* sh0 = reinterpret_cast<int*>(res + 2 * kPgradMax);   // first k of each shell s >= 2, then the end
+    const int np1 = p.nmax + 1, nsh = norb - 1, npairs = nup * ndn;
+    double2* E = reinterpret_cast<double2*>(slice_g + (size_t)blockIdx.x * slice_per);   // [P][3][np1]
+    double2* cs = E + (size_t)3 * P * np1;                                             // [nq][P]
+    double2* dsm = cs + (size_t)P * (nq > 0 ? nq : 1);                                 // [nsh][npairs]
     const int npb = norb + nbeta;      // parameters of the pair function
     const double imu = p.imass[0], imd = p.imass[1], ims = imu + imd;
     if (threadIdx.x == 0) {
@@ -266,39 +286,83 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
         for (size_t t = threadIdx.x; t < nd2; t += kThreads) Si[t] = sinv[(size_t)wk * nd2 + t];
         for (int t = threadIdx.x; t < 3 * P; t += kThreads) {
             const size_t g = (size_t)wk * 3 * P + t;
-            xs[t] = x[g];
+            const double xv = x[g];
+            xs[t] = xv;
             const int sp = (t / 3) < nup ? 0 : 1;
             w[t] = (dpsi[g] - dphi[g]) * p.isqm[sp];
             gt[t] = dpsi[g] * p.isqm[sp];
+            // powers of e^{i 2 pi x_a / L}, m = 0..nmax
+            double s1, c1;
+            sincospi(2.0 * xv * p.eli, &s1, &c1);
+            double2* e = E + (size_t)t * np1;
+            e[0] = make_double2(1.0, 0.0);
+            double cr = c1, ci = s1;
+            if (np1 > 1) e[1] = make_double2(c1, s1);
+            for (int m = 2; m < np1; ++m) {
+                const double nr = cr * c1 - ci * s1, ni = cr * s1 + ci * c1;
+                cr = nr;
+                ci = ni;
+                e[m] = make_double2(cr, ci);
+            }
         }
         __syncthreads();
+        // e^{i k_q . x_p} as the product of the three axis powers
         for (int t = threadIdx.x; t < nq * P; t += kThreads) {
-            const int q = t / P + 1, pp = t % P;
+            const int q = t / P + 1, pp = t - (q - 1) * P;
             const KVecDev& K = kv[q];
-            double sn, c;
-            sincos(K.k[0] * xs[3 * pp] + K.k[1] * xs[3 * pp + 1] + K.k[2] * xs[3 * pp + 2], &sn, &c);
-            cs[2 * t] = c;
-            cs[2 * t + 1] = sn;
+            const double2* eb = E + (size_t)pp * 3 * np1;
+            const int n0 = K.n[0];
+            const double2 e0 = eb[n0 < 0 ? -n0 : n0];
+            double zr = e0.x, zi = n0 < 0 ? -e0.y : e0.y;
+#pragma unroll
+            for (int a = 1; a < 3; ++a) {
+                const int n = K.n[a];
+                const double2 e = eb[a * np1 + (n < 0 ? -n : n)];
+                const double er = e.x, ei = n < 0 ? -e.y : e.y;
+                const double nr = zr * er - zi * ei, ni = zr * ei + zi * er;
+                zr = nr;
+                zi = ni;
+            }
+            cs[t] = make_double2(zr, zi);
         }
         __syncthreads();
-        // M (psislaterbcs.f90:171-206, 249-293 for the entries and their derivatives)
+        // M (psislaterbcs.f90:171-206, 249-293 for the entries and their
+        // derivatives), with every pair's shell derivatives on the side
         for (size_t t = threadIdx.x; t < nd2; t += kThreads) {
             const int i = (int)(t % nd), j = (int)(t / nd);
             double m = 0.0;
             if (i < nup && j < ndn) {
                 const int pj = nup + j;
+                const double wd0 = w[3 * i] - w[3 * pj], wd1 = w[3 * i + 1] - w[3 * pj + 1];
+                const double wd2 = w[3 * i + 2] - w[3 * pj + 2];
                 double l = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
-                for (int q = 1; q <= nq; ++q) {
-                    const KVecDev& K = kv[q];
-                    const double* ci = cs + 2 * ((size_t)(q - 1) * P + i);
-                    const double* cj = cs + 2 * ((size_t)(q - 1) * P + pj);
-                    const double co = ci[0] * cj[0] + ci[1] * cj[1];
-                    const double si = ci[1] * cj[0] - ci[0] * cj[1];
-                    l -= K.v * K.k2 * co;
-                    const double vs = K.v * si;
-                    g0 -= vs * K.k[0];
-                    g1 -= vs * K.k[1];
-                    g2 -= vs * K.k[2];
+                double2* dp = dsm + (size_t)i * ndn + j;
+                for (int s = 0; s < nsh; ++s) {
+                    const int q0 = sh0[s], q1 = sh0[s + 1];
+                    double cc = 0.0, h0 = 0.0, h1 = 0.0, h2 = 0.0;
+                    for (int q = q0; q < q1; ++q) {
+                        const KVecDev& K = kv[q];
+                        const double2 ci = cs[(size_t)(q - 1) * P + i];
+                        const double2 cj = cs[(size_t)(q - 1) * P + pj];
+                        const double co = fma(ci.x, cj.x, ci.y * cj.y);
+                        const double si = fma(ci.y, cj.x, -ci.x * cj.y);
+                        cc += co;
+                        h0 = fma(si, K.k[0], h0);
+                        h1 = fma(si, K.k[1], h1);
+                        h2 = fma(si, K.k[2], h2);
+                    }
+                    double ds = 0.0, dm = 0.0;
+                    if (q1 > q0) {
+                        const double v = kv[q0].v, k2c = kv[q0].k2 * cc;
+                        const double hw = h0 * wd0 + h1 * wd1 + h2 * wd2;
+                        l -= v * k2c;
+                        g0 -= v * h0;
+                        g1 -= v * h1;
+                        g2 -= v * h2;
+                        ds = 2.0 * cc;
+                        dm = -2.0 * k2c * ims - 4.0 * hw;
+                    }
+                    dp[(size_t)s * npairs] = make_double2(ds, dm);
                 }
                 if (!p.nobeta) {
                     double d[3];
@@ -314,8 +378,7 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                     }
                     l += d2f;
                 }
-                m = l * ims + 2.0 * (g0 * (w[3 * i] - w[3 * pj]) + g1 * (w[3 * i + 1] - w[3 * pj + 1]) +
-                                     g2 * (w[3 * i + 2] - w[3 * pj + 2]));
+                m = l * ims + 2.0 * (g0 * wd0 + g1 * wd1 + g2 * wd2);
             } else if (i < nup) {
                 // unpaired up plane wave in column j (depends on up particle i)
                 const int u = j - ndn;
@@ -353,44 +416,31 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
             M[t] = s;
         }
         __syncthreads();
-        // per parameter: sums over the up-down pairs of S^-1_ji S'_ij and
-        // S^-1_ji M'_ij - T_ji S'_ij
-        const int npairs = nup * ndn;
-        for (int th = 0; th < norb; ++th) {
-            double sl = 0.0, sq = 0.0;
+        // per pair-function shell parameter (eight at a time): sums over the
+        // up-down pairs of S^-1_ji S'_ij and S^-1_ji M'_ij - T_ji S'_ij
+        for (int th0 = 0; th0 < norb; th0 += 8) {
+            double acc[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) acc[k] = 0.0;
             for (int t = threadIdx.x; t < npairs; t += kThreads) {
-                const int i = t / ndn, j = t % ndn, pj = nup + j;
+                const int i = t / ndn, j = t - i * ndn;
                 const double a = Si[j + (size_t)i * nd], tt = M[j + (size_t)i * nd];
-                if (th == 0) {   // vorb(1): S' = 1
-                    sl += a;
-                    sq -= tt;
-                } else if (th < norb) {
-                    const int q0 = sh0[th - 1], q1 = sh0[th];
-                    double ds = 0.0, dl = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
-                    for (int q = q0; q < q1; ++q) {
-                        const KVecDev& K = kv[q];
-                        const double* ci = cs + 2 * ((size_t)(q - 1) * P + i);
-                        const double* cj = cs + 2 * ((size_t)(q - 1) * P + pj);
-                        const double co = ci[0] * cj[0] + ci[1] * cj[1];
-                        const double si = ci[1] * cj[0] - ci[0] * cj[1];
-                        ds += 2.0 * co;
-                        dl -= 2.0 * K.k2 * co;
-                        g0 -= 2.0 * si * K.k[0];
-                        g1 -= 2.0 * si * K.k[1];
-                        g2 -= 2.0 * si * K.k[2];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int th = th0 + u;
+                    if (th < norb) {
+                        if (th == 0) {   // vorb(1): S' = 1, M' = 0
+                            acc[u] += a;
+                            acc[8 + u] -= tt;
+                        } else {
+                            const double2 v = dsm[(size_t)(th - 1) * npairs + t];
+                            acc[u] = fma(a, v.x, acc[u]);
+                            acc[8 + u] += a * v.y - tt * v.x;
+                        }
                     }
-                    const double dm = dl * ims + 2.0 * (g0 * (w[3 * i] - w[3 * pj]) + g1 * (w[3 * i + 1] - w[3 * pj + 1]) +
-                                                        g2 * (w[3 * i + 2] - w[3 * pj + 2]));
-                    sl += a * ds;
-                    sq += a * dm - tt * ds;
                 }
             }
-            sl = block_sum1(sl, red);
-            sq = block_sum1(sq, red);
-            if (threadIdx.x == 0) {
-                res[th] = sl;
-                res[kPgradMax + th] = sq;
-            }
+            block_sum_n<16>(acc, red, res + th0, res + kPgradMax + th0);
         }
         if (nbeta > 0) {
             // bfact (beta / bfact), b and d (their derivative tables) in one
@@ -437,9 +487,11 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
             double acc[2 * kJastrowKnots];
 #pragma unroll
             for (int k = 0; k < 2 * kJastrowKnots; ++k) acc[k] = 0.0;
-            // grid points in units of the knot spacing: t = r / h with
-            // r = (idx - 1 + m) / scale; no divisions in the pair loop
-            const double h = p.el / kJastrowCells, ih = 1.0 / h, ih2 = ih * ih, tstep = ih / p.scale;
+            // grid rows in units of the knot spacing (t = r / h): the knots
+            // whose support [k - 2, k + 2] (and the mirror image of k = 1
+            // below one spacing) reaches the pair's four grid rows
+            const double tstep = kJastrowCells / (p.el * p.scale);
+            const size_t kstride = (size_t)p.ntab + 1;
             for (int t = threadIdx.x; t < npairs; t += kThreads) {
                 const int i = t / ndn, j = t % ndn, pj = nup + j;
                 double d[3];
@@ -447,38 +499,22 @@ __global__ void __launch_bounds__(kThreads) pgrad_kernel(const __grid_constant__
                 const double r = fmax(sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), 1.0e-14);
                 if (!(r < p.range)) continue;
                 const walker::Lagrange<double> W = walker::lagrange(r, p.scale, p.ntab);
-                const double cw[4] = {W.c1, W.c2, W.c3, W.c4};
                 const double ri = 1.0 / r;
                 const double gd = d[0] * (gt[3 * i] - gt[3 * pj]) + d[1] * (gt[3 * i + 1] - gt[3 * pj + 1]) +
                                   d[2] * (gt[3 * i + 2] - gt[3 * pj + 2]);
-                const double t0 = (W.idx - 1) * tstep;
-                // knots whose support [k - 2, k + 2] (and the mirror image of
-                // k = 1 below one spacing) reaches the four grid points
+                const double cp = 2.0 * ri * (ims + gd);   // weight of phi' (phi'' has ims)
+                const int o = W.idx - 1;
+                const double t0 = o * tstep;
                 const int klo = max(0, (int)t0 - 2);
-                const int khi = min(kJastrowKnots - 1, (int)(t0 + 3.0 * tstep) + 3);
+                const int khi = min(kJastrowKnots - 1, (int)(t0 + 3.0 * tstep) + 2);
 #pragma unroll 1
                 for (int k = klo; k <= khi; ++k) {
-                    double f = 0.0, fp = 0.0, fpp = 0.0;
-#pragma unroll
-                    for (int m = 0; m < 4; ++m) {
-                        const double tm = t0 + m * tstep;
-                        double a, b, c;
-                        bspline3(tm - k, a, b, c);
-                        if (k > 0) {
-                            double a2, b2, c2;
-                            bspline3(tm + k, a2, b2, c2);
-                            a += a2;
-                            b += b2;
-                            c += c2;
-                        }
-                        f += cw[m] * a;
-                        fp += cw[m] * b;
-                        fpp += cw[m] * c;
-                    }
-                    fp *= ih;
-                    fpp *= ih2;
+                    const PgTab* T = ktd + k * kstride + o;
+                    const double f = W.c1 * T[0].f + W.c2 * T[1].f + W.c3 * T[2].f + W.c4 * T[3].f;
+                    const double fp = W.c1 * T[0].df + W.c2 * T[1].df + W.c3 * T[2].df + W.c4 * T[3].df;
+                    const double fpp = W.c1 * T[0].d2f + W.c2 * T[1].d2f + W.c3 * T[2].d2f + W.c4 * T[3].d2f;
                     acc[k] += f;
-                    acc[kJastrowKnots + k] += ims * (fpp + 2.0 * fp * ri) + 2.0 * fp * ri * gd;
+                    acc[kJastrowKnots + k] += ims * fpp + cp * fp;
                 }
             }
             block_sum_n<2 * kJastrowKnots>(acc, red, res + npb, res + kPgradMax + npb);
@@ -614,22 +650,46 @@ cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x
     return cudaGetLastError();
 }
 
-// Layout of one pgrad CTA, in doubles: inverse, M, product buffer (nd^2
-// each), positions and Jastrow gradient (3 npart each), cos/sin of every
-// k vector at every particle (2 npart (nk-1)), reduction buffer, results.
+// Layout of one pgrad CTA's core, in doubles: inverse, M, product buffer
+// (nd^2 each), positions, grad J / m and grad log Psi / m (3 npart each),
+// reduction buffer, results, first k of each shell.
 size_t pgrad_doubles(const DevParams& p)
 {
     const size_t nd2 = (size_t)p.nd * p.nd;
-    return 3 * nd2 + 9 * (size_t)p.npart + 2 * (size_t)p.npart * (p.nk > 1 ? p.nk - 1 : 1) + kThreads +
-           2 * (size_t)kPgradMax + (size_t)(p.norb + 2);
+    return 3 * nd2 + 9 * (size_t)p.npart + kThreads + 2 * (size_t)kPgradMax + (size_t)(p.norb + 2);
+}
+
+// The CTA's global slice, in doubles (even): axis powers (3 npart (nmax+1)
+// complex), plane waves (npart (nk-1) complex), shell derivatives
+// ((norb-1) nup ndn pairs of doubles).
+size_t pgrad_slice_doubles(const DevParams& p)
+{
+    const size_t nq = p.nk > 1 ? (size_t)p.nk - 1 : 1, nsh = p.norb > 1 ? (size_t)p.norb - 1 : 1;
+    return 2 * (3 * (size_t)p.npart * (p.nmax + 1) + (size_t)p.npart * nq + nsh * p.nup * p.ndn);
+}
+
+// CTAs of one pgrad launch: as many as are resident on the device's SMs
+// together, at most one per walker.
+int pgrad_grid(const DevParams& p, int nw, int nsm, int smem_limit)
+{
+    const size_t need = pgrad_doubles(p) * 8;
+    const int smem = need <= (size_t)smem_limit ? (int)need : 0;
+    int per_sm = 1;
+    if (smem > 0 && cudaFuncSetAttribute(pgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pgrad_kernel, kThreads, smem) != cudaSuccess)
+        return 0;
+    const long long g = (long long)(per_sm > 0 ? per_sm : 1) * nsm;
+    return (int)(g < nw ? g : (nw > 0 ? nw : 1));
 }
 
 cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud, const double* x, const double* sinv,
                          const double* dpsi, const double* dphi, double* dlog, double* deloc, int nw, int np,
-                         double bfact, const PgTab* btd, int nbeta, int nknot, int grid, double* gscr, int smem_limit,
-                         cudaStream_t st)
+                         double bfact, const PgTab* btd, const PgTab* ktd, int nbeta, int nknot, int grid,
+                         double* gscr, double* slices, int smem_limit, cudaStream_t st)
 {
-    if (np > kPgradMax || nknot > kJastrowKnots || np != p.norb + nbeta + nknot || (nbeta > 1 && !btd))
+    if (np > kPgradMax || nknot > kJastrowKnots || np != p.norb + nbeta + nknot || (nbeta > 1 && !btd) ||
+        (nknot > 0 && !ktd) || !slices || grid < 1)
         return cudaErrorInvalidValue;
     if (nw <= 0) return cudaSuccess;
     const size_t need = pgrad_doubles(p);
@@ -642,8 +702,9 @@ cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud
         return cudaErrorInvalidValue;
     }
     pgrad_kernel<<<grid < nw ? grid : nw, kThreads, smem, st>>>(p, kv, tud, x, sinv, dpsi, dphi, dlog, deloc, nw, np,
-                                                                bfact, btd, nbeta, nknot, on_chip ? nullptr : gscr,
-                                                                need);
+                                                                bfact, btd, ktd, nbeta, nknot,
+                                                                on_chip ? nullptr : gscr, need, slices,
+                                                                pgrad_slice_doubles(p));
     return cudaGetLastError();
 }
 
