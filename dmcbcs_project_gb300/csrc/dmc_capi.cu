@@ -414,7 +414,8 @@ KernelArgs base_args(dmc_ctx* c)
 int grid_for(dmc_ctx* c, int nw) { return std::max(1, std::min(nw, c->grid)); }
 
 int run_eval(dmc_ctx* c, int mode, int nw, const double* dx, double* psil, int* is, double* dpsi, double* d2psi,
-             double* v, double* vext, double* psigl, double* dpsig, double* d2psig, double* sinv, cudaStream_t st)
+             double* v, double* vext, double* psigl, double* dpsig, double* d2psig, double* sinv, cudaStream_t st,
+             double* dphi = nullptr)
 {
     if (nw <= 0) return DMC_OK;
     KernelArgs a = base_args(c);
@@ -422,7 +423,7 @@ int run_eval(dmc_ctx* c, int mode, int nw, const double* dx, double* psil, int* 
     a.nw = nw;
     a.xin = dx;
     a.o_psil = psil; a.o_is = is; a.o_dpsi = dpsi; a.o_d2psi = d2psi; a.o_v = v; a.o_vext = vext;
-    a.o_psigl = psigl; a.o_dpsig = dpsig; a.o_d2psig = d2psig; a.o_sinv = sinv;
+    a.o_psigl = psigl; a.o_dpsig = dpsig; a.o_d2psig = d2psig; a.o_sinv = sinv; a.o_dphi = dphi;
     CK(c->wstat.alloc(nw));
     a.wstatus = c->wstat.p;
     c->wstat_n = nw;
@@ -1654,17 +1655,15 @@ static int pgrad_device(dmc_ctx* c, int nw, const double* dx, double* dlog, doub
     CK(c->pg_dpsi.alloc(nw * n3));
     CK(c->pg_dphi.alloc(nw * n3));
     CK(c->ssinv.alloc(nw * nd2));
-    // the total drift and the determinant's drift and inverse, in FP64
+    // the total drift, the determinant's drift and the inverse, in FP64, from
+    // one evaluation
     const int prec = c->precision;
     c->precision = DMC_PREC_FP64;
     int rc = run_eval(c, MODE_HPSI, nw, dx, nullptr, nullptr, c->pg_dpsi.p, nullptr, nullptr, nullptr, nullptr,
-                      nullptr, nullptr, nullptr, c->stream);
-    if (rc == DMC_OK)
-        rc = run_eval(c, MODE_BCS, nw, dx, nullptr, nullptr, c->pg_dphi.p, nullptr, nullptr, nullptr, nullptr,
-                      nullptr, nullptr, c->ssinv.p, c->stream);
+                      nullptr, nullptr, c->ssinv.p, c->stream, c->pg_dphi.p);
     c->precision = prec;
     if (rc) return rc;
-    c->launches += 2;
+    ++c->launches;
     rc = pgrad_btab(c);
     if (rc == DMC_OK) rc = pgrad_ktab(c);
     if (rc) return rc;

@@ -120,6 +120,7 @@ struct KernelArgs {
     const int* pn;               // MODE_STEP: walker count on the device (nullptr: nw)
     const double* xin;
     double *o_psil, *o_dpsi, *o_d2psi, *o_v, *o_vext, *o_psigl, *o_dpsig, *o_d2psig, *o_sinv;
+    double* o_dphi;              // MODE_HPSI: also the determinant's drift alone (as MODE_BCS gives it)
     int* o_is;
     DevStack in, out;
     double* est;                 // [nw][nest][2]: (val, wt) per estimator

@@ -2060,6 +2060,10 @@ __device__ HRes hpsi_eval(const Ctx<R, NT, BIG>& c, int mode)
                 dtot[k] += l;
             }
         sums[5] += dtot[0] * dph[0] + dtot[1] * dph[1] + dtot[2] * dph[2];
+        // the determinant's drift alone replaces this particle's Jastrow
+        // gradient (read above) when the caller asks for it
+        if (mode == MODE_HPSI && c.a.o_dphi)
+            for (int k = 0; k < 3; ++k) du[3 * pt + k] = dph[k];
         // dpsi = dphi + du (+ dg)
         for (int k = 0; k < 3; ++k) acc[3 * pt + k] = dph[k] + dtot[k];
     }

@@ -395,6 +395,8 @@ walker_kernel(const __grid_constant__ DevParams p, const __grid_constant__ Kerne
                 }
             if (a.o_dpsig)
                 for (int e = threadIdx.x; e < n3; e += NT) a.o_dpsig[(size_t)w * n3 + e] = dpsig[e];
+            if (a.o_dphi && a.mode == MODE_HPSI)
+                for (int e = threadIdx.x; e < n3; e += NT) a.o_dphi[(size_t)w * n3 + e] = sm[L.acc + 4 * P + e];
             if (a.o_sinv) {
                 const int nd = p.nd;
                 // column-major nd x nd as the reference's smati(nd,nd)
