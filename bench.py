@@ -336,21 +336,32 @@ def uneven_batch(args, rank, precision="fp64"):
         grids, tune_ms = b.tune(3)
         b.generations(max(args.warmup, 3), opcomp_last=False, flush_l2=True)
         steps, ms, nl = b.generations(gens, opcomp_last=True, flush_l2=True)
-    seq_steps, seq_ms = 0, 0.0
-    for c in ctxs:
+    seq_steps, seq_ms, seq_flops = 0, 0.0, 0.0
+    # algorithmic flops of one walker-step of each system (the reference
+    # algorithm's count, as for the headline roofline)
+    flops = [algorithmic_flops(c.info.nup, c.info.ndn, c.info.nd, c.info.ncol, c.info.npart) for c in ctxs]
+    for c, f in zip(ctxs, flops):
         c.timed_generations(max(args.warmup, 3), opcomp_last=False, flush_l2=True)
         st, m, _ = c.timed_generations(gens, opcomp_last=True, flush_l2=True)
         seq_steps += st
         seq_ms += m
+        seq_flops += f * st
     for c in ctxs:
         c.close()
     value = steps / (ms * 1e-3)
     seq = seq_steps / (seq_ms * 1e-3)
+    # the batch's walker-steps split over the systems in proportion to their
+    # target populations (population control holds each near its target)
+    batch_flops = steps * float(np.dot(flops, nws)) / float(nws.sum())
     return {"workload": "uneven_batch_6_systems", "systems": systems, "walkers": BATCH_WALKERS, "precision": precision,
             "steps": gens, "unit": UNIT, "value": value, "ms_per_step": ms / max(gens, 1), "gpu_launches": nl,
             "grids_tuned": [int(g) for g in grids], "grids_initial": initial, "tune_pass_ms": tune_ms,
-            "sequential": {"value": seq, "ms_per_step": seq_ms / max(gens, 1)},
-            "speedup_vs_sequential": value / seq}
+            "sequential": {"value": seq, "ms_per_step": seq_ms / max(gens, 1),
+                           "algorithmic_tflops": seq_flops / (seq_ms * 1e-3) / 1e12},
+            "speedup_vs_sequential": value / seq,
+            "algorithmic_tflops": batch_flops / (ms * 1e-3) / 1e12,
+            "algorithmic_tflops_note": "reference-algorithm flops per walker-step of each system x its walker-steps "
+                                       "(batched: the measured total split by the systems' target populations)"}
 
 
 def param_gradients(args, rank):
@@ -632,8 +643,13 @@ def run_gpu(args):
         batch = uneven_batch(args, rank)
         mixed_batch = uneven_batch(args, rank, "mixed")
         batch["mixed"] = {k: mixed_batch[k] for k in ("value", "ms_per_step", "gpu_launches", "grids_tuned",
-                                                      "sequential", "speedup_vs_sequential")}
+                                                      "sequential", "speedup_vs_sequential", "algorithmic_tflops")}
         batch["mixed"]["speedup_vs_fp64_batch"] = mixed_batch["value"] / batch["value"]
+        if dgemm:
+            # the FP64 batch against the FP64 roofline: what any split of the
+            # SMs over the systems could still gain
+            batch["frac_of_measured_dgemm"] = batch["algorithmic_tflops"] / dgemm
+            batch["sequential"]["frac_of_measured_dgemm"] = batch["sequential"]["algorithmic_tflops"] / dgemm
     pgrad = param_gradients(args, rank) if args.pgrad_walkers > 0 else None
     sweeps = sm_sweeps(args, rank) if args.sweeps > 0 else None
 
