@@ -243,6 +243,31 @@ def test_union_in_global_scratch_gradients_and_sweeps():
     assert rel_each(wg["psil"], ref["psil"]) < 1e-9
 
 
+def test_gradients_with_the_adjoint_core_in_global_scratch():
+    """At N = 256 (128/128, ten shells) the adjoint kernel's core (the
+    inverse, M and the product buffer: 3 x 128^2 doubles) does not fit one
+    CTA's shared memory and runs from a global slice per CTA: d log|det| /
+    d vorb against the oracle's analytic getderbcs, and every parameter
+    against relative-step central differences of the oracle."""
+    from test_gpu_pgrad import rel_err
+
+    sysd, rund = system(128, 128, 10, nwalk=4, idmc=0)
+    orc = oracle.Oracle(sysd, rund)
+    orc.init_walkers()
+    x = orc.walkers()["x"][:1] + np.random.default_rng(13).normal(scale=0.3, size=(1, 256, 3))
+    with capi.Context(sysd, rund) as ctx:
+        dl, de = ctx.param_grad(x)
+    norb = int(sysd.norb)
+    od = np.array([orc.getderbcs(x[0])])
+    assert np.max(np.abs(dl[:, :norb] - od)) < 1e-9 * np.max(np.abs(od))
+    l1, e1 = _fd_relative(sysd, rund, x, 1e-4)
+    l2, e2 = _fd_relative(sysd, rund, x, 5e-5)
+    fl, fe = (4 * l2 - l1) / 3, (4 * e2 - e1) / 3
+    print(f"N = 256 ({dl.shape[1]} parameters): d log Psi rel err {rel_err(dl, fl):.2e}, "
+          f"d E_L rel err {rel_err(de, fe):.2e}")
+    assert rel_err(dl, fl) < 1e-5 and rel_err(de, fe) < 1e-5
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_union_in_global_scratch_two_point_moves(prec):
     """idmc = 10 (two wavefunction evaluations per move) with the union
