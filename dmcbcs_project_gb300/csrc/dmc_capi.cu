@@ -166,10 +166,11 @@ struct dmc_ctx {
     int wstat_n = 0;        // its walker count
     int hstatus = 0;        // DMC_STATUS_* flags met on the host (stack overflow)
     DevBuf<unsigned long long> irn1, wtisto;
-    // estimator block sums valblk, valblk2, wtblk: one buffer of
-    // 3 DMC_NEST_MAX doubles (vb2 and wb point into it), read with one copy
+    // estimator block sums valblk, valblk2, wtblk and their compensation
+    // terms: one buffer of 6 DMC_NEST_MAX doubles (vb2, wb and vbc point
+    // into it), read with one copy
     DevBuf<double> vb;
-    double *vb2 = nullptr, *wb = nullptr;
+    double *vb2 = nullptr, *wb = nullptr, *vbc = nullptr;
     // batch staging
     DevBuf<double> bx, bpsil, bdpsi, bd2psi, bv, bvext, bpsigl, bdpsig, bd2psig, bsinv;
     DevBuf<int> bis;
@@ -630,7 +631,7 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     const int nest = c->P.nest;
     if (c->st[0].alloc(c->cap, c->n3) || c->st[1].alloc(c->cap, c->n3) || c->est.alloc((size_t)c->cap * nest * 2) ||
         c->counts.alloc(c->cap) || c->offs.alloc(c->cap + 1) || c->irn1.alloc(c->cap) ||
-        c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(3 * DMC_NEST_MAX) || c->status.alloc(1) ||
+        c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(6 * DMC_NEST_MAX) || c->status.alloc(1) ||
         c->pop.alloc(4) || c->popf.alloc(1) ||
         c->psteps.alloc(1)) {
         dmc_destroy(c);
@@ -639,7 +640,8 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     cudaMemset(c->wtisto.p, 0, DMC_WTISTO * sizeof(unsigned long long));
     c->vb2 = c->vb.p + DMC_NEST_MAX;
     c->wb = c->vb.p + 2 * DMC_NEST_MAX;
-    cudaMemset(c->vb.p, 0, 3 * DMC_NEST_MAX * sizeof(double));
+    c->vbc = c->vb.p + 3 * DMC_NEST_MAX;
+    cudaMemset(c->vb.p, 0, 6 * DMC_NEST_MAX * sizeof(double));
     cudaMemset(c->status.p, 0, sizeof(int));
     cudaMemset(c->pop.p, 0, 4 * sizeof(int));
     cudaMemset(c->psteps.p, 0, sizeof(unsigned long long));
@@ -1160,7 +1162,7 @@ int dmc_initial_eval(dmc_ctx* c, double* sums)
         rc = reverse_stacks(c);
         if (rc) return rc;
     }
-    CK(cudaMemsetAsync(c->vb.p, 0, 3 * DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->vb.p, 0, 6 * DMC_NEST_MAX * 8, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return DMC_OK;
 }
@@ -1188,7 +1190,7 @@ int dmc_step(dmc_ctx* c, int opcomp)
     CK(launch_walker(c->P, a, c->L, grid_for(c, n), c->stream, c->precision == DMC_PREC_MIXED));
     if (a.defer) CK(launch_step_decide(c->P, a, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
-    CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2, c->wb, c->stream));
+    CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2, c->wb, c->vbc, c->stream));
     c->launches += a.defer ? 3 : 2;
     c->istin = 1 - c->istin;
     return DMC_OK;
@@ -1281,7 +1283,7 @@ static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch, const DevStack* in_ho
         ++nl;
     }
     CK(cudaEventRecordWithFlags(c->ev1, c->stream, evflags));
-    CK(launch_estimators(c->est.p, 0, c->P.nest, c->vb.p, c->vb2, c->wb, c->stream, a.pn, c->psteps.p));
+    CK(launch_estimators(c->est.p, 0, c->P.nest, c->vb.p, c->vb2, c->wb, c->vbc, c->stream, a.pn, c->psteps.p));
     ++nl;
     c->istin = 1 - c->istin;
     int* pop = c->pop.p;
@@ -1476,7 +1478,7 @@ int dmc_generation_host(dmc_ctx* c, const dmc_walkers* in, dmc_walkers* out, int
 int dmc_zero_estimators(dmc_ctx* c)
 {
     if (!c) return DMC_ERR_INVALID;
-    CK(cudaMemsetAsync(c->vb.p, 0, 3 * DMC_NEST_MAX * 8, c->stream));
+    CK(cudaMemsetAsync(c->vb.p, 0, 6 * DMC_NEST_MAX * 8, c->stream));
     return DMC_OK;
 }
 
@@ -1484,12 +1486,15 @@ int dmc_get_estimators(dmc_ctx* c, double* valblk, double* valblk2, double* wtbl
 {
     if (!c || !valblk || !valblk2 || !wtblk) return DMC_ERR_INVALID;
     const int ne = c->P.nest;
-    double h[3 * DMC_NEST_MAX];
+    double h[6 * DMC_NEST_MAX];
     CK(cudaMemcpyAsync(h, c->vb.p, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    std::memcpy(valblk, h, ne * 8);
-    std::memcpy(valblk2, h + DMC_NEST_MAX, ne * 8);
-    std::memcpy(wtblk, h + 2 * DMC_NEST_MAX, ne * 8);
+    // the compensated sums: each block sum plus its error term
+    for (int e = 0; e < ne; ++e) {
+        valblk[e] = h[e] + h[3 * DMC_NEST_MAX + e];
+        valblk2[e] = h[DMC_NEST_MAX + e] + h[4 * DMC_NEST_MAX + e];
+        wtblk[e] = h[2 * DMC_NEST_MAX + e] + h[5 * DMC_NEST_MAX + e];
+    }
     return DMC_OK;
 }
 

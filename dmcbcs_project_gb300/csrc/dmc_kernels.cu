@@ -52,21 +52,35 @@ cudaError_t launch_step_decide(const DevParams& p, const KernelArgs& a, cudaStre
 // Estimator block sums (estimator.f90:72-82): est[n][nest][2] -> valblk,
 // valblk2, wtblk (accumulated), fixed-order tree per estimator.
 // ---------------------------------------------------------------------------
+// s + x with the rounding error of the addition collected in c (Neumaier's
+// variant of Kahan summation: also exact when |x| > |s|)
+__device__ __forceinline__ void comp_add(double& s, double& c, double x)
+{
+    const double t = s + x;
+    c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+    s = t;
+}
+
+// The estimator sums of one generation (addval, estimator.f90:72-84) added
+// to the block sums with compensation: each thread's walkers and the block
+// sums carried across the block's generations are compensated sums (the
+// block sum's error term in comp[3][DMC_NEST_MAX], added back when the sums
+// are read); the tree over threads is a plain FP64 tree.
 __global__ void estimator_kernel(const double* est, int n, const int* pn, int nest, double* valblk, double* valblk2,
-                                 double* wtblk, unsigned long long* steps)
+                                 double* wtblk, double* comp, unsigned long long* steps)
 {
     if (pn) n = *pn;
     const int e = blockIdx.x;
     if (steps && e == 0 && threadIdx.x == 0) *steps += (unsigned long long)n;   // walker-steps of the generation
-    double s[3] = {0.0, 0.0, 0.0};
+    double s[3] = {0.0, 0.0, 0.0}, c[3] = {0.0, 0.0, 0.0};
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         const double v = est[((size_t)k * nest + e) * 2], wt = est[((size_t)k * nest + e) * 2 + 1];
-        s[0] += v * wt;
-        s[1] += v * v * wt;
-        s[2] += wt;
+        comp_add(s[0], c[0], v * wt);
+        comp_add(s[1], c[1], v * v * wt);
+        comp_add(s[2], c[2], wt);
     }
     __shared__ double red[3 * 32];
-    for (int q = 0; q < 3; ++q) s[q] = warp_sum(s[q]);
+    for (int q = 0; q < 3; ++q) s[q] = warp_sum(s[q] + c[q]);
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     if (lane == 0)
         for (int q = 0; q < 3; ++q) red[wp * 3 + q] = s[q];
@@ -75,9 +89,9 @@ __global__ void estimator_kernel(const double* est, int n, const int* pn, int ne
         double t[3] = {0.0, 0.0, 0.0};
         for (int k = 0; k < (int)(blockDim.x / 32); ++k)
             for (int q = 0; q < 3; ++q) t[q] += red[k * 3 + q];
-        valblk[e] += t[0];
-        valblk2[e] += t[1];
-        wtblk[e] += t[2];
+        comp_add(valblk[e], comp[e], t[0]);
+        comp_add(valblk2[e], comp[DMC_NEST_MAX + e], t[1]);
+        comp_add(wtblk[e], comp[2 * DMC_NEST_MAX + e], t[2]);
     }
 }
 
@@ -375,11 +389,12 @@ cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLay
     return cudaGetLastError();
 }
 
-cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, cudaStream_t st,
+cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, double* comp,
+                              cudaStream_t st,
                               const int* pn, unsigned long long* steps)
 {
     if (n <= 0 && !pn) return cudaSuccess;
-    estimator_kernel<<<nest, 256, 0, st>>>(est, n, pn, nest, vb, vb2, wb, steps);
+    estimator_kernel<<<nest, 256, 0, st>>>(est, n, pn, nest, vb, vb2, wb, comp, steps);
     return cudaGetLastError();
 }
 
