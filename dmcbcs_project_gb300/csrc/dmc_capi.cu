@@ -171,6 +171,8 @@ struct dmc_ctx {
     // into it), read with one copy
     DevBuf<double> vb;
     double *vb2 = nullptr, *wb = nullptr, *vbc = nullptr;
+    DevBuf<double> estpart;            // the estimator kernel's per-CTA partial sums
+    DevBuf<unsigned int> estticket;    // its last-CTA counter (zero between launches)
     // batch staging
     DevBuf<double> bx, bpsil, bdpsi, bd2psi, bv, bvext, bpsigl, bdpsig, bd2psig, bsinv;
     DevBuf<int> bis;
@@ -631,7 +633,8 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     const int nest = c->P.nest;
     if (c->st[0].alloc(c->cap, c->n3) || c->st[1].alloc(c->cap, c->n3) || c->est.alloc((size_t)c->cap * nest * 2) ||
         c->counts.alloc(c->cap) || c->offs.alloc(c->cap + 1) || c->irn1.alloc(c->cap) ||
-        c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(6 * DMC_NEST_MAX) || c->status.alloc(1) ||
+        c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(6 * DMC_NEST_MAX) || c->estpart.alloc(kEstBlocks * 3 * DMC_NEST_MAX) ||
+        c->estticket.alloc(1) || c->status.alloc(1) ||
         c->pop.alloc(4) || c->popf.alloc(1) ||
         c->psteps.alloc(1)) {
         dmc_destroy(c);
@@ -642,6 +645,7 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     c->wb = c->vb.p + 2 * DMC_NEST_MAX;
     c->vbc = c->vb.p + 3 * DMC_NEST_MAX;
     cudaMemset(c->vb.p, 0, 6 * DMC_NEST_MAX * sizeof(double));
+    cudaMemset(c->estticket.p, 0, sizeof(unsigned int));
     cudaMemset(c->status.p, 0, sizeof(int));
     cudaMemset(c->pop.p, 0, 4 * sizeof(int));
     cudaMemset(c->psteps.p, 0, sizeof(unsigned long long));
@@ -1190,7 +1194,8 @@ int dmc_step(dmc_ctx* c, int opcomp)
     CK(launch_walker(c->P, a, c->L, grid_for(c, n), c->stream, c->precision == DMC_PREC_MIXED));
     if (a.defer) CK(launch_step_decide(c->P, a, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
-    CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2, c->wb, c->vbc, c->stream));
+    CK(launch_estimators(c->est.p, n, c->P.nest, c->vb.p, c->vb2, c->wb, c->vbc, c->estpart.p, c->estticket.p,
+                         c->stream));
     c->launches += a.defer ? 3 : 2;
     c->istin = 1 - c->istin;
     return DMC_OK;
@@ -1283,7 +1288,8 @@ static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch, const DevStack* in_ho
         ++nl;
     }
     CK(cudaEventRecordWithFlags(c->ev1, c->stream, evflags));
-    CK(launch_estimators(c->est.p, 0, c->P.nest, c->vb.p, c->vb2, c->wb, c->vbc, c->stream, a.pn, c->psteps.p));
+    CK(launch_estimators(c->est.p, 0, c->P.nest, c->vb.p, c->vb2, c->wb, c->vbc, c->estpart.p, c->estticket.p,
+                         c->stream, a.pn, c->psteps.p));
     ++nl;
     c->istin = 1 - c->istin;
     int* pop = c->pop.p;

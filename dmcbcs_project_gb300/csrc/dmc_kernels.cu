@@ -61,38 +61,61 @@ __device__ __forceinline__ void comp_add(double& s, double& c, double x)
     s = t;
 }
 
-// The estimator sums of one generation (addval, estimator.f90:72-84) added
-// to the block sums with compensation: each thread's walkers and the block
-// sums carried across the block's generations are compensated sums (the
-// block sum's error term in comp[3][DMC_NEST_MAX], added back when the sums
-// are read); the tree over threads is a plain FP64 tree.
-__global__ void estimator_kernel(const double* est, int n, const int* pn, int nest, double* valblk, double* valblk2,
-                                 double* wtblk, double* comp, unsigned long long* steps)
+// The estimator sums of one generation (addval, estimator.f90:72-84) over
+// kEstBlocks CTAs, each a contiguous share of the walkers: thread (e, sub)
+// sums estimator e over every nsub-th walker of the share, so that a warp
+// reads consecutive records and the FP64 work is spread over many SMs.  The
+// CTA that finishes last combines the shares' partial sums in CTA order and
+// adds them to the block sums with compensation: the block sums carried
+// across a block's generations keep their error terms in
+// comp[3][DMC_NEST_MAX], added back when the sums are read.  The partition
+// and every order are fixed, so the sums are the same run to run.
+__global__ void __launch_bounds__(256) estimator_kernel(const double* est, int n, const int* pn, int nest,
+                                                        double* valblk, double* valblk2, double* wtblk, double* comp,
+                                                        double* part, unsigned int* ticket, unsigned long long* steps)
 {
     if (pn) n = *pn;
-    const int e = blockIdx.x;
-    if (steps && e == 0 && threadIdx.x == 0) *steps += (unsigned long long)n;   // walker-steps of the generation
-    double s[3] = {0.0, 0.0, 0.0}, c[3] = {0.0, 0.0, 0.0};
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double v = est[((size_t)k * nest + e) * 2], wt = est[((size_t)k * nest + e) * 2 + 1];
-        comp_add(s[0], c[0], v * wt);
-        comp_add(s[1], c[1], v * v * wt);
-        comp_add(s[2], c[2], wt);
+    if (steps && blockIdx.x == 0 && threadIdx.x == 0) *steps += (unsigned long long)n;   // walker-steps of the generation
+    const int nsub = (int)blockDim.x / nest;   // threads per estimator
+    const int e = (int)threadIdx.x % nest, sub = (int)threadIdx.x / nest;
+    const int per = (n + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int k0 = (int)blockIdx.x * per, k1 = min(n, k0 + per);
+    __shared__ double red[256 * 3];
+    if (sub < nsub) {
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int k = k0 + sub; k < k1; k += nsub) {
+            const double v = est[((size_t)k * nest + e) * 2], wt = est[((size_t)k * nest + e) * 2 + 1];
+            s0 += v * wt;
+            s1 += v * v * wt;
+            s2 += wt;
+        }
+        red[threadIdx.x * 3] = s0;
+        red[threadIdx.x * 3 + 1] = s1;
+        red[threadIdx.x * 3 + 2] = s2;
     }
-    __shared__ double red[3 * 32];
-    for (int q = 0; q < 3; ++q) s[q] = warp_sum(s[q] + c[q]);
-    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    if (lane == 0)
-        for (int q = 0; q < 3; ++q) red[wp * 3 + q] = s[q];
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t[3] = {0.0, 0.0, 0.0};
-        for (int k = 0; k < (int)(blockDim.x / 32); ++k)
-            for (int q = 0; q < 3; ++q) t[q] += red[k * 3 + q];
-        comp_add(valblk[e], comp[e], t[0]);
-        comp_add(valblk2[e], comp[DMC_NEST_MAX + e], t[1]);
-        comp_add(wtblk[e], comp[2 * DMC_NEST_MAX + e], t[2]);
+    if ((int)threadIdx.x < 3 * nest) {
+        const int ee = (int)threadIdx.x / 3, q = (int)threadIdx.x % 3;
+        double t = 0.0;
+        for (int u = 0; u < nsub; ++u) t += red[(u * nest + ee) * 3 + q];
+        part[((size_t)blockIdx.x * DMC_NEST_MAX + ee) * 3 + q] = t;
     }
+    // the last CTA to finish (threadFenceReduction pattern) combines them
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if ((int)threadIdx.x < 3 * nest) {
+        const int ee = (int)threadIdx.x / 3, q = (int)threadIdx.x % 3;
+        double t = 0.0;
+        for (int blk = 0; blk < (int)gridDim.x; ++blk) t += __ldcg(part + ((size_t)blk * DMC_NEST_MAX + ee) * 3 + q);
+        double* dst = q == 0 ? valblk : (q == 1 ? valblk2 : wtblk);
+        comp_add(dst[ee], comp[q * DMC_NEST_MAX + ee], t);
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -390,11 +413,12 @@ cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLay
 }
 
 cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, double* comp,
-                              cudaStream_t st,
+                              double* part, unsigned int* ticket, cudaStream_t st,
                               const int* pn, unsigned long long* steps)
 {
     if (n <= 0 && !pn) return cudaSuccess;
-    estimator_kernel<<<nest, 256, 0, st>>>(est, n, pn, nest, vb, vb2, wb, comp, steps);
+    if (nest < 1 || nest > DMC_NEST_MAX) return cudaErrorInvalidValue;
+    estimator_kernel<<<kEstBlocks, 256, 0, st>>>(est, n, pn, nest, vb, vb2, wb, comp, part, ticket, steps);
     return cudaGetLastError();
 }
 

@@ -39,9 +39,13 @@ cudaError_t launch_walker(const DevParams& p, const KernelArgs& a, const SmemLay
 int matinv_fits(int n, bool* two_buffers = nullptr);
 
 // estimator block sums with compensation (comp: their error terms,
-// [3][DMC_NEST_MAX] for valblk, valblk2, wtblk)
+// [3][DMC_NEST_MAX] for valblk, valblk2, wtblk); part: kEstBlocks x 3
+// DMC_NEST_MAX doubles of partial sums, ticket: one counter, zero between
+// launches (the kernel leaves it zero)
+constexpr int kEstBlocks = 64;
 cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, double* vb2, double* wb, double* comp,
-                              cudaStream_t st, const int* pn = nullptr, unsigned long long* steps = nullptr);
+                              double* part, unsigned int* ticket, cudaStream_t st, const int* pn = nullptr,
+                              unsigned long long* steps = nullptr);
 
 cudaError_t launch_branch(const DevStack& in, const DevStack& out, int n, int n3, int cap, double factor,
                           int* counts, int* offs, unsigned long long* irn1, unsigned long long* wtisto,
