@@ -499,7 +499,9 @@ int dmc_sm_inverse(dmc_ctx* ctx, int nw, double* sinv);
 int dmc_zero_estimators(dmc_ctx* ctx);
 
 /* Current block sums of the estimators (estimator.f90:72-82):
- * valblk, valblk2, wtblk, each [nest]. */
+ * valblk, valblk2, wtblk, each [nest].  The library accumulates them across
+ * a block's generations as compensated sums (Neumaier) and returns each
+ * sum with its error term added. */
 int dmc_get_estimators(dmc_ctx* ctx, double* valblk, double* valblk2, double* wtblk);
 
 /* Replaces update (estimator.f90:84-113): block averages valnow[nest],
