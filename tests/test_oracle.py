@@ -566,3 +566,41 @@ def test_chkder_optional_terms(label, extra, nbin, ikup, ikdn):
             d2gnum += (gp - gm) / (2 * h)
     assert abs(d2num - h0["d2psi"][0]) < 1e-4 * max(1.0, abs(h0["d2psi"][0])), label
     assert abs(d2gnum - h0["d2psig"][0]) < 1e-4 * max(1.0, abs(h0["d2psig"][0])), label
+
+
+def test_jastrow_spline_table_against_scipy_bsplines():
+    """The oracle's opt-in up-down Jastrow spline (the 16-knot basis the
+    library shares through its spline header) against an independent
+    construction: scipy's cardinal cubic B-spline on the knots -2..2,
+    phi_0(r) = B(r/h), phi_k(r) = B(r/h - k) + B(r/h + k), h = L/34, summed
+    with the knot values and differentiated in r, on every point of the
+    up-down table grid (r_i = i L / (2 ntab)); also zero with its first two
+    derivatives at L/2."""
+    interpolate = pytest.importorskip("scipy.interpolate")
+    sysd, rund, _ = configs.workload("n14", nwalk=4, ntab=2000)
+    knots = np.random.default_rng(21).uniform(-0.3, 0.3, 16)
+    base = oracle.Oracle(sysd, rund, threads=1)
+    spl = oracle.Oracle(sysd, rund, threads=1)
+    spl.set_jastrow_spline(knots)
+    nt = base.info.ntab + 1
+    diff = [spl.table(m).reshape(2, nt)[0] - base.table(m).reshape(2, nt)[0] for m in range(3)]
+    for m in range(3):   # the same-spin rows are untouched
+        assert np.array_equal(spl.table(m).reshape(2, nt)[1], base.table(m).reshape(2, nt)[1])
+    el = base.info.el
+    h = el / 34.0
+    r = np.arange(nt) * (0.5 * el / base.info.ntab)
+    B = interpolate.BSpline.basis_element(np.arange(-2.0, 3.0), extrapolate=False)
+    dB, d2B = B.derivative(1), B.derivative(2)
+
+    def ev(f, t):
+        return np.nan_to_num(f(t), nan=0.0)
+
+    want = [np.zeros(nt) for _ in range(3)]
+    for k, tk in enumerate(knots):
+        for m, f in enumerate((B, dB, d2B)):
+            v = ev(f, r / h - k) + (ev(f, r / h + k) if k > 0 else 0.0)
+            want[m] += tk * v / h ** m
+    scale = [np.max(np.abs(w)) for w in want]
+    for m in range(3):
+        assert np.max(np.abs(diff[m] - want[m])) < 1e-12 * scale[m], m
+    assert max(abs(want[m][-1]) for m in range(3)) < 1e-12 * max(scale)
