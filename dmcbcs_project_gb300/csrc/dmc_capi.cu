@@ -173,7 +173,6 @@ struct dmc_ctx {
     double *vb2 = nullptr, *wb = nullptr, *vbc = nullptr;
     DevBuf<double> estpart;            // the estimator kernel's per-CTA partial sums
     DevBuf<unsigned int> estticket;    // its last-CTA counter (zero between launches)
-    DevBuf<unsigned int> brticket;     // the branch count-and-scan kernel's last-CTA counter
     // batch staging
     DevBuf<double> bx, bpsil, bdpsi, bd2psi, bv, bvext, bpsigl, bdpsig, bd2psig, bsinv;
     DevBuf<int> bis;
@@ -635,7 +634,7 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     if (c->st[0].alloc(c->cap, c->n3) || c->st[1].alloc(c->cap, c->n3) || c->est.alloc((size_t)c->cap * nest * 2) ||
         c->counts.alloc(c->cap) || c->offs.alloc(c->cap + 1) || c->irn1.alloc(c->cap) ||
         c->wtisto.alloc(DMC_WTISTO) || c->vb.alloc(6 * DMC_NEST_MAX) || c->estpart.alloc(kEstBlocks * 3 * DMC_NEST_MAX) ||
-        c->estticket.alloc(1) || c->brticket.alloc(1) || c->status.alloc(1) ||
+        c->estticket.alloc(1) || c->status.alloc(1) ||
         c->pop.alloc(4) || c->popf.alloc(1) ||
         c->psteps.alloc(1)) {
         dmc_destroy(c);
@@ -647,7 +646,6 @@ int dmc_create(const dmc_system_desc* sd, const dmc_run_desc* rd, dmc_ctx** out)
     c->vbc = c->vb.p + 3 * DMC_NEST_MAX;
     cudaMemset(c->vb.p, 0, 6 * DMC_NEST_MAX * sizeof(double));
     cudaMemset(c->estticket.p, 0, sizeof(unsigned int));
-    cudaMemset(c->brticket.p, 0, sizeof(unsigned int));
     cudaMemset(c->status.p, 0, sizeof(int));
     cudaMemset(c->pop.p, 0, 4 * sizeof(int));
     cudaMemset(c->psteps.p, 0, sizeof(unsigned long long));
@@ -1295,27 +1293,24 @@ static int gen_async(dmc_ctx* c, int opcomp, int* nlaunch, const DevStack* in_ho
     ++nl;
     c->istin = 1 - c->istin;
     int* pop = c->pop.p;
-    // the population-control decision (dmcbcs.f90:441-448), taken in the
-    // branch's count-and-scan launch when the generation branches
-    const PopCtlDev pc{(double)c->rd.nwalk, c->rd.popup, c->rd.popdn, pop + 3, c->popf.p};
-    auto branch = [&](const int* need, const double* fac, const PopCtlDev* decide) -> int {
+    auto branch = [&](const int* need, const double* fac) -> int {
         CK(launch_branch_dev(c->st[c->istin].view(), c->st[1 - c->istin].view(), pop + c->pcur, pop + (1 - c->pcur),
                              need, fac, pop + 2, c->n3, c->cap, c->nsm, c->counts.p, c->offs.p, c->irn1.p,
-                             c->wtisto.p, c->brticket.p, decide, c->stream));
-        nl += need ? 3 : 2;
+                             c->wtisto.p, c->stream));
+        nl += need ? 4 : 3;
         if (!need) c->istin = 1 - c->istin;   // the conditional pass leaves the walkers in place
         c->pcur = 1 - c->pcur;
         return DMC_OK;
     };
     const int idmc = c->rd.idmc;
     if (idmc > 0 || idmc == -2) {
-        const int rc = branch(nullptr, nullptr, &pc);
+        const int rc = branch(nullptr, nullptr);
         if (rc) return rc;
-    } else {
-        CK(launch_popctl(pop + c->pcur, pc.nwalk, pc.popup, pc.popdn, pc.need, pc.factor, pop + 2, c->stream));
-        ++nl;
     }
-    const int rc = branch(pop + 3, c->popf.p, nullptr);
+    CK(launch_popctl(pop + c->pcur, (double)c->rd.nwalk, c->rd.popup, c->rd.popdn, pop + 3, c->popf.p, pop + 2,
+                     c->stream));
+    ++nl;
+    const int rc = branch(pop + 3, c->popf.p);
     if (rc) return rc;
     c->launches += nl;
     if (nlaunch) *nlaunch = nl;

@@ -133,31 +133,6 @@ struct BranchDev {
     int* flags;             // bit 1: the output stack overflowed
 };
 
-// copies of every walker: int(w * factor + u) with u from ran1 on the
-// walker's own state (the advanced state kept for the copies), and the
-// multiplicity histogram; pop index m = n-1-j, grid-stride over m
-__device__ __forceinline__ void branch_counts(const DevStack& in, int n, double factor, int* counts,
-                                              unsigned long long* irn1, unsigned long long* wtisto, int cap)
-{
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
-        const int j = n - 1 - m;
-        const double wt = in.weight[j] * factor;
-        // ran1 on the walker's own state
-        const unsigned long long s = in.irn[j] & kMask48;
-        const unsigned long long s1 = (44485709377909ull * s + 96309754297ull) & kMask48;
-        const double rn = lcg_uniform(s1);
-        // int(w + u) as the reference truncates it, for weights in range; a
-        // non-finite or huge weight gives at most cap + 1 copies (the pass then
-        // reports an overflow) so the prefix sums stay bounded, NaN gives none
-        const double xw = wt + rn;
-        const double lim = (double)cap + 1.0;
-        const int iwt = xw != xw ? 0 : (xw >= lim ? (int)lim : (xw <= -lim ? -(int)lim : (int)xw));
-        counts[m] = iwt > 0 ? iwt : 0;
-        irn1[m] = s1;
-        if (iwt >= 0 && iwt < DMC_WTISTO) atomicAdd(&wtisto[iwt], 1ull);
-    }
-}
-
 __global__ void branch_count_kernel(DevStack in, int n, double factor, int* counts,
                                     unsigned long long* irn1, unsigned long long* wtisto, BranchDev bd, int cap)
 {
@@ -168,59 +143,22 @@ __global__ void branch_count_kernel(DevStack in, int n, double factor, int* coun
             factor = *bd.factor;
         }
     }
-    branch_counts(in, n, factor, counts, irn1, wtisto, cap);
-}
-
-// the population-control decision (dmcbcs.f90:441-448) for a population of
-// n: another pass with factor nwalk / n when n left [popdn, popup] nwalk;
-// bit 0 of *flags when the population died out
-__device__ __forceinline__ void popctl_decide(int n, const PopCtlDev& pc, int* flags)
-{
-    const bool out = n > pc.popup * pc.nwalk || n < pc.popdn * pc.nwalk;
-    if (n == 0) atomicOr(flags, 1);
-    *pc.need = (out && n > 0) ? 1 : 0;
-    *pc.factor = n > 0 ? pc.nwalk / n : 1.0;
-}
-
-// exclusive scan of counts[0..n) -> offs (total in offs[n]) by one CTA of
-// any size (part: blockDim.x long longs of shared memory); the output count
-// and the overflow bit with a device count, then the population control
-// decided on it when pc is given.  cg: counts written by other CTAs of the
-// same launch, read from L2.
-__device__ void scan_counts(const int* counts, int n, int* offs, int cap, const BranchDev& bd, long long* part,
-                            bool cg, const PopCtlDev* pc)
-{
-    const int t = threadIdx.x, T = blockDim.x;
-    const int chunk = (n + T - 1) / T;
-    const int b = t * chunk, e = min(n, b + chunk);
-    // sums in 64 bits, offsets stored saturated at cap + 1: copies at or
-    // beyond cap are dropped by the scatter, so no offset past cap is used
-    const long long sat = (long long)cap + 1;
-    long long s = 0;
-    for (int i = b; i < e; ++i) s += cg ? __ldcg(counts + i) : counts[i];
-    part[t] = s;
-    __syncthreads();
-    // Hillis-Steele on the partials
-    for (int o = 1; o < T; o <<= 1) {
-        const long long v = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    long long run = part[t] - s;
-    for (int i = b; i < e; ++i) {
-        offs[i] = (int)(run < sat ? run : sat);
-        run += cg ? __ldcg(counts + i) : counts[i];
-    }
-    if (t == T - 1) {
-        const long long tot = part[T - 1];
-        offs[n] = (int)(tot < sat ? tot : sat);
-        if (bd.pn_out) {
-            const int nout = (int)(tot < cap ? tot : cap);
-            *bd.pn_out = nout;
-            if (tot > cap) atomicOr(bd.flags, 2);
-            if (pc) popctl_decide(nout, *pc, bd.flags);
-        }
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+    const int j = n - 1 - m;
+    const double wt = in.weight[j] * factor;
+    // ran1 on the walker's own state
+    const unsigned long long s = in.irn[j] & kMask48;
+    const unsigned long long s1 = (44485709377909ull * s + 96309754297ull) & kMask48;
+    const double rn = lcg_uniform(s1);
+    // int(w + u) as the reference truncates it, for weights in range; a
+    // non-finite or huge weight gives at most cap + 1 copies (the pass then
+    // reports an overflow) so the prefix sums stay bounded, NaN gives none
+    const double xw = wt + rn;
+    const double lim = (double)cap + 1.0;
+    const int iwt = xw != xw ? 0 : (xw >= lim ? (int)lim : (xw <= -lim ? -(int)lim : (int)xw));
+    counts[m] = iwt > 0 ? iwt : 0;
+    irn1[m] = s1;
+    if (iwt >= 0 && iwt < DMC_WTISTO) atomicAdd(&wtisto[iwt], 1ull);
     }
 }
 
@@ -235,38 +173,36 @@ __global__ void scan_kernel(const int* counts, int n, int* offs, int cap, Branch
             return;
         }
     }
-    scan_counts(counts, n, offs, cap, bd, part, false, nullptr);
-}
-
-// Device-count form of the copy counts and their scan in one launch: every
-// CTA counts its share of the walkers, and the CTA that finishes last
-// (threadFenceReduction pattern: counts fenced, one ticket per CTA) scans
-// them, sets the output count and, with pc, decides the population control
-// on it.  The ticket is zero between launches.
-__global__ void __launch_bounds__(256) branch_count_scan_kernel(DevStack in, int* counts, unsigned long long* irn1,
-                                                                unsigned long long* wtisto, BranchDev bd, int cap,
-                                                                int* offs, unsigned int* ticket, PopCtlDev pc)
-{
-    __shared__ long long part[256];
-    __shared__ bool last;
-    const int n = *bd.pn;
-    double factor = 1.0;
-    if (bd.need) {
-        if (!*bd.need) {   // plain copy pass: the count stays
-            if (blockIdx.x == 0 && threadIdx.x == 0) *bd.pn_out = n;
-            return;
-        }
-        factor = *bd.factor;
+    const int t = threadIdx.x, T = blockDim.x;
+    const int chunk = (n + T - 1) / T;
+    const int b = t * chunk, e = min(n, b + chunk);
+    // sums in 64 bits, offsets stored saturated at cap + 1: copies at or
+    // beyond cap are dropped by the scatter, so no offset past cap is used
+    const long long sat = (long long)cap + 1;
+    long long s = 0;
+    for (int i = b; i < e; ++i) s += counts[i];
+    part[t] = s;
+    __syncthreads();
+    // Hillis-Steele on the partials
+    for (int o = 1; o < T; o <<= 1) {
+        const long long v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
     }
-    branch_counts(in, n, factor, counts, irn1, wtisto, cap);
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    scan_counts(counts, n, offs, cap, bd, part, true, pc.need ? &pc : nullptr);
-    if (threadIdx.x == 0) *ticket = 0u;
+    long long run = part[t] - s;
+    for (int i = b; i < e; ++i) {
+        offs[i] = (int)(run < sat ? run : sat);
+        run += counts[i];
+    }
+    if (t == T - 1) {
+        const long long tot = part[T - 1];
+        offs[n] = (int)(tot < sat ? tot : sat);
+        if (bd.pn_out) {
+            *bd.pn_out = (int)(tot < cap ? tot : cap);
+            if (tot > cap) atomicOr(bd.flags, 2);
+        }
+    }
 }
 
 // ran2 (ran.f90:29-48) applied k times: the affine map s -> a s + c mod 2^48
@@ -375,7 +311,11 @@ __global__ void stack_copy_kernel(DevStack from, DevStack to, const int* pn, con
 __global__ void popctl_kernel(const int* pn, double nwalk, double popup, double popdn, int* need, double* factor,
                               int* flags)
 {
-    popctl_decide(*pn, PopCtlDev{nwalk, popup, popdn, need, factor}, flags);
+    const int n = *pn;
+    const bool out = n > popup * nwalk || n < popdn * nwalk;
+    if (n == 0) atomicOr(flags, 1);
+    *need = (out && n > 0) ? 1 : 0;
+    *factor = n > 0 ? nwalk / n : 1.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -496,15 +436,11 @@ cudaError_t launch_branch(const DevStack& in, const DevStack& out, int n, int n3
 
 cudaError_t launch_branch_dev(const DevStack& in, const DevStack& out, const int* pn, int* pn_out, const int* need,
                               const double* dfactor, int* flags, int n3, int cap, int nsm, int* counts, int* offs,
-                              unsigned long long* irn1, unsigned long long* wtisto, unsigned int* ticket,
-                              const PopCtlDev* pc, cudaStream_t st)
+                              unsigned long long* irn1, unsigned long long* wtisto, cudaStream_t st)
 {
-    if (!ticket || (pc && !pc->need)) return cudaErrorInvalidValue;
     const BranchDev bd{pn, pn_out, need, dfactor, flags};
-    const PopCtlDev none{0.0, 0.0, 0.0, nullptr, nullptr};
-    const int want = (cap + 255) / 256, most = nsm * 4;
-    const int grid = want < 1 ? 1 : (want < most ? want : most);
-    branch_count_scan_kernel<<<grid, 256, 0, st>>>(in, counts, irn1, wtisto, bd, cap, offs, ticket, pc ? *pc : none);
+    branch_count_kernel<<<nsm * 4, 256, 0, st>>>(in, 0, 1.0, counts, irn1, wtisto, bd, cap);
+    scan_kernel<<<1, 1024, 0, st>>>(counts, 0, offs, cap, bd);
     branch_scatter_kernel<<<nsm * 16, 256, 0, st>>>(in, out, 0, n3, cap, counts, offs, irn1, bd);
     if (need) stack_copy_kernel<<<nsm * 16, 256, 0, st>>>(out, in, pn_out, need, n3);
     return cudaGetLastError();

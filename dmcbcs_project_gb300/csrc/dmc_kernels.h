@@ -50,25 +50,14 @@ cudaError_t launch_estimators(const double* est, int n, int nest, double* vb, do
 cudaError_t launch_branch(const DevStack& in, const DevStack& out, int n, int n3, int cap, double factor,
                           int* counts, int* offs, unsigned long long* irn1, unsigned long long* wtisto,
                           cudaStream_t st);
-// population control (dmcbcs.f90:441-448): target population nwalk, limits
-// popup and popdn (fractions of it); the decision goes to *need, the
-// factor of the extra pass to *factor
-struct PopCtlDev {
-    double nwalk, popup, popdn;
-    int* need;
-    double* factor;
-};
 // the same with the walker count on the device: *pn walkers in, the count
 // out to *pn_out; with need != nullptr a population-control pass that
 // branches with *dfactor only when *need is set and then copies the result
 // back into `in` (the walkers stay in `in` either way); overflow sets bit 1
-// of *flags.  The copy counts and their scan are one launch (ticket: a
-// device counter, zero between launches); with pc the population control
-// is decided on the output count in the same launch.
+// of *flags
 cudaError_t launch_branch_dev(const DevStack& in, const DevStack& out, const int* pn, int* pn_out, const int* need,
                               const double* dfactor, int* flags, int n3, int cap, int nsm, int* counts, int* offs,
-                              unsigned long long* irn1, unsigned long long* wtisto, unsigned int* ticket,
-                              const PopCtlDev* pc, cudaStream_t st);
+                              unsigned long long* irn1, unsigned long long* wtisto, cudaStream_t st);
 // population control decision (dmcbcs.f90): *need, *factor for the next pass
 cudaError_t launch_popctl(const int* pn, double nwalk, double popup, double popdn, int* need, double* factor,
                           int* flags, cudaStream_t st);
