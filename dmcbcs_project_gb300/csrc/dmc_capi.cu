@@ -187,6 +187,7 @@ struct dmc_ctx {
     // cos/sin tables, accepted moves per walker
     DevBuf<float> sm_inv;
     DevBuf<float2> sm_tab;
+    DevBuf<double> sm_prop;       // each sweep's proposals and acceptance uniforms, [n][npart][4]
     DevBuf<unsigned long long> sm_acc, sm_jA, sm_jC;   // accepted moves; ran1 jumps of 0..5 npart steps
     int sm_n = 0;                 // walkers whose FP32 inverse sm_inv holds (0: none)
     DevBuf<int> sip;
@@ -1747,6 +1748,7 @@ int dmc_sm_sweeps(dmc_ctx* c, int nsweeps, int recompute_every, int64_t* accepte
     c->sm_n = 0;                       // no carried inverse until these sweeps end
     CK(c->sm_inv.alloc((size_t)n * nd2));
     CK(c->sm_tab.alloc((size_t)n * nq * c->S.npart));
+    CK(c->sm_prop.alloc((size_t)n * 4 * c->S.npart));
     CK(c->sm_acc.alloc((size_t)n));
     CK(cudaMemsetAsync(c->sm_acc.p, 0, (size_t)n * sizeof(unsigned long long), c->stream));
     if (!c->sm_jA.p) {
@@ -1784,7 +1786,7 @@ int dmc_sm_sweeps(dmc_ctx* c, int nsweeps, int recompute_every, int64_t* accepte
             ++c->launches;
         }
         CK(launch_sweeps(c->P, view, n, ns, fresh ? c->ssinv.p : nullptr, c->sm_inv.p, c->sm_tab.p, c->kv_mp.p,
-                         c->tud_mp.p, c->tss_mp.p, c->sm_jA.p, c->sm_jC.p, c->sm_acc.p, c->stream));
+                         c->tud_mp.p, c->tss_mp.p, c->sm_jA.p, c->sm_jC.p, c->sm_acc.p, c->sm_prop.p, c->stream));
         ++c->launches;
     }
     c->sm_n = n;

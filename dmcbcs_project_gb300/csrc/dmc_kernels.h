@@ -104,13 +104,14 @@ cudaError_t launch_pgrad(const DevParams& p, const KVecDev* kv, const TabUD* tud
 // nsweep sweeps of the n walkers of stack st (positions and random states
 // updated in place); the inverse comes from inv64 (FP64, fresh) or, when
 // inv64 is null, from inv32, and leaves in inv32; tab is cos/sin scratch
-// [n][nk-1][npart]; accepted[w] counts the walker's accepted moves
+// [n][nk-1][npart]; accepted[w] counts the walker's accepted moves; prop
+// is scratch for each sweep's proposals, [n][npart][4] doubles
 size_t sweep_smem_bytes(const DevParams& p, int walkers_per_cta);
 // jA/jC: ran1 jump-ahead tables for 0 .. 5 npart steps
 cudaError_t launch_sweeps(const DevParams& p, const DevStack& st, int n, int nsweep, const double* inv64,
                           float* inv32, float2* tab, const KVecMP* kv, const TabUDmp* tud, const TabSSmp* tss,
                           const unsigned long long* jA, const unsigned long long* jC, unsigned long long* accepted,
-                          cudaStream_t stream);
+                          double* prop, cudaStream_t stream);
 // dpsi[w*stride + off + shell]; stride < 0 means norb
 cudaError_t launch_derbcs(const DevParams& p, const KVecDev* kv, const double* x, const double* smati, double* dpsi,
                           int nw, int grid, cudaStream_t st, int stride = -1, int off = 0);

@@ -39,16 +39,17 @@ namespace {
 
 constexpr int kSweepWarps = 4;   // most walkers per CTA, one warp each
 
-// floats of one warp's shared memory: positions (3 npart FP64, then 3 npart
-// FP32 for distances), the sweep's draws (npart x 4 FP64: three deviates and
-// the acceptance uniform of each move), X (nd x ldx), the new entries s' and
-// the v / w vector (nd each), the moved particle's orbitals (v-scaled and
-// plain, 2 (nk-1) float2)
+// floats of one warp's shared memory: FP32 positions for the distances (3
+// npart), X (nd x ldx), the new entries s' and the v / w vector (nd each),
+// the moved particle's orbitals (v-scaled and plain, 2 (nk-1) float2).  The
+// FP64 positions stay in the walker stack and the sweep's proposals in a
+// global slice per walker, so that a warp's share is small enough for all
+// walkers of a 4096-walker population at N = 66 to be resident at once.
 __host__ __device__ inline int sweep_warp_floats(const DevParams& p)
 {
     const int ldx = p.nd | 1;
     const int nq = p.nk > 1 ? p.nk - 1 : 1;
-    return 2 * 3 * p.npart + 3 * p.npart + 2 * 4 * p.npart + p.nd * ldx + 2 * p.nd + 8 * nq + 8;
+    return 3 * p.npart + 2 + p.nd * ldx + 2 * p.nd + 8 * nq + 8;
 }
 
 // FP32 4-point Lagrange grid position (index clamp of coshpot.f90:174)
@@ -106,14 +107,13 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
                                                                  const TabSSmp* __restrict__ tss,
                                                                  const unsigned long long* __restrict__ jA,
                                                                  const unsigned long long* __restrict__ jC,
-                                                                 unsigned long long* __restrict__ accepted, int wpc)
+                                                                 unsigned long long* __restrict__ accepted, int wpc,
+                                                                 double* __restrict__ prop)
 {
     extern __shared__ __align__(16) double smw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int P = p.npart, nd = p.nd, ldx = nd | 1, nq = p.nk - 1, nup = p.nup;
-    double* xs = smw + (size_t)wib * (sweep_warp_floats(p) / 2 + 1);
-    double* drw = xs + 3 * P;                          // [P][4]: g0, g1, g2, u of move i
-    float* xsf = reinterpret_cast<float*>(drw + 4 * P);
+    float* xsf = reinterpret_cast<float*>(smw + (size_t)wib * (sweep_warp_floats(p) / 2 + 1));
     float* X = xsf + 3 * P + (P & 1);                  // X(r, c) = X[r + c ldx]: column-major as smati
     float* snew = X + nd * ldx;
     float* vw = snew + nd;
@@ -123,10 +123,13 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
     const float elf = (float)p.el, elif = (float)p.eli;
     const int w = blockIdx.x * wpc + wib;
     if (w >= n) return;   // whole warps only: the warp is the unit below
+    double* xs = st.x + (size_t)w * 3 * P;     // FP64 positions, wrapped in place
+    double* drw = prop + (size_t)w * 4 * P;    // [P][4]: the proposal x_i + sigma g and u of move i
     // ---- load the walker: positions (wrapped), inverse, cos/sin table ----
     for (int e = lane; e < 3 * P; e += 32) {
-        xs[e] = walker::min_image(st.x[(size_t)w * 3 * P + e], p);
-        xsf[e] = (float)xs[e];
+        const double xv = walker::min_image(xs[e], p);
+        xs[e] = xv;
+        xsf[e] = (float)xv;
     }
     if (inv64) {
         for (int e = lane; e < nd * nd; e += 32) {
@@ -174,9 +177,15 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
         }
         s = (jA[5 * P] * s + jC[5 * P]) & walker::kMask48;
         __syncwarp();
+        // lanes 0-3 hold move i's proposal and uniform, read one move ahead
+        double pv = lane < 4 ? drw[lane] : 0.0;
         for (int i = 0; i < P; ++i) {
             const bool up = i < nup;
-            const double* xn = drw + 4 * i;   // the proposal, FP64
+            const double xn[3] = {__shfl_sync(0xffffffffu, pv, 0), __shfl_sync(0xffffffffu, pv, 1),
+                                  __shfl_sync(0xffffffffu, pv, 2)};   // the proposal, FP64
+            const double rn = __shfl_sync(0xffffffffu, pv, 3);
+            const double pcur = pv;
+            if (lane < 4 && i + 1 < P) pv = drw[4 * (i + 1) + lane];
             const float xf[3] = {(float)xn[0], (float)xn[1], (float)xn[2]};
             // the moved particle's plane waves
             for (int q = lane; q < nq; q += 32) {
@@ -261,7 +270,7 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
             __syncwarp();
             const float R = vw[cix];
             const float prob = R * R * expf(2.0f * du);
-            const bool acc = drw[4 * i + 3] < (double)prob;   // R = 0 or NaN: rejected
+            const bool acc = rn < (double)prob;   // R = 0 or NaN: rejected
             if (acc) {
                 const float iR = 1.0f / R;
                 // Sherman-Morrison (rank one): every column (row) but cix first
@@ -284,16 +293,15 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
                 }
                 for (int q = lane; q < nq; q += 32) T[q * P + i] = oraw[q];
                 if (lane < 3) {
-                    xs[3 * i + lane] = xn[lane];
-                    xsf[3 * i + lane] = xf[lane];
+                    xs[3 * i + lane] = pcur;
+                    xsf[3 * i + lane] = (float)pcur;
                 }
                 ++nacc;
             }
             __syncwarp();
         }
     }
-    // ---- write back ----
-    for (int e = lane; e < 3 * P; e += 32) st.x[(size_t)w * 3 * P + e] = xs[e];
+    // ---- write back (the positions are already in the stack) ----
     for (int e = lane; e < nd * nd; e += 32) {
         const int r = e % nd, c = e / nd;
         inv32[(size_t)w * nd * nd + e] = X[r + c * ldx];
@@ -311,9 +319,10 @@ size_t sweep_smem_bytes(const DevParams& p, int wpc) { return (size_t)wpc * (swe
 cudaError_t launch_sweeps(const DevParams& p, const DevStack& st, int n, int nsweep, const double* inv64,
                           float* inv32, float2* tab, const KVecMP* kv, const TabUDmp* tud, const TabSSmp* tss,
                           const unsigned long long* jA, const unsigned long long* jC, unsigned long long* accepted,
-                          cudaStream_t stream)
+                          double* prop, cudaStream_t stream)
 {
     if (n <= 0 || nsweep <= 0) return cudaSuccess;
+    if (!prop) return cudaErrorInvalidValue;
     // walkers per CTA: four, or fewer where a walker's shared memory (its
     // inverse is nd^2 floats) would not fit four times
     int dev = 0, optin = 0;
@@ -328,9 +337,14 @@ cudaError_t launch_sweeps(const DevParams& p, const DevStack& st, int n, int nsw
         e = cudaFuncSetAttribute(sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
+    // the largest shared-memory share of the SM: eight 4-walker CTAs per SM
+    // at N = 66, so that 4096 walkers are resident at once
+    e = cudaFuncSetAttribute(sweep_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
     const int grid = (n + wpc - 1) / wpc;
     sweep_kernel<<<grid, 32 * wpc, smem, stream>>>(p, st, n, nsweep, inv64, inv32, tab, kv, tud, tss, jA, jC,
-                                                   accepted, wpc);
+                                                   accepted, wpc, prop);
     return cudaGetLastError();
 }
 
