@@ -250,21 +250,34 @@ __global__ void __launch_bounds__(32 * kSweepWarps) sweep_kernel(const __grid_co
                 for (; q < nd; ++q) a[0] = fmaf(snew[q], xb[q * rs], a[0]);
                 vw[k] = (a[0] + a[1]) + (a[2] + a[3]);
             }
-            // Jastrow: U(r_i') - U(r_i) over the pairs getphione counts
+            // Jastrow: U(r_i') - U(r_i) over the pairs getphione counts.  A
+            // lane takes its partners j = lane + 32 u kJasLanes at a time, all
+            // their table lookups in flight before any is used; the
+            // differences are added in partner order (skipped pairs add 0).
+            constexpr int kJasLanes = 3;
             float du = 0.0f;
-            for (int j = lane; j < P; j += 32) {
-                if (j == i) continue;
-                const bool opp = up != (j < nup);
-                if (!opp && !p.ieq) continue;
-                float dn = 0.0f, dold = 0.0f;
-                for (int c = 0; c < 3; ++c) {
-                    const float a = min_image_f(xf[c] - xsf[3 * j + c], elf, elif);
-                    const float b = min_image_f(xsf[3 * i + c] - xsf[3 * j + c], elf, elif);
-                    dn = fmaf(a, a, dn);
-                    dold = fmaf(b, b, dold);
+            for (int j0 = lane; j0 < P; j0 += 32 * kJasLanes) {
+                float dj[kJasLanes];
+#pragma unroll
+                for (int u = 0; u < kJasLanes; ++u) {
+                    const int j = j0 + 32 * u;
+                    dj[u] = 0.0f;
+                    const bool opp = up != (j < nup);
+                    if (j < P && j != i && (opp || p.ieq)) {
+                        float dn = 0.0f, dold = 0.0f;
+                        for (int c = 0; c < 3; ++c) {
+                            const float a = min_image_f(xf[c] - xsf[3 * j + c], elf, elif);
+                            const float b = min_image_f(xsf[3 * i + c] - xsf[3 * j + c], elf, elif);
+                            dn = fmaf(a, a, dn);
+                            dold = fmaf(b, b, dold);
+                        }
+                        dj[u] = jas_u(p, tud, tss, opp, fmaxf(sqrtf(dn), 1.0e-14f)) -
+                                jas_u(p, tud, tss, opp, fmaxf(sqrtf(dold), 1.0e-14f));
+                    }
                 }
-                du += jas_u(p, tud, tss, opp, fmaxf(sqrtf(dn), 1.0e-14f)) -
-                      jas_u(p, tud, tss, opp, fmaxf(sqrtf(dold), 1.0e-14f));
+#pragma unroll
+                for (int u = 0; u < kJasLanes; ++u)
+                    if (j0 + 32 * u < P) du += dj[u];
             }
             du = warp_sum_f(du);
             __syncwarp();
